@@ -1,0 +1,294 @@
+"""Benchmark of the plain single-job path tracer on the large seeded workload.
+
+Workload: 800 subdivision-3 icospheres + ground (1,024,002 triangles), FP32
+2048x1024 procedural sky (importance sampled), 1920x1080, thin lens with 6
+aperture blades, max depth 12; one step = SPP_PER_STEP passes (camera samples
+per pixel) over the full frame. Inputs stay resident on the device; the
+working set (path state ~1.4 GB, BVH + triangles ~0.3 GB) is far larger than
+L2, so no explicit flush is done between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). `value` is camera samples per second over all
+ranks (each rank renders its own pass range of the same job: weak scaling);
+`e2e` is the same metric through the C ABI including the job load (host
+parse, BVH build, host->device upload) and a device->host read of the colour
+estimate after every step. `cpu_baseline` times the CPU checker (oracle/)
+on this host's cores on a bounded crop of the same job.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SPP_PER_STEP = 4
+WORKLOAD = "sphere_field_800x_icosphere3_1024002tri_1920x1080_dof6_sky2048x1024_depth12"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0:
+                    self.rows.append([c.strip() for c in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=6)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = sorted(float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit())
+        mx = max((float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()), default=None)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def make_job(base: str, seed: int = 0) -> str:
+    from hastyrenderer_gb300 import scenes
+    path = os.path.join(base, "renderJob.json")
+    if not os.path.exists(path):
+        scenes.sphere_field(base, seed=seed, n_spheres=800, subdiv=3, width=1920, height=1080, spp=256, max_depth=12)
+    return path
+
+
+def cpu_baseline(job_path: str, budget_s: float = 12.0, threads: int = 0):
+    """CPU checker on this host's cores: rows of a centred 128-pixel-wide crop,
+    one pass each, until the time budget is spent. Also returns the BVH node
+    visits and triangle tests per ray of the checker's binary BVH."""
+    from oracle.oracle import Oracle
+    ora = Oracle(job_path)
+    info = ora.info()
+    threads = threads or (os.cpu_count() or 1)
+    W, H = info["width"], info["height"]
+    cw = 128
+    x0 = (W - cw) // 2
+    y = H // 2 - 32
+    samples = 0
+    rays = nodes = tris = 0
+    t0 = time.perf_counter()
+    rows = 0
+    while time.perf_counter() - t0 < budget_s and rows < 512:
+        r = ora.render(0, 1, x0, y + rows % 64, cw, 8, threads)
+        st = r["stats"]
+        samples += cw * 8
+        rays += int(st[0]); nodes += int(st[2]); tris += int(st[3])
+        rows += 8
+    dt = time.perf_counter() - t0
+    ora.close()
+    return {"value": samples / dt, "unit": "samples/s", "cores": threads, "kind": "port",
+            "sample": f"{samples} camera samples: centred {cw}-pixel-wide crop, 1 pass per row band, {dt:.1f} s",
+            "mrays_per_s": rays / dt * 1e-6}, {"nodes_per_ray": nodes / max(rays, 1), "tris_per_ray": tris / max(rays, 1)}
+
+
+def run_reference_arm(args, job_path: str, rank: int):
+    if rank != 0:
+        return
+    from oracle.oracle import Oracle
+    threads = os.cpu_count() or 1
+    ora = Oracle(job_path)
+    info = ora.info()
+    cw, ch = 96, 16
+    x0, y0 = (info["width"] - cw) // 2, info["height"] // 2 - ch
+    for _ in range(args.warmup):
+        ora.render(0, 1, x0, y0, cw, ch, threads)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        ora.render(k, 1, x0, y0, cw, ch, threads)
+    dt = time.perf_counter() - t0
+    v = args.steps * cw * ch / dt
+    line = {"impl": "reference", "metric": "samples/s", "value": v, "unit": "samples/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": WORKLOAD, "step": f"{cw}x{ch} crop x 1 pass on {threads} host threads"},
+            "cpu_baseline": {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
+                             "sample": f"{cw}x{ch} centred crop, 1 pass per step, {args.steps} steps"},
+            "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--spp-per-step", type=int, default=SPP_PER_STEP)
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+
+    base = os.environ.get("HASTY_BENCH_DIR", os.path.join(tempfile.gettempdir(), "hasty_bench_c1"))
+    if rank == 0:
+        os.makedirs(base, exist_ok=True)
+        job_path = make_job(base)
+    if dist is not None:
+        dist.barrier()
+    job_path = os.path.join(base, "renderJob.json")
+
+    if args.impl == "reference":
+        run_reference_arm(args, job_path, rank)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    import torch
+    from hastyrenderer_gb300 import Context, RenderJob
+    torch.cuda.init()
+    ctx = Context(local_rank)
+
+    # ---- end to end through the C ABI: load (parse, BVH, upload) + steps with read-back
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    job = RenderJob(job_path, ctx)
+    info = job.info
+    W, H = info.width, info.height
+    for k in range(args.steps):
+        job.render_passes(args.spp_per_step)
+        est = job.compute_estimate()
+    e2e_s = time.perf_counter() - t0
+    e2e_bytes_up = info.device_bytes
+    del est
+
+    # ---- device-resident timing
+    job.reset()
+    job.set_seed(1000 + rank)
+    job.set_stage_timing(True)
+    for _ in range(args.warmup):
+        job.render_passes(args.spp_per_step)
+    job.sync()
+    s0 = job.stats()
+    sampler = ClockSampler(local_rank)
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    with sampler:
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        start.record()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            job.render_passes(args.spp_per_step)
+        job.sync()
+        torch.cuda.synchronize()
+        end.record()
+        end.synchronize()
+        wall = time.perf_counter() - w0
+        if dist is not None:
+            dist.barrier()
+    s1 = job.stats()
+    dev_s = (s1["kernel_ms"] - s0["kernel_ms"]) * 1e-3
+    t = max(dev_s, 1e-9)
+    if dist is not None:
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    samples = args.steps * args.spp_per_step * W * H
+    rays = s1["rays"] - s0["rays"]
+    trace_ms = s1["trace_ms"] - s0["trace_ms"]
+    shade_ms = s1["shade_ms"] - s0["shade_ms"]
+    launches = s1["kernel_launches"] - s0["kernel_launches"]
+    trace_launches = s1["trace_launches"] - s0["trace_launches"]
+    clocks = sampler.summary()
+
+    if rank == 0:
+        hbm, peak_kind = peaks()
+        cpu, bvh_costs = (None, None)
+        if not args.no_cpu_baseline:
+            cpu, bvh_costs = cpu_baseline(job_path, args.cpu_budget)
+        b_ray = None
+        roof = None
+        if bvh_costs is not None:
+            b_ray = 32 + 16 + 64 * bvh_costs["nodes_per_ray"] + 48 * bvh_costs["tris_per_ray"]
+            per_launch_bytes = rays * b_ray / max(trace_launches, 1)
+            per_launch_s = trace_ms * 1e-3 / max(trace_launches, 1)
+            achieved = per_launch_bytes / per_launch_s / 1e9
+            roof = {"bound": "hbm", "kernel": "k_trace (closest hit)", "achieved": achieved, "peak": hbm,
+                    "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
+                    "algorithmic_bytes_per_ray": b_ray, "bvh_nodes_per_ray": bvh_costs["nodes_per_ray"],
+                    "tris_per_ray": bvh_costs["tris_per_ray"]}
+        line = {
+            "metric": "samples/s", "value": samples * world / t, "unit": "samples/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": WORKLOAD, "spp_per_step": args.spp_per_step, "width": W, "height": H,
+                       "max_depth": info.max_depth, "triangles": info.n_triangles,
+                       "l2": "working set > L2 (path state + BVH), no flush", "parallelism": f"replicas x{world}"},
+            "mrays_per_s": rays * world / t * 1e-6,
+            "stage_ms_per_step": {"trace": trace_ms / args.steps, "shade": shade_ms / args.steps},
+            "wall_ms_per_step": wall / args.steps * 1e3,
+            "gpu_launches": launches,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": args.steps * args.spp_per_step * W * H * world / e2e_s, "unit": "samples/s",
+                    "h2d_bytes_per_step": int(e2e_bytes_up // args.steps), "d2h_bytes_per_step": W * H * 3 * 4,
+                    "includes": "job load (parse, BVH build, upload) + steps + colour read-back"},
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    job.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

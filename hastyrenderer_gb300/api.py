@@ -1,0 +1,167 @@
+"""Python mirror of the reference's render-job interface over the C ABI.
+
+Names follow the reference: ``RenderJob.loadJSON`` (core/src/RenderJob.cpp:21-28),
+``render_passes`` for the renderThread pass loop (core/src/PathTracing.cpp:98-160),
+``compute_estimate`` for computeEstimate (apps/ViewerUtils.cpp:95-121),
+``write_outputs`` for postProcessAndSaveToDisk without the denoiser
+(apps/ViewerUtils.cpp:137-152). Load errors raise ``HastyError`` with code
+HASTY_ERR_LOAD, the counterpart of the reference's loader exceptions.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import native
+from .native import AOV_ALBEDO, AOV_COLOR, AOV_NORMAL, HastyError, check
+
+__all__ = ["Context", "RenderJob", "debug_bsdf", "AOV_COLOR", "AOV_NORMAL", "AOV_ALBEDO", "HastyError"]
+
+
+class Context:
+    """One CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p()
+        check(native.lib().hasty_ctx_create(device, 0, ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            native.lib().hasty_ctx_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class RenderJob:
+    """A render job resident on the device (scene, BVH, accumulators)."""
+
+    def __init__(self, path: str | None = None, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self._h = ctypes.c_void_p()
+        if path is not None:
+            self.loadJSON(path)
+
+    def loadJSON(self, path: str) -> None:
+        if self._h:
+            self.close()
+        check(native.lib().hasty_job_load(self.ctx._h, path.encode(), ctypes.byref(self._h)))
+
+    def close(self) -> None:
+        if self._h:
+            native.lib().hasty_job_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def info(self) -> native.JobInfo:
+        out = native.JobInfo()
+        check(native.lib().hasty_job_info_get(self._h, ctypes.byref(out)))
+        return out
+
+    @property
+    def width(self) -> int:
+        return self.info.width
+
+    @property
+    def height(self) -> int:
+        return self.info.height
+
+    def set_seed(self, seed: int) -> None:
+        check(native.lib().hasty_job_set_seed(self._h, ctypes.c_uint64(seed)))
+
+    def reset(self) -> None:
+        check(native.lib().hasty_job_reset(self._h))
+
+    def set_paths_in_flight(self, n: int) -> None:
+        check(native.lib().hasty_job_set_paths_in_flight(self._h, ctypes.c_int64(n)))
+
+    def render_passes(self, n: int, sync: bool = False) -> None:
+        check(native.lib().hasty_job_render_passes(self._h, int(n)))
+        if sync:
+            self.sync()
+
+    def sync(self) -> None:
+        check(native.lib().hasty_job_sync(self._h))
+
+    def stop(self) -> None:
+        check(native.lib().hasty_job_stop(self._h))
+
+    def set_stage_timing(self, on: bool = True) -> None:
+        check(native.lib().hasty_job_set_stage_timing(self._h, 1 if on else 0))
+
+    def stats(self) -> dict:
+        s = native.Stats()
+        check(native.lib().hasty_job_stats_get(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in native.Stats._fields_}
+
+    def compute_estimate(self, aov: int = AOV_COLOR) -> np.ndarray:
+        i = self.info
+        out = np.empty((i.height, i.width, 3), dtype=np.float32)
+        n = ctypes.c_int32()
+        check(native.lib().hasty_job_read(self._h, aov, out.ctypes.data, i.width, i.height, ctypes.byref(n)))
+        return out
+
+    def read_sums(self, aov: int = AOV_COLOR) -> tuple[np.ndarray, int]:
+        i = self.info
+        out = np.empty((i.height, i.width, 3), dtype=np.float64)
+        n = ctypes.c_int32()
+        check(native.lib().hasty_job_read_sums(self._h, aov, out.ctypes.data, i.width, i.height, ctypes.byref(n)))
+        return out, n.value
+
+    def write_outputs(self, out_dir: str, write_pfm: bool = False) -> None:
+        check(native.lib().hasty_job_write_outputs(self._h, out_dir.encode(), 1 if write_pfm else 0))
+
+    def intersect(self, rays: np.ndarray):
+        """Closest hits of rays (n x 6: origin, direction) -> (tri, t, u, v)."""
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        n = r.shape[0]
+        tri = np.empty(n, np.int32)
+        t, u, v = (np.empty(n, np.float32) for _ in range(3))
+        check(native.lib().hasty_debug_intersect(self._h, r.ctypes.data, n, tri.ctypes.data, t.ctypes.data,
+                                                  u.ctypes.data, v.ctypes.data))
+        return tri, t, u, v
+
+    def triangle_ids(self):
+        """Global triangle index -> (OBJ shape id, face id)."""
+        n = self.info.n_triangles
+        g = np.empty(n, np.int32)
+        p = np.empty(n, np.int32)
+        check(native.lib().hasty_debug_tri_ids(self._h, g.ctypes.data, p.ctypes.data, n))
+        return g, p
+
+
+def debug_bsdf(which: int, cases: np.ndarray, replay: np.ndarray) -> np.ndarray:
+    """Device BSDF on known inputs: which 0 sample, 1 evaluate, 2 pdf.
+    cases: n x 33 float32; replay: n x k uint32 (values served in order)."""
+    c = np.ascontiguousarray(cases, dtype=np.float32).reshape(-1, 33)
+    r = np.ascontiguousarray(replay, dtype=np.uint32).reshape(c.shape[0], -1)
+    out = np.zeros((c.shape[0], 12), np.float32)
+    check(native.lib().hasty_debug_bsdf(which, c.ctypes.data, c.shape[0], r.ctypes.data, r.shape[1], out.ctypes.data))
+    return out

@@ -1,0 +1,545 @@
+// C ABI of the GB300 path tracer (include/hasty_gpu.h): job lifecycle, device
+// upload, batch orchestration and outputs. The pass loop replaces the
+// reference's renderThread (core/src/PathTracing.cpp:98-160): instead of one
+// CPU thread rendering whole 1-spp frames, a batch of passes is rendered as
+// one wavefront of W*H*passes camera samples on the job's CUDA stream, and the
+// per-sample results are folded into FP64 accumulators in pass order.
+#include "hasty_gpu.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "bvh_build.h"
+#include "image_out.h"
+#include "scene_load.h"
+#include "wavefront.h"
+
+namespace hasty {
+// integrator.cu
+void launch_debug_bsdf(int which, const float* in, int n, const uint32_t* replay, int n_replay, float* out, cudaStream_t st);
+}
+
+using namespace hasty;
+
+namespace {
+thread_local std::string g_error;
+
+struct ApiError {
+  int code; std::string msg;
+};
+
+int fail(int code, const std::string& m) { g_error = m; return code; }
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    int code = (e == cudaErrorMemoryAllocation) ? HASTY_ERR_MEMORY : HASTY_ERR_CUDA;
+    throw ApiError{code, std::string(what) + ": " + cudaGetErrorString(e)};
+  }
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const ApiError& e) {
+    return fail(e.code, e.msg);
+  } catch (const LoadError& e) {
+    return fail(HASTY_ERR_LOAD, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(HASTY_ERR_MEMORY, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(HASTY_ERR_CUDA, e.what());
+  }
+}
+}  // namespace
+
+struct hasty_ctx {
+  int device = 0;
+  int sm_count = 0;
+};
+
+struct hasty_job {
+  hasty_ctx* ctx = nullptr;
+  HostScene host;
+  int32_t bvh_depth = 0;
+  double bvh_ms = 0;
+  SceneDev sd{};
+  PathsDev pd{};
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+  double* acc[3] = {nullptr, nullptr, nullptr};
+  float* est = nullptr;
+  int64_t capacity = 0;
+  int32_t samples_done = 0;
+  uint64_t seed = 0;
+  std::atomic<bool> stop{false};
+  double kernel_ms = 0.0, trace_ms = 0.0, shade_ms = 0.0;
+  uint64_t trace_launches = 0, kernel_launches = 0;
+  bool stage_timing = false;
+  // (start, end, stage) with stage 0: whole batch, 1: trace, 2: shade
+  struct Ev { cudaEvent_t a, b; int stage; };
+  std::vector<Ev> pending_events;
+
+  template <class T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    size_t b = std::max<size_t>(n, 1) * sizeof(T);
+    ck(cudaMalloc(&p, b), "cudaMalloc");
+    allocs.push_back(p);
+    bytes += int64_t(b);
+    return static_cast<T*>(p);
+  }
+  template <class T>
+  T* upload(const std::vector<T>& v) {
+    if (v.empty()) return nullptr;
+    T* p = alloc<T>(v.size());
+    ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream), "upload");
+    return p;
+  }
+  void collect_events() {
+    for (auto& e : pending_events) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) {
+        if (e.stage == 0) kernel_ms += ms; else if (e.stage == 1) trace_ms += ms; else shade_ms += ms;
+      }
+      cudaEventDestroy(e.a); cudaEventDestroy(e.b);
+    }
+    pending_events.clear();
+  }
+  ~hasty_job() {
+    if (stream) cudaStreamSynchronize(stream);
+    collect_events();
+    for (void* p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+void alloc_paths(hasty_job& j, int64_t cap) {
+  PathsDev& p = j.pd;
+  p.capacity = int32_t(cap);
+  p.rng = j.alloc<uint64_t>(size_t(cap));
+  p.thr = j.alloc<float4>(size_t(cap));
+  p.rad = j.alloc<float4>(size_t(cap));
+  p.pend_b = j.alloc<float4>(size_t(cap));
+  p.nee_c = j.alloc<float4>(size_t(cap));
+  p.nee_t = j.alloc<float4>(size_t(cap));
+  p.med = j.alloc<float4>(size_t(cap) * kMaxMedia);
+  p.med_geom = j.alloc<int32_t>(size_t(cap) * kMaxMedia);
+  p.ray_o = j.alloc<float4>(size_t(cap) * 2);
+  p.ray_d = j.alloc<float4>(size_t(cap) * 2);
+  p.hit = j.alloc<float4>(size_t(cap) * 2);
+  p.pq[0] = j.alloc<int32_t>(size_t(cap));
+  p.pq[1] = j.alloc<int32_t>(size_t(cap));
+  p.rq[0] = j.alloc<int32_t>(size_t(cap) * 2);
+  p.rq[1] = j.alloc<int32_t>(size_t(cap) * 2);
+  p.counts = j.alloc<uint32_t>(4);
+  p.out_color = j.alloc<float4>(size_t(cap));
+  p.out_normal = j.alloc<float4>(size_t(cap));
+  p.out_albedo = j.alloc<float4>(size_t(cap));
+  p.stats = j.alloc<unsigned long long>(ST_COUNT);
+  ck(cudaMemsetAsync(p.stats, 0, sizeof(unsigned long long) * ST_COUNT, j.stream), "memset stats");
+  ck(cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4, j.stream), "memset counts");
+}
+
+void upload_scene(hasty_job& j) {
+  HostScene& h = j.host;
+  SceneDev& s = j.sd;
+  BvhHost bvh;
+  build_bvh_binary(h.tri_pos.data(), h.n_tris(), 4, bvh);
+  if (bvh.depth > 60) throw ApiError{HASTY_ERR_LOAD, "BVH deeper than the traversal stack (64)"};
+  j.bvh_depth = bvh.depth; j.bvh_ms = bvh.build_ms;
+  s.n_tris = int32_t(h.n_tris());
+  s.tri_pos = j.upload(h.tri_pos);
+  s.tri_attr = j.upload(h.tri_attr);
+  s.normals = j.upload(h.normals);
+  s.texcoords = j.upload(h.texcoords);
+  s.n_texcoords = int64_t(h.texcoords.size());
+  s.bvh_kind = 0;
+  {
+    float4* n = j.alloc<float4>(bvh.nodes.size() / 4);
+    ck(cudaMemcpyAsync(n, bvh.nodes.data(), bvh.nodes.size() * sizeof(float), cudaMemcpyHostToDevice, j.stream), "upload nodes");
+    s.nodes = n;
+    float4* t = j.alloc<float4>(bvh.tris.size() / 4);
+    ck(cudaMemcpyAsync(t, bvh.tris.data(), bvh.tris.size() * sizeof(float), cudaMemcpyHostToDevice, j.stream), "upload tris");
+    s.isect_tris = t;
+    ck(cudaStreamSynchronize(j.stream), "sync upload");   // host vectors of bvh go out of scope
+  }
+  s.mats = j.upload(h.mats);
+  s.textures = j.upload(h.textures);
+  s.tex_pool = j.upload(h.tex_pool);
+  s.n_light_tris = int32_t(h.light_tris.size());
+  s.light_tris = j.upload(h.light_tris);
+  s.light_cdf = j.upload(h.light_cdf);
+  s.light_pdf_area = h.light_tris.empty() ? 0.0f : 1.0f / h.total_light_area;
+  EnvDev& e = s.env;
+  e.is_texture = h.env_texture ? 1 : 0;
+  for (int c = 0; c < 3; ++c) e.color[c] = h.bg[c];
+  e.w = h.env_w; e.h = h.env_h;
+  e.texels = j.upload(h.env_texels);
+  e.weights = j.upload(h.env_weights);
+  e.cdf = j.upload(h.env_cdf);
+  e.value_sum = h.env_value_sum;
+  s.cam = h.cam;
+  const RenderSettingsH& st = h.settings;
+  s.width = int32_t(st.width); s.height = int32_t(st.height);
+  s.max_depth = st.max_depth; s.rr_start = st.roulette_start; s.rr_q = st.roulette_q;
+  s.two_strategies = (h.has_light() && st.use_mis) ? 1 : 0;
+  s.env_is_sampled = h.env_texture ? 1 : 0;
+  s.p_surface = !h.env_texture ? 1.0f : (!h.light_tris.empty() ? 0.5f : 0.0f);   // Scene.cpp:545
+  ck(cudaStreamSynchronize(j.stream), "sync upload");
+}
+
+void clear_accumulators(hasty_job& j) {
+  size_t n = size_t(j.sd.width) * size_t(j.sd.height) * 3;
+  for (double* a : j.acc) ck(cudaMemsetAsync(a, 0, n * sizeof(double), j.stream), "memset acc");
+  ck(cudaMemsetAsync(j.pd.stats, 0, sizeof(unsigned long long) * ST_COUNT, j.stream), "memset stats");
+  j.samples_done = 0;
+  j.kernel_ms = j.trace_ms = j.shade_ms = 0.0;
+  j.trace_launches = j.kernel_launches = 0;
+}
+
+int64_t default_capacity(int64_t npix) {
+  int64_t cap = int64_t(1) << 22;   // 4M camera samples in flight (about 1.4 GB of path state)
+  if (npix > cap) cap = npix;
+  return (cap / npix) * npix;
+}
+
+void render_batch(hasty_job& j, int n_passes) {
+  BatchDesc b;
+  b.seed = j.seed;
+  b.pass_base = uint32_t(j.samples_done);
+  b.n_passes = n_passes;
+  b.n_paths = n_passes * j.sd.width * j.sd.height;
+  cudaEvent_t e0, e1;
+  ck(cudaEventCreate(&e0), "event"); ck(cudaEventCreate(&e1), "event");
+  ck(cudaEventRecord(e0, j.stream), "event record");
+  launch_raygen(j.sd, j.pd, b, j.stream);
+  int max_paths = b.n_paths;
+  auto timed = [&](int stage, auto&& fn) {
+    if (!j.stage_timing) { fn(); return; }
+    cudaEvent_t a, c;
+    ck(cudaEventCreate(&a), "event"); ck(cudaEventCreate(&c), "event");
+    ck(cudaEventRecord(a, j.stream), "event record");
+    fn();
+    ck(cudaEventRecord(c, j.stream), "event record");
+    j.pending_events.push_back({a, c, stage});
+  };
+  for (int bounce = 0; bounce < j.sd.max_depth; ++bounce) {
+    int q = bounce & 1;
+    timed(1, [&] { launch_trace(j.sd, j.pd, q, 2 * max_paths, j.stream); });
+    ck(cudaMemsetAsync(&j.pd.counts[q ^ 1], 0, sizeof(uint32_t), j.stream), "memset count");
+    ck(cudaMemsetAsync(&j.pd.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), j.stream), "memset count");
+    timed(2, [&] { launch_shade(j.sd, j.pd, b, q, max_paths, j.stream); });
+  }
+  launch_accumulate(j.sd, j.pd, b, j.acc[0], j.acc[1], j.acc[2], j.stream);
+  ck(cudaGetLastError(), "kernel launch");
+  ck(cudaEventRecord(e1, j.stream), "event record");
+  j.pending_events.push_back({e0, e1, 0});
+  j.trace_launches += uint64_t(j.sd.max_depth);
+  j.kernel_launches += uint64_t(2 + 2 * j.sd.max_depth);
+  j.samples_done += n_passes;
+}
+
+hasty_job* as_job(hasty_job* j) {
+  if (!j) throw ApiError{HASTY_ERR_ARG, "null job handle"};
+  return j;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hasty_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return HASTY_ERR_ARG;
+  std::strncpy(buf, g_error.c_str(), len - 1);
+  buf[len - 1] = 0;
+  return HASTY_OK;
+}
+
+int hasty_version(int* major, int* minor) {
+  if (major) *major = 0;
+  if (minor) *minor = 1;
+  return HASTY_OK;
+}
+
+int hasty_ctx_create(int device, uint32_t flags, hasty_ctx** out) {
+  (void)flags;
+  return guarded([&] {
+    if (!out) throw ApiError{HASTY_ERR_ARG, "null output pointer"};
+    int n = 0;
+    ck(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    if (device < 0 || device >= n) throw ApiError{HASTY_ERR_ARG, "no CUDA device " + std::to_string(device)};
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    auto* c = new hasty_ctx();
+    c->device = device;
+    ck(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "attr");
+    *out = c;
+    return HASTY_OK;
+  });
+}
+
+int hasty_ctx_destroy(hasty_ctx* ctx) { delete ctx; return HASTY_OK; }
+
+int hasty_job_load(hasty_ctx* ctx, const char* path, hasty_job** out) {
+  return guarded([&] {
+    if (!ctx || !path || !out) throw ApiError{HASTY_ERR_ARG, "null argument"};
+    ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+    std::unique_ptr<hasty_job> j(new hasty_job());
+    j->ctx = ctx;
+    load_render_job(path, j->host);
+    j->seed = j->host.settings.seed;
+    ck(cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking), "stream");
+    upload_scene(*j);
+    int64_t npix = int64_t(j->sd.width) * j->sd.height;
+    j->capacity = default_capacity(npix);
+    alloc_paths(*j, j->capacity);
+    for (double*& a : j->acc) a = j->alloc<double>(size_t(npix) * 3);
+    j->est = j->alloc<float>(size_t(npix) * 3);
+    clear_accumulators(*j);
+    ck(cudaStreamSynchronize(j->stream), "sync");
+    // the host copies of the large arrays are not needed after upload
+    std::vector<float>().swap(j->host.tri_pos);
+    std::vector<float>().swap(j->host.env_texels);
+    std::vector<float>().swap(j->host.tex_pool);
+    *out = j.release();
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_destroy(hasty_job* job) { delete job; return HASTY_OK; }
+
+int hasty_job_info_get(hasty_job* job, hasty_job_info* out) {
+  return guarded([&] {
+    as_job(job);
+    if (!out) throw ApiError{HASTY_ERR_ARG, "null output"};
+    const HostScene& h = job->host;
+    out->width = int32_t(h.settings.width); out->height = int32_t(h.settings.height);
+    out->num_samples = h.settings.num_samples; out->max_depth = h.settings.max_depth;
+    out->roulette_start_depth = h.settings.roulette_start; out->roulette_q = h.settings.roulette_q;
+    out->use_mis = h.settings.use_mis ? 1 : 0; out->seed = job->seed;
+    out->n_triangles = int64_t(h.tri_attr.size()); out->n_light_triangles = int64_t(h.light_tris.size());
+    out->n_shapes = int32_t(h.n_shapes); out->n_materials = int32_t(h.mats.size());
+    out->env_is_texture = h.env_texture ? 1 : 0; out->exposure = h.cam.exposure;
+    out->samples_done = job->samples_done; out->bvh_depth = job->bvh_depth; out->bvh_build_ms = job->bvh_ms;
+    out->device_bytes = job->bytes;
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_reset(hasty_job* job) {
+  return guarded([&] {
+    as_job(job);
+    ck(cudaStreamSynchronize(job->stream), "sync");
+    job->collect_events();
+    clear_accumulators(*job);
+    job->stop = false;
+    ck(cudaStreamSynchronize(job->stream), "sync");
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_set_seed(hasty_job* job, uint64_t seed) {
+  int rc = hasty_job_reset(job);
+  if (rc == HASTY_OK) job->seed = seed;
+  return rc;
+}
+
+int hasty_job_set_paths_in_flight(hasty_job* job, int64_t paths) {
+  return guarded([&] {
+    as_job(job);
+    int64_t npix = int64_t(job->sd.width) * job->sd.height;
+    int64_t cap = paths <= 0 ? default_capacity(npix) : std::max<int64_t>(npix, (paths / npix) * npix);
+    if (cap == job->capacity) return HASTY_OK;
+    if (cap > int64_t(INT32_MAX) / 2) throw ApiError{HASTY_ERR_ARG, "too many paths in flight"};
+    ck(cudaStreamSynchronize(job->stream), "sync");
+    // release the old path buffers by rebuilding the allocation list
+    PathsDev old = job->pd;
+    void* olds[] = {old.rng, old.thr, old.rad, old.pend_b, old.nee_c, old.nee_t, old.med, old.med_geom, old.ray_o, old.ray_d,
+                    old.hit, old.pq[0], old.pq[1], old.rq[0], old.rq[1], old.counts, old.out_color, old.out_normal, old.out_albedo};
+    unsigned long long stats_host[ST_COUNT];
+    ck(cudaMemcpy(stats_host, old.stats, sizeof(stats_host), cudaMemcpyDeviceToHost), "copy stats");
+    for (void* p : olds) {
+      auto it = std::find(job->allocs.begin(), job->allocs.end(), p);
+      if (it != job->allocs.end()) { job->allocs.erase(it); cudaFree(p); }
+    }
+    auto sit = std::find(job->allocs.begin(), job->allocs.end(), static_cast<void*>(old.stats));
+    if (sit != job->allocs.end()) { job->allocs.erase(sit); cudaFree(old.stats); }
+    job->capacity = cap;
+    alloc_paths(*job, cap);
+    ck(cudaMemcpy(job->pd.stats, stats_host, sizeof(stats_host), cudaMemcpyHostToDevice), "restore stats");
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_render_passes(hasty_job* job, int n_passes) {
+  return guarded([&] {
+    as_job(job);
+    if (n_passes < 0) throw ApiError{HASTY_ERR_ARG, "negative pass count"};
+    ck(cudaSetDevice(job->ctx->device), "cudaSetDevice");
+    int64_t npix = int64_t(job->sd.width) * job->sd.height;
+    int per_batch = int(std::max<int64_t>(1, job->capacity / npix));
+    int left = n_passes;
+    while (left > 0) {
+      if (job->stop.load()) throw ApiError{HASTY_ERR_STOPPED, "job stopped"};
+      int k = std::min(left, per_batch);
+      render_batch(*job, k);
+      left -= k;
+    }
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_sync(hasty_job* job) {
+  return guarded([&] {
+    as_job(job);
+    ck(cudaStreamSynchronize(job->stream), "cudaStreamSynchronize");
+    job->collect_events();
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_stop(hasty_job* job) {
+  if (!job) return fail(HASTY_ERR_ARG, "null job handle");
+  job->stop = true;
+  return HASTY_OK;
+}
+
+int hasty_job_set_stage_timing(hasty_job* job, int on) {
+  if (!job) return fail(HASTY_ERR_ARG, "null job handle");
+  job->stage_timing = on != 0;
+  return HASTY_OK;
+}
+
+int hasty_job_stats_get(hasty_job* job, hasty_stats* out) {
+  return guarded([&] {
+    as_job(job);
+    if (!out) throw ApiError{HASTY_ERR_ARG, "null output"};
+    ck(cudaStreamSynchronize(job->stream), "sync");
+    job->collect_events();
+    unsigned long long s[ST_COUNT];
+    ck(cudaMemcpy(s, job->pd.stats, sizeof(s), cudaMemcpyDeviceToHost), "copy stats");
+    out->rays = s[ST_RAYS]; out->shaded = s[ST_SHADED]; out->paths = s[ST_PATHS]; out->nan_samples = s[ST_NAN];
+    out->media_overflow = s[ST_MEDIA_OVERFLOW]; out->trial_cap = s[ST_TRIAL_CAP];
+    out->kernel_ms = job->kernel_ms;
+    out->trace_ms = job->trace_ms; out->shade_ms = job->shade_ms;
+    out->trace_launches = job->trace_launches; out->kernel_launches = job->kernel_launches;
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_read_sums(hasty_job* job, int aov, double* host, size_t w, size_t h, int32_t* num_samples) {
+  return guarded([&] {
+    as_job(job);
+    if (aov < 0 || aov > 2 || !host) throw ApiError{HASTY_ERR_ARG, "bad aov or buffer"};
+    if (w != size_t(job->sd.width) || h != size_t(job->sd.height)) throw ApiError{HASTY_ERR_ARG, "buffer size does not match the frame"};
+    ck(cudaStreamSynchronize(job->stream), "sync");
+    job->collect_events();
+    ck(cudaMemcpy(host, job->acc[aov], w * h * 3 * sizeof(double), cudaMemcpyDeviceToHost), "copy sums");
+    if (num_samples) *num_samples = job->samples_done;
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_read(hasty_job* job, int aov, float* host, size_t w, size_t h, int32_t* num_samples) {
+  return guarded([&] {
+    as_job(job);
+    if (aov < 0 || aov > 2 || !host) throw ApiError{HASTY_ERR_ARG, "bad aov or buffer"};
+    if (w != size_t(job->sd.width) || h != size_t(job->sd.height)) throw ApiError{HASTY_ERR_ARG, "buffer size does not match the frame"};
+    int n = int(w * h * 3);
+    float den = 1e-7f + float(job->samples_done);
+    float scale = aov == HASTY_AOV_COLOR ? std::pow(2.0f, job->host.cam.exposure) : 1.0f;
+    launch_estimate(job->acc[aov], n, den, scale, job->est, job->stream);
+    ck(cudaGetLastError(), "estimate launch");
+    ck(cudaMemcpyAsync(host, job->est, size_t(n) * sizeof(float), cudaMemcpyDeviceToHost, job->stream), "copy estimate");
+    ck(cudaStreamSynchronize(job->stream), "sync");
+    job->collect_events();
+    if (num_samples) *num_samples = job->samples_done;
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_write_outputs(hasty_job* job, const char* out_dir, int write_pfm) {
+  return guarded([&] {
+    as_job(job);
+    if (!out_dir) throw ApiError{HASTY_ERR_ARG, "null directory"};
+    struct stat sb;
+    if (stat(out_dir, &sb) != 0 || !S_ISDIR(sb.st_mode)) throw ApiError{HASTY_ERR_IO, std::string("not a directory: ") + out_dir};
+    size_t w = size_t(job->sd.width), h = size_t(job->sd.height);
+    std::vector<float> img(w * h * 3);
+    const char* names[3] = {"output", "outputNormal", "outputAlbedo"};
+    for (int a = 0; a < 3; ++a) {
+      int rc = hasty_job_read(job, a, img.data(), w, h, nullptr);
+      if (rc != HASTY_OK) return rc;
+      std::string base = std::string(out_dir) + "/" + names[a];
+      if (!write_exr_rgb(base + ".exr", img.data(), int(w), int(h))) throw ApiError{HASTY_ERR_IO, "could not write " + base + ".exr"};
+      if (write_pfm && !write_pfm_rgb(base + ".pfm", img.data(), int(w), int(h))) throw ApiError{HASTY_ERR_IO, "could not write " + base + ".pfm"};
+    }
+    return HASTY_OK;
+  });
+}
+
+int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* tri, float* t, float* u, float* v) {
+  return guarded([&] {
+    as_job(job);
+    if (n == 0) return HASTY_OK;
+    if (!rays || !tri || !t || !u || !v) throw ApiError{HASTY_ERR_ARG, "null buffer"};
+    if (n > size_t(INT32_MAX)) throw ApiError{HASTY_ERR_ARG, "too many rays"};
+    float* dr = nullptr; float4* dh = nullptr;
+    ck(cudaMalloc(&dr, n * 6 * sizeof(float)), "cudaMalloc rays");
+    cudaError_t e = cudaMalloc(&dh, n * sizeof(float4));
+    if (e != cudaSuccess) { cudaFree(dr); ck(e, "cudaMalloc hits"); }
+    std::vector<float4> hh(n);
+    cudaError_t err = cudaMemcpyAsync(dr, rays, n * 6 * sizeof(float), cudaMemcpyHostToDevice, job->stream);
+    if (err == cudaSuccess) { launch_trace_rays(job->sd, dr, int(n), dh, job->stream); err = cudaGetLastError(); }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(hh.data(), dh, n * sizeof(float4), cudaMemcpyDeviceToHost, job->stream);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(job->stream);
+    cudaFree(dr); cudaFree(dh);
+    ck(err, "debug intersect");
+    for (size_t i = 0; i < n; ++i) {
+      int32_t id; std::memcpy(&id, &hh[i].w, 4);
+      tri[i] = id; t[i] = hh[i].x; u[i] = hh[i].y; v[i] = hh[i].z;
+    }
+    return HASTY_OK;
+  });
+}
+
+int hasty_debug_tri_ids(hasty_job* job, int32_t* geom, int32_t* prim, size_t n) {
+  return guarded([&] {
+    as_job(job);
+    if (n != job->host.tri_attr.size()) throw ApiError{HASTY_ERR_ARG, "n must equal the triangle count"};
+    for (size_t i = 0; i < n; ++i) { geom[i] = int32_t(job->host.tri_attr[i].geom); prim[i] = int32_t(job->host.tri_attr[i].prim); }
+    return HASTY_OK;
+  });
+}
+
+int hasty_debug_bsdf(int which, const float* in, size_t n_cases, const uint32_t* replay, size_t n_replay, float* out) {
+  return guarded([&] {
+    if (which < 0 || which > 2 || !in || !out || (n_replay && !replay)) throw ApiError{HASTY_ERR_ARG, "bad argument"};
+    if (n_cases == 0) return HASTY_OK;
+    if (n_replay == 0) throw ApiError{HASTY_ERR_ARG, "replay stream must not be empty"};
+    float *din = nullptr, *dout = nullptr; uint32_t* drep = nullptr;
+    ck(cudaMalloc(&din, n_cases * 33 * sizeof(float)), "cudaMalloc");
+    cudaError_t err = cudaMalloc(&dout, n_cases * 12 * sizeof(float));
+    if (err == cudaSuccess) err = cudaMalloc(&drep, n_cases * n_replay * sizeof(uint32_t));
+    if (err == cudaSuccess) err = cudaMemcpy(din, in, n_cases * 33 * sizeof(float), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) err = cudaMemcpy(drep, replay, n_cases * n_replay * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) { launch_debug_bsdf(which, din, int(n_cases), drep, int(n_replay), dout, 0); err = cudaGetLastError(); }
+    if (err == cudaSuccess) err = cudaMemcpy(out, dout, n_cases * 12 * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(din); cudaFree(dout); cudaFree(drep);
+    ck(err, "debug bsdf");
+    return HASTY_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,189 @@
+// Binned-SAH binary BVH builder (host, multi-threaded). See bvh_build.h.
+#include "bvh_build.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+
+namespace hasty {
+namespace {
+
+struct Box {
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  void grow(const Box& b) { for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], b.lo[a]); hi[a] = std::max(hi[a], b.hi[a]); } }
+  void grow(const float* p) { for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], p[a]); hi[a] = std::max(hi[a], p[a]); } }
+  float area() const {
+    float d[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    if (d[0] < 0.f) return 0.f;
+    return 2.f * (d[0] * d[1] + d[1] * d[2] + d[2] * d[0]);
+  }
+};
+
+struct BNode { Box box; int32_t child = -1; int32_t first = 0, count = 0; };
+
+struct Builder {
+  const float* pos; size_t n; int max_leaf;
+  std::vector<Box> tbox;
+  std::vector<float> cen;
+  std::vector<int32_t> idx;
+  std::vector<BNode> nodes;
+  std::atomic<int32_t> next_node{1};
+  std::atomic<int32_t> max_depth{0};
+
+  struct Task { int32_t node, first, count, depth; };
+  std::mutex mu; std::condition_variable cv;
+  std::deque<Task> queue; int active = 0;
+
+  void push(const Task& t) { { std::lock_guard<std::mutex> g(mu); queue.push_back(t); } cv.notify_one(); }
+
+  void run_task(Task t) {
+    // large tasks split here and hand one child to the pool; small ones recurse locally
+    std::vector<Task> local{t};
+    while (!local.empty()) {
+      Task k = local.back(); local.pop_back();
+      int32_t d = k.depth;
+      int32_t md = max_depth.load();
+      while (d > md && !max_depth.compare_exchange_weak(md, d)) {}
+      BNode& nd = nodes[size_t(k.node)];
+      Box cb;
+      nd.box = Box();
+      for (int32_t i = k.first; i < k.first + k.count; ++i) { nd.box.grow(tbox[size_t(idx[size_t(i)])]); cb.grow(&cen[3 * size_t(idx[size_t(i)])]); }
+      int axis = -1, split_bin = -1; float best = FLT_MAX;
+      constexpr int B = 32;
+      if (k.count > 1) {
+        for (int a = 0; a < 3; ++a) {
+          float ext = cb.hi[a] - cb.lo[a];
+          if (!(ext > 0.f)) continue;
+          Box bb[B]; int bc[B] = {0};
+          float sc = float(B) / ext;
+          for (int32_t i = k.first; i < k.first + k.count; ++i) {
+            int32_t t2 = idx[size_t(i)];
+            int b = std::min(B - 1, int((cen[3 * size_t(t2) + a] - cb.lo[a]) * sc));
+            bc[b]++; bb[b].grow(tbox[size_t(t2)]);
+          }
+          float rarea[B]; int rcnt[B];
+          Box acc; int c = 0;
+          for (int b = B - 1; b > 0; --b) { acc.grow(bb[b]); c += bc[b]; rarea[b] = acc.area(); rcnt[b] = c; }
+          Box lacc; int lc = 0;
+          for (int b = 0; b < B - 1; ++b) {
+            lacc.grow(bb[b]); lc += bc[b];
+            if (lc == 0 || rcnt[b + 1] == 0) continue;
+            float cost = lacc.area() * float(lc) + rarea[b + 1] * float(rcnt[b + 1]);
+            if (cost < best) { best = cost; axis = a; split_bin = b; }
+          }
+        }
+      }
+      float leaf_cost = nd.box.area() * float(k.count);
+      bool leaf = k.count <= 1 || (k.count <= max_leaf && (axis < 0 || leaf_cost <= best));
+      if (leaf) { nd.first = k.first; nd.count = k.count; nd.child = -1; continue; }
+      int32_t mid;
+      if (axis >= 0) {
+        float sc = float(B) / (cb.hi[axis] - cb.lo[axis]);
+        float lo = cb.lo[axis];
+        auto it = std::partition(idx.begin() + k.first, idx.begin() + k.first + k.count, [&](int32_t t2) {
+          return std::min(B - 1, int((cen[3 * size_t(t2) + axis] - lo) * sc)) <= split_bin;
+        });
+        mid = int32_t(it - idx.begin());
+      } else {
+        mid = k.first + k.count / 2;   // all centroids coincide: split by index
+      }
+      int32_t c0 = next_node.fetch_add(2);
+      nd.child = c0; nd.count = 0;
+      Task a{c0, k.first, mid - k.first, d + 1}, b{c0 + 1, mid, k.first + k.count - mid, d + 1};
+      if (b.count > 65536) push(b); else local.push_back(b);
+      if (a.count > 65536) push(a); else local.push_back(a);
+    }
+  }
+
+  void worker() {
+    for (;;) {
+      Task t;
+      {
+        std::unique_lock<std::mutex> g(mu);
+        cv.wait(g, [&] { return !queue.empty() || active == 0; });
+        if (queue.empty()) return;
+        t = queue.front(); queue.pop_front(); ++active;
+      }
+      run_task(t);
+      { std::lock_guard<std::mutex> g(mu); --active; }
+      cv.notify_all();
+    }
+  }
+};
+
+}  // namespace
+
+void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out) {
+  auto t0 = std::chrono::steady_clock::now();
+  Builder b;
+  b.pos = tri_pos; b.n = n; b.max_leaf = max_leaf;
+  b.tbox.resize(n); b.cen.resize(3 * n); b.idx.resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    Box bx;
+    for (int k = 0; k < 3; ++k) bx.grow(tri_pos + 9 * i + 3 * k);
+    b.tbox[i] = bx;
+    for (int a = 0; a < 3; ++a) b.cen[3 * i + size_t(a)] = 0.5f * (bx.lo[a] + bx.hi[a]);
+    b.idx[i] = int32_t(i);
+  }
+  b.nodes.resize(std::max<size_t>(2 * n + 1, 3));
+  b.push({0, 0, int32_t(n), 0});
+  unsigned nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (n < 200000) nt = 1;
+  std::vector<std::thread> th;
+  for (unsigned i = 0; i < nt; ++i) th.emplace_back([&] { b.worker(); });
+  for (auto& t : th) t.join();
+
+  // Emit the GPU layout breadth-first (keeps the top levels contiguous).
+  // The root must be an inner node: a single leaf becomes child 0 of a root
+  // whose child 1 is an empty leaf.
+  const std::vector<BNode>& nd = b.nodes;
+  struct Pending { BNode a, b; };
+  BNode empty;
+  std::deque<Pending> q;
+  if (nd[0].child < 0) q.push_back({nd[0], empty});
+  else q.push_back({nd[size_t(nd[0].child)], nd[size_t(nd[0].child) + 1]});
+  std::vector<size_t> fixups;   // float offsets of inner-child links, in push order
+  out.nodes.clear();
+  auto child_fields = [](const BNode& c, float* box6, int32_t& link, int32_t& cnt) {
+    box6[0] = c.box.lo[0]; box6[1] = c.box.hi[0]; box6[2] = c.box.lo[1];
+    box6[3] = c.box.hi[1]; box6[4] = c.box.lo[2]; box6[5] = c.box.hi[2];
+    if (c.child < 0) { link = ~((c.first << 3) | c.count); cnt = c.count; } else { link = 0; cnt = 0; }
+  };
+  while (!q.empty()) {
+    Pending p = q.front(); q.pop_front();
+    size_t base = out.nodes.size();
+    out.nodes.resize(base + 16);
+    float* f = &out.nodes[base];
+    float ba[6], bb[6]; int32_t la, lb, ca, cbn;
+    child_fields(p.a, ba, la, ca); child_fields(p.b, bb, lb, cbn);
+    f[0] = ba[0]; f[1] = ba[1]; f[2] = ba[2]; f[3] = ba[3];
+    f[4] = bb[0]; f[5] = bb[1]; f[6] = bb[2]; f[7] = bb[3];
+    f[8] = ba[4]; f[9] = ba[5]; f[10] = bb[4]; f[11] = bb[5];
+    std::memcpy(&f[12], &la, 4); std::memcpy(&f[13], &lb, 4); std::memcpy(&f[14], &ca, 4); std::memcpy(&f[15], &cbn, 4);
+    if (p.a.child >= 0) { fixups.push_back(base + 12); q.push_back({nd[size_t(p.a.child)], nd[size_t(p.a.child) + 1]}); }
+    if (p.b.child >= 0) { fixups.push_back(base + 13); q.push_back({nd[size_t(p.b.child)], nd[size_t(p.b.child) + 1]}); }
+  }
+  // the k-th node pushed after the root is emitted as gpu node k+1
+  for (size_t k = 0; k < fixups.size(); ++k) { int32_t v = int32_t(k + 1); std::memcpy(&out.nodes[fixups[k]], &v, 4); }
+
+  out.order = b.idx;
+  out.tris.resize(12 * n);
+  for (size_t i = 0; i < n; ++i) {
+    int32_t t = b.idx[i];
+    const float* p = tri_pos + 9 * size_t(t);
+    float* o = &out.tris[12 * i];
+    o[0] = p[0]; o[1] = p[1]; o[2] = p[2]; std::memcpy(&o[3], &t, 4);
+    o[4] = p[0] - p[3]; o[5] = p[1] - p[4]; o[6] = p[2] - p[5]; o[7] = 0.f;
+    o[8] = p[6] - p[0]; o[9] = p[7] - p[1]; o[10] = p[8] - p[2]; o[11] = 0.f;
+  }
+  out.depth = b.max_depth.load() + 1;
+  out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace hasty

@@ -1,0 +1,394 @@
+// Wavefront form of the reference's recursive estimator
+// (estimateRadiance, core/src/PathTracing.cpp:21-95; strategies in
+// core/src/MIS.cpp). Per bounce, `k_shade` finishes the previous vertex's two
+// MIS samples once their rays have been traced (light sample: visibility,
+// light pdf, power-heuristic weight, emitted radiance; BSDF sample: weight and
+// the next vertex), shades the new vertex (Russian roulette, light sample,
+// BSDF sample, medium stack, dispersion band) and queues the rays it needs.
+// Random numbers are drawn in the reference's order, one PCG32 stream per
+// (job seed, pixel, pass).
+#include <cuda_runtime.h>
+#include "device_common.cuh"
+#include "wavefront.h"
+
+namespace hasty {
+namespace {
+using namespace dev;
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ float4 f4(V3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
+__device__ __forceinline__ V3 xyz(float4 v) { return V3(v.x, v.y, v.z); }
+
+// Exclusive offset of this lane's `cnt` items in a per-warp block reserved
+// with one atomic (ballot/shuffle compaction). All 32 lanes must call it.
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t cnt) {
+  uint32_t lane = threadIdx.x & 31u;
+  uint32_t x = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) { uint32_t y = __shfl_up_sync(kFull, x, o); if (lane >= uint32_t(o)) x += y; }
+  uint32_t total = __shfl_sync(kFull, x, 31);
+  uint32_t base = 0;
+  if (lane == 31 && total) base = atomicAdd(counter, total);
+  base = __shfl_sync(kFull, base, 31);
+  return base + x - cnt;
+}
+
+// Medium stack of one path (LightRayInfo, core/src/LightRayInfo.cpp:8-126),
+// bounded to kMaxMedia entries; a push beyond that is dropped and counted.
+struct Media {
+  int n;
+  V3 T[kMaxMedia];
+  float ior[kMaxMedia];
+  int geom[kMaxMedia];
+  __device__ V3 transmittance() const { return n > 0 ? T[0] : V3(1.f, 1.f, 1.f); }
+  __device__ float outside_ior(const Inter& it, V3 wfrom) const {
+    if (dot(wfrom, it.ng) < 0.0f) {
+      int idx = -1;
+      for (int i = 0; i < n; ++i) if (geom[i] == int(it.geom)) { idx = i; break; }
+      if (idx == -1 || n == 1) return 1.0f;
+      return idx == 0 ? ior[1] : ior[0];
+    }
+    return n == 0 ? 1.0f : ior[0];
+  }
+  // returns 1 when a push overflowed
+  __device__ int update(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wfrom, V3 wto, int wl) {
+    float nf = dot(it.ng, wfrom), nt = dot(it.ng, wto);
+    if (nf >= 0.0f && nt < 0.0f) {
+      if (n >= kMaxMedia) return 1;
+      T[n] = mat_albedo(sc, m, it); ior[n] = mat_ior(m, wl); geom[n] = int(it.geom); ++n;
+    } else if (nf < 0.0f && nt >= 0.0f) {
+      for (int i = 0; i < n; ++i) {
+        if (geom[i] == int(it.geom)) {
+          for (int j = i; j < n - 1; ++j) { T[j] = T[j + 1]; ior[j] = ior[j + 1]; geom[j] = geom[j + 1]; }
+          --n;
+          break;
+        }
+      }
+    }
+    return 0;
+  }
+};
+
+__global__ void __launch_bounds__(256) k_raygen(SceneDev sc, PathsDev P, BatchDesc b) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) {
+    uint32_t n = sc.max_depth > 0 ? uint32_t(b.n_paths) : 0u;
+    P.counts[0] = n; P.counts[1] = 0; P.counts[2] = n; P.counts[3] = 0;
+    atomicAdd(&P.stats[ST_PATHS], (unsigned long long)b.n_paths);
+  }
+  if (s >= b.n_paths) return;
+  int npix = sc.width * sc.height;
+  int k = s / npix, px = s - k * npix;
+  uint32_t pass = b.pass_base + uint32_t(k);
+  int x = px % sc.width, y = px / sc.width;
+  Rng r; r.seed(path_key(b.seed, uint32_t(px), pass));
+  float ox = halton(2, pass), oy = halton(3, pass);
+  V3 o, d; int capped = 0;
+  camera_ray(sc.cam, r, float(x) + ox, float(y) + oy, float(sc.width), float(sc.height), o, d, capped);
+  if (capped) atomicAdd(&P.stats[ST_TRIAL_CAP], 1ull);
+  P.rng[s] = r.state;
+  P.thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
+  P.rad[s] = make_float4(0.f, 0.f, 0.f, __uint_as_float(PF_CAMERA | PF_PEND_B));
+  P.out_color[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  P.out_albedo[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (sc.max_depth <= 0) return;
+  P.ray_o[2 * s] = f4(o, 0.f);
+  P.ray_d[2 * s] = f4(d, 0.f);
+  P.pq[0][s] = s;
+  P.rq[0][s] = 2 * s;
+}
+
+__global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDesc b, int q) {
+  const uint32_t n_in = P.counts[q];
+  uint32_t* pq_cnt = &P.counts[q ^ 1];
+  uint32_t* rq_cnt = &P.counts[2 + (q ^ 1)];
+  int32_t* pq_out = P.pq[q ^ 1];
+  int32_t* rq_out = P.rq[q ^ 1];
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((i & ~31u) >= n_in) return;                 // whole warp past the queue
+  const bool valid = i < n_in;
+  const int npix = sc.width * sc.height;
+
+  bool keep = false, emitB = false, emitL = false;
+  int s = valid ? P.pq[q][i] : 0;
+  int shaded = 0, overflow = 0, capped = 0;
+  if (valid) {
+    float4 rad = P.rad[s];
+    uint32_t flags = __float_as_uint(rad.w);
+    V3 L = xyz(rad);
+    bool done = false;
+
+    // ---- resolve the pending light sample (MIS.cpp:32-54 + PathTracing.cpp:62-81)
+    if (flags & PF_PEND_L) {
+      float4 h = P.hit[2 * s + 1];
+      float4 nc = P.nee_c[s], nt = P.nee_t[s];
+      int ltri = __float_as_int(nt.w), htri = __float_as_int(h.w);
+      bool vis = ltri >= 0 ? (htri == ltri) : (htri < 0 || sc.mats[sc.tri_attr[htri].mat].is_light);
+      if (vis) {
+        V3 o = xyz(P.ray_o[2 * s + 1]), d = xyz(P.ray_d[2 * s + 1]);
+        V3 x2, ng2;
+        if (htri >= 0) { x2 = hit_point(sc, htri, h.y, h.z); ng2 = normalize(tri_ng_raw(sc.tri_pos + 9 * int64_t(htri))); }
+        float pdfL = light_density(sc, o, d, htri, x2, ng2);
+        if (pdfL != 0.0f) {
+          float pB = nc.w;
+          float w = (pdfL * pdfL) / ((0.0f + pdfL * pdfL) + pB * pB);
+          V3 Li = htri >= 0 ? cwise(beers(xyz(nt), norm(x2 - o)), emission(sc, sc.tri_attr[htri].mat, ng2, -d))
+                            : cwise(beers(xyz(nt), 1e6f), env_eval(sc, d));
+          L = L + cwise(Li, (xyz(nc) / pdfL) * w);
+        }
+      }
+    }
+
+    // ---- resolve the pending BSDF sample and shade the vertex it reached
+    if (!(flags & PF_PEND_B)) {
+      done = true;
+    } else {
+      float4 h = P.hit[2 * s];
+      int htri = __float_as_int(h.w);
+      V3 o = xyz(P.ray_o[2 * s]), d = xyz(P.ray_d[2 * s]);
+      float4 thr4 = P.thr[s];
+      V3 thr = xyz(thr4);
+      int depth = 0;
+      Inter it;
+      bool have_it = false;
+      if (!(flags & PF_CAMERA)) {
+        float4 pb = P.pend_b[s];
+        if (htri == __float_as_int(pb.w)) {          // isSelfIntersection, PathTracing.h:41-45
+          done = true;
+        } else {
+          float wB = 1.0f;
+          if (sc.two_strategies) {
+            V3 x2, ng2;
+            if (htri >= 0) { it = inter_from_hit(sc, htri, h.y, h.z); have_it = true; x2 = it.x; ng2 = it.ng; }
+            float pdfL = light_density(sc, o, d, htri, x2, ng2);
+            float pB = thr4.w;
+            wB = (pB * pB) / ((0.0f + pdfL * pdfL) + pB * pB);
+          }
+          thr = cwise(thr, xyz(pb) * wB);
+          depth = int(flags & PF_DEPTH_MASK) + 1;
+        }
+      }
+      if (!done && depth >= sc.max_depth) done = true;
+      if (!done) {
+        Media M; M.n = int((flags & PF_NMED_MASK) >> PF_NMED_SHIFT);
+        for (int k = 0; k < M.n; ++k) { float4 m4 = P.med[4 * s + k]; M.T[k] = xyz(m4); M.ior[k] = m4.w; M.geom[k] = P.med_geom[4 * s + k]; }
+        V3 Tp = M.transmittance();
+        if (htri < 0) {                              // miss: PathTracing.cpp:86-94
+          V3 Le = cwise(beers(Tp, 1e6f), env_eval(sc, d));
+          L = L + cwise(thr, Le);
+          if (depth == 0) { P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f); P.out_albedo[s] = f4(Le, 0.f); }
+          done = true;
+        } else {
+          if (!have_it) it = inter_from_hit(sc, htri, h.y, h.z);
+          const MaterialDev m = sc.mats[it.mat];
+          if (depth == 0) { P.out_normal[s] = f4(it.ns, 0.f); P.out_albedo[s] = f4(mat_albedo(sc, m, it), 0.f); }
+          V3 tl = beers(Tp, norm(it.x - o));
+          if (m.is_light) {                          // PathTracing.cpp:38-41
+            L = L + cwise(thr, cwise(tl, emission(sc, it.mat, it.ng, -d)));
+            done = true;
+          } else {
+            shaded = 1;
+            uint64_t key = path_key(b.seed, uint32_t(s % npix), b.pass_base + uint32_t(s / npix));
+            Rng r; r.inc = Rng::inc_of(key); r.state = P.rng[s];
+            float qrr = depth >= sc.rr_start ? sc.rr_q : 0.0f;      // PathTracing.cpp:49-56
+            if (r.u01() < qrr) {
+              done = true;
+            } else {
+              tl = tl / (1.0f - qrr);
+              V3 wo = -d;
+              int wl = int((flags & PF_WL_MASK) >> PF_WL_SHIFT) - 1;
+              float eta_out = M.outside_ior(it, wo);
+              bool next_ok = depth + 1 < sc.max_depth;
+              // light strategy (Scene.cpp:538-586)
+              if (sc.two_strategies) {
+                float xi = r.u01();
+                V3 oL, dL; int ltri = -1;
+                if (xi < sc.p_surface) {
+                  uint32_t kk = sample_cdf(sc.light_cdf, uint32_t(sc.n_light_tris), r);
+                  ltri = sc.light_tris[kk];
+                  V3 bb = triangle_uniform(r);
+                  const float* lp = sc.tri_pos + 9 * int64_t(ltri);
+                  V3 xl = bb.x * ld3(lp) + bb.y * ld3(lp + 3) + bb.z * ld3(lp + 6);
+                  oL = ray_x(it, dot(it.ng, xl - it.x) >= 0.0f);
+                  dL = normalize(xl - oL);
+                } else {
+                  float dens;
+                  dL = env_sample(sc, r, dens, capped);
+                  oL = ray_x(it, dot(it.ng, dL) >= 0.0f);
+                }
+                if (next_ok) {
+                  BsdfEval ev = bsdf_eval(sc, m, it, wo, dL);
+                  V3 c3 = cwise(tl, ev.fD + ev.fC) * fabsf(dot(dL, it.ng));
+                  if (!is_zero(c3)) {
+                    float pBL = bsdf_pdf(sc, m, it, wo, dL, eta_out);
+                    Media ML = M;
+                    overflow |= ML.update(sc, m, it, wo, dL, wl);
+                    P.nee_c[s] = f4(cwise(thr, c3), pBL);
+                    P.nee_t[s] = f4(ML.transmittance(), __int_as_float(ltri));
+                    P.ray_o[2 * s + 1] = f4(oL, 0.f);
+                    P.ray_d[2 * s + 1] = f4(dL, 0.f);
+                    emitL = true;
+                  }
+                }
+              }
+              // BSDF strategy (MIS.cpp:6-26, Scene.cpp:328-338)
+              float prob = 1.0f;
+              if (wl == -1 && m.vary_ior) {              // LightRayInfo.cpp:52-79
+                float p3 = 1.0f / 3.0f;
+                float xi = r.u01();
+                if (xi < p3) wl = 0; else if (xi < p3 + p3) wl = 1; else wl = 2;
+                prob = p3;
+              }
+              BsdfSample bs = bsdf_sample(sc, m, it, wo, wl, eta_out, r, capped);
+              if (bs.pdf != 0.0f) {
+                V3 t2 = cwise(tl, bs.thrD / prob + bs.thrC / prob);
+                if (!is_zero(t2) && next_ok) {
+                  overflow |= M.update(sc, m, it, wo, bs.dir, wl);
+                  P.thr[s] = f4(thr, bs.pdf);
+                  P.pend_b[s] = f4(t2, __int_as_float(it.tri));
+                  P.ray_o[2 * s] = f4(ray_x(it, bs.outside), 0.f);
+                  P.ray_d[2 * s] = f4(bs.dir, 0.f);
+                  for (int k = 0; k < M.n; ++k) { P.med[4 * s + k] = f4(M.T[k], M.ior[k]); P.med_geom[4 * s + k] = M.geom[k]; }
+                  emitB = true;
+                }
+              }
+              P.rng[s] = r.state;
+              uint32_t nf = uint32_t(depth) | (uint32_t(wl + 1) << PF_WL_SHIFT) | (uint32_t(M.n) << PF_NMED_SHIFT) |
+                            (emitB ? PF_PEND_B : 0u) | (emitL ? PF_PEND_L : 0u);
+              flags = nf;
+              done = !(emitB || emitL);
+            }
+          }
+        }
+      }
+    }
+    keep = !done;
+    if (keep) P.rad[s] = f4(L, __uint_as_float(flags));
+    else P.out_color[s] = f4(L, 0.f);
+  }
+
+  // warp-ballot compaction of the surviving paths and their rays
+  uint32_t nrays = (emitB ? 1u : 0u) + (emitL ? 1u : 0u);
+  uint32_t roff = warp_reserve(rq_cnt, nrays);
+  if (emitB) rq_out[roff++] = 2 * s;
+  if (emitL) rq_out[roff] = 2 * s + 1;
+  unsigned kb = __ballot_sync(kFull, keep);
+  uint32_t lane = threadIdx.x & 31u;
+  uint32_t pbase = 0;
+  if (lane == 0 && kb) pbase = atomicAdd(pq_cnt, uint32_t(__popc(kb)));
+  pbase = __shfl_sync(kFull, pbase, 0);
+  if (keep) pq_out[pbase + __popc(kb & ((1u << lane) - 1u))] = s;
+  unsigned sb = __ballot_sync(kFull, shaded != 0);
+  unsigned ob = __ballot_sync(kFull, overflow != 0);
+  unsigned cb = __ballot_sync(kFull, capped != 0);
+  if (lane == 0) {
+    if (sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
+    if (ob) atomicAdd(&P.stats[ST_MEDIA_OVERFLOW], (unsigned long long)__popc(ob));
+    if (cb) atomicAdd(&P.stats[ST_TRIAL_CAP], (unsigned long long)__popc(cb));
+  }
+}
+
+// Adds one batch of per-sample values into the FP64 accumulators, passes in
+// order; a sample whose radiance has a NaN is dropped with its AOVs
+// (core/src/PathTracing.cpp:132-142).
+__global__ void k_accumulate(PathsDev P, BatchDesc b, int npix, double* acc_c, double* acc_n, double* acc_a) {
+  int px = blockIdx.x * blockDim.x + threadIdx.x;
+  if (px >= npix) return;
+  double c[3] = {0, 0, 0}, n[3] = {0, 0, 0}, a[3] = {0, 0, 0};
+  unsigned nan = 0;
+  for (int k = 0; k < b.n_passes; ++k) {
+    int s = k * npix + px;
+    float4 cc = P.out_color[s];
+    if (cc.x != cc.x || cc.y != cc.y || cc.z != cc.z) { ++nan; continue; }
+    float4 nn = P.out_normal[s], aa = P.out_albedo[s];
+    c[0] += cc.x; c[1] += cc.y; c[2] += cc.z;
+    n[0] += nn.x; n[1] += nn.y; n[2] += nn.z;
+    a[0] += aa.x; a[1] += aa.y; a[2] += aa.z;
+  }
+  for (int q = 0; q < 3; ++q) { acc_c[3 * px + q] += c[q]; acc_n[3 * px + q] += n[q]; acc_a[3 * px + q] += a[q]; }
+  if (nan) atomicAdd(&P.stats[ST_NAN], (unsigned long long)nan);
+}
+
+// computeEstimate (apps/ViewerUtils.cpp:95-121): sum / (1e-7 + N), then the
+// exposure scale 2^exposure for the colour AOV (PathTracingViewer.cpp:160).
+__global__ void k_estimate(const double* acc, int n, float den, float scale, float* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = (float(acc[i]) / den) * scale;
+}
+
+}  // namespace
+
+void launch_raygen(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, cudaStream_t st) {
+  int blocks = (b.n_paths + 255) / 256;
+  k_raygen<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(sc, p, b);
+}
+
+void launch_shade(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, int q, int max_paths, cudaStream_t st) {
+  int blocks = (max_paths + 127) / 128;
+  k_shade<<<blocks > 0 ? blocks : 1, 128, 0, st>>>(sc, p, b, q);
+}
+
+void launch_accumulate(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, double* ac, double* an, double* aa, cudaStream_t st) {
+  int npix = sc.width * sc.height;
+  k_accumulate<<<(npix + 255) / 256, 256, 0, st>>>(p, b, npix, ac, an, aa);
+}
+
+void launch_estimate(const double* acc, int n, float den, float scale, float* out, cudaStream_t st) {
+  k_estimate<<<(n + 255) / 256, 256, 0, st>>>(acc, n, den, scale, out);
+}
+
+}  // namespace hasty
+
+// ----------------------------------------------------------------------------
+// Known-answer evaluation of the device BSDF (parity tests): case c reads 33
+// floats (x, Ng, Ns, tangent, bitangent, albedo, metallic, specular, roughness,
+// anisotropy, transmission, IOR, vary-IOR flag, wo, wi, wavelength, outside
+// IOR) and draws from replay[c*n_replay ...].
+namespace hasty {
+namespace {
+using namespace dev;
+__global__ void k_debug_bsdf(int which, const float* in, int n, const uint32_t* replay, int n_replay, float* out) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const float* p = in + 33 * int64_t(c);
+  float* o = out + 12 * int64_t(c);
+  SceneDev sc{};
+  Inter it;
+  it.x = ld3(p); it.ng = ld3(p + 3); it.ns = ld3(p + 6); it.tan = ld3(p + 9); it.bit = ld3(p + 12);
+  it.h = 0.f; it.u = it.v = 0.f; it.tri = 0; it.mat = 0; it.geom = 0; it.has_uv = false;
+  MaterialDev m{};
+  m.albedo[0] = p[15]; m.albedo[1] = p[16]; m.albedo[2] = p[17];
+  m.albedo_tex = m.roughness_tex = m.metallic_tex = m.normal_tex = -1;
+  m.metallic = p[18]; m.specular = p[19]; m.roughness = p[20]; m.anisotropy = p[21];
+  m.transmission = p[22]; m.ior = p[23]; m.vary_ior = p[24] != 0.0f;
+  V3 wo = ld3(p + 25), wi = ld3(p + 28);
+  int wl = int(p[31]);
+  float eta = p[32];
+  for (int k = 0; k < 12; ++k) o[k] = 0.f;
+  if (which == 0) {
+    ReplayRng r{replay + int64_t(c) * n_replay, uint32_t(n_replay), 0u};
+    int capped = 0;
+    BsdfSample s = bsdf_sample(sc, m, it, wo, wl, eta, r, capped);
+    o[0] = s.outside ? 1.f : 0.f;
+    o[1] = s.dir.x; o[2] = s.dir.y; o[3] = s.dir.z;
+    o[4] = s.thrD.x; o[5] = s.thrD.y; o[6] = s.thrD.z;
+    o[7] = s.thrC.x; o[8] = s.thrC.y; o[9] = s.thrC.z;
+    o[10] = s.pdf; o[11] = float(r.pos);
+  } else if (which == 1) {
+    BsdfEval e = bsdf_eval(sc, m, it, wo, wi);
+    V3 ns = shading_normal(sc, m, it, wo, dot(it.ng, wo));
+    o[0] = e.fD.x; o[1] = e.fD.y; o[2] = e.fD.z; o[3] = e.fC.x; o[4] = e.fC.y; o[5] = e.fC.z;
+    o[6] = ns.x; o[7] = ns.y; o[8] = ns.z;
+  } else {
+    o[0] = bsdf_pdf(sc, m, it, wo, wi, eta);
+  }
+}
+}  // namespace
+
+void launch_debug_bsdf(int which, const float* in, int n, const uint32_t* replay, int n_replay, float* out, cudaStream_t st) {
+  k_debug_bsdf<<<(n + 127) / 128, 128, 0, st>>>(which, in, n, replay, n_replay, out);
+}
+}  // namespace hasty

@@ -1,0 +1,501 @@
+// Host-side job loader: JSON, OBJ/MTL and image readers plus the scene
+// assembly of core/src/Scene.cpp:12-194. See scene_load.h.
+#include "scene_load.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <unordered_map>
+
+namespace hasty {
+namespace {
+
+// ------------------------------------------------------------------ JSON --
+struct JNode {
+  enum T { NUL, BOOL, NUM, STR, ARR, OBJ } t = NUL;
+  double num = 0; bool b = false; std::string s;
+  std::vector<JNode> items;
+  std::vector<std::string> keys;
+  const JNode* get(const char* k) const {
+    if (t != OBJ) return nullptr;
+    for (size_t i = 0; i < keys.size(); ++i) if (keys[i] == k) return &items[i];
+    return nullptr;
+  }
+  const JNode& req(const char* k) const {
+    const JNode* n = get(k);
+    if (!n) throw LoadError(std::string("json: key '") + k + "' not found");
+    return *n;
+  }
+  double number() const {
+    if (t == NUM) return num;
+    if (t == BOOL) return b ? 1.0 : 0.0;
+    throw LoadError("json: expected a number");
+  }
+  bool boolean() const { return t == BOOL ? b : number() != 0.0; }
+  const std::string& str() const { if (t != STR) throw LoadError("json: expected a string"); return s; }
+};
+
+class JReader {
+ public:
+  explicit JReader(const std::string& txt) : p_(txt.c_str()), end_(txt.c_str() + txt.size()) {}
+  JNode parse() { JNode n = val(); skip(); if (p_ != end_) bad("trailing characters"); return n; }
+ private:
+  const char* p_; const char* end_;
+  [[noreturn]] void bad(const char* m) { throw LoadError(std::string("json syntax error: ") + m); }
+  void skip() { while (p_ < end_ && std::strchr(" \t\r\n", *p_)) ++p_; }
+  bool lit(const char* w) { size_t n = std::strlen(w); if (size_t(end_ - p_) >= n && !std::strncmp(p_, w, n)) { p_ += n; return true; } return false; }
+  std::string str() {
+    std::string o; ++p_;
+    while (p_ < end_ && *p_ != '"') {
+      char c = *p_++;
+      if (c == '\\' && p_ < end_) {
+        char e = *p_++;
+        switch (e) { case 'n': o += '\n'; break; case 't': o += '\t'; break; case 'r': o += '\r'; break;
+          case 'b': o += '\b'; break; case 'f': o += '\f'; break; case 'u': o += '?'; p_ += std::min<ptrdiff_t>(4, end_ - p_); break;
+          default: o += e; }
+      } else o += c;
+    }
+    if (p_ >= end_) bad("unterminated string");
+    ++p_;
+    return o;
+  }
+  JNode val() {
+    skip();
+    if (p_ >= end_) bad("unexpected end of input");
+    JNode n;
+    if (*p_ == '{') {
+      n.t = JNode::OBJ; ++p_; skip();
+      if (p_ < end_ && *p_ == '}') { ++p_; return n; }
+      while (true) {
+        skip(); if (p_ >= end_ || *p_ != '"') bad("object key expected");
+        n.keys.push_back(str()); skip();
+        if (p_ >= end_ || *p_ != ':') bad("':' expected");
+        ++p_;
+        n.items.push_back(val()); skip();
+        if (p_ < end_ && *p_ == ',') { ++p_; continue; }
+        if (p_ < end_ && *p_ == '}') { ++p_; break; }
+        bad("',' or '}' expected");
+      }
+    } else if (*p_ == '[') {
+      n.t = JNode::ARR; ++p_; skip();
+      if (p_ < end_ && *p_ == ']') { ++p_; return n; }
+      while (true) {
+        n.items.push_back(val()); skip();
+        if (p_ < end_ && *p_ == ',') { ++p_; continue; }
+        if (p_ < end_ && *p_ == ']') { ++p_; break; }
+        bad("',' or ']' expected");
+      }
+    } else if (*p_ == '"') { n.t = JNode::STR; n.s = str(); }
+    else if (lit("true")) { n.t = JNode::BOOL; n.b = true; }
+    else if (lit("false")) { n.t = JNode::BOOL; n.b = false; }
+    else if (lit("null")) { n.t = JNode::NUL; }
+    else {
+      char buf[80]; size_t k = 0;
+      while (p_ < end_ && k < 79 && std::strchr("+-0123456789.eE", *p_)) buf[k++] = *p_++;
+      buf[k] = 0;
+      char* e = nullptr; n.num = std::strtod(buf, &e);
+      if (k == 0 || e != buf + k) bad("invalid number");
+      n.t = JNode::NUM;
+    }
+    return n;
+  }
+};
+
+std::string slurp(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw LoadError("could not open " + path + " for reading");
+  std::ostringstream ss; ss << f.rdbuf();
+  return ss.str();
+}
+JNode read_json(const std::string& path) { return JReader(slurp(path)).parse(); }
+
+std::string folder_of(const std::string& p) { size_t k = p.rfind('/'); return k == std::string::npos ? "." : p.substr(0, k); }
+std::string resolve(const std::string& dir, const std::string& f) { return (!f.empty() && f[0] == '/') ? f : dir + "/" + f; }
+
+void vec3_of(const JNode& n, float* out) {
+  if (n.t != JNode::ARR || n.items.size() < 3) throw LoadError("json: expected a 3-vector");
+  for (int i = 0; i < 3; ++i) out[i] = float(n.items[size_t(i)].number());
+}
+
+// ---------------------------------------------------------------- images --
+struct Img { int w = 0, h = 0, ch = 0; std::vector<float> px; };
+
+// PFM (scanlines bottom-up in the file, returned top-down) and binary PNM.
+Img read_image(const std::string& path) {
+  std::string data = slurp(path);
+  const char* p = data.c_str(); const char* e = p + data.size();
+  auto token = [&]() {
+    while (p < e) {
+      if (*p == '#') { while (p < e && *p != '\n') ++p; continue; }
+      if (std::isspace(static_cast<unsigned char>(*p))) { ++p; continue; }
+      break;
+    }
+    const char* b = p;
+    while (p < e && !std::isspace(static_cast<unsigned char>(*p))) ++p;
+    return std::string(b, p);
+  };
+  std::string magic = token();
+  Img im;
+  if (magic == "PF" || magic == "Pf") {
+    im.w = std::atoi(token().c_str()); im.h = std::atoi(token().c_str());
+    double scale = std::atof(token().c_str());
+    ++p;
+    im.ch = magic == "PF" ? 3 : 1;
+    size_t n = size_t(im.w) * im.h * im.ch;
+    if (im.w <= 0 || im.h <= 0 || size_t(e - p) < n * 4) throw LoadError("truncated PFM " + path);
+    im.px.resize(n);
+    size_t row = size_t(im.w) * im.ch;
+    for (int y = 0; y < im.h; ++y) {
+      const char* src = p + 4 * row * size_t(im.h - 1 - y);
+      for (size_t i = 0; i < row; ++i) {
+        uint32_t u; std::memcpy(&u, src + 4 * i, 4);
+        if (scale > 0) u = (u >> 24) | ((u >> 8) & 0xFF00u) | ((u << 8) & 0xFF0000u) | (u << 24);
+        float f; std::memcpy(&f, &u, 4);
+        im.px[size_t(y) * row + i] = f;
+      }
+    }
+    return im;
+  }
+  if (magic == "P6" || magic == "P5") {
+    im.w = std::atoi(token().c_str()); im.h = std::atoi(token().c_str());
+    int maxv = std::atoi(token().c_str());
+    ++p;
+    im.ch = magic == "P6" ? 3 : 1;
+    size_t n = size_t(im.w) * im.h * im.ch;
+    size_t bps = maxv < 256 ? 1 : 2;
+    if (im.w <= 0 || im.h <= 0 || maxv <= 0 || size_t(e - p) < n * bps) throw LoadError("truncated PNM " + path);
+    im.px.resize(n);
+    const unsigned char* q = reinterpret_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) {
+      unsigned v = bps == 1 ? q[i] : (unsigned(q[2 * i]) << 8 | q[2 * i + 1]);
+      im.px[i] = float(v) / float(maxv);
+    }
+    return im;
+  }
+  throw LoadError("unsupported image format: " + path + " (PFM, PPM, PGM are accepted)");
+}
+
+// ----------------------------------------------------------------- OBJ ----
+struct MtlRec {
+  std::string name;
+  float Ka[3] = {0, 0, 0}, Kd[3] = {0, 0, 0}, Ks[3] = {0, 0, 0}, Ke[3] = {0, 0, 0};
+  float Ns = 1.f, Ni = 1.f, d = 1.f, aniso = 0.f;
+  std::string map_Kd, map_Ns, map_Pm, map_bump;
+};
+struct Corner { int v, vt, vn; };
+struct ObjShapeRec { std::vector<Corner> corners; std::vector<int> mat; std::vector<uint32_t> sg; };
+struct ObjFile {
+  std::vector<float> v, vn, vt;
+  std::vector<ObjShapeRec> shapes;
+  std::vector<MtlRec> mtls;
+};
+
+const char* ws(const char* s) { while (*s == ' ' || *s == '\t') ++s; return s; }
+std::string word(const char*& s) {
+  s = ws(s); const char* b = s;
+  while (*s && *s != ' ' && *s != '\t' && *s != '\r' && *s != '\n') ++s;
+  return std::string(b, s);
+}
+float num(const char*& s) {
+  s = ws(s); char* e = nullptr; float f = std::strtof(s, &e);
+  if (e == s) return 0.0f;
+  s = e; return f;
+}
+void num3(const char*& s, float* o) { for (int i = 0; i < 3; ++i) o[i] = num(s); }
+std::string last_word(const char* s) { std::string l; for (std::string t = word(s); !t.empty(); t = word(s)) l = t; return l; }
+
+void read_mtl(const std::string& path, std::vector<MtlRec>& out, std::map<std::string, int>& index) {
+  std::ifstream f(path);
+  if (!f) return;   // tinyobj warns and continues without the library
+  std::string line;
+  MtlRec cur; bool open = false;
+  auto close = [&]() { if (open) { index[cur.name] = int(out.size()); out.push_back(cur); } };
+  while (std::getline(f, line)) {
+    const char* s = ws(line.c_str());
+    if (!*s || *s == '#') continue;
+    std::string k = word(s);
+    if (k == "newmtl") { close(); cur = MtlRec(); cur.name = word(s); open = true; }
+    else if (k == "Ka") num3(s, cur.Ka);
+    else if (k == "Kd") num3(s, cur.Kd);
+    else if (k == "Ks") num3(s, cur.Ks);
+    else if (k == "Ke") num3(s, cur.Ke);
+    else if (k == "Ns") cur.Ns = num(s);
+    else if (k == "Ni") cur.Ni = num(s);
+    else if (k == "d") cur.d = num(s);
+    else if (k == "Tr") cur.d = 1.0f - num(s);
+    else if (k == "aniso") cur.aniso = num(s);
+    else if (k == "map_Kd") cur.map_Kd = last_word(s);
+    else if (k == "map_Ns") cur.map_Ns = last_word(s);
+    else if (k == "map_Pm") cur.map_Pm = last_word(s);
+    else if (k == "map_bump" || k == "map_Bump" || k == "bump") cur.map_bump = last_word(s);
+  }
+  close();
+}
+
+int rel_index(long idx, size_t count) {
+  if (idx > 0) return int(idx - 1);
+  if (idx < 0) return int(long(count) + idx);
+  return -1;
+}
+
+ObjFile read_obj(const std::string& path, const std::string& mtl_dir) {
+  std::ifstream f(path);
+  if (!f) throw LoadError("TinyObjReader error Cannot open file [" + path + "]");
+  ObjFile o;
+  std::map<std::string, int> mindex;
+  ObjShapeRec cur;
+  int mat = -1; uint32_t sg = 0;
+  auto flush = [&]() { if (!cur.corners.empty()) o.shapes.push_back(std::move(cur)); cur = ObjShapeRec(); };
+  std::string line;
+  std::vector<Corner> poly;
+  while (std::getline(f, line)) {
+    const char* s = ws(line.c_str());
+    if (!*s || *s == '#') continue;
+    if (s[0] == 'v' && (s[1] == ' ' || s[1] == '\t')) { s += 1; for (int i = 0; i < 3; ++i) o.v.push_back(num(s)); continue; }
+    if (s[0] == 'v' && s[1] == 'n' && (s[2] == ' ' || s[2] == '\t')) { s += 2; for (int i = 0; i < 3; ++i) o.vn.push_back(num(s)); continue; }
+    if (s[0] == 'v' && s[1] == 't' && (s[2] == ' ' || s[2] == '\t')) { s += 2; o.vt.push_back(num(s)); o.vt.push_back(num(s)); continue; }
+    if (s[0] == 'f' && (s[1] == ' ' || s[1] == '\t')) {
+      s += 1; poly.clear();
+      for (std::string t = word(s); !t.empty(); t = word(s)) {
+        Corner c{-1, -1, -1};
+        const char* q = t.c_str();
+        char* e = nullptr;
+        long a = std::strtol(q, &e, 10);
+        c.v = rel_index(a, o.v.size() / 3);
+        if (*e == '/') {
+          q = e + 1;
+          if (*q != '/') { long b = std::strtol(q, &e, 10); if (e != q) c.vt = rel_index(b, o.vt.size() / 2); q = e; }
+          if (*q == '/') { ++q; long cc = std::strtol(q, &e, 10); if (e != q) c.vn = rel_index(cc, o.vn.size() / 3); }
+        }
+        poly.push_back(c);
+      }
+      if (poly.size() < 3) continue;
+      auto tri = [&](size_t a, size_t b, size_t c) {
+        cur.corners.push_back(poly[a]); cur.corners.push_back(poly[b]); cur.corners.push_back(poly[c]);
+        cur.mat.push_back(mat); cur.sg.push_back(sg);
+      };
+      if (poly.size() == 3) tri(0, 1, 2);
+      else if (poly.size() == 4) {
+        // tinyobjloader splits a quad along its shorter diagonal
+        auto P = [&](size_t k, int a) { return o.v[3 * size_t(poly[k].v) + size_t(a)]; };
+        float d02 = 0, d13 = 0;
+        for (int a = 0; a < 3; ++a) { float x = P(2, a) - P(0, a), y = P(3, a) - P(1, a); d02 += x * x; d13 += y * y; }
+        if (d02 < d13) { tri(0, 1, 2); tri(0, 2, 3); } else { tri(0, 1, 3); tri(1, 2, 3); }
+      } else {
+        for (size_t k = 1; k + 1 < poly.size(); ++k) tri(0, k, k + 1);
+      }
+      continue;
+    }
+    std::string k = word(s);
+    if (k == "o" || k == "g") flush();
+    else if (k == "usemtl") { auto it = mindex.find(word(s)); mat = it == mindex.end() ? -1 : it->second; }
+    else if (k == "mtllib") read_mtl(resolve(mtl_dir, word(s)), o.mtls, mindex);
+    else if (k == "s") { std::string v = word(s); sg = v == "off" ? 0u : uint32_t(std::strtoul(v.c_str(), nullptr, 10)); }
+  }
+  flush();
+  return o;
+}
+
+int add_texture(HostScene& sc, const std::string& path, int want, bool srgb) {
+  Img im = read_image(path);
+  TextureDev t{};
+  t.w = im.w; t.h = im.h;
+  t.offset = int64_t(sc.tex_pool.size());
+  if (want == 1) {
+    if (im.ch != 1) throw LoadError("could not read " + path + ", wrong number of channels, expected 1, found " + std::to_string(im.ch));
+    t.ch = 1;
+    sc.tex_pool.insert(sc.tex_pool.end(), im.px.begin(), im.px.end());
+  } else {
+    if (im.ch != 3 && im.ch != 4) throw LoadError("could not read " + path + ", wrong number of channels, expected 3 or 4, found " + std::to_string(im.ch));
+    t.ch = 3;
+    size_t n = size_t(im.w) * im.h;
+    for (size_t i = 0; i < n; ++i)
+      for (int c = 0; c < 3; ++c) sc.tex_pool.push_back(im.px[i * size_t(im.ch) + size_t(c)]);
+  }
+  if (srgb) {  // clampAndPowInplace(image, 0, FLT_MAX, 2.2), core/src/Texture.cpp:43
+    for (size_t i = size_t(t.offset); i < sc.tex_pool.size(); ++i)
+      sc.tex_pool[i] = std::pow(std::max(0.0f, std::min(FLT_MAX, sc.tex_pool[i])), 2.2f);
+  }
+  sc.textures.push_back(t);
+  return int(sc.textures.size() - 1);
+}
+
+void setup_camera(const JNode& cj, CameraDev& c) {      // Camera.cpp:9-38
+  float pos[3], look[3];
+  vec3_of(cj.req("position"), pos);
+  if (const JNode* la = cj.get("look_at")) vec3_of(*la, look);
+  else { look[0] = pos[0]; look[1] = pos[1]; look[2] = pos[2] + -1.0f; }
+  float f[3] = {look[0] - pos[0], look[1] - pos[1], look[2] - pos[2]};
+  float fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+  for (float& x : f) x = x / fl;
+  float up[3] = {0.f, 1.f, 0.f};
+  float d = up[0] * f[0] + up[1] * f[1] + up[2] * f[2];
+  for (int i = 0; i < 3; ++i) up[i] = up[i] - d * f[i];
+  float ul = std::sqrt(up[0] * up[0] + up[1] * up[1] + up[2] * up[2]);
+  for (float& x : up) x = x / ul;
+  float r[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
+  for (int i = 0; i < 3; ++i) { c.pos[i] = pos[i]; c.fwd[i] = f[i]; c.up[i] = up[i]; c.right[i] = r[i]; }
+  c.aperture = cj.get("aperture") ? float(cj.get("aperture")->number()) : 0.0f;
+  c.focal = cj.get("focal_distance") ? float(cj.get("focal_distance")->number()) : 1.0f;
+  c.exposure = cj.get("exposure") ? float(cj.get("exposure")->number()) : 0.0f;
+  c.blades = cj.get("num_blades") ? int(cj.get("num_blades")->number()) : 8;
+  c.blade_rot = cj.get("blade_rotation") ? float(cj.get("blade_rotation")->number()) : 0.0f;
+  if (c.aperture > 0.0f && c.blades < 3) throw LoadError("camera: num_blades must be at least 3");
+  const double kPi = 3.1415926535897932384;
+  float fov = float(kPi) * 45.0f / 180.0f;                // fixed 45 degrees, Camera.h:41
+  c.q = std::tan(fov * 0.5f);
+  c.ngon_per = float(2.0 * kPi / c.blades);
+  c.ngon_nx = std::cos(c.ngon_per * 0.5f);
+  c.ngon_ny = std::sin(c.ngon_per * 0.5f);
+}
+
+}  // namespace
+
+std::vector<double> build_discrete_cdf(const float* w, size_t n) {
+  std::vector<double> cdf;
+  if (n < 2) return cdf;
+  double total = 0.0;
+  for (size_t i = 0; i < n; ++i) total += double(w[i]);
+  cdf.resize(n);
+  double run = 0.0;
+  for (size_t i = 0; i < n; ++i) { double p = double(w[i]) / total; run = i == 0 ? p : run + p; cdf[i] = run; }
+  cdf[n - 1] = 1.0;
+  return cdf;
+}
+
+float halton_value(uint32_t base, uint32_t k) {
+  uint32_t i = k + 1, n = 0, d = 1;
+  while (i) { n = n * base + i % base; i /= base; d *= base; }
+  return float(n) / float(d);
+}
+
+void load_render_job(const std::string& job_path, HostScene& sc) {
+  JNode job = read_json(job_path);
+  RenderSettingsH& st = sc.settings;
+  if (const JNode* s = job.get("settings")) {                 // RenderJob.cpp:10-20
+    if (const JNode* v = s->get("roulette_start_depth")) st.roulette_start = int(v->number());
+    if (const JNode* v = s->get("roulette_q")) st.roulette_q = float(v->number());
+    if (const JNode* v = s->get("width")) st.width = uint32_t(v->number());
+    if (const JNode* v = s->get("height")) st.height = uint32_t(v->number());
+    if (const JNode* v = s->get("num_threads")) st.num_threads = uint32_t(v->number());
+    if (const JNode* v = s->get("max_depth")) st.max_depth = int(v->number());
+    if (const JNode* v = s->get("num_samples")) st.num_samples = int(v->number());
+    if (const JNode* v = s->get("use_mis")) st.use_mis = v->boolean();
+  }
+  if (const JNode* g = job.get("gb300")) if (const JNode* v = g->get("seed")) st.seed = uint64_t(v->number());
+  if (st.width == 0 || st.height == 0) throw LoadError("settings: width and height must be positive");
+  std::string scene_path = resolve(folder_of(job_path), job.req("scene").str());
+  std::string folder = folder_of(scene_path);
+  JNode scene = read_json(scene_path);
+  setup_camera(scene.req("camera"), sc.cam);
+
+  const JNode& world = scene.req("world");
+  if (const JNode* bg = world.get("background_color")) {
+    sc.env_texture = false; vec3_of(*bg, sc.bg);
+  } else {
+    Img im = read_image(resolve(folder, world.req("environment_texture").str()));
+    if (im.ch != 3 && im.ch != 4) throw LoadError("environment texture: expected 3 or 4 channels");
+    sc.env_texture = true; sc.env_w = im.w; sc.env_h = im.h;
+    size_t n = size_t(im.w) * im.h;
+    sc.env_texels.resize(3 * n);
+    for (size_t i = 0; i < n; ++i) for (int c = 0; c < 3; ++c) sc.env_texels[3 * i + size_t(c)] = im.px[i * size_t(im.ch) + size_t(c)];
+    // pixel weights |rgb| sin(theta_center), Environment.h:107-112
+    sc.env_weights.resize(n);
+    const double kPi = 3.1415926535897932384;
+    float hf = float(im.h);
+    for (int y = 0; y < im.h; ++y) {
+      float theta = ((float(y) + 0.5f) / hf) * float(kPi);
+      float s = std::sin(theta);
+      for (int x = 0; x < im.w; ++x) {
+        const float* px = &sc.env_texels[3 * (size_t(y) * size_t(im.w) + size_t(x))];
+        float nn = std::sqrt(px[0] * px[0] + px[1] * px[1] + px[2] * px[2]);
+        sc.env_weights[size_t(y) * size_t(im.w) + size_t(x)] = nn * s;
+      }
+    }
+    sc.env_cdf = build_discrete_cdf(sc.env_weights.data(), n);
+    float vs = 0.f;
+    for (float v : sc.env_weights) vs += v;
+    sc.env_value_sum = vs;
+    if (!(vs > 0.f)) throw LoadError("environment texture is black; it cannot be importance sampled");
+  }
+  if (const JNode* v = world.get("vary_glass_ior")) sc.vary_glass_ior = v->boolean();
+
+  ObjFile obj = read_obj(resolve(folder, scene.req("mesh").str()), folder);
+  sc.vertices = std::move(obj.v); sc.normals = std::move(obj.vn); sc.texcoords = std::move(obj.vt);
+
+  for (const MtlRec& m : obj.mtls) {                       // Scene.cpp:66-118
+    MaterialDev d{};
+    d.transmission = 1.0f - m.d;
+    d.vary_ior = (sc.vary_glass_ior && d.transmission > 0.0f) ? 1 : 0;
+    d.normal_tex = m.map_bump.empty() ? -1 : add_texture(sc, resolve(folder, m.map_bump), 3, false);
+    d.albedo_tex = m.map_Kd.empty() ? -1 : add_texture(sc, resolve(folder, m.map_Kd), 3, true);
+    for (int c = 0; c < 3; ++c) { d.albedo[c] = m.Kd[c]; d.emission[c] = m.Ke[c]; }
+    d.roughness_tex = m.map_Ns.empty() ? -1 : add_texture(sc, resolve(folder, m.map_Ns), 1, false);
+    d.roughness = 1.0f - std::sqrt(m.Ns / 1000.0f);
+    d.metallic_tex = m.map_Pm.empty() ? -1 : add_texture(sc, resolve(folder, m.map_Pm), 1, false);
+    d.metallic = m.Ka[0];
+    d.specular = m.Ks[0];
+    d.ior = m.Ni;
+    d.anisotropy = m.aniso;
+    d.is_light = (m.Ke[0] > 0.0f || m.Ke[1] > 0.0f || m.Ke[2] > 0.0f) ? 1 : 0;
+    // A transmissive surface with a rough lobe makes the reference throw
+    // "not implemented" at the first shade (BRDF.cpp:386-389); refuse it here.
+    if (d.transmission > 0.0f) {
+      float a = d.roughness * d.roughness;
+      if (d.roughness_tex >= 0 || a != 0.0f)
+        throw LoadError("material '" + m.name + "': transmission > 0 needs roughness 0 (Ns 1000); rough dielectrics are not implemented");
+    }
+    sc.mats.push_back(d);
+  }
+
+  std::vector<float> areas;
+  for (size_t s = 0; s < obj.shapes.size(); ++s) {         // Scene.cpp:122-189
+    const ObjShapeRec& sh = obj.shapes[s];
+    size_t nf = sh.mat.size();
+    for (size_t f = 0; f < nf; ++f) {
+      TriAttr a{};
+      for (int k = 0; k < 3; ++k) {
+        const Corner& c = sh.corners[3 * f + size_t(k)];
+        if (c.v < 0 || size_t(c.v) * 3 + 2 >= sc.vertices.size()) throw LoadError("OBJ: vertex index out of range");
+        if (c.vn >= 0 && size_t(c.vn) * 3 + 2 >= sc.normals.size()) throw LoadError("OBJ: normal index out of range");
+        a.vi[k] = c.v; a.ni[k] = c.vn; a.ti[k] = c.vt;
+      }
+      a.mat = sh.mat[f];
+      if (a.mat < 0) throw LoadError(" error face has no material ");
+      a.geom = uint32_t(s); a.prim = uint32_t(f); a.smooth = sh.sg[f] != 0 ? 1u : 0u;
+      for (int k = 0; k < 3; ++k)
+        for (int c = 0; c < 3; ++c) sc.tri_pos.push_back(sc.vertices[3 * size_t(a.vi[k]) + size_t(c)]);
+      const MtlRec& m = obj.mtls[size_t(a.mat)];
+      if (m.Ke[0] > 0.0f || m.Ke[1] > 0.0f || m.Ke[2] > 0.0f) {
+        if (m.Kd[0] > 0.0f || m.Kd[1] > 0.0f || m.Kd[2] > 0.0f || m.Ks[0] > 0.0f || m.Ks[1] > 0.0f || m.Ks[2] > 0.0f)
+          throw LoadError(" don't support non black diffuse materials with emission ");
+        sc.light_tris.push_back(int32_t(sc.tri_attr.size()));
+        const float* q = &sc.tri_pos[sc.tri_pos.size() - 9];
+        float e1[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]}, e2[3] = {q[6] - q[0], q[7] - q[1], q[8] - q[2]};
+        float cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
+        areas.push_back(0.5f * std::sqrt(cx * cx + cy * cy + cz * cz));
+      }
+      sc.tri_attr.push_back(a);
+    }
+  }
+  sc.n_shapes = uint32_t(obj.shapes.size());
+  if (sc.tri_attr.empty()) throw LoadError("scene has no triangles");
+  if (sc.tri_attr.size() >= (size_t(1) << 31) - 2) throw LoadError("scene has too many triangles");
+  sc.light_cdf = build_discrete_cdf(areas.data(), areas.size());
+  float ta = 0.f;
+  for (float a : areas) ta += a;
+  sc.total_light_area = ta;
+  // Constant non-black background, MIS on, no emissive triangle: the
+  // reference exits at its first light sample (Scene.cpp:506-511).
+  if (st.use_mis && sc.light_tris.empty() && !sc.env_texture && sc.has_light())
+    throw LoadError("error: no light triangle found (constant background with MIS needs an emissive triangle)");
+}
+
+}  // namespace hasty

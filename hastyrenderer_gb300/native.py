@@ -1,0 +1,96 @@
+"""ctypes binding of the C ABI declared in include/hasty_gpu.h.
+
+The library is built in-tree (``python -m hastyrenderer_gb300.build``) at
+``hastyrenderer_gb300/lib/libhasty_gb300.so``. Loading fails loudly when it is
+missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libhasty_gb300.so")
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "hasty_gpu.h")
+
+HASTY_OK = 0
+ERRORS = {-1: "HASTY_ERR_ARG", -2: "HASTY_ERR_LOAD", -3: "HASTY_ERR_CUDA", -4: "HASTY_ERR_MEMORY",
+          -5: "HASTY_ERR_IO", -6: "HASTY_ERR_STOPPED", -7: "HASTY_ERR_MISSING"}
+AOV_COLOR, AOV_NORMAL, AOV_ALBEDO = 0, 1, 2
+
+
+class HastyError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("num_samples", ctypes.c_int32),
+                ("max_depth", ctypes.c_int32), ("roulette_start_depth", ctypes.c_int32), ("roulette_q", ctypes.c_float),
+                ("use_mis", ctypes.c_int32), ("seed", ctypes.c_uint64), ("n_triangles", ctypes.c_int64),
+                ("n_light_triangles", ctypes.c_int64), ("n_shapes", ctypes.c_int32), ("n_materials", ctypes.c_int32),
+                ("env_is_texture", ctypes.c_int32), ("exposure", ctypes.c_float), ("samples_done", ctypes.c_int32),
+                ("bvh_depth", ctypes.c_int32), ("bvh_build_ms", ctypes.c_double), ("device_bytes", ctypes.c_int64)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("rays", ctypes.c_uint64), ("shaded", ctypes.c_uint64), ("paths", ctypes.c_uint64),
+                ("nan_samples", ctypes.c_uint64), ("media_overflow", ctypes.c_uint64), ("trial_cap", ctypes.c_uint64),
+                ("kernel_ms", ctypes.c_double), ("trace_ms", ctypes.c_double), ("shade_ms", ctypes.c_double),
+                ("trace_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
+
+
+def declared_symbols(header: str = HEADER) -> list[str]:
+    """Function names declared in the C header."""
+    text = open(header).read()
+    return sorted(set(re.findall(r"^\s*int\s+(hasty_\w+)\s*\(", text, flags=re.M)))
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"native library missing: {LIB_PATH} (run python -m hastyrenderer_gb300.build)")
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, U64, I64, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_int64, ctypes.c_size_t
+    sig = {
+        "hasty_last_error": [ctypes.c_char_p, SZ],
+        "hasty_version": [P, P],
+        "hasty_ctx_create": [I, ctypes.c_uint32, P],
+        "hasty_ctx_destroy": [P],
+        "hasty_job_load": [P, ctypes.c_char_p, P],
+        "hasty_job_destroy": [P],
+        "hasty_job_info_get": [P, P],
+        "hasty_job_set_seed": [P, U64],
+        "hasty_job_reset": [P],
+        "hasty_job_set_paths_in_flight": [P, I64],
+        "hasty_job_render_passes": [P, I],
+        "hasty_job_sync": [P],
+        "hasty_job_stop": [P],
+        "hasty_job_stats_get": [P, P],
+        "hasty_job_set_stage_timing": [P, I],
+        "hasty_job_read": [P, I, P, SZ, SZ, P],
+        "hasty_job_read_sums": [P, I, P, SZ, SZ, P],
+        "hasty_job_write_outputs": [P, ctypes.c_char_p, I],
+        "hasty_debug_intersect": [P, P, SZ, P, P, P, P],
+        "hasty_debug_tri_ids": [P, P, P, SZ],
+        "hasty_debug_bsdf": [I, P, SZ, P, SZ, P],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != HASTY_OK:
+        buf = ctypes.create_string_buffer(2048)
+        lib().hasty_last_error(buf, 2048)
+        raise HastyError(rc, buf.value.decode(errors="replace"))

@@ -1,0 +1,129 @@
+/*
+ * hasty_gpu.h - C ABI of the GB300 path tracer.
+ *
+ * A drop-in for HastyRenderer's unidirectional CPU integrator behind the
+ * reference's render-job surface. Plain C types only; every call returns an
+ * int status (HASTY_OK or a negative HASTY_ERR_*) and never throws. The
+ * message of the calling thread's last failure is available through
+ * hasty_last_error().
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   hasty_job_load           RenderJob::loadJSON + Scene::Scene
+ *                            (core/src/RenderJob.cpp:21-28, core/src/Scene.cpp:12-194)
+ *   hasty_job_render_passes  renderThread pass loop over estimateRadiance
+ *                            (core/src/PathTracing.cpp:98-160, :21-95)
+ *   hasty_job_stop           RenderJob::stopFlag (core/include/Hasty/RenderJob.h:51)
+ *   hasty_job_read           computeEstimate (apps/ViewerUtils.cpp:95-121)
+ *   hasty_job_write_outputs  postProcessAndSaveToDisk without the denoiser
+ *                            (apps/ViewerUtils.cpp:137-152)
+ *   hasty_debug_intersect    Scene::rayHit / rtcIntersect1 (core/src/Scene.cpp:281-303)
+ *   hasty_debug_bsdf         PrincipledBRDF::sample / evaluate / evaluateSamplePDF
+ *                            (core/src/BRDF.cpp:630-742)
+ *
+ * Threading: a context and its jobs may be used from one host thread at a
+ * time. Rendering is asynchronous on the job's CUDA stream; hasty_job_sync,
+ * hasty_job_read and hasty_job_write_outputs wait for it.
+ */
+#ifndef HASTY_GPU_H
+#define HASTY_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HASTY_OK 0
+#define HASTY_ERR_ARG (-1)        /* bad argument (CLI exit code 1) */
+#define HASTY_ERR_LOAD (-2)       /* job/scene/mesh/image could not be loaded (CLI exit code 2) */
+#define HASTY_ERR_CUDA (-3)       /* CUDA runtime error or no device */
+#define HASTY_ERR_MEMORY (-4)     /* device allocation failed */
+#define HASTY_ERR_IO (-5)         /* output could not be written (CLI exit code 5) */
+#define HASTY_ERR_STOPPED (-6)    /* job was stopped before the requested passes ran */
+#define HASTY_ERR_MISSING (-7)    /* entry point unavailable in this build */
+
+#define HASTY_AOV_COLOR 0
+#define HASTY_AOV_NORMAL 1
+#define HASTY_AOV_ALBEDO 2
+
+typedef struct hasty_ctx hasty_ctx;
+typedef struct hasty_job hasty_job;
+
+typedef struct hasty_job_info {
+  int32_t width, height;
+  int32_t num_samples;         /* settings.num_samples */
+  int32_t max_depth;
+  int32_t roulette_start_depth;
+  float roulette_q;
+  int32_t use_mis;
+  uint64_t seed;
+  int64_t n_triangles;
+  int64_t n_light_triangles;
+  int32_t n_shapes;
+  int32_t n_materials;
+  int32_t env_is_texture;
+  float exposure;
+  int32_t samples_done;        /* passes accumulated so far */
+  int32_t bvh_depth;
+  double bvh_build_ms;
+  int64_t device_bytes;        /* device memory held by the job */
+} hasty_job_info;
+
+typedef struct hasty_stats {
+  uint64_t rays;               /* closest-hit queries (camera, BSDF and light rays) */
+  uint64_t shaded;             /* non-emissive surface vertices shaded */
+  uint64_t paths;              /* camera samples started */
+  uint64_t nan_samples;        /* samples dropped for NaN radiance */
+  uint64_t media_overflow;     /* medium-stack pushes beyond 4 nested media */
+  uint64_t trial_cap;          /* rejection loops stopped at the trial limit */
+  double kernel_ms;            /* device time of the passes rendered so far */
+  double trace_ms;             /* device time in closest-hit kernels (stage timing on) */
+  double shade_ms;             /* device time in shading kernels (stage timing on) */
+  uint64_t trace_launches;     /* closest-hit kernel launches */
+  uint64_t kernel_launches;    /* all kernel launches of the passes rendered so far */
+} hasty_stats;
+
+int hasty_last_error(char* buf, size_t len);
+int hasty_version(int* major, int* minor);
+
+int hasty_ctx_create(int device, uint32_t flags, hasty_ctx** out);
+int hasty_ctx_destroy(hasty_ctx* ctx);
+
+int hasty_job_load(hasty_ctx* ctx, const char* render_job_path, hasty_job** out);
+int hasty_job_destroy(hasty_job* job);
+int hasty_job_info_get(hasty_job* job, hasty_job_info* out);
+int hasty_job_set_seed(hasty_job* job, uint64_t seed);      /* also clears the accumulators */
+int hasty_job_reset(hasty_job* job);                        /* clears accumulators, pass counter, stats */
+/* Maximum camera samples in flight per batch (paths); 0 = automatic. */
+int hasty_job_set_paths_in_flight(hasty_job* job, int64_t paths);
+
+int hasty_job_render_passes(hasty_job* job, int n_passes);  /* asynchronous */
+int hasty_job_sync(hasty_job* job);
+int hasty_job_stop(hasty_job* job);
+int hasty_job_stats_get(hasty_job* job, hasty_stats* out);
+/* Time every stage with CUDA events (adds two events per kernel). */
+int hasty_job_set_stage_timing(hasty_job* job, int on);
+
+/* Estimate sum / (1e-7 + N); colour scaled by 2^exposure. host_rgb holds w*h*3 floats, row-major. */
+int hasty_job_read(hasty_job* job, int aov, float* host_rgb, size_t w, size_t h, int32_t* num_samples);
+/* Raw FP64 sums over the passes rendered so far (w*h*3 doubles). */
+int hasty_job_read_sums(hasty_job* job, int aov, double* host_rgb, size_t w, size_t h, int32_t* num_samples);
+/* output.exr, outputNormal.exr, outputAlbedo.exr (+ .pfm copies when write_pfm != 0). */
+int hasty_job_write_outputs(hasty_job* job, const char* out_dir, int write_pfm);
+
+/* Closest hits of n rays given as n x 6 host floats (origin, direction):
+ * global triangle index (-1 miss), t, u, v. */
+int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* tri, float* t, float* u, float* v);
+/* Triangle index -> (OBJ shape = Embree geomID, face = primID). */
+int hasty_debug_tri_ids(hasty_job* job, int32_t* geom, int32_t* prim, size_t n);
+/* BSDF known-answer evaluation on the device. which: 0 sample, 1 evaluate, 2 pdf.
+ * in: n_cases x 33 floats; replay: n_cases x n_replay u32 values, case c draws
+ * replay[c*n_replay ...] in order; out: n_cases x 12 floats. */
+int hasty_debug_bsdf(int which, const float* in, size_t n_cases, const uint32_t* replay, size_t n_replay, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HASTY_GPU_H */

@@ -1,0 +1,146 @@
+"""Oracle (test infrastructure only): ctypes access to the CPU checker.
+
+``Oracle`` drives the CPU restatement (oracle/port, built to
+oracle/_build/liboracle.so); ``ReferenceBuild`` drives the reference's own
+integrator compiled under oracle/_ref (development machine only). Only tests,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg use this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "_build", "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libhasty_ref.so")
+
+_libs: dict[str, ctypes.CDLL] = {}
+
+
+def _load(path: str, prefix: str) -> ctypes.CDLL:
+    if path in _libs:
+        return _libs[path]
+    if not os.path.exists(path):
+        raise RuntimeError(f"oracle library missing: {path} (make -C oracle)")
+    L = ctypes.CDLL(path)
+    P, I = ctypes.c_void_p, ctypes.c_int
+    getattr(L, prefix + "_load").restype = P
+    getattr(L, prefix + "_load").argtypes = [ctypes.c_char_p, ctypes.c_char_p, I]
+    getattr(L, prefix + "_free").argtypes = [P]
+    getattr(L, prefix + "_render").argtypes = [P] + [I] * 7 + [P] * 5
+    getattr(L, prefix + "_render_samples").argtypes = [P, I, I, I, I, I, P, P, P]
+    getattr(L, prefix + "_kat").argtypes = [I, P, P, I, P]
+    if prefix == "hor":
+        L.hor_info.argtypes = [P, P]
+        L.hor_set_seed.argtypes = [P, ctypes.c_uint64]
+        L.hor_intersect.argtypes = [P, P, ctypes.c_int64, I, P, P, P, P, P]
+        L.hor_tri_ids.argtypes = [P, P, P]
+        L.hor_rng_stream.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, I, P]
+        L.hor_halton.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+        L.hor_halton.restype = ctypes.c_float
+    _libs[path] = L
+    return L
+
+
+class _Base:
+    prefix = ""
+    path = ""
+
+    def __init__(self, job_path: str):
+        self.L = _load(self.path, self.prefix)
+        err = ctypes.create_string_buffer(1024)
+        self.h = getattr(self.L, self.prefix + "_load")(job_path.encode(), err, 1024)
+        if not self.h:
+            raise RuntimeError("oracle load failed: " + err.value.decode())
+
+    def close(self):
+        if self.h:
+            getattr(self.L, self.prefix + "_free")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, pass0: int, npasses: int, x0: int, y0: int, w: int, h: int, nthreads: int = 0) -> dict:
+        c = np.zeros((h, w, 3)); c2 = np.zeros_like(c); n = np.zeros_like(c); a = np.zeros_like(c)
+        st = np.zeros(6, np.uint64)
+        getattr(self.L, self.prefix + "_render")(self.h, pass0, npasses, x0, y0, w, h, nthreads, c.ctypes.data,
+                                                 c2.ctypes.data, n.ctypes.data, a.ctypes.data, st.ctypes.data)
+        return {"color": c, "color_sq": c2, "normal": n, "albedo": a, "stats": st}
+
+    def render_samples(self, pass_idx: int, x0: int, y0: int, w: int, h: int):
+        c = np.zeros((h, w, 3), np.float32); n = np.zeros_like(c); a = np.zeros_like(c)
+        getattr(self.L, self.prefix + "_render_samples")(self.h, pass_idx, x0, y0, w, h, c.ctypes.data, n.ctypes.data,
+                                                         a.ctypes.data)
+        return c, n, a
+
+
+class Oracle(_Base):
+    prefix = "hor"
+    path = PORT_LIB
+
+    def info(self) -> dict:
+        out = np.zeros(12, np.int64)
+        self.L.hor_info(self.h, out.ctypes.data)
+        keys = ["width", "height", "num_samples", "max_depth", "n_tris", "n_light_tris", "env_is_texture", "use_mis",
+                "roulette_start", "n_shapes", "n_materials", "seed"]
+        return dict(zip(keys, out.tolist()))
+
+    def set_seed(self, seed: int) -> None:
+        self.L.hor_set_seed(self.h, ctypes.c_uint64(seed))
+
+    def intersect(self, rays: np.ndarray, fp64: bool = False):
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+        n = r.shape[0]
+        tri = np.empty(n, np.int32)
+        t, u, v = (np.empty(n, np.float32) for _ in range(3))
+        st = np.zeros(2, np.uint64)
+        self.L.hor_intersect(self.h, r.ctypes.data, n, 1 if fp64 else 0, tri.ctypes.data, t.ctypes.data,
+                             u.ctypes.data, v.ctypes.data, st.ctypes.data)
+        return tri, t, u, v, st
+
+    def triangle_ids(self):
+        n = self.info()["n_tris"]
+        g = np.empty(n, np.int32); p = np.empty(n, np.int32)
+        self.L.hor_tri_ids(self.h, g.ctypes.data, p.ctypes.data)
+        return g, p
+
+
+class ReferenceBuild(_Base):
+    prefix = "ref"
+    path = REF_LIB
+
+    @staticmethod
+    def available() -> bool:
+        return os.path.exists(REF_LIB)
+
+
+def kat(which: int, inputs: np.ndarray, replay: np.ndarray, reference: bool = False) -> np.ndarray:
+    """Known-answer call of one routine per row of `inputs` with the matching
+    row of `replay` as its uniform stream. Output rows have 12 floats."""
+    L = _load(REF_LIB, "ref") if reference else _load(PORT_LIB, "hor")
+    f = L.ref_kat if reference else L.hor_kat
+    x = np.ascontiguousarray(inputs, np.float32)
+    r = np.ascontiguousarray(replay, np.uint32)
+    out = np.full((x.shape[0], 12), np.nan, np.float32)
+    for i in range(x.shape[0]):
+        rc = f(which, x[i].ctypes.data, r[i].ctypes.data, r.shape[1], out[i].ctypes.data)
+        if rc < 0:
+            raise RuntimeError(f"kat {which} case {i} failed ({rc})")
+    return out
+
+
+def rng_stream(seed: int, pixel: int, pass_idx: int, n: int) -> np.ndarray:
+    L = _load(PORT_LIB, "hor")
+    out = np.empty(n, np.uint32)
+    L.hor_rng_stream(ctypes.c_uint64(seed), pixel, pass_idx, n, out.ctypes.data)
+    return out
+
+
+def halton(base: int, k: int) -> float:
+    return float(_load(PORT_LIB, "hor").hor_halton(base, k))
