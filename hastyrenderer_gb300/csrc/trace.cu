@@ -41,7 +41,9 @@ __device__ __forceinline__ void tri_test(float ox, float oy, float oz, float dx,
   float V = mulr(dotr(rx, ry, rz, e1.x, e1.y, e1.z), sg);
   if (!(den != 0.f && U >= 0.f && V >= 0.f && addr(U, V) <= ad)) return;
   float T = mulr(dotr(nx, ny, nz, cx, cy, cz), sg);
-  if (!(mulr(ad, 1e-6f) < T && T <= mulr(ad, best.t))) return;
+  if (!(mulr(ad, 1e-6f) < T)) return;
+  // compare divided distances: the closest hit then does not depend on the
+  // order in which triangles are tested
   float t = __fdiv_rn(T, ad);
   int id = __float_as_int(v0.w);
   if (t < best.t || (t == best.t && (best.tri < 0 || id < best.tri))) {
@@ -51,13 +53,20 @@ __device__ __forceinline__ void tri_test(float ox, float oy, float oz, float dx,
 
 constexpr int kStack = 64;
 
+// Slab distance (b - o) / d with each step rounded once: relative error of a
+// few ulps whatever the magnitudes, so padding the interval keeps the test
+// conservative (robust traversal in the sense of Ize 2013).
+__device__ __forceinline__ float slab(float b, float o, float id) { return __fmul_rn(__fsub_rn(b, o), id); }
+
+constexpr float kPadHi = 1.0000008f;   // 1 + 2*gamma(3), rounded up
+constexpr float kPadLo = 0.9999992f;
+
 __device__ __forceinline__ Hit trace_binary(const SceneDev& sc, float ox, float oy, float oz, float dx, float dy, float dz) {
   Hit best; best.t = __int_as_float(0x7f800000); best.u = best.v = 0.f; best.tri = -1;
   const float eps = 1e-20f;
   float idx = 1.0f / (fabsf(dx) > eps ? dx : copysignf(eps, dx));
   float idy = 1.0f / (fabsf(dy) > eps ? dy : copysignf(eps, dy));
   float idz = 1.0f / (fabsf(dz) > eps ? dz : copysignf(eps, dz));
-  float oox = ox * idx, ooy = oy * idy, ooz = oz * idz;
   int stack[kStack];
   int sp = 0;
   int link = 0;   // root (always an inner node)
@@ -69,17 +78,19 @@ __device__ __forceinline__ Hit trace_binary(const SceneDev& sc, float ox, float 
       float4 n1 = __ldg(&nodes[4 * link + 1]);
       float4 n2 = __ldg(&nodes[4 * link + 2]);
       float4 n3 = __ldg(&nodes[4 * link + 3]);
-      float tlim = best.t * 1.0000008f;
-      float a0 = n0.x * idx - oox, a1 = n0.y * idx - oox;
-      float b0 = n0.z * idy - ooy, b1 = n0.w * idy - ooy;
-      float c0 = n2.x * idz - ooz, c1 = n2.y * idz - ooz;
-      float t0min = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f));
-      float t0max = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(c0, c1), tlim)) * 1.0000008f;
-      float d0 = n1.x * idx - oox, d1 = n1.y * idx - oox;
-      float e0 = n1.z * idy - ooy, e1v = n1.w * idy - ooy;
-      float f0 = n2.z * idz - ooz, f1 = n2.w * idz - ooz;
-      float t1min = fmaxf(fmaxf(fminf(d0, d1), fminf(e0, e1v)), fmaxf(fminf(f0, f1), 0.0f));
-      float t1max = fminf(fminf(fmaxf(d0, d1), fmaxf(e0, e1v)), fminf(fmaxf(f0, f1), tlim)) * 1.0000008f;
+      float tlim = best.t * kPadHi;
+      float a0 = slab(n0.x, ox, idx), a1 = slab(n0.y, ox, idx);
+      float b0 = slab(n0.z, oy, idy), b1 = slab(n0.w, oy, idy);
+      float c0 = slab(n2.x, oz, idz), c1 = slab(n2.y, oz, idz);
+      float t0min = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f)) * kPadLo;
+      float t0max = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fmaxf(c0, c1)) * kPadHi;
+      t0max = fminf(t0max, tlim);
+      float d0 = slab(n1.x, ox, idx), d1 = slab(n1.y, ox, idx);
+      float e0 = slab(n1.z, oy, idy), e1v = slab(n1.w, oy, idy);
+      float f0 = slab(n2.z, oz, idz), f1 = slab(n2.w, oz, idz);
+      float t1min = fmaxf(fmaxf(fminf(d0, d1), fminf(e0, e1v)), fmaxf(fminf(f0, f1), 0.0f)) * kPadLo;
+      float t1max = fminf(fminf(fmaxf(d0, d1), fmaxf(e0, e1v)), fmaxf(f0, f1)) * kPadHi;
+      t1max = fminf(t1max, tlim);
       bool h0 = t0min <= t0max, h1 = t1min <= t1max;
       int l0 = __float_as_int(n3.x), l1 = __float_as_int(n3.y);
       if (h0 && h1) {

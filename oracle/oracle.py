@@ -94,13 +94,13 @@ class Oracle(_Base):
     def set_seed(self, seed: int) -> None:
         self.L.hor_set_seed(self.h, ctypes.c_uint64(seed))
 
-    def intersect(self, rays: np.ndarray, fp64: bool = False):
+    def intersect(self, rays: np.ndarray, fp64: bool = False, brute: bool = False):
         r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
         n = r.shape[0]
         tri = np.empty(n, np.int32)
         t, u, v = (np.empty(n, np.float32) for _ in range(3))
         st = np.zeros(2, np.uint64)
-        self.L.hor_intersect(self.h, r.ctypes.data, n, 1 if fp64 else 0, tri.ctypes.data, t.ctypes.data,
+        self.L.hor_intersect(self.h, r.ctypes.data, n, 1 if fp64 else (2 if brute else 0), tri.ctypes.data, t.ctypes.data,
                              u.ctypes.data, v.ctypes.data, st.ctypes.data)
         return tri, t, u, v, st
 
@@ -144,3 +144,15 @@ def rng_stream(seed: int, pixel: int, pass_idx: int, n: int) -> np.ndarray:
 
 def halton(base: int, k: int) -> float:
     return float(_load(PORT_LIB, "hor").hor_halton(base, k))
+
+
+def property_test(which: int, n: int, seed: int = 0) -> np.ndarray:
+    """The reference's unit tests (apps/Tests.cpp) run as loops in the CPU
+    checker; returns the quantities each test asserts on."""
+    L = _load(PORT_LIB, "hor")
+    L.hor_property.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, ctypes.c_void_p]
+    out = np.zeros(8, np.float64)
+    k = L.hor_property(which, n, ctypes.c_uint64(seed), out.ctypes.data)
+    if k < 0:
+        raise RuntimeError(f"property test {which} unknown")
+    return out[:k]

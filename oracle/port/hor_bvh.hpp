@@ -45,8 +45,12 @@ inline bool tri_intersect(const float o[3], const float d[3], const float* v0, c
   float V = (r[0] * e1[0] + r[1] * e1[1] + r[2] * e1[2]) * sgn;
   if (!(den != 0.f && U >= 0.f && V >= 0.f && U + V <= absden)) return false;
   float T = (n[0] * c[0] + n[1] * c[1] + n[2] * c[2]) * sgn;
-  if (!(absden * tnear < T && T <= absden * tfar)) return false;
-  t = T / absden; u = U / absden; v = V / absden;
+  if (!(absden * tnear < T)) return false;
+  // the far limit is applied to the divided distance, so that the closest
+  // hit over a set of triangles does not depend on the order they are tested
+  t = T / absden;
+  if (!(t <= tfar)) return false;
+  u = U / absden; v = V / absden;
   ng[0] = n[0]; ng[1] = n[1]; ng[2] = n[2];
   return true;
 }
@@ -151,14 +155,18 @@ struct Bvh2 {
     }
   }
 
+  // Slab test with each distance rounded once and the interval widened by
+  // 1 +/- 2*gamma(3), so that rounding never culls a box the ray touches.
   static bool ray_box(const float o[3], const float inv[3], const float* lo, const float* hi, float tmax, float& tent) {
-    float t0 = 0.f, t1 = tmax;
+    float t0 = 0.f, t1 = INFINITY;
     for (int a = 0; a < 3; ++a) {
       float ta = (lo[a] - o[a]) * inv[a], tb = (hi[a] - o[a]) * inv[a];
       if (ta > tb) std::swap(ta, tb);
       if (!(ta <= tb)) { ta = -INFINITY; tb = INFINITY; }  // 0*inf on a slab edge
       t0 = std::max(t0, ta); t1 = std::min(t1, tb);
     }
+    t0 *= 0.9999992f;
+    t1 = std::min(t1 * 1.0000008f, tmax * 1.0000008f);
     tent = t0;
     return t0 <= t1;
   }
@@ -200,6 +208,22 @@ struct Bvh2 {
         } else if (ha) stack[sp++] = nd.left_or_first;
         else if (hb) stack[sp++] = nd.left_or_first + 1;
         if (sp > 124) sp = 124;  // depth guard; binned SAH trees stay far below
+      }
+    }
+    return h;
+  }
+
+  // Every triangle with the same FP32 test: the exact closest hit for this
+  // triangle test, independent of any tree.
+  BvhHit intersect_brute(const float o[3], const float d[3], float tnear, float tfar) const {
+    BvhHit h; float best = tfar;
+    for (size_t i = 0; i < ntri; ++i) {
+      const float* p = tv + 9 * i;
+      float t, u, v, ng[3];
+      if (tri_intersect(o, d, p, p + 3, p + 6, tnear, best, t, u, v, ng) &&
+          (t < best || (t == best && (h.prim < 0 || int(i) < h.prim)))) {
+        best = t; h.prim = int(i); h.t = t; h.u = u; h.v = v;
+        h.ng[0] = ng[0]; h.ng[1] = ng[1]; h.ng[2] = ng[2];
       }
     }
     return h;

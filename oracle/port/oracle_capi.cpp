@@ -121,7 +121,8 @@ int hor_render_samples(void* p, int pass, int x0, int y0, int w, int h, float* c
   return 0;
 }
 
-// rays: n x 6 floats (origin, direction). mode 0: BVH (FP32), 1: brute force (FP64).
+// rays: n x 6 floats (origin, direction). mode 0: BVH (FP32), 1: brute force (FP64),
+// 2: brute force with the FP32 triangle test.
 // Outputs: triangle index (global, shape-major order; -1 miss), t, u, v.
 // stats[2]: nodes visited, triangle tests (mode 0).
 int hor_intersect(void* p, const float* rays, int64_t n, int mode, int32_t* prim, float* t, float* u, float* v, uint64_t* stats) {
@@ -129,7 +130,9 @@ int hor_intersect(void* p, const float* rays, int64_t n, int mode, int32_t* prim
   BvhStats st;
   for (int64_t i = 0; i < n; ++i) {
     const float* r = rays + 6 * i;
-    BvhHit hh = mode == 0 ? sc.bvh.intersect(r, r + 3, 1e-6f, INFINITY, &st) : sc.bvh.intersect_fp64(r, r + 3, 1e-6f, INFINITY);
+    BvhHit hh = mode == 0 ? sc.bvh.intersect(r, r + 3, 1e-6f, INFINITY, &st)
+               : mode == 2 ? sc.bvh.intersect_brute(r, r + 3, 1e-6f, INFINITY)
+                           : sc.bvh.intersect_fp64(r, r + 3, 1e-6f, INFINITY);
     prim[i] = hh.prim; t[i] = hh.t; u[i] = hh.u; v[i] = hh.v;
   }
   if (stats) { stats[0] = st.nodes; stats[1] = st.tris; }
@@ -148,6 +151,124 @@ void hor_rng_stream(uint64_t seed, uint32_t pixel, uint32_t pass, int n, uint32_
 }
 
 float hor_halton(uint32_t base, uint32_t k) { return halton(base, k); }
+
+// The reference's unit tests (apps/Tests.cpp:40-232) as loops over the
+// oracle's routines, seeded with the project stream of `seed`. Writes the
+// quantities each test asserts on; returns the number written.
+//   0 rodriguesRotation (Tests.cpp:40-52): max |x - R^-1 R x| over n trials
+//   1 sphericalCoordinates (:54-74): max |d - to(from(d))|, min/max theta, phi
+//   2 sampleCosineLobe (:76-90): max rel |pdf - evalpdf|, max ||w|-1|
+//   3 sampleHemisphereCosImportance (:93-106): same quantities
+//   4 DGGX (:107-131): MC estimate of int D(h) (n.h) dh (alpha 0.3)
+//   5 sampleDGGX (:132-147): max rel |pdf - density|
+//   6 sampleDGGX2 (:148-168): MC estimate of E[cos/pdf] (alpha 1)
+//   7 sampleGGXVNDFGlobal (:169-187): max rel |pdf - density|, min pdf
+//   8 sampleGGXVNDFGlobal2 (:188-210): MC estimate of E[cos/pdf] (alpha 1)
+//   9 refraction (:212-232): max |wi - wi2|, |F1 - F2|
+int hor_property(int which, int64_t n, uint64_t seed, double* out) {
+  Rng r(path_key(seed, 0, 0));
+  float pd;
+  switch (which) {
+    case 0: {
+      double m = 0;
+      for (int64_t i = 0; i < n; ++i) {
+        V3 a = sample_sphere_uniformly(r, pd), b = sample_sphere_uniformly(r, pd);
+        Rotation rot(a, b);
+        V3 x(r.uniform01f(), r.uniform01f(), r.uniform01f());
+        V3 y = rot.apply_inverse(rot.apply(x));
+        m = std::max(m, double(norm(x - y)));
+      }
+      out[0] = m; return 1;
+    }
+    case 1: {
+      double m = 0, tmin = 1e9, tmax = -1e9, pmin = 1e9, pmax = -1e9;
+      for (int64_t i = 0; i < n; ++i) {
+        V3 d = sample_sphere_uniformly(r, pd);
+        float th, ph; sph_from_dir(d, th, ph);
+        SphDir back = sph_to_dir(th, ph);
+        m = std::max(m, double(norm(d - back.dir)));
+        tmin = std::min(tmin, double(th)); tmax = std::max(tmax, double(th));
+        pmin = std::min(pmin, double(ph)); pmax = std::max(pmax, double(ph));
+      }
+      out[0] = m; out[1] = tmin; out[2] = tmax; out[3] = pmin; out[4] = pmax; return 5;
+    }
+    case 2: case 3: {
+      double mrel = 0, mlen = 0;
+      for (int64_t i = 0; i < n; ++i) {
+        V3 lobe = sample_sphere_uniformly(r, pd);
+        float p1, p2; V3 w;
+        if (which == 2) { float e = 1.0f + r.uniform01f() * 10.0f; w = sample_cosine_lobe(r, lobe, e, p1); p2 = eval_cosine_lobe_pdf(lobe, e, w); }
+        else { w = sample_hemisphere_cos(r, lobe, p1); p2 = eval_hemisphere_cos_pdf(lobe, w); }
+        mrel = std::max(mrel, std::fabs(double(p1) - p2) / std::max(1.0, std::fabs(double(p2))));
+        mlen = std::max(mlen, std::fabs(double(norm(w)) - 1.0));
+      }
+      out[0] = mrel; out[1] = mlen; return 2;
+    }
+    case 4: {
+      float alpha = 0.3f;
+      V3 nrm = sample_sphere_uniformly(r, pd);
+      V3 wo = sample_hemisphere_uniformly(r, nrm, pd);
+      V3 t = any_orthonormal(nrm), b = cross(nrm, t);
+      double sum = 0; float mind = 1;
+      for (int64_t i = 0; i < n; ++i) {
+        wo = sample_hemisphere_uniformly(r, nrm, pd);
+        float d = dggx(dot(nrm, wo), dot(t, wo), dot(b, wo), alpha, alpha);
+        mind = std::min(mind, d);
+        sum += double(d) * dot(nrm, wo) / pd;
+      }
+      out[0] = sum / double(n); out[1] = mind; return 2;
+    }
+    case 5: {
+      double mrel = 0;
+      for (int64_t i = 0; i < n; ++i) {
+        float alpha = std::max(1e-2f, r.uniform01f());
+        V3 nrm = sample_sphere_uniformly(r, pd);
+        V3 wo = sample_hemisphere_uniformly(r, nrm, pd);
+        float p1; V3 wi = sample_dggx(r, nrm, alpha, wo, p1);
+        float p2 = sample_dggx_density(nrm, alpha, wo, wi);
+        mrel = std::max(mrel, std::fabs(double(p1) - p2) / std::max(1.0, std::fabs(double(p2))));
+      }
+      out[0] = mrel; return 1;
+    }
+    case 6: case 8: {
+      float alpha = 1.0f;
+      V3 nrm = sample_sphere_uniformly(r, pd);
+      V3 wo = nrm;
+      double sum = 0; float minp = 1e30f;
+      for (int64_t i = 0; i < n; ++i) {
+        float p; V3 wi;
+        if (which == 6) wi = sample_dggx(r, nrm, alpha, wo, p);
+        else { V3 t = any_orthonormal(nrm), b = cross(nrm, t); wi = sample_ggx_vndf_global(r, nrm, alpha, alpha, t, b, wo, p); }
+        minp = std::min(minp, p);
+        sum += std::max(0.0f, dot(nrm, wi)) / p;
+      }
+      out[0] = sum / double(n); out[1] = minp; return 2;
+    }
+    case 7: {
+      double mrel = 0; float minp = 1e30f;
+      for (int64_t i = 0; i < n; ++i) {
+        float alpha = std::max(1e-2f, r.uniform01f());
+        V3 nrm = sample_sphere_uniformly(r, pd);
+        V3 wo = sample_hemisphere_uniformly(r, nrm, pd);
+        V3 t = any_orthonormal(nrm), b = cross(nrm, t);
+        float p1; V3 wi = sample_ggx_vndf_global(r, nrm, alpha, alpha, t, b, wo, p1);
+        float p2 = sample_ggx_vndf_global_density(nrm, alpha, alpha, t, b, wo, wi);
+        minp = std::min(minp, p1);
+        mrel = std::max(mrel, std::fabs(double(p1) - p2) / std::max(1.0, std::fabs(double(p2))));
+      }
+      out[0] = mrel; out[1] = minp; return 2;
+    }
+    case 9: {
+      V3 nrm = normalize(V3(0.1f, 0.2f, 1.0f)), wi = normalize(V3(0.15f, 0.05f, 1.0f)), wo, wi2;
+      refraction_direction(wi, nrm, 1.45f, 1.0f, wo);
+      refraction_direction(wo, -nrm, 1.0f, 1.45f, wi2);
+      out[0] = norm(wi - wi2);
+      out[1] = std::fabs(fresnel_dielectric(0.3f, 0.6f, 1.0f, 1.4f) - fresnel_dielectric(0.6f, 0.3f, 1.4f, 1.0f));
+      return 2;
+    }
+    default: return -1;
+  }
+}
 
 // Known-answer entry points with replayed uniforms; layouts are listed in
 // tests/golden/make_golden.py. Returns the number of outputs written.

@@ -1,11 +1,22 @@
-"""CUDA path vs the CPU checker (oracle/) on the same seeded scenes and the
-same per-path random streams."""
+"""CUDA path against the reference's own outputs (golden fixtures written by
+the reference build, tests/golden/) and against the CPU checker (oracle/) on
+the same seeded scenes and per-path random streams. All calls go through the
+C ABI (hastyrenderer_gb300.native)."""
+import os
+
 import numpy as np
 import pytest
 
 from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+SCENES = ["cornell", "field", "room", "room_nomis"]
+
+
+def golden_job(name):
+    return os.path.join(GOLDEN, "scenes", name, "renderJob.json")
 
 
 def _job(path):
@@ -20,57 +31,118 @@ def _random_rays(n, rng, lo, hi):
     return np.concatenate([o, d], 1).astype(np.float32)
 
 
-@pytest.mark.parametrize("name,lo,hi", [("cornell", -1.0, 2.0), ("field", -3.0, 4.0)])
-def test_intersect_matches_checker(scene_dir, name, lo, hi):
-    """Closest-hit queries: triangle ids agree on >= 99.99% of rays, t within 1e-5 relative."""
-    job = _job(scene_dir[name])
-    ora = Oracle(scene_dir[name])
-    rays = _random_rays(20000, np.random.default_rng(5), lo, hi)
-    g_tri, g_t, g_u, g_v = job.intersect(rays)
-    c_tri, c_t, c_u, c_v, _ = ora.intersect(rays)
+def _check_hits(g, c):
+    g_tri, g_t = g[0], g[1]
+    c_tri, c_t = c[0], c[1]
     agree = g_tri == c_tri
     assert agree.mean() >= 0.9999, agree.mean()
     both = agree & (c_tri >= 0)
     rel = np.abs(g_t[both] - c_t[both]) / np.maximum(np.abs(c_t[both]), 1e-30)
-    assert rel.max() <= 1e-5
-    assert (c_tri >= 0).mean() > 0.3
+    assert rel.max() <= 1e-5, rel.max()
+    return agree.mean()
 
 
-@pytest.mark.parametrize("name", ["cornell", "field", "room", "room_nomis"])
-def test_first_pass_samples_match_checker(scene_dir, name):
-    """One pass: each camera sample follows the same random stream on both
-    sides, so nearly every pixel's radiance is equal to 1e-3 relative."""
-    job = _job(scene_dir[name])
+@pytest.mark.parametrize("name,lo,hi", [("cornell", -1.0, 2.0), ("field", -3.0, 4.0), ("room", -2.0, 3.0)])
+def test_intersect_matches_checker(name, lo, hi):
+    """Closest hits: triangle ids agree on >= 99.99% of rays (exactly, in
+    practice), t within 1e-5 relative; the checker's BVH answer is the same
+    as a brute-force scan with the same FP32 triangle test."""
+    job = _job(golden_job(name))
+    ora = Oracle(golden_job(name))
+    rays = _random_rays(50000, np.random.default_rng(5), lo, hi)
+    g = job.intersect(rays)
+    c = ora.intersect(rays)
+    b = ora.intersect(rays, brute=True)
+    assert np.array_equal(c[0], b[0])
+    assert _check_hits(g, c) == 1.0
+    assert (c[0] >= 0).mean() > 0.3
+
+
+def test_intersect_full_size_scene(tmp_path):
+    """The 1,024,002-triangle benchmark scene: camera-like and random rays."""
+    from hastyrenderer_gb300 import scenes
+    path = scenes.sphere_field(str(tmp_path / "c1"), seed=0)
+    job = _job(path)
+    ora = Oracle(path)
+    rng = np.random.default_rng(11)
+    rays = _random_rays(30000, rng, -10.0, 10.0)
+    rays[:, 1] = np.abs(rays[:, 1]) + 0.01
+    g = job.intersect(rays)
+    c = ora.intersect(rays)
+    _check_hits(g, c)
+    assert job.info.n_triangles == 1024002
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_first_pass_matches_reference(name):
+    """Pass 0 of each golden job: every camera sample follows the same random
+    stream as in the reference's own estimateRadiance, so nearly every pixel
+    equals the reference's value (1e-3 relative); AOVs likewise."""
+    g = np.load(os.path.join(GOLDEN, f"render_{name}.npz"))
+    job = _job(golden_job(name))
     job.render_passes(1, sync=True)
-    gpu, n = job.read_sums()
+    col, n = job.read_sums()
+    nrm, _ = job.read_sums(1)
+    alb, _ = job.read_sums(2)
     assert n == 1
-    ora = Oracle(scene_dir[name])
-    w, h = job.width, job.height
-    cpu, cn, ca = ora.render_samples(0, 0, 0, w, h)
-    cpu = np.where(np.isnan(cpu).any(-1, keepdims=True), 0.0, cpu)
-    close = np.all(np.abs(gpu - cpu) <= 1e-3 * np.maximum(1.0, np.abs(cpu)), axis=-1)
+    ref = g["sample_color"]
+    ref = np.where(np.isnan(ref).any(-1, keepdims=True), 0.0, ref)
+    close = np.all(np.abs(col - ref) <= 1e-3 * np.maximum(1.0, np.abs(ref)), axis=-1)
     assert close.mean() >= 0.97, close.mean()
-    gn, _ = job.read_sums(1)
-    assert np.all(np.abs(gn - cn) <= 1e-4 + 1e-4 * np.abs(cn), axis=-1).mean() >= 0.99
+    for ours, key in ((nrm, "sample_normal"), (alb, "sample_albedo")):
+        c2 = np.all(np.abs(ours - g[key]) <= 1e-4 + 1e-4 * np.abs(g[key]), axis=-1)
+        assert c2.mean() >= 0.99, (key, c2.mean())
+
+
+@pytest.mark.parametrize("name", SCENES)
+def test_sixteen_passes_match_reference(name):
+    """16 passes against the reference's sums over the same 16 streams."""
+    g = np.load(os.path.join(GOLDEN, f"render_{name}.npz"))
+    job = _job(golden_job(name))
+    P = int(g["passes"])
+    job.render_passes(P, sync=True)
+    col, n = job.read_sums()
+    assert n == P
+    rel = np.abs(col - g["color"]) / np.maximum(1.0, np.abs(g["color"]))
+    assert (rel.max(-1) <= 1e-3).mean() >= 0.9, (rel.max(-1) <= 1e-3).mean()
+    assert abs(col.mean() - g["color"].mean()) <= 0.02 * abs(g["color"].mean()) + 1e-6
 
 
 @pytest.mark.parametrize("name", ["cornell", "field", "room"])
-def test_image_ztest(scene_dir, name):
-    """Per-pixel means at S spp against the checker at 16*S spp from the same
-    streams: |mean_gpu - mean_cpu| <= 4 sigma, sigma from both sides' sample
-    variances (Monte Carlo noise of the reference image included)."""
+def test_image_ztest(name):
+    """Per-pixel means at S = 16 spp against the checker at 16*S spp: every
+    pixel within 4 sigma, sigma from the sample variance of both estimates
+    (the checker image's own Monte Carlo noise included)."""
     S = 16
-    job = _job(scene_dir[name])
+    job = _job(golden_job(name))
+    job.set_seed(777)
     job.render_passes(S, sync=True)
     g, n = job.read_sums()
-    ora = Oracle(scene_dir[name])
+    ora = Oracle(golden_job(name))
+    ora.set_seed(777)
     w, h = job.width, job.height
-    r = ora.render(0, 16 * S, 0, 0, w, h)
     N = 16 * S
+    r = ora.render(0, N, 0, 0, w, h)
     mc = r["color"] / N
     var_c = np.maximum(r["color_sq"] / N - mc ** 2, 0.0)
     mg = g / S
-    sig = np.sqrt(var_c / S + var_c / N) + 1e-6
+    sig = np.sqrt(var_c / S + var_c / N) + 1e-6 + 1e-5 * np.abs(mc)
     z = np.abs(mg - mc) / sig
-    frac_bad = (z > 4.0).mean()
-    assert frac_bad <= 0.001, (frac_bad, z.max())
+    assert (z > 4.0).mean() <= 0.001, ((z > 4.0).mean(), z.max())
+
+
+def test_device_bsdf_matches_reference():
+    """Device PrincipledBRDF sample/evaluate/pdf on the reference's
+    known-answer cases (replayed uniforms): within 1e-5 relative on >= 99.5%
+    of cases (CUDA's sinf/cosf/powf differ from glibc's by an ulp or two)."""
+    from hastyrenderer_gb300 import debug_bsdf
+    g = np.load(os.path.join(GOLDEN, "kat_bsdf.npz"))
+    for which, name, cols in ((0, "sample", 11), (1, "evaluate", 9), (2, "pdf", 1)):
+        ours = debug_bsdf(which, g["inputs"], g["replay"])[:, :cols]
+        ref = g[name][:, :cols]
+        ok = np.isfinite(ref).all(1)
+        rel = np.abs(ours - ref) / np.maximum(1e-3, np.abs(ref))
+        good = (rel <= 1e-5).all(1) | ~ok
+        assert good.mean() >= 0.995, (name, good.mean())
+        if which == 0:
+            assert (debug_bsdf(0, g["inputs"], g["replay"])[:, 11] == g["sample"][:, 11]).mean() >= 0.995
