@@ -30,7 +30,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-SPP_PER_STEP = 4
+SPP_PER_STEP = 8
 WORKLOAD = "sphere_field_800x_icosphere3_1024002tri_1920x1080_dof6_sky2048x1024_depth12"
 
 
@@ -113,20 +113,21 @@ def cpu_baseline(job_path: str, budget_s: float = 12.0, threads: int = 0):
     x0 = (W - cw) // 2
     y = H // 2 - 32
     samples = 0
-    rays = nodes = tris = 0
+    rays = nodes = tris = shaded = 0
     t0 = time.perf_counter()
-    rows = 0
-    while time.perf_counter() - t0 < budget_s and rows < 512:
-        r = ora.render(0, 1, x0, y + rows % 64, cw, 8, threads)
+    k = 0
+    while time.perf_counter() - t0 < budget_s:
+        r = ora.render(k // 8, 1, x0, y + 8 * (k % 8), cw, 8, threads)
         st = r["stats"]
         samples += cw * 8
-        rays += int(st[0]); nodes += int(st[2]); tris += int(st[3])
-        rows += 8
+        rays += int(st[0]); nodes += int(st[2]); tris += int(st[3]); shaded += int(st[4])
+        k += 1
     dt = time.perf_counter() - t0
     ora.close()
     return {"value": samples / dt, "unit": "samples/s", "cores": threads, "kind": "port",
-            "sample": f"{samples} camera samples: centred {cw}-pixel-wide crop, 1 pass per row band, {dt:.1f} s",
-            "mrays_per_s": rays / dt * 1e-6}, {"nodes_per_ray": nodes / max(rays, 1), "tris_per_ray": tris / max(rays, 1)}
+            "sample": f"{samples} camera samples of a centred {cw}x64 crop (passes 0..{k // 8}), {dt:.1f} s",
+            "mrays_per_s": rays / dt * 1e-6}, {"nodes_per_ray": nodes / max(rays, 1), "tris_per_ray": tris / max(rays, 1),
+                                               "shaded_per_sample": shaded / max(samples, 1), "rays_per_sample": rays / max(samples, 1)}
 
 
 def run_reference_arm(args, job_path: str, rank: int):
@@ -158,7 +159,7 @@ def run_reference_arm(args, job_path: str, rank: int):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=32)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--spp-per-step", type=int, default=SPP_PER_STEP)

@@ -165,3 +165,16 @@ def debug_bsdf(which: int, cases: np.ndarray, replay: np.ndarray) -> np.ndarray:
     out = np.zeros((c.shape[0], 12), np.float32)
     check(native.lib().hasty_debug_bsdf(which, c.ctypes.data, c.shape[0], r.ctypes.data, r.shape[1], out.ctypes.data))
     return out
+
+
+def host_trace(job_path: str, rays: np.ndarray, kind: int = 1):
+    """The device traversal code run on the CPU over a host-built BVH (kind 0
+    binary, 1 compressed 8-wide); no GPU needed. Returns (tri, t, u, v, info)."""
+    r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+    n = r.shape[0]
+    tri = np.empty(n, np.int32)
+    t, u, v = (np.empty(n, np.float32) for _ in range(3))
+    info = np.zeros(3, np.int64)
+    check(native.lib().hasty_debug_host_trace(job_path.encode(), kind, r.ctypes.data, n, tri.ctypes.data, t.ctypes.data,
+                                               u.ctypes.data, v.ctypes.data, info.ctypes.data))
+    return tri, t, u, v, {"triangles": int(info[0]), "nodes": int(info[1]), "depth": int(info[2])}

@@ -25,6 +25,8 @@
 namespace hasty {
 // integrator.cu
 void launch_debug_bsdf(int which, const float* in, int n, const uint32_t* replay, int n_replay, float* out, cudaStream_t st);
+// trace.cu
+void host_trace_rays(int kind, const float4* nodes, const float4* tris, const float* rays, int64_t n, float4* hits);
 }
 
 using namespace hasty;
@@ -64,6 +66,7 @@ int guarded(F&& f) {
 struct hasty_ctx {
   int device = 0;
   int sm_count = 0;
+  uint32_t flags = 0;
 };
 
 struct hasty_job {
@@ -156,8 +159,14 @@ void upload_scene(hasty_job& j) {
   HostScene& h = j.host;
   SceneDev& s = j.sd;
   BvhHost bvh;
-  build_bvh_binary(h.tri_pos.data(), h.n_tris(), 4, bvh);
-  if (bvh.depth > 60) throw ApiError{HASTY_ERR_LOAD, "BVH deeper than the traversal stack (64)"};
+  bool binary = (j.ctx->flags & HASTY_CTX_BINARY_BVH) != 0;
+  if (binary) {
+    build_bvh_binary(h.tri_pos.data(), h.n_tris(), 4, bvh);
+    if (bvh.depth > 60) throw ApiError{HASTY_ERR_LOAD, "BVH deeper than the traversal stack (64)"};
+  } else {
+    build_bvh_wide(h.tri_pos.data(), h.n_tris(), bvh);
+    if (bvh.depth > 30) throw ApiError{HASTY_ERR_LOAD, "wide BVH deeper than the traversal stack (32)"};
+  }
   j.bvh_depth = bvh.depth; j.bvh_ms = bvh.build_ms;
   s.n_tris = int32_t(h.n_tris());
   s.tri_pos = j.upload(h.tri_pos);
@@ -165,7 +174,7 @@ void upload_scene(hasty_job& j) {
   s.normals = j.upload(h.normals);
   s.texcoords = j.upload(h.texcoords);
   s.n_texcoords = int64_t(h.texcoords.size());
-  s.bvh_kind = 0;
+  s.bvh_kind = binary ? 0 : 1;
   {
     float4* n = j.alloc<float4>(bvh.nodes.size() / 4);
     ck(cudaMemcpyAsync(n, bvh.nodes.data(), bvh.nodes.size() * sizeof(float), cudaMemcpyHostToDevice, j.stream), "upload nodes");
@@ -274,7 +283,6 @@ int hasty_version(int* major, int* minor) {
 }
 
 int hasty_ctx_create(int device, uint32_t flags, hasty_ctx** out) {
-  (void)flags;
   return guarded([&] {
     if (!out) throw ApiError{HASTY_ERR_ARG, "null output pointer"};
     int n = 0;
@@ -283,6 +291,7 @@ int hasty_ctx_create(int device, uint32_t flags, hasty_ctx** out) {
     ck(cudaSetDevice(device), "cudaSetDevice");
     auto* c = new hasty_ctx();
     c->device = device;
+    c->flags = flags;
     ck(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "attr");
     *out = c;
     return HASTY_OK;
@@ -510,6 +519,30 @@ int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* 
       int32_t id; std::memcpy(&id, &hh[i].w, 4);
       tri[i] = id; t[i] = hh[i].x; u[i] = hh[i].y; v[i] = hh[i].z;
     }
+    return HASTY_OK;
+  });
+}
+
+int hasty_debug_host_trace(const char* job_path, int kind, const float* rays, size_t n, int32_t* tri, float* t, float* u,
+                           float* v, int64_t* info) {
+  return guarded([&] {
+    if (!job_path || (n && (!rays || !tri || !t || !u || !v)) || (kind != 0 && kind != 1))
+      throw ApiError{HASTY_ERR_ARG, "bad argument"};
+    HostScene h;
+    load_render_job(job_path, h);
+    BvhHost bvh;
+    if (kind == 0) build_bvh_binary(h.tri_pos.data(), h.n_tris(), 4, bvh);
+    else build_bvh_wide(h.tri_pos.data(), h.n_tris(), bvh);
+    std::vector<float4> nodes(bvh.nodes.size() / 4), tris(bvh.tris.size() / 4);
+    std::memcpy(nodes.data(), bvh.nodes.data(), bvh.nodes.size() * sizeof(float));
+    std::memcpy(tris.data(), bvh.tris.data(), bvh.tris.size() * sizeof(float));
+    std::vector<float4> hits(n);
+    host_trace_rays(kind, nodes.data(), tris.data(), rays, int64_t(n), hits.data());
+    for (size_t i = 0; i < n; ++i) {
+      int32_t id; std::memcpy(&id, &hits[i].w, 4);
+      tri[i] = id; t[i] = hits[i].x; u[i] = hits[i].y; v[i] = hits[i].z;
+    }
+    if (info) { info[0] = int64_t(h.n_tris()); info[1] = int64_t(nodes.size() / (kind == 1 ? 5 : 4)); info[2] = bvh.depth; }
     return HASTY_OK;
   });
 }

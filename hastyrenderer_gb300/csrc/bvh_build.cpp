@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cfloat>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -117,11 +118,7 @@ struct Builder {
   }
 };
 
-}  // namespace
-
-void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out) {
-  auto t0 = std::chrono::steady_clock::now();
-  Builder b;
+void run_builder(Builder& b, const float* tri_pos, size_t n, int max_leaf) {
   b.pos = tri_pos; b.n = n; b.max_leaf = max_leaf;
   b.tbox.resize(n); b.cen.resize(3 * n); b.idx.resize(n);
   for (size_t i = 0; i < n; ++i) {
@@ -138,6 +135,27 @@ void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out
   std::vector<std::thread> th;
   for (unsigned i = 0; i < nt; ++i) th.emplace_back([&] { b.worker(); });
   for (auto& t : th) t.join();
+}
+
+void leaf_ordered_tris(const float* tri_pos, const std::vector<int32_t>& order, std::vector<float>& tris) {
+  size_t n = order.size();
+  tris.resize(12 * n);
+  for (size_t i = 0; i < n; ++i) {
+    int32_t t = order[i];
+    const float* p = tri_pos + 9 * size_t(t);
+    float* o = &tris[12 * i];
+    o[0] = p[0]; o[1] = p[1]; o[2] = p[2]; std::memcpy(&o[3], &t, 4);
+    o[4] = p[0] - p[3]; o[5] = p[1] - p[4]; o[6] = p[2] - p[5]; o[7] = 0.f;
+    o[8] = p[6] - p[0]; o[9] = p[7] - p[1]; o[10] = p[8] - p[2]; o[11] = 0.f;
+  }
+}
+
+}  // namespace
+
+void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out) {
+  auto t0 = std::chrono::steady_clock::now();
+  Builder b;
+  run_builder(b, tri_pos, n, max_leaf);
 
   // Emit the GPU layout breadth-first (keeps the top levels contiguous).
   // The root must be an inner node: a single leaf becomes child 0 of a root
@@ -173,16 +191,150 @@ void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out
   for (size_t k = 0; k < fixups.size(); ++k) { int32_t v = int32_t(k + 1); std::memcpy(&out.nodes[fixups[k]], &v, 4); }
 
   out.order = b.idx;
-  out.tris.resize(12 * n);
-  for (size_t i = 0; i < n; ++i) {
-    int32_t t = b.idx[i];
-    const float* p = tri_pos + 9 * size_t(t);
-    float* o = &out.tris[12 * i];
-    o[0] = p[0]; o[1] = p[1]; o[2] = p[2]; std::memcpy(&o[3], &t, 4);
-    o[4] = p[0] - p[3]; o[5] = p[1] - p[4]; o[6] = p[2] - p[5]; o[7] = 0.f;
-    o[8] = p[6] - p[0]; o[9] = p[7] - p[1]; o[10] = p[8] - p[2]; o[11] = 0.f;
-  }
+  leaf_ordered_tris(tri_pos, out.order, out.tris);
   out.depth = b.max_depth.load() + 1;
+  out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// ------------------------------------------------------------------------
+// Compressed 8-wide BVH (the node format of Ylitie, Karras and Laine 2017):
+// binary nodes are collapsed greedily (the child with the largest surface
+// area is opened until 8 children), children are assigned to slots so that
+// visiting slot (k ^ octant) for k = 7..0 is roughly front to back for a ray
+// of that direction octant, and child boxes are quantised to 8 bits on a
+// per-node power-of-two grid, conservatively (decoded in float, widened by
+// one step when rounding would cut into the box).
+namespace {
+
+struct WideOut {
+  std::vector<uint8_t> nodes;     // 80 bytes per node
+  std::vector<int32_t> order;     // wide triangle position -> global id
+  int depth = 0;
+};
+
+float pow2f(int e) { return std::ldexp(1.0f, e); }
+
+int grid_exponent(float extent) {
+  if (!(extent > 0.f)) return -100;
+  int e = int(std::ceil(std::log2(double(extent) / 255.0)));
+  while (255.0 * std::ldexp(1.0, e) < double(extent)) ++e;
+  return std::max(-100, std::min(127, e));
+}
+
+void emit_wide(const Builder& b, WideOut& out) {
+  const std::vector<BNode>& nd = b.nodes;
+  struct Job { int32_t bnode; uint32_t wide; int depth; };
+  std::deque<Job> q;
+  out.nodes.assign(80, 0);
+  q.push_back({0, 0, 1});
+  uint32_t next_node = 1;
+  out.order.clear();
+  while (!q.empty()) {
+    Job jb = q.front(); q.pop_front();
+    out.depth = std::max(out.depth, jb.depth);
+    // gather up to 8 children
+    std::vector<int32_t> kids;
+    const BNode& root = nd[size_t(jb.bnode)];
+    if (root.child < 0) kids.push_back(jb.bnode);
+    else { kids.push_back(root.child); kids.push_back(root.child + 1); }
+    while (kids.size() < 8) {
+      int best = -1; float area = -1.f;
+      for (size_t i = 0; i < kids.size(); ++i) {
+        const BNode& c = nd[size_t(kids[i])];
+        if (c.child >= 0 && c.box.area() > area) { area = c.box.area(); best = int(i); }
+      }
+      if (best < 0) break;
+      int32_t c = kids[size_t(best)];
+      kids[size_t(best)] = nd[size_t(c)].child;
+      kids.push_back(nd[size_t(c)].child + 1);
+    }
+    // node box
+    Box nb;
+    for (int32_t k : kids) nb.grow(nd[size_t(k)].box);
+    float ctr[3] = {0.5f * (nb.lo[0] + nb.hi[0]), 0.5f * (nb.lo[1] + nb.hi[1]), 0.5f * (nb.lo[2] + nb.hi[2])};
+    // slot assignment: slot s is entered first by rays whose direction signs
+    // are ((s&4)?+:-, (s&2)?+:-, (s&1)?+:-); it takes the child that lies
+    // furthest back along that direction.
+    struct Cand { float cost; int kid, slot; };
+    std::vector<Cand> cands;
+    for (size_t i = 0; i < kids.size(); ++i) {
+      const Box& cb = nd[size_t(kids[i])].box;
+      float c[3] = {0.5f * (cb.lo[0] + cb.hi[0]) - ctr[0], 0.5f * (cb.lo[1] + cb.hi[1]) - ctr[1], 0.5f * (cb.lo[2] + cb.hi[2]) - ctr[2]};
+      for (int s = 0; s < 8; ++s) {
+        float d[3] = {(s & 4) ? 1.f : -1.f, (s & 2) ? 1.f : -1.f, (s & 1) ? 1.f : -1.f};
+        cands.push_back({c[0] * d[0] + c[1] * d[1] + c[2] * d[2], int(i), s});
+      }
+    }
+    std::sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& c) { return a.cost < c.cost; });
+    int slot_of[8]; int kid_in[8];
+    for (int i = 0; i < 8; ++i) { slot_of[i] = -1; kid_in[i] = -1; }
+    for (const Cand& c : cands)
+      if (slot_of[c.kid] < 0 && kid_in[c.slot] < 0) { slot_of[c.kid] = c.slot; kid_in[c.slot] = c.kid; }
+    // quantisation grid
+    int ex[3];
+    for (int a = 0; a < 3; ++a) ex[a] = grid_exponent(nb.hi[a] - nb.lo[a]);
+    uint8_t* node = &out.nodes[size_t(jb.wide) * 80];
+    std::memcpy(node + 0, &nb.lo[0], 4); std::memcpy(node + 4, &nb.lo[1], 4); std::memcpy(node + 8, &nb.lo[2], 4);
+    node[12] = uint8_t(int8_t(ex[0])); node[13] = uint8_t(int8_t(ex[1])); node[14] = uint8_t(int8_t(ex[2]));
+    uint8_t imask = 0;
+    uint32_t child_base = next_node;
+    uint32_t tri_base = uint32_t(out.order.size());
+    uint32_t tri_off = 0;
+    // internal children get consecutive node indices in slot order
+    for (int s = 0; s < 8; ++s) {
+      uint8_t* meta = node + 24 + s;
+      uint8_t* qlo[3] = {node + 32 + s, node + 40 + s, node + 48 + s};
+      uint8_t* qhi[3] = {node + 56 + s, node + 64 + s, node + 72 + s};
+      if (kid_in[s] < 0) { *meta = 0; for (int a = 0; a < 3; ++a) { *qlo[a] = 255; *qhi[a] = 0; } continue; }
+      const BNode& c = nd[size_t(kids[size_t(kid_in[s])])];
+      for (int a = 0; a < 3; ++a) {
+        float sc = pow2f(ex[a]);
+        float lo = nb.lo[a];
+        double ql = std::floor((double(c.box.lo[a]) - double(lo)) / double(sc));
+        double qh = std::ceil((double(c.box.hi[a]) - double(lo)) / double(sc));
+        int il = int(std::max(0.0, std::min(255.0, ql)));
+        int ih = int(std::max(0.0, std::min(255.0, qh)));
+        // the device decodes fma(q, 2^e, p) rounded once; widen until conservative
+        while (il > 0 && std::fma(float(il), sc, lo) > c.box.lo[a]) --il;
+        while (ih < 255 && std::fma(float(ih), sc, lo) < c.box.hi[a]) ++ih;
+        *qlo[a] = uint8_t(il); *qhi[a] = uint8_t(ih);
+      }
+      if (c.child >= 0) {
+        imask |= uint8_t(1u << s);
+        *meta = uint8_t((1u << 5) | uint32_t(24 + s));
+      } else {
+        int cnt = c.count;          // 0..3
+        uint8_t unary = cnt == 0 ? 0 : (cnt == 1 ? 1 : (cnt == 2 ? 3 : 7));
+        *meta = cnt == 0 ? 0 : uint8_t((unary << 5) | tri_off);
+        for (int k = 0; k < cnt; ++k) out.order.push_back(b.idx[size_t(c.first + k)]);
+        tri_off += uint32_t(cnt);
+      }
+    }
+    for (int s = 0; s < 8; ++s) {
+      if (kid_in[s] < 0) continue;
+      int32_t k = kids[size_t(kid_in[s])];
+      if (nd[size_t(k)].child >= 0) q.push_back({k, next_node++, jb.depth + 1});
+    }
+    node[15] = imask;
+    std::memcpy(node + 16, &child_base, 4);
+    std::memcpy(node + 20, &tri_base, 4);
+    if (out.nodes.size() < size_t(next_node) * 80) out.nodes.resize(size_t(next_node) * 80, 0);
+  }
+}
+
+}  // namespace
+
+void build_bvh_wide(const float* tri_pos, size_t n, BvhHost& out) {
+  auto t0 = std::chrono::steady_clock::now();
+  Builder b;
+  run_builder(b, tri_pos, n, 3);
+  WideOut w;
+  emit_wide(b, w);
+  out.nodes.resize(w.nodes.size() / 4);
+  std::memcpy(out.nodes.data(), w.nodes.data(), w.nodes.size());
+  out.order = w.order;
+  leaf_ordered_tris(tri_pos, out.order, out.tris);
+  out.depth = w.depth;
   out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 

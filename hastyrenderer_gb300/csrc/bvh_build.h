@@ -23,4 +23,12 @@ struct BvhHost {
 // tri_pos: 9 floats per triangle (v0, v1, v2). max_leaf: triangles per leaf.
 void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out);
 
+// Compressed 8-wide layout, 80 bytes per node (5 x float4):
+//   p.xyz (float grid origin), e.xyz (int8 exponents of the power-of-two grid
+//   step), inner-child mask (u8), first inner child (u32), first triangle
+//   (u32), meta (8 x u8: 0 empty; 001|24+slot inner; unary count|offset leaf),
+//   quantised child boxes qlo.x[8] qlo.y[8] qlo.z[8] qhi.x[8] qhi.y[8] qhi.z[8].
+// Leaves hold up to 3 triangles; triangles are stored in slot order.
+void build_bvh_wide(const float* tri_pos, size_t n, BvhHost& out);
+
 }  // namespace hasty

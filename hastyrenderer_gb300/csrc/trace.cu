@@ -1,32 +1,105 @@
-// Closest-hit ray queries over the binary BVH (the role of Embree's
-// rtcIntersect1 in core/src/Scene.cpp:281-303: tnear 1e-6, tfar +inf,
-// u/v = weights of the 2nd/3rd vertex). One thread per queued ray, stack of
-// 64 node links in registers/local memory, nearer child first.
+// Closest-hit ray queries (the role of Embree's rtcIntersect1 in
+// core/src/Scene.cpp:281-303: tnear 1e-6, tfar +inf, u/v = weights of the
+// triangle's 2nd/3rd vertex) over the compressed 8-wide BVH (default) or the
+// binary BVH. One thread per queued ray.
 //
 // The ray/triangle test is Moeller-Trumbore in Embree's sign conventions and
 // rounds every product and sum separately (no FMA contraction), so t, u, v
-// and the chosen triangle are the ones the CPU checker computes. Ties at
-// equal t go to the smaller triangle id. Box tests may contract; their exit
-// distance is padded by a few ulps so that no box holding the closest hit is
-// culled by rounding.
+// and the chosen triangle are the ones the CPU checker computes. The far
+// limit is applied to the divided distance and ties at equal t go to the
+// smaller triangle id, so the answer does not depend on traversal order.
+// Box tests round each step once and are padded by 1 +/- 2*gamma(3), so no
+// box that holds the closest hit is culled by rounding (Ize 2013).
+//
+// The traversal routines are host+device: the host build runs the same code
+// on the CPU for the loader/builder tests (hasty_debug_host_trace).
 #include <cuda_runtime.h>
+#include <cstring>
 #include "hasty_types.h"
 #include "wavefront.h"
 
 namespace hasty {
 namespace {
 
+#define HDI __host__ __device__ __forceinline__
+
 struct Hit { float t, u, v; int tri; };
 
-__device__ __forceinline__ float mulr(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float addr(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ float subr(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ float dotr(float ax, float ay, float az, float bx, float by, float bz) {
+HDI float mulr(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fmul_rn(a, b);
+#else
+  return a * b;        // host objects are built with -ffp-contract=off
+#endif
+}
+HDI float addr(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+HDI float subr(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+HDI float divr(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdiv_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+HDI uint32_t f2u(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(f);
+#else
+  uint32_t u; std::memcpy(&u, &f, 4); return u;
+#endif
+}
+HDI float u2f(uint32_t u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float f; std::memcpy(&f, &u, 4); return f;
+#endif
+}
+HDI uint32_t popc(uint32_t x) {
+#ifdef __CUDA_ARCH__
+  return __popc(x);
+#else
+  return uint32_t(__builtin_popcount(x));
+#endif
+}
+HDI uint32_t highest_bit(uint32_t x) {   // x != 0
+#ifdef __CUDA_ARCH__
+  return 31u - __clz(x);
+#else
+  return 31u - uint32_t(__builtin_clz(x));
+#endif
+}
+HDI uint32_t lowest_bit(uint32_t x) {    // x != 0
+#ifdef __CUDA_ARCH__
+  return uint32_t(__ffs(x)) - 1u;
+#else
+  return uint32_t(__builtin_ctz(x));
+#endif
+}
+HDI float4 ld(const float4* p) {
+#ifdef __CUDA_ARCH__
+  return __ldg(p);
+#else
+  return *p;
+#endif
+}
+HDI float dotr(float ax, float ay, float az, float bx, float by, float bz) {
   return addr(addr(mulr(ax, bx), mulr(ay, by)), mulr(az, bz));
 }
 
-__device__ __forceinline__ void tri_test(float ox, float oy, float oz, float dx, float dy, float dz,
-                                         float4 v0, float4 e1, float4 e2, Hit& best) {
+HDI void tri_test(float ox, float oy, float oz, float dx, float dy, float dz, float4 v0, float4 e1, float4 e2, Hit& best) {
   float nx = subr(mulr(e2.y, e1.z), mulr(e2.z, e1.y));
   float ny = subr(mulr(e2.z, e1.x), mulr(e2.x, e1.z));
   float nz = subr(mulr(e2.x, e1.y), mulr(e2.y, e1.x));
@@ -42,57 +115,57 @@ __device__ __forceinline__ void tri_test(float ox, float oy, float oz, float dx,
   if (!(den != 0.f && U >= 0.f && V >= 0.f && addr(U, V) <= ad)) return;
   float T = mulr(dotr(nx, ny, nz, cx, cy, cz), sg);
   if (!(mulr(ad, 1e-6f) < T)) return;
-  // compare divided distances: the closest hit then does not depend on the
-  // order in which triangles are tested
-  float t = __fdiv_rn(T, ad);
-  int id = __float_as_int(v0.w);
+  float t = divr(T, ad);
+  int id = int(f2u(v0.w));
   if (t < best.t || (t == best.t && (best.tri < 0 || id < best.tri))) {
-    best.t = t; best.u = __fdiv_rn(U, ad); best.v = __fdiv_rn(V, ad); best.tri = id;
+    best.t = t; best.u = divr(U, ad); best.v = divr(V, ad); best.tri = id;
   }
 }
 
-constexpr int kStack = 64;
-
-// Slab distance (b - o) / d with each step rounded once: relative error of a
-// few ulps whatever the magnitudes, so padding the interval keeps the test
-// conservative (robust traversal in the sense of Ize 2013).
-__device__ __forceinline__ float slab(float b, float o, float id) { return __fmul_rn(__fsub_rn(b, o), id); }
+HDI float slab(float b, float o, float id) { return mulr(subr(b, o), id); }
 
 constexpr float kPadHi = 1.0000008f;   // 1 + 2*gamma(3), rounded up
 constexpr float kPadLo = 0.9999992f;
+constexpr float kInf = __builtin_huge_valf();
 
-__device__ __forceinline__ Hit trace_binary(const SceneDev& sc, float ox, float oy, float oz, float dx, float dy, float dz) {
-  Hit best; best.t = __int_as_float(0x7f800000); best.u = best.v = 0.f; best.tri = -1;
+struct RayInv { float ix, iy, iz; };
+HDI RayInv inverse_dir(float dx, float dy, float dz) {
   const float eps = 1e-20f;
-  float idx = 1.0f / (fabsf(dx) > eps ? dx : copysignf(eps, dx));
-  float idy = 1.0f / (fabsf(dy) > eps ? dy : copysignf(eps, dy));
-  float idz = 1.0f / (fabsf(dz) > eps ? dz : copysignf(eps, dz));
+  RayInv r;
+  r.ix = 1.0f / (fabsf(dx) > eps ? dx : copysignf(eps, dx));
+  r.iy = 1.0f / (fabsf(dy) > eps ? dy : copysignf(eps, dy));
+  r.iz = 1.0f / (fabsf(dz) > eps ? dz : copysignf(eps, dz));
+  return r;
+}
+
+// ---------------------------------------------------------- binary BVH ----
+constexpr int kStack = 64;
+
+HDI Hit trace_binary(const float4* nodes, const float4* tris, float ox, float oy, float oz, float dx, float dy, float dz) {
+  Hit best; best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
+  RayInv iv = inverse_dir(dx, dy, dz);
   int stack[kStack];
   int sp = 0;
   int link = 0;   // root (always an inner node)
-  const float4* nodes = sc.nodes;
-  const float4* tris = sc.isect_tris;
   while (true) {
     while (link >= 0) {
-      float4 n0 = __ldg(&nodes[4 * link + 0]);
-      float4 n1 = __ldg(&nodes[4 * link + 1]);
-      float4 n2 = __ldg(&nodes[4 * link + 2]);
-      float4 n3 = __ldg(&nodes[4 * link + 3]);
+      float4 n0 = ld(&nodes[4 * link + 0]);
+      float4 n1 = ld(&nodes[4 * link + 1]);
+      float4 n2 = ld(&nodes[4 * link + 2]);
+      float4 n3 = ld(&nodes[4 * link + 3]);
       float tlim = best.t * kPadHi;
-      float a0 = slab(n0.x, ox, idx), a1 = slab(n0.y, ox, idx);
-      float b0 = slab(n0.z, oy, idy), b1 = slab(n0.w, oy, idy);
-      float c0 = slab(n2.x, oz, idz), c1 = slab(n2.y, oz, idz);
+      float a0 = slab(n0.x, ox, iv.ix), a1 = slab(n0.y, ox, iv.ix);
+      float b0 = slab(n0.z, oy, iv.iy), b1 = slab(n0.w, oy, iv.iy);
+      float c0 = slab(n2.x, oz, iv.iz), c1 = slab(n2.y, oz, iv.iz);
       float t0min = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f)) * kPadLo;
-      float t0max = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fmaxf(c0, c1)) * kPadHi;
-      t0max = fminf(t0max, tlim);
-      float d0 = slab(n1.x, ox, idx), d1 = slab(n1.y, ox, idx);
-      float e0 = slab(n1.z, oy, idy), e1v = slab(n1.w, oy, idy);
-      float f0 = slab(n2.z, oz, idz), f1 = slab(n2.w, oz, idz);
+      float t0max = fminf(fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fmaxf(c0, c1)) * kPadHi, tlim);
+      float d0 = slab(n1.x, ox, iv.ix), d1 = slab(n1.y, ox, iv.ix);
+      float e0 = slab(n1.z, oy, iv.iy), e1v = slab(n1.w, oy, iv.iy);
+      float f0 = slab(n2.z, oz, iv.iz), f1 = slab(n2.w, oz, iv.iz);
       float t1min = fmaxf(fmaxf(fminf(d0, d1), fminf(e0, e1v)), fmaxf(fminf(f0, f1), 0.0f)) * kPadLo;
-      float t1max = fminf(fminf(fmaxf(d0, d1), fmaxf(e0, e1v)), fmaxf(f0, f1)) * kPadHi;
-      t1max = fminf(t1max, tlim);
+      float t1max = fminf(fminf(fminf(fmaxf(d0, d1), fmaxf(e0, e1v)), fmaxf(f0, f1)) * kPadHi, tlim);
       bool h0 = t0min <= t0max, h1 = t1min <= t1max;
-      int l0 = __float_as_int(n3.x), l1 = __float_as_int(n3.y);
+      int l0 = int(f2u(n3.x)), l1 = int(f2u(n3.y));
       if (h0 && h1) {
         int far_l = l1;
         link = l0;
@@ -112,16 +185,100 @@ __device__ __forceinline__ Hit trace_binary(const SceneDev& sc, float ox, float 
     int first = code >> 3, cnt = code & 7;
     for (int k = 0; k < cnt; ++k) {
       int ti = first + k;
-      float4 v0 = __ldg(&tris[3 * ti + 0]);
-      float4 e1 = __ldg(&tris[3 * ti + 1]);
-      float4 e2 = __ldg(&tris[3 * ti + 2]);
-      tri_test(ox, oy, oz, dx, dy, dz, v0, e1, e2, best);
+      tri_test(ox, oy, oz, dx, dy, dz, ld(&tris[3 * ti]), ld(&tris[3 * ti + 1]), ld(&tris[3 * ti + 2]), best);
     }
     if (sp == 0) return best;
     link = stack[--sp];
   }
 }
 
+// ------------------------------------------------- compressed 8-wide BVH ----
+// Node groups of Ylitie, Karras and Laine 2017: (base index, mask) where bits
+// 24..31 are children still to visit, each at bit 24 + (slot ^ octant) so the
+// highest bit is the nearest child, and bits 0..7 hold the parent's
+// inner-child mask; for triangle groups bits 0..23 are triangles to test.
+// Child boxes are decoded as the builder verified them (fma of the 8-bit
+// coordinate and the power-of-two step) and tested with the padded slabs.
+constexpr int kWideStack = 32;
+
+HDI uint32_t byte_of(uint32_t w, uint32_t k) { return (w >> (8 * k)) & 0xFFu; }
+
+HDI Hit trace_wide(const float4* nodes, const float4* tris, float ox, float oy, float oz, float dx, float dy, float dz) {
+  Hit best; best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
+  RayInv iv = inverse_dir(dx, dy, dz);
+  const uint32_t oct = (iv.ix < 0.f ? 4u : 0u) | (iv.iy < 0.f ? 2u : 0u) | (iv.iz < 0.f ? 1u : 0u);
+  const uint32_t oct4 = oct * 0x01010101u;
+  uint2 stack[kWideStack];
+  int sp = 0;
+  uint2 ng = make_uint2(0u, 0x80000000u);
+  uint2 tg = make_uint2(0u, 0u);
+  while (true) {
+    while (tg.y) {
+      uint32_t b = lowest_bit(tg.y);
+      tg.y &= tg.y - 1u;
+      int ti = int(tg.x + b);
+      tri_test(ox, oy, oz, dx, dy, dz, ld(&tris[3 * ti]), ld(&tris[3 * ti + 1]), ld(&tris[3 * ti + 2]), best);
+    }
+    if (ng.y <= 0x00FFFFFFu) {
+      if (sp == 0) break;
+      ng = stack[--sp];
+    }
+    uint32_t bit = highest_bit(ng.y);
+    uint32_t slot = (bit - 24u) ^ oct;
+    uint32_t imask = ng.y & 0xFFu;
+    uint32_t node = ng.x + popc(imask & ~(0xFFFFFFFFu << slot));
+    ng.y &= ~(1u << bit);
+    if (ng.y > 0x00FFFFFFu && sp < kWideStack) stack[sp++] = ng;
+
+    float4 f0 = ld(&nodes[5 * node + 0]);
+    float4 f1 = ld(&nodes[5 * node + 1]);
+    float4 f2 = ld(&nodes[5 * node + 2]);
+    float4 f3 = ld(&nodes[5 * node + 3]);
+    float4 f4 = ld(&nodes[5 * node + 4]);
+    uint32_t eword = f2u(f0.w);
+    int ex = int(int8_t(eword & 0xFFu)), ey = int(int8_t((eword >> 8) & 0xFFu)), ez = int(int8_t((eword >> 16) & 0xFFu));
+    uint32_t node_imask = eword >> 24;
+    float sx = u2f(uint32_t(ex + 127) << 23), sy = u2f(uint32_t(ey + 127) << 23), sz = u2f(uint32_t(ez + 127) << 23);
+    uint32_t child_base = f2u(f1.x), tri_base = f2u(f1.y);
+    uint32_t meta_w[2] = {f2u(f1.z), f2u(f1.w)};
+    uint32_t qlx[2] = {f2u(f2.x), f2u(f2.y)}, qly[2] = {f2u(f2.z), f2u(f2.w)};
+    uint32_t qlz[2] = {f2u(f3.x), f2u(f3.y)}, qhx[2] = {f2u(f3.z), f2u(f3.w)};
+    uint32_t qhy[2] = {f2u(f4.x), f2u(f4.y)}, qhz[2] = {f2u(f4.z), f2u(f4.w)};
+    float tlim = best.t * kPadHi;
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      uint32_t meta4 = meta_w[h];
+      uint32_t inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;     // 24..31 marks an inner child
+      uint32_t inner_mask4 = (inner4 >> 4) * 0xFFu;
+      uint32_t bit_index4 = (meta4 ^ (oct4 & inner_mask4)) & 0x1F1F1F1Fu;
+      uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k) {
+        float lx = fmaf(float(byte_of(qlx[h], k)), sx, f0.x), hx = fmaf(float(byte_of(qhx[h], k)), sx, f0.x);
+        float ly = fmaf(float(byte_of(qly[h], k)), sy, f0.y), hy = fmaf(float(byte_of(qhy[h], k)), sy, f0.y);
+        float lz = fmaf(float(byte_of(qlz[h], k)), sz, f0.z), hz = fmaf(float(byte_of(qhz[h], k)), sz, f0.z);
+        float a0 = slab(lx, ox, iv.ix), a1 = slab(hx, ox, iv.ix);
+        float b0 = slab(ly, oy, iv.iy), b1 = slab(hy, oy, iv.iy);
+        float c0 = slab(lz, oz, iv.iz), c1 = slab(hz, oz, iv.iz);
+        float tmin = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f)) * kPadLo;
+        float tmax = fminf(fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fmaxf(c0, c1)) * kPadHi, tlim);
+        if (tmin <= tmax) hitmask |= byte_of(child_bits4, k) << byte_of(bit_index4, k);
+      }
+    }
+    ng = make_uint2(child_base, (hitmask & 0xFF000000u) | node_imask);
+    tg = make_uint2(tri_base, hitmask & 0x00FFFFFFu);
+  }
+  return best;
+}
+
+template <int KIND>
+HDI Hit trace_any(const float4* nodes, const float4* tris, float ox, float oy, float oz, float dx, float dy, float dz) {
+  if (KIND == 1) return trace_wide(nodes, tris, ox, oy, oz, dx, dy, dz);
+  return trace_binary(nodes, tris, ox, oy, oz, dx, dy, dz);
+}
+
+template <int KIND>
 __global__ void __launch_bounds__(128) k_trace(SceneDev sc, PathsDev P, int q) {
   uint32_t n = P.counts[2 + q];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -129,15 +286,16 @@ __global__ void __launch_bounds__(128) k_trace(SceneDev sc, PathsDev P, int q) {
   if (i >= n) return;
   int rid = P.rq[q][i];
   float4 o = P.ray_o[rid], d = P.ray_d[rid];
-  Hit h = trace_binary(sc, o.x, o.y, o.z, d.x, d.y, d.z);
+  Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
   P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
 }
 
+template <int KIND>
 __global__ void k_trace_rays(SceneDev sc, const float* rays, int n, float4* hits) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float* r = rays + 6 * int64_t(i);
-  Hit h = trace_binary(sc, r[0], r[1], r[2], r[3], r[4], r[5]);
+  Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, r[0], r[1], r[2], r[3], r[4], r[5]);
   hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
 }
 
@@ -145,12 +303,27 @@ __global__ void k_trace_rays(SceneDev sc, const float* rays, int n, float4* hits
 
 void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cudaStream_t st) {
   int blocks = (max_rays + 127) / 128;
-  k_trace<<<blocks > 0 ? blocks : 1, 128, 0, st>>>(sc, p, q);
+  if (blocks < 1) blocks = 1;
+  if (sc.bvh_kind == 1) k_trace<1><<<blocks, 128, 0, st>>>(sc, p, q);
+  else k_trace<0><<<blocks, 128, 0, st>>>(sc, p, q);
 }
 
 void launch_trace_rays(const SceneDev& sc, const float* rays, int n, float4* hits, cudaStream_t st) {
   if (n <= 0) return;
-  k_trace_rays<<<(n + 127) / 128, 128, 0, st>>>(sc, rays, n, hits);
+  if (sc.bvh_kind == 1) k_trace_rays<1><<<(n + 127) / 128, 128, 0, st>>>(sc, rays, n, hits);
+  else k_trace_rays<0><<<(n + 127) / 128, 128, 0, st>>>(sc, rays, n, hits);
+}
+
+// CPU run of the same traversal over host copies of the BVH arrays.
+void host_trace_rays(int kind, const float4* nodes, const float4* tris, const float* rays, int64_t n, float4* hits) {
+  for (int64_t i = 0; i < n; ++i) {
+    const float* r = rays + 6 * i;
+    Hit h = kind == 1 ? trace_wide(nodes, tris, r[0], r[1], r[2], r[3], r[4], r[5])
+                      : trace_binary(nodes, tris, r[0], r[1], r[2], r[3], r[4], r[5]);
+    int32_t id = h.tri;
+    float w; std::memcpy(&w, &id, 4);
+    hits[i] = make_float4(h.t, h.u, h.v, w);
+  }
 }
 
 }  // namespace hasty

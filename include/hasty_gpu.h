@@ -43,6 +43,9 @@ extern "C" {
 #define HASTY_ERR_STOPPED (-6)    /* job was stopped before the requested passes ran */
 #define HASTY_ERR_MISSING (-7)    /* entry point unavailable in this build */
 
+/* hasty_ctx_create flags */
+#define HASTY_CTX_BINARY_BVH 1u   /* binary BVH instead of the compressed 8-wide one */
+
 #define HASTY_AOV_COLOR 0
 #define HASTY_AOV_NORMAL 1
 #define HASTY_AOV_ALBEDO 2
@@ -115,6 +118,11 @@ int hasty_job_write_outputs(hasty_job* job, const char* out_dir, int write_pfm);
 /* Closest hits of n rays given as n x 6 host floats (origin, direction):
  * global triangle index (-1 miss), t, u, v. */
 int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* tri, float* t, float* u, float* v);
+/* The same closest-hit traversal run on the CPU (no device needed): loads the
+ * job on the host, builds the BVH (kind 0 binary, 1 compressed 8-wide) and
+ * answers n rays. info (may be NULL): triangles, nodes, tree depth. */
+int hasty_debug_host_trace(const char* render_job_path, int kind, const float* rays, size_t n, int32_t* tri, float* t,
+                           float* u, float* v, int64_t* info);
 /* Triangle index -> (OBJ shape = Embree geomID, face = primID). */
 int hasty_debug_tri_ids(hasty_job* job, int32_t* geom, int32_t* prim, size_t n);
 /* BSDF known-answer evaluation on the device. which: 0 sample, 1 evaluate, 2 pdf.

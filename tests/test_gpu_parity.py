@@ -55,7 +55,7 @@ def test_intersect_matches_checker(name, lo, hi):
     b = ora.intersect(rays, brute=True)
     assert np.array_equal(c[0], b[0])
     assert _check_hits(g, c) == 1.0
-    assert (c[0] >= 0).mean() > 0.3
+    assert (c[0] >= 0).mean() > 0.2
 
 
 def test_intersect_full_size_scene(tmp_path):
