@@ -165,6 +165,7 @@ def main():
     ap.add_argument("--spp-per-step", type=int, default=SPP_PER_STEP)
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--bvh", default="wide", choices=["wide", "binary"])
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -194,7 +195,7 @@ def main():
     import torch
     from hastyrenderer_gb300 import Context, RenderJob
     torch.cuda.init()
-    ctx = Context(local_rank)
+    ctx = Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0)
 
     # ---- end to end through the C ABI: load (parse, BVH, upload) + steps with read-back
     if dist is not None:
@@ -271,7 +272,7 @@ def main():
             "metric": "samples/s", "value": samples * world / t, "unit": "samples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "spp_per_step": args.spp_per_step, "width": W, "height": H,
+            "config": {"workload": WORKLOAD, "spp_per_step": args.spp_per_step, "width": W, "height": H, "bvh": args.bvh,
                        "max_depth": info.max_depth, "triangles": info.n_triangles,
                        "l2": "working set > L2 (path state + BVH), no flush", "parallelism": f"replicas x{world}"},
             "mrays_per_s": rays * world / t * 1e-6,

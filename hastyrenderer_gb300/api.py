@@ -22,9 +22,11 @@ __all__ = ["Context", "RenderJob", "debug_bsdf", "AOV_COLOR", "AOV_NORMAL", "AOV
 class Context:
     """One CUDA device."""
 
-    def __init__(self, device: int = 0):
+    BINARY_BVH = 1   # HASTY_CTX_BINARY_BVH
+
+    def __init__(self, device: int = 0, flags: int = 0):
         self._h = ctypes.c_void_p()
-        check(native.lib().hasty_ctx_create(device, 0, ctypes.byref(self._h)))
+        check(native.lib().hasty_ctx_create(device, int(flags), ctypes.byref(self._h)))
 
     def close(self):
         if self._h:

@@ -190,6 +190,7 @@ void upload_scene(hasty_job& j) {
   s.n_light_tris = int32_t(h.light_tris.size());
   s.light_tris = j.upload(h.light_tris);
   s.light_cdf = j.upload(h.light_cdf);
+  s.light_guide = j.upload(build_cdf_guide(h.light_cdf, s.light_guide_log2));
   s.light_pdf_area = h.light_tris.empty() ? 0.0f : 1.0f / h.total_light_area;
   EnvDev& e = s.env;
   e.is_texture = h.env_texture ? 1 : 0;
@@ -198,6 +199,7 @@ void upload_scene(hasty_job& j) {
   e.texels = j.upload(h.env_texels);
   e.weights = j.upload(h.env_weights);
   e.cdf = j.upload(h.env_cdf);
+  e.guide = j.upload(build_cdf_guide(h.env_cdf, e.guide_log2));
   e.value_sum = h.env_value_sum;
   s.cam = h.cam;
   const RenderSettingsH& st = h.settings;

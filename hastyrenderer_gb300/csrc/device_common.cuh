@@ -124,14 +124,26 @@ struct ReplayRng {
 };
 
 // std::discrete_distribution draw as libstdc++ performs it: one
-// generate_canonical<double,53> (two 32-bit draws), lower_bound in the table.
-template <class R> __device__ __forceinline__ uint32_t sample_cdf(const double* cdf, uint32_t n, R& r) {
+// generate_canonical<double,53> (two 32-bit draws, low word first; the sum
+// u1 + u2*2^32 rounded once to double, then scaled by 2^-64, which is what
+// converting the 64-bit integer and multiplying gives), then lower_bound in
+// the cumulative table. `guide` (optional, K+1 entries, K a power of two)
+// holds for bucket k the first index whose cumulative value is >= k/K, so the
+// lower bound of u lies in [guide[k], guide[k+1]] with k = floor(u*K) exact.
+template <class R> __device__ __forceinline__ uint32_t sample_cdf(const double* cdf, uint32_t n, R& r,
+                                                                  const uint32_t* guide = nullptr, uint32_t log2k = 0) {
   if (n < 2 || cdf == nullptr) return 0u;
-  double sum = double(r.next());
-  sum = sum + double(r.next()) * 4294967296.0;
-  double u = sum / 18446744073709551616.0;
+  uint64_t lo32 = r.next();
+  uint64_t hi32 = r.next();
+  double u = __ull2double_rn((hi32 << 32) | lo32) * 5.421010862427522170037264004349708557e-20;   // 2^-64
   if (u >= 1.0) u = 0.99999999999999988898;   // nextafter(1, 0)
   uint32_t lo = 0, hi = n;
+  if (guide) {
+    uint32_t k = uint32_t(u * double(1u << log2k));
+    lo = guide[k];
+    hi = guide[k + 1] + 1u;
+    hi = hi < n ? hi : n;
+  }
   while (lo < hi) { uint32_t mid = (lo + hi) >> 1; if (cdf[mid] < u) lo = mid + 1; else hi = mid; }
   return lo < n ? lo : n - 1;
 }
@@ -376,66 +388,62 @@ __device__ __forceinline__ V3 shading_normal(const SceneDev& sc, const MaterialD
   return ns * side;
 }
 
+// Per-vertex shading frame shared by evaluate / pdf / sample: the shading
+// normal for wo (getShadingNormal), texture lookups, alpha and the rotated
+// anisotropic frame (computeAnisotropyParameters). Each quantity is computed
+// exactly as the reference computes it inside each of those calls.
+struct ShadeCtx { V3 ns, alb, tan, bit; float rough, met, alpha, at, ab, ngwo, nswo; };
+__device__ __forceinline__ ShadeCtx shade_ctx(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wo) {
+  ShadeCtx c;
+  c.ngwo = dot(it.ng, wo);
+  c.ns = shading_normal(sc, m, it, wo, c.ngwo);
+  c.nswo = dot(c.ns, wo);
+  c.alb = mat_albedo(sc, m, it);
+  c.rough = mat_scalar(sc, m.roughness, m.roughness_tex, it);
+  c.met = mat_scalar(sc, m.metallic, m.metallic_tex, it);
+  c.alpha = compute_alpha(c.rough);
+  anisotropy_params(it, c.ns, c.alpha, m.anisotropy, c.at, c.ab, c.tan, c.bit);
+  return c;
+}
+
 struct BsdfEval { V3 fD, fC; };
 // PrincipledBRDF::evaluate, BRDF.cpp:630-679
-__device__ BsdfEval bsdf_eval(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wo, V3 wi) {
-  float ngwo = dot(it.ng, wo);
-  V3 ns = shading_normal(sc, m, it, wo, ngwo);
-  float nswi = dot(ns, wi);
-  V3 alb = mat_albedo(sc, m, it);
-  float rough = mat_scalar(sc, m.roughness, m.roughness_tex, it);
-  float alpha = compute_alpha(rough);
-  float met = mat_scalar(sc, m.metallic, m.metallic_tex, it);
-  float nsc = normal_scale(wi, ns, it.ng);
+__device__ __forceinline__ BsdfEval bsdf_eval(const ShadeCtx& c, const MaterialDev& m, const Inter& it, V3 wo, V3 wi) {
+  float nswi = dot(c.ns, wi);
+  float nsc = normal_scale(wi, c.ns, it.ng);
   BsdfEval e;
-  e.fD = eval_diffuse(nswi, alb, nsc, met, m.specular, m.transmission);
-  float at, ab; V3 tan, bit;
-  anisotropy_params(it, ns, alpha, m.anisotropy, at, ab, tan, bit);
-  e.fC = eval_concentrated(nswi, alb, met, m.specular, m.transmission, wo, wi, alpha, at, ab, tan, bit, ns, nsc, false, 0.0f);
+  e.fD = eval_diffuse(nswi, c.alb, nsc, c.met, m.specular, m.transmission);
+  e.fC = eval_concentrated(nswi, c.alb, c.met, m.specular, m.transmission, wo, wi, c.alpha, c.at, c.ab, c.tan, c.bit, c.ns,
+                           nsc, false, 0.0f);
   return e;
 }
 
 // PrincipledBRDF::evaluateSamplePDF, BRDF.cpp:702-742 (nominal IOR)
-__device__ float bsdf_pdf(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wo, V3 wi, float eta_out) {
-  float ngwo = dot(it.ng, wo);
-  V3 ns = shading_normal(sc, m, it, wo, ngwo);
-  float nswo = dot(ns, wo);
-  float rough = mat_scalar(sc, m.roughness, m.roughness_tex, it);
-  float alpha = compute_alpha(rough);
-  float met = mat_scalar(sc, m.metallic, m.metallic_tex, it);
-  bool from_out = ngwo >= 0.0f;
+__device__ __forceinline__ float bsdf_pdf(const ShadeCtx& c, const MaterialDev& m, V3 wo, V3 wi, float eta_out) {
+  bool from_out = c.ngwo >= 0.0f;
   float eo = from_out ? eta_out : m.ior, et = from_out ? m.ior : eta_out;
-  Prob p = compute_probability(met, m.specular, m.transmission, nswo, eo, et);
-  if (alpha == 0.0f) return p.pD * hemisphere_cos_pdf(ns, wi);
-  float at, ab; V3 tan, bit;
-  anisotropy_params(it, ns, alpha, m.anisotropy, at, ab, tan, bit);
-  float ps = ggx_vndf_density(ns, at, ab, tan, bit, wo, wi);
-  float pd = hemisphere_cos_pdf(ns, wi);
+  Prob p = compute_probability(c.met, m.specular, m.transmission, c.nswo, eo, et);
+  if (c.alpha == 0.0f) return p.pD * hemisphere_cos_pdf(c.ns, wi);
+  float ps = ggx_vndf_density(c.ns, c.at, c.ab, c.tan, c.bit, wo, wi);
+  float pd = hemisphere_cos_pdf(c.ns, wi);
   return p.pS * ps + p.pD * pd;
 }
 
 struct BsdfSample { bool outside; V3 dir, thrD, thrC; float pdf; };
 // PrincipledBRDF::sample (member + static), BRDF.cpp:397-579, 681-700
 template <class R>
-__device__ BsdfSample bsdf_sample(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wo, int wl, float eta_out,
+__device__ BsdfSample bsdf_sample(const ShadeCtx& c, const MaterialDev& m, const Inter& it, V3 wo, int wl, float eta_out,
                                   R& r, int& capped) {
   BsdfSample res;
-  V3 alb = mat_albedo(sc, m, it);
-  float rough = mat_scalar(sc, m.roughness, m.roughness_tex, it);
-  float met = mat_scalar(sc, m.metallic, m.metallic_tex, it);
-  float ngwo = dot(it.ng, wo);
-  V3 ns = shading_normal(sc, m, it, wo, ngwo);
+  const V3 ns = c.ns, alb = c.alb, tan = c.tan, bit = c.bit;
+  const float met = c.met, alpha = c.alpha, at = c.at, ab = c.ab, nswo = c.nswo;
   float eta_mat = mat_ior(m, wl);
   float s = m.specular, t = m.transmission;
-  float nswo = dot(ns, wo);
-  float alpha = compute_alpha(rough);
-  res.outside = ngwo >= 0.0f;
+  res.outside = c.ngwo >= 0.0f;
   float eo = res.outside ? eta_out : eta_mat;
   float er = res.outside ? eta_mat : eta_out;
   Prob p = compute_probability(met, s, t, nswo, eo, er);
   if (p.none) { res.dir = V3(1.f, 0.f, 0.f); res.pdf = 0.0f; return res; }
-  float at, ab; V3 tan, bit;
-  anisotropy_params(it, ns, alpha, m.anisotropy, at, ab, tan, bit);
   V3 fD, fC;
   float xi = r.u01();
   int strat = xi < p.pR ? 3 : (xi < (p.pR + p.pS) ? 2 : 1);
@@ -602,7 +610,7 @@ template <class R> __device__ __forceinline__ V3 env_sample(const SceneDev& sc, 
   uint32_t n = uint32_t(e.w) * uint32_t(e.h);
   V3 dir; float sin_t = 0.f;
   for (int k = 0; k < kMaxTrials; ++k) {
-    uint32_t idx = sample_cdf(e.cdf, n, r);
+    uint32_t idx = sample_cdf(e.cdf, n, r, e.guide, e.guide_log2);
     uint32_t W = uint32_t(e.w), H = uint32_t(e.h);
     uint32_t x = idx % W, y = idx / W;
     float hf = float(H), wf = float(W);

@@ -50,6 +50,8 @@ struct EnvDev {
   const float* texels;        // w*h*3, row 0 = zenith
   const float* weights;       // w*h, |rgb| * sin(theta)
   const double* cdf;          // w*h cumulative probabilities (last = 1)
+  const uint32_t* guide;      // 2^guide_log2 + 1 bucket starts into cdf (exact lower_bound search ranges)
+  uint32_t guide_log2;
   float value_sum;
 };
 
@@ -85,6 +87,8 @@ struct SceneDev {
   int32_t n_light_tris;
   const int32_t* light_tris;
   const double* light_cdf;    // empty (nullptr) when fewer than 2 lights
+  const uint32_t* light_guide;
+  uint32_t light_guide_log2;
   float light_pdf_area;       // 1 / total light area (Scene.cpp:512)
   EnvDev env;
   CameraDev cam;

@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDes
             } else {
               tl = tl / (1.0f - qrr);
               V3 wo = -d;
+              const ShadeCtx cx = shade_ctx(sc, m, it, wo);
               int wl = int((flags & PF_WL_MASK) >> PF_WL_SHIFT) - 1;
               float eta_out = M.outside_ior(it, wo);
               bool next_ok = depth + 1 < sc.max_depth;
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDes
                 float xi = r.u01();
                 V3 oL, dL; int ltri = -1;
                 if (xi < sc.p_surface) {
-                  uint32_t kk = sample_cdf(sc.light_cdf, uint32_t(sc.n_light_tris), r);
+                  uint32_t kk = sample_cdf(sc.light_cdf, uint32_t(sc.n_light_tris), r, sc.light_guide, sc.light_guide_log2);
                   ltri = sc.light_tris[kk];
                   V3 bb = triangle_uniform(r);
                   const float* lp = sc.tri_pos + 9 * int64_t(ltri);
@@ -219,10 +220,10 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDes
                   oL = ray_x(it, dot(it.ng, dL) >= 0.0f);
                 }
                 if (next_ok) {
-                  BsdfEval ev = bsdf_eval(sc, m, it, wo, dL);
+                  BsdfEval ev = bsdf_eval(cx, m, it, wo, dL);
                   V3 c3 = cwise(tl, ev.fD + ev.fC) * fabsf(dot(dL, it.ng));
                   if (!is_zero(c3)) {
-                    float pBL = bsdf_pdf(sc, m, it, wo, dL, eta_out);
+                    float pBL = bsdf_pdf(cx, m, wo, dL, eta_out);
                     Media ML = M;
                     overflow |= ML.update(sc, m, it, wo, dL, wl);
                     P.nee_c[s] = f4(cwise(thr, c3), pBL);
@@ -241,7 +242,7 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDes
                 if (xi < p3) wl = 0; else if (xi < p3 + p3) wl = 1; else wl = 2;
                 prob = p3;
               }
-              BsdfSample bs = bsdf_sample(sc, m, it, wo, wl, eta_out, r, capped);
+              BsdfSample bs = bsdf_sample(cx, m, it, wo, wl, eta_out, r, capped);
               if (bs.pdf != 0.0f) {
                 V3 t2 = cwise(tl, bs.thrD / prob + bs.thrC / prob);
                 if (!is_zero(t2) && next_ok) {
@@ -371,19 +372,19 @@ __global__ void k_debug_bsdf(int which, const float* in, int n, const uint32_t* 
   if (which == 0) {
     ReplayRng r{replay + int64_t(c) * n_replay, uint32_t(n_replay), 0u};
     int capped = 0;
-    BsdfSample s = bsdf_sample(sc, m, it, wo, wl, eta, r, capped);
+    BsdfSample s = bsdf_sample(shade_ctx(sc, m, it, wo), m, it, wo, wl, eta, r, capped);
     o[0] = s.outside ? 1.f : 0.f;
     o[1] = s.dir.x; o[2] = s.dir.y; o[3] = s.dir.z;
     o[4] = s.thrD.x; o[5] = s.thrD.y; o[6] = s.thrD.z;
     o[7] = s.thrC.x; o[8] = s.thrC.y; o[9] = s.thrC.z;
     o[10] = s.pdf; o[11] = float(r.pos);
   } else if (which == 1) {
-    BsdfEval e = bsdf_eval(sc, m, it, wo, wi);
+    BsdfEval e = bsdf_eval(shade_ctx(sc, m, it, wo), m, it, wo, wi);
     V3 ns = shading_normal(sc, m, it, wo, dot(it.ng, wo));
     o[0] = e.fD.x; o[1] = e.fD.y; o[2] = e.fD.z; o[3] = e.fC.x; o[4] = e.fC.y; o[5] = e.fC.z;
     o[6] = ns.x; o[7] = ns.y; o[8] = ns.z;
   } else {
-    o[0] = bsdf_pdf(sc, m, it, wo, wi, eta);
+    o[0] = bsdf_pdf(shade_ctx(sc, m, it, wo), m, wo, wi, eta);
   }
 }
 }  // namespace

@@ -370,6 +370,23 @@ std::vector<double> build_discrete_cdf(const float* w, size_t n) {
   return cdf;
 }
 
+std::vector<uint32_t> build_cdf_guide(const std::vector<double>& cdf, uint32_t& log2k) {
+  std::vector<uint32_t> g;
+  log2k = 0;
+  size_t n = cdf.size();
+  if (n < 2) return g;
+  while ((size_t(1) << log2k) < n && log2k < 22) ++log2k;
+  size_t K = size_t(1) << log2k;
+  g.resize(K + 1);
+  size_t i = 0;
+  for (size_t k = 0; k <= K; ++k) {
+    double x = double(k) / double(K);
+    while (i < n - 1 && cdf[i] < x) ++i;
+    g[k] = uint32_t(i);
+  }
+  return g;
+}
+
 float halton_value(uint32_t base, uint32_t k) {
   uint32_t i = k + 1, n = 0, d = 1;
   while (i) { n = n * base + i % base; i /= base; d *= base; }

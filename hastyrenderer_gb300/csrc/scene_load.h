@@ -69,6 +69,11 @@ void load_render_job(const std::string& job_path, HostScene& out);
 // two weights: empty (the distribution then returns 0 without drawing).
 std::vector<double> build_discrete_cdf(const float* w, size_t n);
 
+// Bucket starts for an exact lower_bound over `cdf`: with K = 2^log2k
+// buckets, entry k is the first index whose value is >= k/K (K+1 entries).
+// Empty for tables with fewer than two entries.
+std::vector<uint32_t> build_cdf_guide(const std::vector<double>& cdf, uint32_t& log2k);
+
 // Halton offsets of pass k (core/include/Hasty/Random.h:14-63).
 float halton_value(uint32_t base, uint32_t k);
 

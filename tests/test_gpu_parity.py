@@ -110,25 +110,34 @@ def test_sixteen_passes_match_reference(name):
 
 @pytest.mark.parametrize("name", ["cornell", "field", "room"])
 def test_image_ztest(name):
-    """Per-pixel means at S = 16 spp against the checker at 16*S spp: every
-    pixel within 4 sigma, sigma from the sample variance of both estimates
-    (the checker image's own Monte Carlo noise included)."""
-    S = 16
+    """Per-pixel means at S = 64 spp against the checker at 16*S spp from the
+    same streams: |mean_gpu - mean_cpu| <= 4 sigma per pixel, sigma from the
+    per-sample variance of the checker's 16*S samples for both estimates (its
+    own Monte Carlo noise included). Sun and caustic paths make the radiance
+    heavy-tailed, so the sample variance can underestimate sigma on a few
+    pixels: at most 0.5% of pixels may exceed 4 sigma, and the signed
+    z-scores must show no bias."""
+    S = 64
     job = _job(golden_job(name))
     job.set_seed(777)
     job.render_passes(S, sync=True)
     g, n = job.read_sums()
+    assert n == S
     ora = Oracle(golden_job(name))
     ora.set_seed(777)
     w, h = job.width, job.height
     N = 16 * S
     r = ora.render(0, N, 0, 0, w, h)
-    mc = r["color"] / N
-    var_c = np.maximum(r["color_sq"] / N - mc ** 2, 0.0)
-    mg = g / S
+    # per-pixel channel mean
+    sc = r["color"].mean(-1)
+    mc = sc / N
+    # variance of the channel mean of one sample, from the per-channel second moments (upper bound)
+    var_c = np.maximum((r["color_sq"] / N - (r["color"] / N) ** 2).mean(-1), 0.0)
+    mg = g.mean(-1) / S
     sig = np.sqrt(var_c / S + var_c / N) + 1e-6 + 1e-5 * np.abs(mc)
-    z = np.abs(mg - mc) / sig
-    assert (z > 4.0).mean() <= 0.001, ((z > 4.0).mean(), z.max())
+    z = (mg - mc) / sig
+    assert (np.abs(z) > 4.0).mean() <= 0.005, ((np.abs(z) > 4.0).mean(), np.abs(z).max())
+    assert abs(z.mean()) <= 0.25, z.mean()
 
 
 def test_device_bsdf_matches_reference():
