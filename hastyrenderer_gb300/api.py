@@ -180,3 +180,18 @@ def host_trace(job_path: str, rays: np.ndarray, kind: int = 1):
     check(native.lib().hasty_debug_host_trace(job_path.encode(), kind, r.ctypes.data, n, tri.ctypes.data, t.ctypes.data,
                                                u.ctypes.data, v.ctypes.data, info.ctypes.data))
     return tri, t, u, v, {"triangles": int(info[0]), "nodes": int(info[1]), "depth": int(info[2])}
+
+
+def batch_render(jobs, passes, paths_in_flight: int = 0, regen_fraction: float = 0.0, max_iterations: int = 0,
+                 ctx: Context | None = None) -> dict:
+    """Renders passes[i] further passes of jobs[i] in one multi-job run (path
+    regeneration over a shared pool; one CUDA-graph launch); the results are
+    added to each job's accumulators. Returns the batch statistics."""
+    ctx = ctx or jobs[0].ctx
+    n = len(jobs)
+    handles = (ctypes.c_void_p * n)(*[j._h.value for j in jobs])
+    ps = (ctypes.c_int32 * n)(*[int(p) for p in passes])
+    cfg = native.BatchConfig(int(paths_in_flight), float(regen_fraction), int(max_iterations))
+    st = native.BatchStats()
+    check(native.lib().hasty_batch_render(ctx._h, handles, ps, n, ctypes.byref(cfg), ctypes.byref(st)))
+    return {k: getattr(st, k) for k, _ in native.BatchStats._fields_}

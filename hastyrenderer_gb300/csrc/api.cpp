@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "bvh_build.h"
+#include "job.h"
 #include "image_out.h"
 #include "scene_load.h"
 #include "wavefront.h"
@@ -31,129 +32,47 @@ void host_trace_rays(int kind, const float4* nodes, const float4* tris, const fl
 
 using namespace hasty;
 
-namespace {
+namespace hasty {
 thread_local std::string g_error;
-
-struct ApiError {
-  int code; std::string msg;
-};
-
-int fail(int code, const std::string& m) { g_error = m; return code; }
-
-void ck(cudaError_t e, const char* what) {
-  if (e != cudaSuccess) {
-    int code = (e == cudaErrorMemoryAllocation) ? HASTY_ERR_MEMORY : HASTY_ERR_CUDA;
-    throw ApiError{code, std::string(what) + ": " + cudaGetErrorString(e)};
-  }
 }
 
-template <class F>
-int guarded(F&& f) {
-  try {
-    return f();
-  } catch (const ApiError& e) {
-    return fail(e.code, e.msg);
-  } catch (const LoadError& e) {
-    return fail(HASTY_ERR_LOAD, e.what());
-  } catch (const std::bad_alloc&) {
-    return fail(HASTY_ERR_MEMORY, "host allocation failed");
-  } catch (const std::exception& e) {
-    return fail(HASTY_ERR_CUDA, e.what());
-  }
-}
+namespace {
+
 }  // namespace
 
-struct hasty_ctx {
-  int device = 0;
-  int sm_count = 0;
-  uint32_t flags = 0;
-};
+void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st) {
+  auto A = [&](size_t bytes) { return alloc(bytes); };
+  p.capacity = int32_t(cap);
+  size_t c = size_t(cap);
+  p.rng = static_cast<uint64_t*>(A(c * sizeof(uint64_t)));
+  p.thr = static_cast<float4*>(A(c * sizeof(float4)));
+  p.rad = static_cast<float4*>(A(c * sizeof(float4)));
+  p.pend_b = static_cast<float4*>(A(c * sizeof(float4)));
+  p.nee_c = static_cast<float4*>(A(c * sizeof(float4)));
+  p.nee_t = static_cast<float4*>(A(c * sizeof(float4)));
+  p.med = static_cast<float4*>(A(c * kMaxMedia * sizeof(float4)));
+  p.med_geom = static_cast<int32_t*>(A(c * kMaxMedia * sizeof(int32_t)));
+  p.ray_o = static_cast<float4*>(A(2 * c * sizeof(float4)));
+  p.ray_d = static_cast<float4*>(A(2 * c * sizeof(float4)));
+  p.hit = static_cast<float4*>(A(2 * c * sizeof(float4)));
+  p.pq[0] = static_cast<int32_t*>(A(c * sizeof(int32_t)));
+  p.pq[1] = static_cast<int32_t*>(A(c * sizeof(int32_t)));
+  p.rq[0] = static_cast<int32_t*>(A(2 * c * sizeof(int32_t)));
+  p.rq[1] = static_cast<int32_t*>(A(2 * c * sizeof(int32_t)));
+  p.counts = static_cast<uint32_t*>(A(4 * sizeof(uint32_t)));
+  p.out_color = static_cast<float4*>(A(c * sizeof(float4)));
+  p.out_normal = static_cast<float4*>(A(c * sizeof(float4)));
+  p.out_albedo = static_cast<float4*>(A(c * sizeof(float4)));
+  p.stats = static_cast<unsigned long long*>(A(size_t(n_stats) * sizeof(unsigned long long)));
+  ck(cudaMemsetAsync(p.stats, 0, sizeof(unsigned long long) * size_t(n_stats), st), "memset stats");
+  ck(cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4, st), "memset counts");
+}
 
-struct hasty_job {
-  hasty_ctx* ctx = nullptr;
-  HostScene host;
-  int32_t bvh_depth = 0;
-  double bvh_ms = 0;
-  SceneDev sd{};
-  PathsDev pd{};
-  cudaStream_t stream = nullptr;
-  std::vector<void*> allocs;
-  int64_t bytes = 0;
-  double* acc[3] = {nullptr, nullptr, nullptr};
-  float* est = nullptr;
-  int64_t capacity = 0;
-  int32_t samples_done = 0;
-  uint64_t seed = 0;
-  std::atomic<bool> stop{false};
-  double kernel_ms = 0.0, trace_ms = 0.0, shade_ms = 0.0;
-  uint64_t trace_launches = 0, kernel_launches = 0;
-  bool stage_timing = false;
-  // (start, end, stage) with stage 0: whole batch, 1: trace, 2: shade
-  struct Ev { cudaEvent_t a, b; int stage; };
-  std::vector<Ev> pending_events;
-
-  template <class T>
-  T* alloc(size_t n) {
-    void* p = nullptr;
-    size_t b = std::max<size_t>(n, 1) * sizeof(T);
-    ck(cudaMalloc(&p, b), "cudaMalloc");
-    allocs.push_back(p);
-    bytes += int64_t(b);
-    return static_cast<T*>(p);
-  }
-  template <class T>
-  T* upload(const std::vector<T>& v) {
-    if (v.empty()) return nullptr;
-    T* p = alloc<T>(v.size());
-    ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream), "upload");
-    return p;
-  }
-  void collect_events() {
-    for (auto& e : pending_events) {
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) {
-        if (e.stage == 0) kernel_ms += ms; else if (e.stage == 1) trace_ms += ms; else shade_ms += ms;
-      }
-      cudaEventDestroy(e.a); cudaEventDestroy(e.b);
-    }
-    pending_events.clear();
-  }
-  ~hasty_job() {
-    if (stream) cudaStreamSynchronize(stream);
-    collect_events();
-    for (void* p : allocs) cudaFree(p);
-    if (stream) cudaStreamDestroy(stream);
-  }
-};
+void hasty::alloc_paths(hasty_job& j, int64_t cap) {
+  alloc_paths_into(j.pd, cap, ST_COUNT, [&](size_t b) { return static_cast<void*>(j.alloc<uint8_t>(b)); }, j.stream);
+}
 
 namespace {
-
-void alloc_paths(hasty_job& j, int64_t cap) {
-  PathsDev& p = j.pd;
-  p.capacity = int32_t(cap);
-  p.rng = j.alloc<uint64_t>(size_t(cap));
-  p.thr = j.alloc<float4>(size_t(cap));
-  p.rad = j.alloc<float4>(size_t(cap));
-  p.pend_b = j.alloc<float4>(size_t(cap));
-  p.nee_c = j.alloc<float4>(size_t(cap));
-  p.nee_t = j.alloc<float4>(size_t(cap));
-  p.med = j.alloc<float4>(size_t(cap) * kMaxMedia);
-  p.med_geom = j.alloc<int32_t>(size_t(cap) * kMaxMedia);
-  p.ray_o = j.alloc<float4>(size_t(cap) * 2);
-  p.ray_d = j.alloc<float4>(size_t(cap) * 2);
-  p.hit = j.alloc<float4>(size_t(cap) * 2);
-  p.pq[0] = j.alloc<int32_t>(size_t(cap));
-  p.pq[1] = j.alloc<int32_t>(size_t(cap));
-  p.rq[0] = j.alloc<int32_t>(size_t(cap) * 2);
-  p.rq[1] = j.alloc<int32_t>(size_t(cap) * 2);
-  p.counts = j.alloc<uint32_t>(4);
-  p.out_color = j.alloc<float4>(size_t(cap));
-  p.out_normal = j.alloc<float4>(size_t(cap));
-  p.out_albedo = j.alloc<float4>(size_t(cap));
-  p.stats = j.alloc<unsigned long long>(ST_COUNT);
-  ck(cudaMemsetAsync(p.stats, 0, sizeof(unsigned long long) * ST_COUNT, j.stream), "memset stats");
-  ck(cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4, j.stream), "memset counts");
-}
 
 void upload_scene(hasty_job& j) {
   HostScene& h = j.host;

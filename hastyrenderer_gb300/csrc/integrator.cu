@@ -100,21 +100,23 @@ __global__ void __launch_bounds__(256) k_raygen(SceneDev sc, PathsDev P, BatchDe
   P.rq[0][s] = 2 * s;
 }
 
-__global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDesc b, int q) {
-  const uint32_t n_in = P.counts[q];
-  uint32_t* pq_cnt = &P.counts[q ^ 1];
-  uint32_t* rq_cnt = &P.counts[2 + (q ^ 1)];
-  int32_t* pq_out = P.pq[q ^ 1];
-  int32_t* rq_out = P.rq[q ^ 1];
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if ((i & ~31u) >= n_in) return;                 // whole warp past the queue
-  const bool valid = i < n_in;
-  const int npix = sc.width * sc.height;
+// One bounce of one path (slot s): resolve the previous vertex's light and
+// BSDF samples, shade the vertex reached, queue its rays in the slot's ray
+// entries. `key` is the path's stream key. The caller handles a finished path
+// (res.keep false) and the queues.
+struct ShadeRes { bool keep, emitB, emitL; int shaded, overflow, capped; V3 L; };
 
-  bool keep = false, emitB = false, emitL = false;
-  int s = valid ? P.pq[q][i] : 0;
-  int shaded = 0, overflow = 0, capped = 0;
-  if (valid) {
+__device__ __forceinline__ ShadeRes shade_path(const SceneDev& sc, const PathsDev& P, int s, uint64_t key) {
+  ShadeRes res;
+  res.keep = res.emitB = res.emitL = false;
+  res.shaded = res.overflow = res.capped = 0;
+  bool& keep = res.keep;
+  bool& emitB = res.emitB;
+  bool& emitL = res.emitL;
+  int& shaded = res.shaded;
+  int& overflow = res.overflow;
+  int& capped = res.capped;
+  {
     float4 rad = P.rad[s];
     uint32_t flags = __float_as_uint(rad.w);
     V3 L = xyz(rad);
@@ -190,7 +192,6 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDes
             done = true;
           } else {
             shaded = 1;
-            uint64_t key = path_key(b.seed, uint32_t(s % npix), b.pass_base + uint32_t(s / npix));
             Rng r; r.inc = Rng::inc_of(key); r.state = P.rng[s];
             float qrr = depth >= sc.rr_start ? sc.rr_q : 0.0f;      // PathTracing.cpp:49-56
             if (r.u01() < qrr) {
@@ -267,8 +268,33 @@ __global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDes
     }
     keep = !done;
     if (keep) P.rad[s] = f4(L, __uint_as_float(flags));
-    else P.out_color[s] = f4(L, 0.f);
+    res.L = L;
   }
+
+  return res;
+}
+
+__global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDesc b, int q) {
+  const uint32_t n_in = P.counts[q];
+  uint32_t* pq_cnt = &P.counts[q ^ 1];
+  uint32_t* rq_cnt = &P.counts[2 + (q ^ 1)];
+  int32_t* pq_out = P.pq[q ^ 1];
+  int32_t* rq_out = P.rq[q ^ 1];
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((i & ~31u) >= n_in) return;                 // whole warp past the queue
+  const bool valid = i < n_in;
+  const int npix = sc.width * sc.height;
+
+  int s = valid ? P.pq[q][i] : 0;
+  ShadeRes res;
+  res.keep = res.emitB = res.emitL = false;
+  res.shaded = res.overflow = res.capped = 0;
+  if (valid) {
+    res = shade_path(sc, P, s, path_key(b.seed, uint32_t(s % npix), b.pass_base + uint32_t(s / npix)));
+    if (!res.keep) P.out_color[s] = f4(res.L, 0.f);
+  }
+  const bool keep = res.keep, emitB = res.emitB, emitL = res.emitL;
+  const int shaded = res.shaded, overflow = res.overflow, capped = res.capped;
 
   // warp-ballot compaction of the surviving paths and their rays
   uint32_t nrays = (emitB ? 1u : 0u) + (emitL ? 1u : 0u);
@@ -392,4 +418,204 @@ __global__ void k_debug_bsdf(int which, const float* in, int n, const uint32_t* 
 void launch_debug_bsdf(int which, const float* in, int n, const uint32_t* replay, int n_replay, float* out, cudaStream_t st) {
   k_debug_bsdf<<<(n + 127) / 128, 128, 0, st>>>(which, in, n, replay, n_replay, out);
 }
+}  // namespace hasty
+
+// ============================================================================
+// Multi-job engine kernels (see MultiDev in wavefront.h). One iteration:
+// k_multi_plan (1 thread) decides how many new camera samples to issue into
+// free slots, k_multi_regen starts them, the closest-hit kernel traces every
+// queued ray, k_shade_multi advances every queued path by one bounce (the
+// same shade_path as the single-job kernel), and k_multi_cond flips the queue
+// parity and sets the enclosing CUDA-graph while-loop's condition.
+namespace hasty {
+namespace {
+using namespace dev;
+
+__device__ __forceinline__ int find_job(const MultiDev& m, unsigned long long g) {
+  int lo = 0, hi = *m.n_jobs - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (m.jobs[mid].sample_begin <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_multi_init(PathsDev P, MultiDev m, int cap) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cap) m.free_slots[i] = cap - 1 - i;
+  if (i == 0) {
+    *m.free_count = uint32_t(cap);
+    for (int k = 0; k < 4; ++k) P.counts[k] = 0;
+    for (int k = 0; k < 8; ++k) m.ctl[k] = 0;
+  }
+}
+
+__global__ void k_multi_plan(PathsDev P, MultiDev m) {
+  uint32_t q = m.ctl[0];
+  P.counts[q ^ 1] = 0;
+  P.counts[2 + (q ^ 1)] = 0;
+  uint32_t live = P.counts[q];
+  uint32_t n_new = 0;
+  unsigned long long next = *m.next_sample, total = *m.total_samples;
+  if (live < m.regen_below && next < total) {
+    unsigned long long left = total - next;
+    uint32_t fc = *m.free_count;
+    n_new = left < fc ? uint32_t(left) : fc;
+  }
+  m.ctl[1] = n_new;
+  m.ctl[2] = *m.free_count;
+  m.ctl[3] = P.counts[q];
+  m.ctl[4] = P.counts[2 + q];
+  *m.regen_base = next;
+  P.counts[q] += n_new;
+  P.counts[2 + q] += n_new;
+  *m.free_count -= n_new;
+  *m.next_sample = next + n_new;
+}
+
+__global__ void __launch_bounds__(256) k_multi_regen(PathsDev P, MultiDev m) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t n_new = m.ctl[1];
+  if (i >= n_new) return;
+  uint32_t q = m.ctl[0];
+  int s = m.free_slots[m.ctl[2] - 1 - i];
+  unsigned long long g = *m.regen_base + i;
+  int j = find_job(m, g);
+  const JobDev& job = m.jobs[j];
+  const SceneDev& sc = job.sc;
+  uint32_t l = uint32_t(g - job.sample_begin);
+  uint32_t pass = job.pass_base + l / job.npix;
+  uint32_t px = l % job.npix;
+  m.slot_job[s] = j;
+  m.slot_sample[s] = l;
+  int x = int(px % uint32_t(sc.width)), y = int(px / uint32_t(sc.width));
+  Rng r; r.seed(path_key(job.seed, px, pass));
+  float ox = halton(2, pass), oy = halton(3, pass);
+  V3 o, d; int capped = 0;
+  camera_ray(sc.cam, r, float(x) + ox, float(y) + oy, float(sc.width), float(sc.height), o, d, capped);
+  if (capped) atomicAdd(&P.stats[ST_TRIAL_CAP], 1ull);
+  P.rng[s] = r.state;
+  P.thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
+  P.rad[s] = make_float4(0.f, 0.f, 0.f, __uint_as_float(PF_CAMERA | PF_PEND_B));
+  P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  P.out_albedo[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  P.ray_o[2 * s] = f4(o, 0.f);
+  P.ray_d[2 * s] = f4(d, 0.f);
+  P.pq[q][m.ctl[3] + i] = s;
+  P.rq[q][m.ctl[4] + i] = 2 * s;
+  if (i == 0) atomicAdd(&P.stats[ST_PATHS], (unsigned long long)n_new);
+}
+
+// Fixed-point addition of one finished sample (NaN radiance drops the sample
+// and its AOVs, core/src/PathTracing.cpp:132-142). Values beyond +/-2^30 are
+// clamped and counted.
+__device__ __forceinline__ void add_fixed(unsigned long long* acc, V3 L, float4 n, float4 a, unsigned long long* stats) {
+  float v[9] = {L.x, L.y, L.z, n.x, n.y, n.z, a.x, a.y, a.z};
+  bool sat = false;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    float x = v[k];
+    if (fabsf(x) > 1073741824.0f) { x = copysignf(1073741824.0f, x); sat = true; }
+    long long qv = __float2ll_rn(x * 4294967296.0f);
+    if (qv) atomicAdd(&acc[k], (unsigned long long)qv);
+  }
+  if (sat) atomicAdd(&stats[MS_SATURATED], 1ull);
+}
+
+__global__ void __launch_bounds__(128) k_shade_multi(PathsDev P, MultiDev m) {
+  const uint32_t q = m.ctl[0];
+  const uint32_t n_in = P.counts[q];
+  uint32_t* pq_cnt = &P.counts[q ^ 1];
+  uint32_t* rq_cnt = &P.counts[2 + (q ^ 1)];
+  int32_t* pq_out = P.pq[q ^ 1];
+  int32_t* rq_out = P.rq[q ^ 1];
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((i & ~31u) >= n_in) return;
+  const bool valid = i < n_in;
+  int s = valid ? P.pq[q][i] : 0;
+  int j = valid ? m.slot_job[s] : 0;
+  ShadeRes res;
+  res.keep = res.emitB = res.emitL = false;
+  res.shaded = res.overflow = res.capped = 0;
+  bool finished = false;
+  if (valid) {
+    const JobDev& job = m.jobs[j];
+    uint32_t l = m.slot_sample[s];
+    uint32_t px = l % job.npix;
+    res = shade_path(job.sc, P, s, path_key(job.seed, px, job.pass_base + l / job.npix));
+    if (!res.keep) {
+      finished = true;
+      if (has_nan(res.L)) atomicAdd(&P.stats[ST_NAN], 1ull);
+      else add_fixed(job.acc + 9 * int64_t(px), res.L, P.out_normal[s], P.out_albedo[s], P.stats);
+    }
+  }
+  const bool keep = res.keep, emitB = res.emitB, emitL = res.emitL;
+  uint32_t lane = threadIdx.x & 31u;
+  uint32_t nrays = (emitB ? 1u : 0u) + (emitL ? 1u : 0u);
+  uint32_t roff = warp_reserve(rq_cnt, nrays);
+  if (emitB) rq_out[roff++] = 2 * s;
+  if (emitL) rq_out[roff] = 2 * s + 1;
+  unsigned kb = __ballot_sync(kFull, keep);
+  uint32_t pbase = 0;
+  if (lane == 0 && kb) pbase = atomicAdd(pq_cnt, uint32_t(__popc(kb)));
+  pbase = __shfl_sync(kFull, pbase, 0);
+  if (keep) pq_out[pbase + __popc(kb & ((1u << lane) - 1u))] = s;
+  // finished slots go back on the free stack; per-job completion counts
+  unsigned fb = __ballot_sync(kFull, finished);
+  uint32_t fbase = 0;
+  if (lane == 0 && fb) fbase = atomicAdd(m.free_count, uint32_t(__popc(fb)));
+  fbase = __shfl_sync(kFull, fbase, 0);
+  if (finished) m.free_slots[fbase + __popc(fb & ((1u << lane) - 1u))] = s;
+  unsigned same = __match_any_sync(kFull, finished ? j : -1);
+  if (finished && (__ffs(same) - 1) == int(lane)) atomicAdd(m.jobs[j].done, (unsigned long long)__popc(same));
+  unsigned sb = __ballot_sync(kFull, res.shaded != 0);
+  unsigned ob = __ballot_sync(kFull, res.overflow != 0);
+  unsigned cb = __ballot_sync(kFull, res.capped != 0);
+  if (lane == 0) {
+    if (sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
+    if (ob) atomicAdd(&P.stats[ST_MEDIA_OVERFLOW], (unsigned long long)__popc(ob));
+    if (cb) atomicAdd(&P.stats[ST_TRIAL_CAP], (unsigned long long)__popc(cb));
+  }
+}
+
+__global__ void k_multi_cond(PathsDev P, MultiDev m, cudaGraphConditionalHandle h, int use_cond) {
+  uint32_t q = m.ctl[0];
+  m.ctl[0] = q ^ 1;
+  uint32_t it = ++m.ctl[5];
+  bool more = P.counts[q ^ 1] > 0 || *m.next_sample < *m.total_samples;
+  if (more && it >= m.max_iter) { m.ctl[6] = 1; more = false; }
+  if (it >= m.ctl[7]) more = false;      // end of this wave; the host resumes it
+  if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+__global__ void k_fixed_to_double(const unsigned long long* acc, int npix, double* c, double* n, double* a) {
+  int px = blockIdx.x * blockDim.x + threadIdx.x;
+  if (px >= npix) return;
+  const double inv = 1.0 / kFixedScale;
+  for (int k = 0; k < 3; ++k) {
+    c[3 * px + k] += double((long long)acc[9 * int64_t(px) + k]) * inv;
+    n[3 * px + k] += double((long long)acc[9 * int64_t(px) + 3 + k]) * inv;
+    a[3 * px + k] += double((long long)acc[9 * int64_t(px) + 6 + k]) * inv;
+  }
+}
+
+}  // namespace
+
+void launch_multi_init(const PathsDev& p, const MultiDev& m, int cap, cudaStream_t st) {
+  k_multi_init<<<(cap + 255) / 256, 256, 0, st>>>(p, m, cap);
+}
+
+void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int cap, unsigned long long cond, int use_cond,
+                            cudaStream_t st) {
+  k_multi_plan<<<1, 1, 0, st>>>(p, m);
+  k_multi_regen<<<(cap + 255) / 256, 256, 0, st>>>(p, m);
+  launch_trace_multi(p, m, 2 * cap, st);
+  k_shade_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m);
+  k_multi_cond<<<1, 1, 0, st>>>(p, m, cudaGraphConditionalHandle(cond), use_cond);
+}
+
+void launch_fixed_to_double(const unsigned long long* acc, int npix, double* c, double* n, double* a, cudaStream_t st) {
+  k_fixed_to_double<<<(npix + 255) / 256, 256, 0, st>>>(acc, npix, c, n, a);
+}
+
 }  // namespace hasty

@@ -1,0 +1,123 @@
+// Internal state behind the C ABI: context, job and the error helpers
+// shared by api.cpp (single-job path) and engine.cpp (multi-job engine).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <functional>
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "hasty_gpu.h"
+#include "scene_load.h"
+#include "wavefront.h"
+
+namespace hasty {
+
+extern thread_local std::string g_error;
+
+struct ApiError {
+  int code; std::string msg;
+};
+
+inline int fail(int code, const std::string& m) { g_error = m; return code; }
+
+inline void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    int code = (e == cudaErrorMemoryAllocation) ? HASTY_ERR_MEMORY : HASTY_ERR_CUDA;
+    throw ApiError{code, std::string(what) + ": " + cudaGetErrorString(e)};
+  }
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const ApiError& e) {
+    return fail(e.code, e.msg);
+  } catch (const LoadError& e) {
+    return fail(HASTY_ERR_LOAD, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(HASTY_ERR_MEMORY, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(HASTY_ERR_CUDA, e.what());
+  }
+}
+}  // namespace hasty
+
+using hasty::ApiError;
+using hasty::ck;
+using hasty::HostScene;
+using hasty::SceneDev;
+using hasty::PathsDev;
+
+struct hasty_ctx {
+  int device = 0;
+  int sm_count = 0;
+  uint32_t flags = 0;
+};
+
+struct hasty_job {
+  hasty_ctx* ctx = nullptr;
+  HostScene host;
+  int32_t bvh_depth = 0;
+  double bvh_ms = 0;
+  SceneDev sd{};
+  PathsDev pd{};
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+  double* acc[3] = {nullptr, nullptr, nullptr};
+  float* est = nullptr;
+  int64_t capacity = 0;
+  int32_t samples_done = 0;
+  uint64_t seed = 0;
+  std::atomic<bool> stop{false};
+  double kernel_ms = 0.0, trace_ms = 0.0, shade_ms = 0.0;
+  uint64_t trace_launches = 0, kernel_launches = 0;
+  bool stage_timing = false;
+  // (start, end, stage) with stage 0: whole batch, 1: trace, 2: shade
+  struct Ev { cudaEvent_t a, b; int stage; };
+  std::vector<Ev> pending_events;
+
+  template <class T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    size_t b = std::max<size_t>(n, 1) * sizeof(T);
+    ck(cudaMalloc(&p, b), "cudaMalloc");
+    allocs.push_back(p);
+    bytes += int64_t(b);
+    return static_cast<T*>(p);
+  }
+  template <class T>
+  T* upload(const std::vector<T>& v) {
+    if (v.empty()) return nullptr;
+    T* p = alloc<T>(v.size());
+    ck(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream), "upload");
+    return p;
+  }
+  void collect_events() {
+    for (auto& e : pending_events) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) {
+        if (e.stage == 0) kernel_ms += ms; else if (e.stage == 1) trace_ms += ms; else shade_ms += ms;
+      }
+      cudaEventDestroy(e.a); cudaEventDestroy(e.b);
+    }
+    pending_events.clear();
+  }
+  ~hasty_job() {
+    if (stream) cudaStreamSynchronize(stream);
+    collect_events();
+    for (void* p : allocs) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+
+namespace hasty {
+// Path-state buffers for `cap` slots (api.cpp).
+void alloc_paths(hasty_job& j, int64_t cap);
+void alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st);
+}  // namespace hasty

@@ -67,4 +67,57 @@ void launch_estimate(const double* acc, int n, float den, float scale, float* ou
 // Closest-hit queries of arbitrary rays (n x 6 floats, device memory).
 void launch_trace_rays(const SceneDev& sc, const float* rays, int n, float4* hits, cudaStream_t stream);
 
+// ---------------------------------------------------------------------------
+// Multi-job engine (batching and serving). Many resident jobs share one pool
+// of path slots; camera samples are issued in global order (jobs in the order
+// they were added, each job's samples pass-major) into whatever slots are
+// free, so the pool stays full until the last sample (path regeneration).
+// Finished samples are added to per-job int64 fixed-point accumulators
+// (2^-32 units): integer addition is order-independent, so a job's image is
+// bit-identical however it is mixed with other jobs.
+constexpr double kFixedScale = 4294967296.0;   // 2^32
+
+struct JobDev {
+  SceneDev sc;
+  unsigned long long* acc;     // 9 int64 per pixel: colour, normal, albedo (two's complement)
+  unsigned long long* done;    // finished camera samples
+  uint64_t seed;
+  uint64_t sample_begin;       // first global sample index of the job
+  uint64_t n_samples;          // passes * W * H
+  uint32_t pass_base;          // pass index of the job's first sample
+  uint32_t npix;
+};
+
+struct MultiDev {
+  const JobDev* jobs;
+  const int32_t* n_jobs;       // device-resident, so a captured graph stays valid as jobs are added
+  int32_t* slot_job;           // job of the path in each slot
+  uint32_t* slot_sample;       // job-local sample index (pass_local * npix + pixel)
+  int32_t* free_slots;         // stack of free slot ids
+  uint32_t* free_count;
+  unsigned long long* next_sample;
+  unsigned long long* total_samples;
+  unsigned long long* regen_base;   // first global sample of the current regeneration
+  uint32_t* ctl;               // [0] queue parity, [1] regen count, [2] free-stack top before regen,
+                               // [3] path-queue base, [4] ray-queue base, [5] iterations, [6] bound hit,
+                               // [7] iteration at which the current wave ends
+  uint32_t regen_below;        // regenerate only when fewer live paths than this
+  uint32_t max_iter;           // iteration bound of one run (device-side loop guard)
+};
+
+enum MultiStat { MS_RAYS = ST_RAYS, MS_SHADED = ST_SHADED, MS_PATHS = ST_PATHS, MS_NAN = ST_NAN,
+                 MS_MEDIA_OVERFLOW = ST_MEDIA_OVERFLOW, MS_TRIAL_CAP = ST_TRIAL_CAP, MS_SATURATED = ST_COUNT,
+                 MS_COUNT };
+
+// One engine iteration (regenerate, trace, shade, loop condition) launched
+// into `stream`; `cond` is the CUDA-graph conditional handle of the enclosing
+// while node (0 when launched without a graph).
+void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int capacity, unsigned long long cond_handle,
+                            int use_cond, cudaStream_t stream);
+void launch_multi_init(const PathsDev& p, const MultiDev& m, int capacity, cudaStream_t stream);
+// Adds a finished job's fixed-point sums into FP64 accumulators (sum * 2^-32).
+void launch_fixed_to_double(const unsigned long long* acc, int npix, double* c, double* n, double* a, cudaStream_t stream);
+// trace.cu: closest hit of the queued rays of the multi-job engine.
+void launch_trace_multi(const PathsDev& p, const MultiDev& m, int max_rays, cudaStream_t stream);
+
 }  // namespace hasty

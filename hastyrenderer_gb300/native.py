@@ -41,6 +41,18 @@ class Stats(ctypes.Structure):
                 ("trace_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
 
 
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("paths_in_flight", ctypes.c_int64), ("regen_fraction", ctypes.c_float),
+                ("max_iterations", ctypes.c_int32)]
+
+
+class BatchStats(ctypes.Structure):
+    _fields_ = [("device_ms", ctypes.c_double), ("wall_ms", ctypes.c_double), ("samples", ctypes.c_uint64),
+                ("rays", ctypes.c_uint64), ("shaded", ctypes.c_uint64), ("nan_samples", ctypes.c_uint64),
+                ("saturated", ctypes.c_uint64), ("iterations", ctypes.c_uint64), ("paths_in_flight", ctypes.c_int64),
+                ("engine_bytes", ctypes.c_int64)]
+
+
 def declared_symbols(header: str = HEADER) -> list[str]:
     """Function names declared in the C header."""
     text = open(header).read()
@@ -81,6 +93,7 @@ def lib() -> ctypes.CDLL:
         "hasty_debug_tri_ids": [P, P, P, SZ],
         "hasty_debug_host_trace": [ctypes.c_char_p, I, P, SZ, P, P, P, P, P],
         "hasty_debug_bsdf": [I, P, SZ, P, SZ, P],
+        "hasty_batch_render": [P, P, P, SZ, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

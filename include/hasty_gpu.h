@@ -115,6 +115,38 @@ int hasty_job_read_sums(hasty_job* job, int aov, double* host_rgb, size_t w, siz
 /* output.exr, outputNormal.exr, outputAlbedo.exr (+ .pfm copies when write_pfm != 0). */
 int hasty_job_write_outputs(hasty_job* job, const char* out_dir, int write_pfm);
 
+/* ---- Batching: many jobs in one persistent multi-job wavefront ------------
+ * Path slots are shared by all jobs and refilled with new camera samples as
+ * paths finish (regeneration); one CUDA graph launch whose conditional
+ * while-node repeats regenerate/trace/shade on the device runs the whole batch.
+ * Each job's samples are accumulated in int64 fixed point (2^-32), which is
+ * order-independent: a job's result is bit-identical alone or in any mix.
+ * No counterpart in the reference (its jobs run one at a time). */
+typedef struct hasty_batch_config {
+  int64_t paths_in_flight;     /* path-slot pool; 0 = 4M */
+  float regen_fraction;        /* refill when live paths < fraction * pool; 0 = 0.9, >= 1 every iteration */
+  int32_t max_iterations;      /* device-side loop bound; 0 = 50M */
+} hasty_batch_config;
+
+typedef struct hasty_batch_stats {
+  double device_ms;            /* device time of the batch (CUDA events) */
+  double wall_ms;              /* host wall time including engine set-up */
+  uint64_t samples;            /* camera samples rendered */
+  uint64_t rays;
+  uint64_t shaded;
+  uint64_t nan_samples;
+  uint64_t saturated;          /* samples clamped to +/-2^30 in fixed point */
+  uint64_t iterations;         /* engine iterations (one bounce of every live path each) */
+  int64_t paths_in_flight;
+  int64_t engine_bytes;        /* device memory of the engine (path pool, fixed-point sums) */
+} hasty_batch_stats;
+
+/* Renders passes[i] further passes of jobs[i] (all from ctx) in one run and
+ * adds the results to each job's accumulators, as hasty_job_render_passes
+ * would; synchronous. */
+int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, size_t n_jobs,
+                       const hasty_batch_config* cfg, hasty_batch_stats* stats);
+
 /* Closest hits of n rays given as n x 6 host floats (origin, direction):
  * global triangle index (-1 miss), t, u, v. */
 int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* tri, float* t, float* u, float* v);
