@@ -94,6 +94,7 @@ def lib() -> ctypes.CDLL:
         "hasty_debug_host_trace": [ctypes.c_char_p, I, P, SZ, P, P, P, P, P],
         "hasty_debug_bsdf": [I, P, SZ, P, SZ, P],
         "hasty_batch_render": [P, P, P, SZ, P, P],
+        "hasty_job_render_pass_static": [P, I, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -147,6 +147,21 @@ typedef struct hasty_batch_stats {
 int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, size_t n_jobs,
                        const hasty_batch_config* cfg, hasty_batch_stats* stats);
 
+/* ---- One pass without device allocation ------------------------------------
+ * Renders camera-sample pass `pass` of the job (seed and settings as loaded)
+ * into d_color, a caller-owned DEVICE buffer of w*h*3 doubles (row-major RGB
+ * radiance of that one sample per pixel, before exposure), which it
+ * overwrites. Asynchronous on the job's stream (hasty_job_sync waits). Leaves
+ * the job's accumulators, pass counter and statistics untouched.
+ * For callers that may not allocate device memory while rendering: the call
+ * makes no cudaMalloc/cudaFree and uses one fixed 7 MiB static device array
+ * as scratch, so frames above 16384 pixels (e.g. 128 x 128) are rejected
+ * with HASTY_ERR_ARG. The first call on each device looks up that array's
+ * address; make it before any stream capture begins. All calls share the
+ * array: calls whose GPU work overlaps (other streams, other threads) race.
+ * No counterpart in the reference (it renders through its own buffers). */
+int hasty_job_render_pass_static(hasty_job* job, int pass, double* d_color);
+
 /* Closest hits of n rays given as n x 6 host floats (origin, direction):
  * global triangle index (-1 miss), t, u, v. */
 int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* tri, float* t, float* u, float* v);
