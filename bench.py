@@ -32,6 +32,14 @@ sys.path.insert(0, ROOT)
 
 SPP_PER_STEP = 8
 WORKLOAD = "sphere_field_800x_icosphere3_1024002tri_1920x1080_dof6_sky2048x1024_depth12"
+# Algorithmic bytes per shaded vertex: path state read + write (2 x 96 B) and
+# the triangle's attributes (92 B); texel reads are not counted.
+B_SHADE = 2 * 96 + 92
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, averaged
+# over the 12 bounces of one 4,147,200-path batch, wide BVH) from one ncu
+# capture of `bench.py --steps 1 --warmup 3 --spp-per-step 2`; the default run
+# renders the same batches (profiles/dram_per_launch_sphere_field_1920x1080.md).
+MEASURED_TRAFFIC = {"wide": {"k_trace": 114.2e6, "k_shade": 273.5e6}}
 
 
 def peaks():
@@ -246,6 +254,7 @@ def main():
         t = float(tt.item())
     samples = args.steps * args.spp_per_step * W * H
     rays = s1["rays"] - s0["rays"]
+    shaded = s1["shaded"] - s0["shaded"]
     trace_ms = s1["trace_ms"] - s0["trace_ms"]
     shade_ms = s1["shade_ms"] - s0["shade_ms"]
     launches = s1["kernel_launches"] - s0["kernel_launches"]
@@ -257,17 +266,23 @@ def main():
         cpu, bvh_costs = (None, None)
         if not args.no_cpu_baseline:
             cpu, bvh_costs = cpu_baseline(job_path, args.cpu_budget)
-        b_ray = None
-        roof = None
+        roof, kernels = None, []
         if bvh_costs is not None:
             b_ray = 32 + 16 + 64 * bvh_costs["nodes_per_ray"] + 48 * bvh_costs["tris_per_ray"]
-            per_launch_bytes = rays * b_ray / max(trace_launches, 1)
-            per_launch_s = trace_ms * 1e-3 / max(trace_launches, 1)
-            achieved = per_launch_bytes / per_launch_s / 1e9
-            roof = {"bound": "hbm", "kernel": "k_trace (closest hit)", "achieved": achieved, "peak": hbm,
-                    "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": None,
-                    "algorithmic_bytes_per_ray": b_ray, "bvh_nodes_per_ray": bvh_costs["nodes_per_ray"],
-                    "tris_per_ray": bvh_costs["tris_per_ray"]}
+            traffic = MEASURED_TRAFFIC.get(args.bvh, {}) if args.spp_per_step % 2 == 0 else {}
+            n_launch = max(trace_launches, 1)
+            for name, work, unit_bytes, ms in (("k_trace", rays, b_ray, trace_ms), ("k_shade", shaded, B_SHADE, shade_ms)):
+                per_launch_bytes = work * unit_bytes / n_launch
+                achieved = per_launch_bytes / (ms * 1e-3 / n_launch) / 1e9
+                kernels.append({"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                                "frac": achieved / hbm, "peak_kind": peak_kind,
+                                "traffic": traffic.get(name), "algorithmic_bytes_per_launch": per_launch_bytes,
+                                "ms_per_launch": ms / n_launch,
+                                "bytes_per_unit": unit_bytes, "unit_of_work": "ray" if name == "k_trace" else "shaded vertex"})
+            kernels[0].update({"bvh_nodes_per_ray": bvh_costs["nodes_per_ray"], "tris_per_ray": bvh_costs["tris_per_ray"]})
+            roof = dict(max(kernels, key=lambda k: k["ms_per_launch"]))
+            roof["note"] = ("dominant kernel by device time; traffic = measured DRAM bytes per launch (ncu), "
+                            "well below the algorithmic bytes because L1/L2 hold the upper BVH levels")
         line = {
             "metric": "samples/s", "value": samples * world / t, "unit": "samples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
@@ -280,6 +295,7 @@ def main():
             "wall_ms_per_step": wall / args.steps * 1e3,
             "gpu_launches": launches,
             "roofline": roof,
+            "kernels": kernels,
             "cpu_baseline": cpu,
             "e2e": {"value": args.steps * args.spp_per_step * W * H * world / e2e_s, "unit": "samples/s",
                     "h2d_bytes_per_step": int(e2e_bytes_up // args.steps), "d2h_bytes_per_step": W * H * 3 * 4,
