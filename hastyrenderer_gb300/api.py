@@ -195,3 +195,85 @@ def batch_render(jobs, passes, paths_in_flight: int = 0, regen_fraction: float =
     st = native.BatchStats()
     check(native.lib().hasty_batch_render(ctx._h, handles, ps, n, ctypes.byref(cfg), ctypes.byref(st)))
     return {k: getattr(st, k) for k, _ in native.BatchStats._fields_}
+
+
+class Server:
+    """Request loop over the multi-job engine (hasty_server_* in the C ABI):
+    requests are admitted by device-memory footprint, scenes stay resident
+    and are shared, and the passes of resident requests are interleaved in
+    one continuously running engine.
+
+        srv = Server(max_resident_jobs=32, memory_budget=120 << 30)
+        rid = srv.submit("job/renderJob.json", passes=64, seed=7)
+        for res in srv.poll(wait_ms=1000): img = srv.read(res["id"])
+    """
+
+    def __init__(self, ctx: Context | None = None, **cfg):
+        self.ctx = ctx or default_context()
+        c = native.ServerConfig()
+        for k, v in cfg.items():
+            if not hasattr(c, k):
+                raise TypeError(f"unknown server option {k!r}")
+            setattr(c, k, v)
+        self._h = ctypes.c_void_p()
+        check(native.lib().hasty_server_start(self.ctx._h, ctypes.byref(c), ctypes.byref(self._h)))
+        self._sizes = {}
+
+    def submit(self, job_path: str, passes: int = 0, seed: int | None = None) -> int:
+        rid = ctypes.c_int64()
+        sp = ctypes.byref(ctypes.c_uint64(int(seed))) if seed is not None else None
+        check(native.lib().hasty_server_submit(self._h, job_path.encode(), int(passes), sp, ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self, max_results: int = 256, wait_ms: int = 0) -> list[dict]:
+        buf = (native.ServerResult * max_results)()
+        n = ctypes.c_size_t()
+        check(native.lib().hasty_server_poll(self._h, buf, max_results, ctypes.byref(n), int(wait_ms)))
+        out = []
+        for r in buf[: n.value]:
+            d = {k: getattr(r, k) for k, _ in native.ServerResult._fields_}
+            d["error"] = r.error.decode(errors="replace")
+            self._sizes[r.id] = (r.height, r.width)
+            out.append(d)
+        return out
+
+    def read(self, rid: int, aov: int = AOV_COLOR) -> np.ndarray:
+        h, w = self._sizes[rid]
+        out = np.empty((h, w, 3), dtype=np.float32)
+        check(native.lib().hasty_server_read(self._h, rid, aov, out.ctypes.data, w, h))
+        return out
+
+    def read_sums(self, rid: int, aov: int = AOV_COLOR) -> np.ndarray:
+        h, w = self._sizes[rid]
+        out = np.empty((h, w, 3), dtype=np.float64)
+        check(native.lib().hasty_server_read_sums(self._h, rid, aov, out.ctypes.data, w, h))
+        return out
+
+    def release(self, rid: int) -> None:
+        check(native.lib().hasty_server_release(self._h, rid))
+        self._sizes.pop(rid, None)
+
+    def stats(self) -> dict:
+        s = native.ServerStats()
+        check(native.lib().hasty_server_stats_get(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in native.ServerStats._fields_}
+
+    def wait_idle(self, timeout_ms: int = -1) -> None:
+        check(native.lib().hasty_server_wait_idle(self._h, int(timeout_ms)))
+
+    def stop(self) -> None:
+        if self._h:
+            native.lib().hasty_server_stop(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass

@@ -29,7 +29,7 @@ NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contr
 CU_EXTRA = {"integrator.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-sign-compare"]
 CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu"]
-CPP_SOURCES = ["api.cpp", "engine.cpp", "scene_load.cpp", "bvh_build.cpp", "image_out.cpp"]
+CPP_SOURCES = ["api.cpp", "engine.cpp", "server.cpp", "scene_load.cpp", "bvh_build.cpp", "image_out.cpp"]
 
 
 def cuda_home() -> str:

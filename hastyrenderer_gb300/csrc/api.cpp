@@ -40,7 +40,8 @@ namespace {
 
 }  // namespace
 
-void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st) {
+void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st,
+                             unsigned long long* stats) {
   auto A = [&](size_t bytes) { return alloc(bytes); };
   p.capacity = int32_t(cap);
   size_t c = size_t(cap);
@@ -63,53 +64,88 @@ void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::f
   p.out_color = static_cast<float4*>(A(c * sizeof(float4)));
   p.out_normal = static_cast<float4*>(A(c * sizeof(float4)));
   p.out_albedo = static_cast<float4*>(A(c * sizeof(float4)));
-  p.stats = static_cast<unsigned long long*>(A(size_t(n_stats) * sizeof(unsigned long long)));
-  ck(cudaMemsetAsync(p.stats, 0, sizeof(unsigned long long) * size_t(n_stats), st), "memset stats");
+  if (stats) {
+    p.stats = stats;
+  } else {
+    p.stats = static_cast<unsigned long long*>(A(size_t(n_stats) * sizeof(unsigned long long)));
+    ck(cudaMemsetAsync(p.stats, 0, sizeof(unsigned long long) * size_t(n_stats), st), "memset stats");
+  }
   ck(cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4, st), "memset counts");
 }
 
-void hasty::alloc_paths(hasty_job& j, int64_t cap) {
-  alloc_paths_into(j.pd, cap, ST_COUNT, [&](size_t b) { return static_cast<void*>(j.alloc<uint8_t>(b)); }, j.stream);
+// Path-state buffers of the single-job path are allocated at the first
+// render (jobs that only feed the multi-job engine never need them) and
+// re-allocated when the paths-in-flight setting changes.
+void hasty::ensure_paths(hasty_job& j) {
+  if (j.pd.rng && j.pd.capacity == j.capacity) return;
+  ck(cudaStreamSynchronize(j.stream), "sync");
+  void* olds[] = {j.pd.rng, j.pd.thr, j.pd.rad, j.pd.pend_b, j.pd.nee_c, j.pd.nee_t, j.pd.med, j.pd.med_geom, j.pd.ray_o,
+                  j.pd.ray_d, j.pd.hit, j.pd.pq[0], j.pd.pq[1], j.pd.rq[0], j.pd.rq[1], j.pd.counts, j.pd.out_color,
+                  j.pd.out_normal, j.pd.out_albedo};
+  for (void* p : olds) j.release(p);
+  unsigned long long* stats = j.pd.stats;
+  j.pd = PathsDev{};
+  alloc_paths_into(j.pd, j.capacity, ST_COUNT, [&](size_t b) { return static_cast<void*>(j.alloc<uint8_t>(b)); }, j.stream,
+                   stats);
 }
 
 namespace {
 
-void upload_scene(hasty_job& j) {
+// Host half of the upload: BVH and CDF guide tables (no device work).
+void prepare_scene(hasty_job& j) {
+  if (j.prep) return;
   HostScene& h = j.host;
-  SceneDev& s = j.sd;
-  BvhHost bvh;
+  std::unique_ptr<hasty_job::Prepared> p(new hasty_job::Prepared());
   bool binary = (j.ctx->flags & HASTY_CTX_BINARY_BVH) != 0;
   if (binary) {
-    build_bvh_binary(h.tri_pos.data(), h.n_tris(), 4, bvh);
-    if (bvh.depth > 60) throw ApiError{HASTY_ERR_LOAD, "BVH deeper than the traversal stack (64)"};
+    build_bvh_binary(h.tri_pos.data(), h.n_tris(), 4, p->bvh);
+    if (p->bvh.depth > 60) throw ApiError{HASTY_ERR_LOAD, "BVH deeper than the traversal stack (64)"};
   } else {
-    build_bvh_wide(h.tri_pos.data(), h.n_tris(), bvh);
-    if (bvh.depth > 30) throw ApiError{HASTY_ERR_LOAD, "wide BVH deeper than the traversal stack (32)"};
+    build_bvh_wide(h.tri_pos.data(), h.n_tris(), p->bvh);
+    if (p->bvh.depth > 30) throw ApiError{HASTY_ERR_LOAD, "wide BVH deeper than the traversal stack (32)"};
   }
-  j.bvh_depth = bvh.depth; j.bvh_ms = bvh.build_ms;
+  p->binary = binary;
+  p->light_guide = build_cdf_guide(h.light_cdf, p->light_guide_log2);
+  p->env_guide = build_cdf_guide(h.env_cdf, p->env_guide_log2);
+  j.prep = std::move(p);
+}
+
+template <class T>
+int64_t vec_bytes(const std::vector<T>& v) { return int64_t(v.size() * sizeof(T)); }
+
+// Device bytes upload_scene allocates for a prepared job.
+int64_t upload_bytes(const hasty_job& j) {
+  const HostScene& h = j.host;
+  const hasty_job::Prepared& p = *j.prep;
+  return vec_bytes(h.tri_pos) + vec_bytes(h.tri_attr) + vec_bytes(h.normals) + vec_bytes(h.texcoords) +
+         vec_bytes(p.bvh.nodes) + vec_bytes(p.bvh.tris) + vec_bytes(h.mats) + vec_bytes(h.textures) +
+         vec_bytes(h.tex_pool) + vec_bytes(h.light_tris) + vec_bytes(h.light_cdf) + vec_bytes(p.light_guide) +
+         vec_bytes(h.env_texels) + vec_bytes(h.env_weights) + vec_bytes(h.env_cdf) + vec_bytes(p.env_guide);
+}
+
+void upload_scene(hasty_job& j) {
+  prepare_scene(j);
+  HostScene& h = j.host;
+  SceneDev& s = j.sd;
+  hasty_job::Prepared& p = *j.prep;
+  j.bvh_depth = p.bvh.depth; j.bvh_ms = p.bvh.build_ms;
   s.n_tris = int32_t(h.n_tris());
   s.tri_pos = j.upload(h.tri_pos);
   s.tri_attr = j.upload(h.tri_attr);
   s.normals = j.upload(h.normals);
   s.texcoords = j.upload(h.texcoords);
   s.n_texcoords = int64_t(h.texcoords.size());
-  s.bvh_kind = binary ? 0 : 1;
-  {
-    float4* n = j.alloc<float4>(bvh.nodes.size() / 4);
-    ck(cudaMemcpyAsync(n, bvh.nodes.data(), bvh.nodes.size() * sizeof(float), cudaMemcpyHostToDevice, j.stream), "upload nodes");
-    s.nodes = n;
-    float4* t = j.alloc<float4>(bvh.tris.size() / 4);
-    ck(cudaMemcpyAsync(t, bvh.tris.data(), bvh.tris.size() * sizeof(float), cudaMemcpyHostToDevice, j.stream), "upload tris");
-    s.isect_tris = t;
-    ck(cudaStreamSynchronize(j.stream), "sync upload");   // host vectors of bvh go out of scope
-  }
+  s.bvh_kind = p.binary ? 0 : 1;
+  s.nodes = reinterpret_cast<const float4*>(j.upload(p.bvh.nodes));
+  s.isect_tris = reinterpret_cast<const float4*>(j.upload(p.bvh.tris));
   s.mats = j.upload(h.mats);
   s.textures = j.upload(h.textures);
   s.tex_pool = j.upload(h.tex_pool);
   s.n_light_tris = int32_t(h.light_tris.size());
   s.light_tris = j.upload(h.light_tris);
   s.light_cdf = j.upload(h.light_cdf);
-  s.light_guide = j.upload(build_cdf_guide(h.light_cdf, s.light_guide_log2));
+  s.light_guide = j.upload(p.light_guide);
+  s.light_guide_log2 = p.light_guide_log2;
   s.light_pdf_area = h.light_tris.empty() ? 0.0f : 1.0f / h.total_light_area;
   EnvDev& e = s.env;
   e.is_texture = h.env_texture ? 1 : 0;
@@ -118,7 +154,8 @@ void upload_scene(hasty_job& j) {
   e.texels = j.upload(h.env_texels);
   e.weights = j.upload(h.env_weights);
   e.cdf = j.upload(h.env_cdf);
-  e.guide = j.upload(build_cdf_guide(h.env_cdf, e.guide_log2));
+  e.guide = j.upload(p.env_guide);
+  e.guide_log2 = p.env_guide_log2;
   e.value_sum = h.env_value_sum;
   s.cam = h.cam;
   const RenderSettingsH& st = h.settings;
@@ -127,7 +164,8 @@ void upload_scene(hasty_job& j) {
   s.two_strategies = (h.has_light() && st.use_mis) ? 1 : 0;
   s.env_is_sampled = h.env_texture ? 1 : 0;
   s.p_surface = !h.env_texture ? 1.0f : (!h.light_tris.empty() ? 0.5f : 0.0f);   // Scene.cpp:545
-  ck(cudaStreamSynchronize(j.stream), "sync upload");
+  ck(cudaStreamSynchronize(j.stream), "sync upload");   // the host arrays may be freed after this
+  j.prep.reset();
 }
 
 void clear_accumulators(hasty_job& j) {
@@ -188,6 +226,45 @@ hasty_job* as_job(hasty_job* j) {
 
 }  // namespace
 
+std::unique_ptr<hasty_job> hasty::load_job_host(hasty_ctx* ctx, const std::string& path) {
+  std::unique_ptr<hasty_job> j(new hasty_job());
+  j->ctx = ctx;
+  load_render_job(path, j->host);
+  j->seed = j->host.settings.seed;
+  return j;
+}
+
+void hasty::finish_job_load(hasty_job& job, bool plain) {
+  hasty_job* j = &job;
+  ck(cudaSetDevice(j->ctx->device), "cudaSetDevice");
+  ck(cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking), "stream");
+  upload_scene(*j);
+  int64_t npix = int64_t(j->sd.width) * j->sd.height;
+  j->capacity = default_capacity(npix);
+  if (plain) {
+    j->pd.stats = j->alloc<unsigned long long>(ST_COUNT);
+    for (double*& a : j->acc) a = j->alloc<double>(size_t(npix) * 3);
+    j->est = j->alloc<float>(size_t(npix) * 3);
+    clear_accumulators(*j);
+  }
+  ck(cudaStreamSynchronize(j->stream), "sync");
+  // the host copies of the large arrays are not needed after upload
+  std::vector<float>().swap(j->host.tri_pos);
+  std::vector<float>().swap(j->host.env_texels);
+  std::vector<float>().swap(j->host.tex_pool);
+}
+
+std::unique_ptr<hasty_job> hasty::load_job(hasty_ctx* ctx, const std::string& path, bool plain) {
+  std::unique_ptr<hasty_job> j = load_job_host(ctx, path);
+  finish_job_load(*j, plain);
+  return j;
+}
+
+int64_t hasty::prepare_job_upload(hasty_job& j) {
+  prepare_scene(j);
+  return upload_bytes(j);
+}
+
 extern "C" {
 
 int hasty_last_error(char* buf, size_t len) {
@@ -224,25 +301,7 @@ int hasty_ctx_destroy(hasty_ctx* ctx) { delete ctx; return HASTY_OK; }
 int hasty_job_load(hasty_ctx* ctx, const char* path, hasty_job** out) {
   return guarded([&] {
     if (!ctx || !path || !out) throw ApiError{HASTY_ERR_ARG, "null argument"};
-    ck(cudaSetDevice(ctx->device), "cudaSetDevice");
-    std::unique_ptr<hasty_job> j(new hasty_job());
-    j->ctx = ctx;
-    load_render_job(path, j->host);
-    j->seed = j->host.settings.seed;
-    ck(cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking), "stream");
-    upload_scene(*j);
-    int64_t npix = int64_t(j->sd.width) * j->sd.height;
-    j->capacity = default_capacity(npix);
-    alloc_paths(*j, j->capacity);
-    for (double*& a : j->acc) a = j->alloc<double>(size_t(npix) * 3);
-    j->est = j->alloc<float>(size_t(npix) * 3);
-    clear_accumulators(*j);
-    ck(cudaStreamSynchronize(j->stream), "sync");
-    // the host copies of the large arrays are not needed after upload
-    std::vector<float>().swap(j->host.tri_pos);
-    std::vector<float>().swap(j->host.env_texels);
-    std::vector<float>().swap(j->host.tex_pool);
-    *out = j.release();
+    *out = load_job(ctx, path, true).release();
     return HASTY_OK;
   });
 }
@@ -290,24 +349,8 @@ int hasty_job_set_paths_in_flight(hasty_job* job, int64_t paths) {
     as_job(job);
     int64_t npix = int64_t(job->sd.width) * job->sd.height;
     int64_t cap = paths <= 0 ? default_capacity(npix) : std::max<int64_t>(npix, (paths / npix) * npix);
-    if (cap == job->capacity) return HASTY_OK;
     if (cap > int64_t(INT32_MAX) / 2) throw ApiError{HASTY_ERR_ARG, "too many paths in flight"};
-    ck(cudaStreamSynchronize(job->stream), "sync");
-    // release the old path buffers by rebuilding the allocation list
-    PathsDev old = job->pd;
-    void* olds[] = {old.rng, old.thr, old.rad, old.pend_b, old.nee_c, old.nee_t, old.med, old.med_geom, old.ray_o, old.ray_d,
-                    old.hit, old.pq[0], old.pq[1], old.rq[0], old.rq[1], old.counts, old.out_color, old.out_normal, old.out_albedo};
-    unsigned long long stats_host[ST_COUNT];
-    ck(cudaMemcpy(stats_host, old.stats, sizeof(stats_host), cudaMemcpyDeviceToHost), "copy stats");
-    for (void* p : olds) {
-      auto it = std::find(job->allocs.begin(), job->allocs.end(), p);
-      if (it != job->allocs.end()) { job->allocs.erase(it); cudaFree(p); }
-    }
-    auto sit = std::find(job->allocs.begin(), job->allocs.end(), static_cast<void*>(old.stats));
-    if (sit != job->allocs.end()) { job->allocs.erase(sit); cudaFree(old.stats); }
-    job->capacity = cap;
-    alloc_paths(*job, cap);
-    ck(cudaMemcpy(job->pd.stats, stats_host, sizeof(stats_host), cudaMemcpyHostToDevice), "restore stats");
+    job->capacity = cap;   // the path buffers follow at the next render
     return HASTY_OK;
   });
 }
@@ -317,6 +360,8 @@ int hasty_job_render_passes(hasty_job* job, int n_passes) {
     as_job(job);
     if (n_passes < 0) throw ApiError{HASTY_ERR_ARG, "negative pass count"};
     ck(cudaSetDevice(job->ctx->device), "cudaSetDevice");
+    if (!job->pd.stats) throw ApiError{HASTY_ERR_ARG, "job was loaded for the multi-job engine only"};
+    if (n_passes > 0) ensure_paths(*job);
     int64_t npix = int64_t(job->sd.width) * job->sd.height;
     int per_batch = int(std::max<int64_t>(1, job->capacity / npix));
     int left = n_passes;

@@ -1,166 +1,183 @@
-// Multi-job engine host side: batching (hasty_batch_render) and serving
-// (hasty_server_*). Jobs stay resident (scene, BVH and accumulators are the
-// jobs' own device buffers); the engine owns one pool of path slots and a
-// CUDA graph whose conditional while-node repeats one iteration
-// (regenerate, trace, shade, condition) on the device until every issued
-// sample is finished or the wave's iteration budget is spent.
-#include <cuda_runtime.h>
+// Multi-job engine (engine.h) and batching: hasty_batch_render renders many
+// resident jobs in one persistent wavefront run.
+#include "engine.h"
 
 #include <algorithm>
 #include <chrono>
 #include <cstring>
-#include <deque>
 #include <memory>
-#include <mutex>
-#include <thread>
 #include <vector>
-
-#include "job.h"
 
 namespace hasty {
 
-struct Engine {
-  hasty_ctx* ctx = nullptr;
-  cudaStream_t stream = nullptr;
-  std::vector<void*> allocs;
-  int64_t bytes = 0;
-  PathsDev pd{};
-  MultiDev md{};
-  int64_t cap = 0;
-  int max_jobs = 0;
-  JobDev* d_jobs = nullptr;
-  int32_t* d_njobs = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  uint32_t iterations = 0;
-
-  void* alloc(size_t b) {
-    void* p = nullptr;
-    ck(cudaMalloc(&p, std::max<size_t>(b, 16)), "cudaMalloc (engine)");
-    allocs.push_back(p);
-    bytes += int64_t(b);
-    return p;
-  }
-
-  void init(hasty_ctx* c, int64_t capacity, int jobs_max, uint32_t regen_below, uint32_t max_iter) {
-    ctx = c;
-    ck(cudaSetDevice(ctx->device), "cudaSetDevice");
-    ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
-    cap = capacity;
-    max_jobs = jobs_max;
-    alloc_paths_into(pd, cap, MS_COUNT, [&](size_t b) { return alloc(b); }, stream);
-    d_jobs = static_cast<JobDev*>(alloc(sizeof(JobDev) * size_t(max_jobs)));
-    d_njobs = static_cast<int32_t*>(alloc(sizeof(int32_t)));
-    md.jobs = d_jobs;
-    md.n_jobs = d_njobs;
-    md.slot_job = static_cast<int32_t*>(alloc(sizeof(int32_t) * size_t(cap)));
-    md.slot_sample = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * size_t(cap)));
-    md.free_slots = static_cast<int32_t*>(alloc(sizeof(int32_t) * size_t(cap)));
-    md.free_count = static_cast<uint32_t*>(alloc(sizeof(uint32_t)));
-    md.next_sample = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
-    md.total_samples = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
-    md.regen_base = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
-    md.ctl = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 8));
-    md.regen_below = regen_below;
-    md.max_iter = max_iter;
-    ck(cudaMemsetAsync(d_njobs, 0, sizeof(int32_t), stream), "memset");
-    ck(cudaMemsetAsync(md.next_sample, 0, sizeof(unsigned long long), stream), "memset");
-    ck(cudaMemsetAsync(md.total_samples, 0, sizeof(unsigned long long), stream), "memset");
-    launch_multi_init(pd, md, int(cap), stream);
-    ck(cudaGetLastError(), "engine init");
-    build_graph();
-    ck(cudaStreamSynchronize(stream), "engine init");
-  }
-
-  void build_graph() {
-    ck(cudaGraphCreate(&graph, 0), "cudaGraphCreate");
-    cudaGraphConditionalHandle h;
-    ck(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault), "conditional handle");
-    cudaGraphNodeParams np = {};
-    np.type = cudaGraphNodeTypeConditional;
-    np.conditional.handle = h;
-    np.conditional.type = cudaGraphCondTypeWhile;
-    np.conditional.size = 1;
-    cudaGraphNode_t node;
-    ck(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np), "add conditional node");
-    cudaGraph_t body = np.conditional.phGraph_out[0];
-    ck(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "begin capture");
-    launch_multi_iteration(pd, md, int(cap), (unsigned long long)h, 1, stream);
-    cudaGraph_t captured = nullptr;
-    ck(cudaStreamEndCapture(stream, &captured), "end capture");
-    ck(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
-  }
-
-  // Replace the device job table (jobs in sample order) and the total.
-  void set_jobs(const std::vector<JobDev>& jobs, unsigned long long total) {
-    if (int(jobs.size()) > max_jobs) throw ApiError{HASTY_ERR_ARG, "too many jobs for the engine"};
-    int32_t n = int32_t(jobs.size());
-    if (n) ck(cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(JobDev) * jobs.size(), cudaMemcpyHostToDevice, stream), "jobs");
-    ck(cudaMemcpyAsync(d_njobs, &n, sizeof(n), cudaMemcpyHostToDevice, stream), "n_jobs");
-    ck(cudaMemcpyAsync(md.total_samples, &total, sizeof(total), cudaMemcpyHostToDevice, stream), "total");
-    ck(cudaStreamSynchronize(stream), "set jobs");
-  }
-
-  // Runs up to n_iter iterations on the device (one graph launch); returns
-  // true while work remains.
-  bool run_wave(uint32_t n_iter, bool* bound_hit) {
-    uint32_t end = iterations + n_iter;
-    ck(cudaMemcpyAsync(&md.ctl[7], &end, sizeof(end), cudaMemcpyHostToDevice, stream), "wave end");
-    ck(cudaGraphLaunch(exec, stream), "cudaGraphLaunch");
-    uint32_t ctl[8];
-    unsigned long long ns[2];
-    uint32_t counts[4];
-    ck(cudaMemcpyAsync(ctl, md.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stream), "ctl");
-    ck(cudaMemcpyAsync(ns, md.next_sample, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream), "next");
-    ck(cudaMemcpyAsync(ns + 1, md.total_samples, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream), "total");
-    ck(cudaMemcpyAsync(counts, pd.counts, sizeof(counts), cudaMemcpyDeviceToHost, stream), "counts");
-    ck(cudaStreamSynchronize(stream), "wave");
-    iterations = ctl[5];
-    if (bound_hit) *bound_hit = ctl[6] != 0;
-    return counts[ctl[0]] > 0 || ns[0] < ns[1];
-  }
-
-  void stats(unsigned long long* out) {
-    ck(cudaMemcpy(out, pd.stats, sizeof(unsigned long long) * MS_COUNT, cudaMemcpyDeviceToHost), "stats");
-  }
-
-  ~Engine() {
-    if (stream) cudaStreamSynchronize(stream);
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    for (void* p : allocs) cudaFree(p);
-    if (stream) cudaStreamDestroy(stream);
-  }
-};
-
-namespace {
-
-int64_t pool_size(const hasty_batch_config* cfg) {
-  if (cfg && cfg->paths_in_flight > 0) return cfg->paths_in_flight;
-  return int64_t(1) << 22;
+void* Engine::alloc(size_t b) {
+  void* p = nullptr;
+  ck(cudaMalloc(&p, std::max<size_t>(b, 16)), "cudaMalloc (engine)");
+  allocs.push_back(p);
+  bytes += int64_t(b);
+  return p;
 }
 
-uint32_t regen_threshold(const hasty_batch_config* cfg, int64_t cap) {
-  float f = (cfg && cfg->regen_fraction > 0.f) ? cfg->regen_fraction : 0.9f;
+void Engine::init(hasty_ctx* c, int64_t capacity, int slots, uint32_t segments, uint32_t regen_below, uint32_t max_iter) {
+  ctx = c;
+  ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+  if (capacity < 1 || capacity > int64_t(INT32_MAX) / 2) throw ApiError{HASTY_ERR_ARG, "bad paths-in-flight value"};
+  if (slots < 1) throw ApiError{HASTY_ERR_ARG, "engine needs at least one job slot"};
+  ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
+  cap = capacity;
+  job_slots = slots;
+  seg_cap = 64;
+  while (seg_cap < segments) {
+    if (seg_cap >= (1u << 30)) throw ApiError{HASTY_ERR_ARG, "too many segments"};
+    seg_cap <<= 1;
+  }
+  alloc_paths_into(pd, cap, MS_COUNT, [&](size_t b) { return alloc(b); }, stream);
+  d_jobs = static_cast<JobDev*>(alloc(sizeof(JobDev) * size_t(job_slots)));
+  d_segs = static_cast<SegDev*>(alloc(sizeof(SegDev) * size_t(seg_cap)));
+  d_window = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 2));
+  d_done = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long) * size_t(job_slots)));
+  md.jobs = d_jobs;
+  md.segs = d_segs;
+  md.seg_mask = seg_cap - 1u;
+  md.seg_window = d_window;
+  md.slot_job = static_cast<int32_t*>(alloc(sizeof(int32_t) * size_t(cap)));
+  md.slot_px = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * size_t(cap)));
+  md.slot_pass = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * size_t(cap)));
+  md.free_slots = static_cast<int32_t*>(alloc(sizeof(int32_t) * size_t(cap)));
+  md.free_count = static_cast<uint32_t*>(alloc(sizeof(uint32_t)));
+  md.next_sample = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
+  md.total_samples = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
+  md.regen_base = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
+  md.ctl = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 8));
+  md.regen_below = regen_below;
+  md.max_iter = max_iter;
+  ck(cudaMemsetAsync(d_window, 0, sizeof(uint32_t) * 2, stream), "memset");
+  ck(cudaMemsetAsync(d_done, 0, sizeof(unsigned long long) * size_t(job_slots), stream), "memset");
+  ck(cudaMemsetAsync(d_jobs, 0, sizeof(JobDev) * size_t(job_slots), stream), "memset");
+  ck(cudaMemsetAsync(md.next_sample, 0, sizeof(unsigned long long), stream), "memset");
+  ck(cudaMemsetAsync(md.total_samples, 0, sizeof(unsigned long long), stream), "memset");
+  launch_multi_init(pd, md, int(cap), stream);
+  ck(cudaGetLastError(), "engine init");
+  build_graph();
+  ck(cudaStreamSynchronize(stream), "engine init");
+}
+
+void Engine::build_graph() {
+  ck(cudaGraphCreate(&graph, 0), "cudaGraphCreate");
+  cudaGraphConditionalHandle h;
+  ck(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault), "conditional handle");
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  ck(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np), "add conditional node");
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  ck(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "begin capture");
+  launch_multi_iteration(pd, md, int(cap), (unsigned long long)h, 1, stream);
+  cudaGraph_t captured = nullptr;
+  ck(cudaStreamEndCapture(stream, &captured), "end capture");
+  ck(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
+}
+
+void Engine::set_job(int slot, const JobDev& j) {
+  if (slot < 0 || slot >= job_slots) throw ApiError{HASTY_ERR_ARG, "job slot out of range"};
+  JobDev e = j;
+  e.done = d_done + slot;
+  ck(cudaMemcpyAsync(d_jobs + slot, &e, sizeof(JobDev), cudaMemcpyHostToDevice, stream), "job entry");
+  ck(cudaMemsetAsync(d_done + slot, 0, sizeof(unsigned long long), stream), "done counter");
+}
+
+void Engine::append(int slot, uint32_t pass, uint32_t npix) {
+  if (free_segments() == 0) throw ApiError{HASTY_ERR_ARG, "engine segment ring is full"};
+  SegDev s;
+  s.begin = total;
+  s.job = slot;
+  s.pass = pass;
+  staged.push_back(s);
+  spans.emplace_back(total, npix);
+  total += npix;
+  ++seg_hi;
+}
+
+void Engine::publish() {
+  // staged segments occupy logical indices [seg_hi - staged.size(), seg_hi)
+  uint32_t first = seg_hi - uint32_t(staged.size());
+  size_t k = 0;
+  while (k < staged.size()) {
+    uint32_t phys = (first + uint32_t(k)) & (seg_cap - 1u);
+    size_t run = std::min<size_t>(staged.size() - k, size_t(seg_cap - phys));
+    ck(cudaMemcpyAsync(d_segs + phys, staged.data() + k, sizeof(SegDev) * run, cudaMemcpyHostToDevice, stream), "segments");
+    k += run;
+  }
+  staged.clear();
+  uint32_t window[2] = {seg_lo, seg_hi};
+  ck(cudaMemcpyAsync(d_window, window, sizeof(window), cudaMemcpyHostToDevice, stream), "segment window");
+  unsigned long long t = total;
+  ck(cudaMemcpyAsync(md.total_samples, &t, sizeof(t), cudaMemcpyHostToDevice, stream), "total");
+  // the sources are host stack/heap memory: make the copies complete before they go out of scope
+  ck(cudaStreamSynchronize(stream), "publish");
+}
+
+bool Engine::run_wave(uint32_t n_iter, bool* bound_hit) {
+  if (!staged.empty()) publish();
+  uint32_t end = iterations + std::max<uint32_t>(n_iter, 1u);
+  ck(cudaMemcpyAsync(&md.ctl[7], &end, sizeof(end), cudaMemcpyHostToDevice, stream), "wave end");
+  ck(cudaGraphLaunch(exec, stream), "cudaGraphLaunch");
+  uint32_t ctl[8];
+  unsigned long long ns = 0;
+  uint32_t counts[4];
+  ck(cudaMemcpyAsync(ctl, md.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stream), "ctl");
+  ck(cudaMemcpyAsync(&ns, md.next_sample, sizeof(ns), cudaMemcpyDeviceToHost, stream), "next");
+  ck(cudaMemcpyAsync(counts, pd.counts, sizeof(counts), cudaMemcpyDeviceToHost, stream), "counts");
+  ck(cudaStreamSynchronize(stream), "wave");
+  iterations = ctl[5];
+  if (bound_hit) *bound_hit = ctl[6] != 0;
+  next = ns;
+  live = counts[ctl[0] & 1u];
+  // segments wholly issued are no longer looked up
+  bool moved = false;
+  while (!spans.empty() && spans.front().first + spans.front().second <= next) {
+    spans.pop_front();
+    ++seg_lo;
+    moved = true;
+  }
+  if (moved) {
+    uint32_t lo = seg_lo;
+    ck(cudaMemcpyAsync(d_window, &lo, sizeof(lo), cudaMemcpyHostToDevice, stream), "segment window");
+    ck(cudaStreamSynchronize(stream), "segment window");
+  }
+  return busy();
+}
+
+void Engine::read_done(std::vector<unsigned long long>& out) {
+  out.resize(size_t(job_slots));
+  ck(cudaMemcpyAsync(out.data(), d_done, sizeof(unsigned long long) * out.size(), cudaMemcpyDeviceToHost, stream), "done");
+  ck(cudaStreamSynchronize(stream), "done");
+}
+
+void Engine::stats(unsigned long long* out) {
+  ck(cudaMemcpyAsync(out, pd.stats, sizeof(unsigned long long) * MS_COUNT, cudaMemcpyDeviceToHost, stream), "stats");
+  ck(cudaStreamSynchronize(stream), "stats");
+}
+
+Engine::~Engine() {
+  if (stream) cudaStreamSynchronize(stream);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  for (void* p : allocs) cudaFree(p);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+int64_t engine_pool_size(int64_t requested) { return requested > 0 ? requested : (int64_t(1) << 22); }
+
+uint32_t engine_regen_threshold(float fraction, int64_t cap) {
+  float f = fraction > 0.f ? fraction : 0.9f;
   if (f >= 1.0f) return uint32_t(cap) + 1u;
   return uint32_t(double(cap) * double(f));
 }
 
-JobDev job_entry(hasty_job* j, unsigned long long* acc, unsigned long long* done, unsigned long long begin, int passes) {
-  JobDev d;
-  std::memset(&d, 0, sizeof(d));
-  d.sc = j->sd;
-  d.acc = acc;
-  d.done = done;
-  d.seed = j->seed;
-  d.sample_begin = begin;
-  d.pass_base = uint32_t(j->samples_done);
-  d.npix = uint32_t(j->sd.width) * uint32_t(j->sd.height);
-  d.n_samples = uint64_t(passes) * d.npix;
-  return d;
-}
-
-}  // namespace
 }  // namespace hasty
 
 using namespace hasty;
@@ -171,30 +188,39 @@ int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, 
                        hasty_batch_stats* out) {
   return guarded([&] {
     if (!ctx || (n_jobs && (!jobs || !passes))) throw ApiError{HASTY_ERR_ARG, "null argument"};
+    uint64_t n_segments = 0;
     for (size_t i = 0; i < n_jobs; ++i) {
       if (!jobs[i] || passes[i] < 0) throw ApiError{HASTY_ERR_ARG, "bad job or pass count"};
       if (jobs[i]->ctx != ctx) throw ApiError{HASTY_ERR_ARG, "job belongs to another context"};
       if (jobs[i]->sd.max_depth <= 0) throw ApiError{HASTY_ERR_ARG, "max_depth must be positive for batching"};
+      if (!jobs[i]->acc[0]) throw ApiError{HASTY_ERR_ARG, "job has no accumulators"};
+      n_segments += uint64_t(passes[i]);
       ck(cudaStreamSynchronize(jobs[i]->stream), "job sync");
     }
+    if (n_segments >= (uint64_t(1) << 30)) throw ApiError{HASTY_ERR_ARG, "too many passes in one batch"};
     auto t0 = std::chrono::steady_clock::now();
     Engine e;
-    int64_t cap = pool_size(cfg);
+    int64_t cap = engine_pool_size(cfg ? cfg->paths_in_flight : 0);
     uint32_t max_iter = (cfg && cfg->max_iterations > 0) ? uint32_t(cfg->max_iterations) : 50000000u;
-    e.init(ctx, cap, int(std::max<size_t>(n_jobs, 1)), regen_threshold(cfg, cap), max_iter);
-    std::vector<JobDev> table;
+    e.init(ctx, cap, int(std::max<size_t>(n_jobs, 1)), uint32_t(std::max<uint64_t>(n_segments, 1)),
+           engine_regen_threshold(cfg ? cfg->regen_fraction : 0.f, cap), max_iter);
     std::vector<unsigned long long*> accs(n_jobs);
-    unsigned long long* done = static_cast<unsigned long long*>(e.alloc(sizeof(unsigned long long) * std::max<size_t>(n_jobs, 1)));
-    ck(cudaMemsetAsync(done, 0, sizeof(unsigned long long) * std::max<size_t>(n_jobs, 1), e.stream), "memset");
-    unsigned long long total = 0;
     for (size_t i = 0; i < n_jobs; ++i) {
-      size_t npix = size_t(jobs[i]->sd.width) * size_t(jobs[i]->sd.height);
-      accs[i] = static_cast<unsigned long long*>(e.alloc(sizeof(unsigned long long) * 9 * npix));
-      ck(cudaMemsetAsync(accs[i], 0, sizeof(unsigned long long) * 9 * npix, e.stream), "memset acc");
-      table.push_back(job_entry(jobs[i], accs[i], done + i, total, passes[i]));
-      total += table.back().n_samples;
+      hasty_job* j = jobs[i];
+      uint32_t npix = uint32_t(j->sd.width) * uint32_t(j->sd.height);
+      accs[i] = static_cast<unsigned long long*>(e.alloc(sizeof(unsigned long long) * 9 * size_t(npix)));
+      ck(cudaMemsetAsync(accs[i], 0, sizeof(unsigned long long) * 9 * size_t(npix), e.stream), "memset acc");
+      JobDev d;
+      std::memset(&d, 0, sizeof(d));
+      d.sc = j->sd;
+      d.acc = accs[i];
+      d.seed = j->seed;
+      d.npix = npix;
+      e.set_job(int(i), d);
+      // jobs in order, each job's passes in order
+      for (int32_t p = 0; p < passes[i]; ++p) e.append(int(i), uint32_t(j->samples_done + p), npix);
     }
-    e.set_jobs(table, total);
+    e.publish();
     cudaEvent_t a, b;
     ck(cudaEventCreate(&a), "event"); ck(cudaEventCreate(&b), "event");
     ck(cudaEventRecord(a, e.stream), "event");
@@ -214,13 +240,12 @@ int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, 
     }
     ck(cudaGetLastError(), "fold");
     unsigned long long st[MS_COUNT];
-    ck(cudaStreamSynchronize(e.stream), "fold");
     e.stats(st);
     if (out) {
       std::memset(out, 0, sizeof(*out));
       out->device_ms = ms;
       out->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-      out->samples = total;
+      out->samples = e.total;
       out->rays = st[MS_RAYS]; out->shaded = st[MS_SHADED]; out->nan_samples = st[MS_NAN];
       out->saturated = st[MS_SATURATED]; out->iterations = e.iterations; out->paths_in_flight = e.cap;
       out->engine_bytes = e.bytes;

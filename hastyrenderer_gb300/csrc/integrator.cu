@@ -431,13 +431,15 @@ namespace hasty {
 namespace {
 using namespace dev;
 
-__device__ __forceinline__ int find_job(const MultiDev& m, unsigned long long g) {
-  int lo = 0, hi = *m.n_jobs - 1;
+// Last live segment whose first sample is <= g (segments are contiguous and
+// in increasing order of `begin`).
+__device__ __forceinline__ const SegDev& find_segment(const MultiDev& m, unsigned long long g) {
+  uint32_t lo = m.seg_window[0], hi = m.seg_window[1] - 1u;
   while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (m.jobs[mid].sample_begin <= g) lo = mid; else hi = mid - 1;
+    uint32_t mid = lo + ((hi - lo + 1u) >> 1);
+    if (m.segs[mid & m.seg_mask].begin <= g) lo = mid; else hi = mid - 1u;
   }
-  return lo;
+  return m.segs[lo & m.seg_mask];
 }
 
 __global__ void k_multi_init(PathsDev P, MultiDev m, int cap) {
@@ -480,14 +482,15 @@ __global__ void __launch_bounds__(256) k_multi_regen(PathsDev P, MultiDev m) {
   uint32_t q = m.ctl[0];
   int s = m.free_slots[m.ctl[2] - 1 - i];
   unsigned long long g = *m.regen_base + i;
-  int j = find_job(m, g);
+  const SegDev& seg = find_segment(m, g);
+  const int j = seg.job;
+  const uint32_t pass = seg.pass;
+  const uint32_t px = uint32_t(g - seg.begin);
   const JobDev& job = m.jobs[j];
   const SceneDev& sc = job.sc;
-  uint32_t l = uint32_t(g - job.sample_begin);
-  uint32_t pass = job.pass_base + l / job.npix;
-  uint32_t px = l % job.npix;
   m.slot_job[s] = j;
-  m.slot_sample[s] = l;
+  m.slot_px[s] = px;
+  m.slot_pass[s] = pass;
   int x = int(px % uint32_t(sc.width)), y = int(px / uint32_t(sc.width));
   Rng r; r.seed(path_key(job.seed, px, pass));
   float ox = halton(2, pass), oy = halton(3, pass);
@@ -540,9 +543,8 @@ __global__ void __launch_bounds__(128) k_shade_multi(PathsDev P, MultiDev m) {
   bool finished = false;
   if (valid) {
     const JobDev& job = m.jobs[j];
-    uint32_t l = m.slot_sample[s];
-    uint32_t px = l % job.npix;
-    res = shade_path(job.sc, P, s, path_key(job.seed, px, job.pass_base + l / job.npix));
+    const uint32_t px = m.slot_px[s];
+    res = shade_path(job.sc, P, s, path_key(job.seed, px, m.slot_pass[s]));
     if (!res.keep) {
       finished = true;
       if (has_nan(res.L)) atomicAdd(&P.stats[ST_NAN], 1ull);

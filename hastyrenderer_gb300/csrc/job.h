@@ -4,11 +4,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <functional>
 #include <atomic>
+#include <cstddef>
+#include <functional>
+#include <memory>
 #include <string>
 #include <vector>
 
+#include "bvh_build.h"
 #include "hasty_gpu.h"
 #include "scene_load.h"
 #include "wavefront.h"
@@ -66,7 +69,16 @@ struct hasty_job {
   SceneDev sd{};
   PathsDev pd{};
   cudaStream_t stream = nullptr;
-  std::vector<void*> allocs;
+  // host-side scene data between prepare and upload (BVH, guide tables)
+  struct Prepared {
+    hasty::BvhHost bvh;
+    bool binary = false;
+    std::vector<uint32_t> light_guide, env_guide;
+    uint32_t light_guide_log2 = 0, env_guide_log2 = 0;
+  };
+  std::unique_ptr<Prepared> prep;
+  struct Block { void* p; size_t bytes; };
+  std::vector<Block> allocs;
   int64_t bytes = 0;
   double* acc[3] = {nullptr, nullptr, nullptr};
   float* est = nullptr;
@@ -86,9 +98,21 @@ struct hasty_job {
     void* p = nullptr;
     size_t b = std::max<size_t>(n, 1) * sizeof(T);
     ck(cudaMalloc(&p, b), "cudaMalloc");
-    allocs.push_back(p);
+    allocs.push_back({p, b});
     bytes += int64_t(b);
     return static_cast<T*>(p);
+  }
+  // Frees one block obtained from alloc (no-op for null or foreign pointers).
+  void release(void* p) {
+    if (!p) return;
+    for (size_t i = 0; i < allocs.size(); ++i) {
+      if (allocs[i].p == p) {
+        cudaFree(p);
+        bytes -= int64_t(allocs[i].bytes);
+        allocs.erase(allocs.begin() + std::ptrdiff_t(i));
+        return;
+      }
+    }
   }
   template <class T>
   T* upload(const std::vector<T>& v) {
@@ -110,14 +134,28 @@ struct hasty_job {
   ~hasty_job() {
     if (stream) cudaStreamSynchronize(stream);
     collect_events();
-    for (void* p : allocs) cudaFree(p);
+    for (const Block& b : allocs) cudaFree(b.p);
     if (stream) cudaStreamDestroy(stream);
   }
 };
 
 
 namespace hasty {
-// Path-state buffers for `cap` slots (api.cpp).
-void alloc_paths(hasty_job& j, int64_t cap);
-void alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st);
+// Carves path-state buffers for `cap` slots out of `alloc` and clears the
+// queue counters; statistics are carved and cleared too unless `stats` is
+// given (api.cpp).
+void alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st,
+                      unsigned long long* stats = nullptr);
+// Single-job path state sized to j.capacity, allocated on first use.
+void ensure_paths(hasty_job& j);
+// Loads renderJob.json, builds the BVH and uploads the scene. `plain`: also
+// the FP64 accumulators, estimate buffer and statistics of the single-job
+// path; without it the job holds only the scene (multi-job engine use).
+std::unique_ptr<hasty_job> load_job(hasty_ctx* ctx, const std::string& path, bool plain);
+// The halves of load_job: host parse (no device work), then BVH build and
+// upload. prepare_job_upload builds the BVH and guide tables on the host and
+// returns the exact device bytes the scene upload will take.
+std::unique_ptr<hasty_job> load_job_host(hasty_ctx* ctx, const std::string& path);
+int64_t prepare_job_upload(hasty_job& j);
+void finish_job_load(hasty_job& j, bool plain);
 }  // namespace hasty

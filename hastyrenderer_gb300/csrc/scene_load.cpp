@@ -393,9 +393,8 @@ float halton_value(uint32_t base, uint32_t k) {
   return float(n) / float(d);
 }
 
-void load_render_job(const std::string& job_path, HostScene& sc) {
+void load_job_settings(const std::string& job_path, RenderSettingsH& st, std::string& scene_path) {
   JNode job = read_json(job_path);
-  RenderSettingsH& st = sc.settings;
   if (const JNode* s = job.get("settings")) {                 // RenderJob.cpp:10-20
     if (const JNode* v = s->get("roulette_start_depth")) st.roulette_start = int(v->number());
     if (const JNode* v = s->get("roulette_q")) st.roulette_q = float(v->number());
@@ -408,7 +407,24 @@ void load_render_job(const std::string& job_path, HostScene& sc) {
   }
   if (const JNode* g = job.get("gb300")) if (const JNode* v = g->get("seed")) st.seed = uint64_t(v->number());
   if (st.width == 0 || st.height == 0) throw LoadError("settings: width and height must be positive");
-  std::string scene_path = resolve(folder_of(job_path), job.req("scene").str());
+  scene_path = resolve(folder_of(job_path), job.req("scene").str());
+}
+
+void check_job_settings(const RenderSettingsH& st, const HostScene& sc) {
+  // Constant non-black background, MIS on, no emissive triangle: the
+  // reference exits at its first light sample (Scene.cpp:506-511).
+  if (st.use_mis && sc.light_tris.empty() && !sc.env_texture && sc.has_light())
+    throw LoadError("error: no light triangle found (constant background with MIS needs an emissive triangle)");
+}
+
+void load_render_job(const std::string& job_path, HostScene& sc) {
+  std::string scene_path;
+  load_job_settings(job_path, sc.settings, scene_path);
+  load_scene_file(scene_path, sc);
+  check_job_settings(sc.settings, sc);
+}
+
+void load_scene_file(const std::string& scene_path, HostScene& sc) {
   std::string folder = folder_of(scene_path);
   JNode scene = read_json(scene_path);
   setup_camera(scene.req("camera"), sc.cam);
@@ -509,10 +525,6 @@ void load_render_job(const std::string& job_path, HostScene& sc) {
   float ta = 0.f;
   for (float a : areas) ta += a;
   sc.total_light_area = ta;
-  // Constant non-black background, MIS on, no emissive triangle: the
-  // reference exits at its first light sample (Scene.cpp:506-511).
-  if (st.use_mis && sc.light_tris.empty() && !sc.env_texture && sc.has_light())
-    throw LoadError("error: no light triangle found (constant background with MIS needs an emissive triangle)");
 }
 
 }  // namespace hasty

@@ -63,6 +63,12 @@ struct HostScene {
 
 // Loads renderJob.json and everything it references. Throws LoadError.
 void load_render_job(const std::string& job_path, HostScene& out);
+// The parts of load_render_job: the job file's settings and scene path; the
+// scene file (camera, world, mesh, materials, lights; `out.settings` is left
+// as it is); the checks that depend on both.
+void load_job_settings(const std::string& job_path, RenderSettingsH& st, std::string& scene_path);
+void load_scene_file(const std::string& scene_path, HostScene& out);
+void check_job_settings(const RenderSettingsH& st, const HostScene& sc);
 
 // libstdc++'s std::discrete_distribution table: weights normalised by their
 // sequential double sum, running sums, last entry forced to 1. Fewer than

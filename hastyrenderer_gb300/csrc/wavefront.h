@@ -69,9 +69,11 @@ void launch_trace_rays(const SceneDev& sc, const float* rays, int n, float4* hit
 
 // ---------------------------------------------------------------------------
 // Multi-job engine (batching and serving). Many resident jobs share one pool
-// of path slots; camera samples are issued in global order (jobs in the order
-// they were added, each job's samples pass-major) into whatever slots are
-// free, so the pool stays full until the last sample (path regeneration).
+// of path slots. Work is a sequence of segments, each one pass of one job
+// (W*H camera samples); camera samples are issued in global order through the
+// segments into whatever slots are free, so the pool stays full until the
+// last sample (path regeneration). The host appends segments between engine
+// waves (serving interleaves the passes of the resident jobs this way).
 // Finished samples are added to per-job int64 fixed-point accumulators
 // (2^-32 units): integer addition is order-independent, so a job's image is
 // bit-identical however it is mixed with other jobs.
@@ -82,17 +84,25 @@ struct JobDev {
   unsigned long long* acc;     // 9 int64 per pixel: colour, normal, albedo (two's complement)
   unsigned long long* done;    // finished camera samples
   uint64_t seed;
-  uint64_t sample_begin;       // first global sample index of the job
-  uint64_t n_samples;          // passes * W * H
-  uint32_t pass_base;          // pass index of the job's first sample
   uint32_t npix;
 };
 
+// One pass of one job: global samples [begin, begin + npix) of the job table
+// entry `job`, pixel = global sample - begin.
+struct SegDev {
+  unsigned long long begin;
+  int32_t job;
+  uint32_t pass;
+};
+
 struct MultiDev {
-  const JobDev* jobs;
-  const int32_t* n_jobs;       // device-resident, so a captured graph stays valid as jobs are added
+  const JobDev* jobs;          // job table (entries are reused once a job has finished)
+  const SegDev* segs;          // ring of segments, power-of-two capacity
+  uint32_t seg_mask;
+  const uint32_t* seg_window;  // [lo, hi): logical indices of the live segments (device-resident)
   int32_t* slot_job;           // job of the path in each slot
-  uint32_t* slot_sample;       // job-local sample index (pass_local * npix + pixel)
+  uint32_t* slot_px;           // pixel of the path's camera sample
+  uint32_t* slot_pass;         // pass of the path's camera sample
   int32_t* free_slots;         // stack of free slot ids
   uint32_t* free_count;
   unsigned long long* next_sample;

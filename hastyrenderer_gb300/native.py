@@ -53,6 +53,29 @@ class BatchStats(ctypes.Structure):
                 ("engine_bytes", ctypes.c_int64)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("paths_in_flight", ctypes.c_int64), ("regen_fraction", ctypes.c_float),
+                ("max_resident_jobs", ctypes.c_int32), ("max_resident_scenes", ctypes.c_int32),
+                ("wave_iterations", ctypes.c_int32), ("memory_budget", ctypes.c_int64),
+                ("lookahead_samples", ctypes.c_int64), ("loader_threads", ctypes.c_int32)]
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("status", ctypes.c_int32), ("width", ctypes.c_int32),
+                ("height", ctypes.c_int32), ("passes", ctypes.c_int32), ("samples", ctypes.c_uint64),
+                ("submit_ms", ctypes.c_double), ("admit_ms", ctypes.c_double), ("finish_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double), ("error", ctypes.c_char * 160)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("admitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("samples", ctypes.c_uint64), ("rays", ctypes.c_uint64),
+                ("shaded", ctypes.c_uint64), ("waves", ctypes.c_uint64), ("iterations", ctypes.c_uint64),
+                ("device_ms", ctypes.c_double), ("uptime_ms", ctypes.c_double), ("resident_bytes", ctypes.c_int64),
+                ("peak_resident_bytes", ctypes.c_int64), ("engine_bytes", ctypes.c_int64),
+                ("resident_jobs", ctypes.c_int32), ("resident_scenes", ctypes.c_int32), ("pending", ctypes.c_int32)]
+
+
 def declared_symbols(header: str = HEADER) -> list[str]:
     """Function names declared in the C header."""
     text = open(header).read()
@@ -95,6 +118,15 @@ def lib() -> ctypes.CDLL:
         "hasty_debug_bsdf": [I, P, SZ, P, SZ, P],
         "hasty_batch_render": [P, P, P, SZ, P, P],
         "hasty_job_render_pass_static": [P, I, P],
+        "hasty_server_start": [P, P, P],
+        "hasty_server_submit": [P, ctypes.c_char_p, ctypes.c_int32, P, P],
+        "hasty_server_poll": [P, P, SZ, P, ctypes.c_int32],
+        "hasty_server_read": [P, ctypes.c_int64, I, P, SZ, SZ],
+        "hasty_server_read_sums": [P, ctypes.c_int64, I, P, SZ, SZ],
+        "hasty_server_release": [P, ctypes.c_int64],
+        "hasty_server_stats_get": [P, P],
+        "hasty_server_wait_idle": [P, ctypes.c_int32],
+        "hasty_server_stop": [P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

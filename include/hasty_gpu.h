@@ -147,6 +147,74 @@ typedef struct hasty_batch_stats {
 int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, size_t n_jobs,
                        const hasty_batch_config* cfg, hasty_batch_stats* stats);
 
+/* ---- Serving: a request loop over the multi-job engine ---------------------
+ * Requests (a renderJob.json, a pass count, a seed) are admitted while job
+ * slots and the device-memory budget allow: scene + BVH + textures of each
+ * resident scene, 72 B per pixel of fixed-point sums per resident request,
+ * plus the engine's path pool. Scenes are cached by scene file and shared by
+ * the requests that use them; a scene no request uses is evicted when room is
+ * needed. Loader threads parse scenes and build BVHs on the host while the
+ * engine renders. Resident requests' passes are interleaved round-robin in one
+ * continuously running engine, so requests that arrive while others render
+ * start as soon as path slots free up. A request's result is bit-identical to
+ * hasty_batch_render of the same job, seed and pass count, alone or in any mix.
+ * The server's functions are internally synchronised (any host thread).
+ * No counterpart in the reference (its viewer renders one job per process). */
+typedef struct hasty_server hasty_server;
+
+typedef struct hasty_server_config {
+  int64_t paths_in_flight;     /* engine path pool; 0 = 4M */
+  float regen_fraction;        /* as hasty_batch_config; 0 = 0.9 */
+  int32_t max_resident_jobs;   /* requests rendering at once; 0 = 32 */
+  int32_t max_resident_scenes; /* scenes kept on the device; 0 = 32 */
+  int32_t wave_iterations;     /* engine iterations between host checks; 0 = 16 */
+  int64_t memory_budget;       /* device bytes; 0 = 120 GB */
+  int64_t lookahead_samples;   /* samples queued ahead of the engine; 0 = 4 x paths_in_flight */
+  int32_t loader_threads;      /* 0 = 2 */
+} hasty_server_config;
+
+typedef struct hasty_server_result {
+  int64_t id;
+  int32_t status;              /* HASTY_OK, or the code the request failed with */
+  int32_t width, height;
+  int32_t passes;
+  uint64_t samples;            /* camera samples rendered (passes * width * height) */
+  double submit_ms, admit_ms, finish_ms;   /* since hasty_server_start */
+  double latency_ms;           /* finish_ms - submit_ms */
+  char error[160];             /* message when status != HASTY_OK */
+} hasty_server_result;
+
+typedef struct hasty_server_stats {
+  uint64_t submitted, admitted, completed, failed;
+  uint64_t samples;            /* camera samples of completed requests */
+  uint64_t rays, shaded;
+  uint64_t waves, iterations;
+  double device_ms;            /* device time of the engine's waves (CUDA events) */
+  double uptime_ms;
+  int64_t resident_bytes;      /* engine + scenes + resident requests */
+  int64_t peak_resident_bytes;
+  int64_t engine_bytes;
+  int32_t resident_jobs, resident_scenes, pending;
+} hasty_server_stats;
+
+int hasty_server_start(hasty_ctx* ctx, const hasty_server_config* cfg, hasty_server** out);
+/* passes <= 0: the job file's num_samples; seed NULL: the job file's seed. */
+int hasty_server_submit(hasty_server* srv, const char* render_job_path, int32_t passes, const uint64_t* seed,
+                        int64_t* id);
+/* Up to max finished requests not returned before; waits up to wait_ms for
+ * the first one. */
+int hasty_server_poll(hasty_server* srv, hasty_server_result* out, size_t max, size_t* n, int32_t wait_ms);
+/* Estimate of a finished request (as hasty_job_read) or its raw FP64 sums
+ * (as hasty_job_read_sums); valid until hasty_server_release. */
+int hasty_server_read(hasty_server* srv, int64_t id, int aov, float* host_rgb, size_t w, size_t h);
+int hasty_server_read_sums(hasty_server* srv, int64_t id, int aov, double* host_rgb, size_t w, size_t h);
+int hasty_server_release(hasty_server* srv, int64_t id);
+int hasty_server_stats_get(hasty_server* srv, hasty_server_stats* out);
+/* Waits until every submitted request has finished (HASTY_ERR_STOPPED on timeout). */
+int hasty_server_wait_idle(hasty_server* srv, int32_t timeout_ms);
+/* Stops the loop: requests not finished fail with HASTY_ERR_STOPPED; frees everything. */
+int hasty_server_stop(hasty_server* srv);
+
 /* ---- One pass without device allocation ------------------------------------
  * Renders camera-sample pass `pass` of the job (seed and settings as loaded)
  * into d_color, a caller-owned DEVICE buffer of w*h*3 doubles (row-major RGB
