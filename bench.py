@@ -174,7 +174,16 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--bvh", default="wide", choices=["wide", "binary"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve"],
+                    help="plain: the large single job (default); batch: the 64-job mix batched vs one by one; "
+                         "serve: Poisson arrivals over the server")
+    ap.add_argument("--jobs", type=int, default=64, help="batch/serve: jobs in the mix (serve: scene pool = half)")
+    ap.add_argument("--rate", type=float, default=20.0, help="serve: arrivals per second")
+    ap.add_argument("--duration", type=float, default=120.0, help="serve: seconds of arrivals")
+    ap.add_argument("--no-tune", action="store_true", help="batch/serve: skip the autotuner (engine defaults)")
     args = ap.parse_args()
+    if args.workload != "plain":
+        return run_mixed(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -306,6 +315,160 @@ def main():
     job.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def _rel_diff(a, b):
+    import numpy as np
+    den = float(np.linalg.norm(b.astype(np.float64)))
+    return float(np.linalg.norm(a.astype(np.float64) - b.astype(np.float64))) / max(den, 1e-30)
+
+
+def _tuned(args, jobs, ctx):
+    """Engine parameters from the autotuner (cached per GPU name)."""
+    import torch
+    from hastyrenderer_gb300 import RenderJob, autotune
+    path = autotune.default_path(torch.cuda.get_device_name())
+    if args.no_tune:
+        return {"paths_in_flight": 1 << 22, "regen_fraction": 0.9, "source": "defaults"}
+    cached = autotune.load(path)
+    if cached:
+        cached["source"] = path
+        return cached
+    calib = [RenderJob(j["path"], ctx) for j in jobs[:16]]
+    res = autotune.tune_batch(calib, passes=2, out_path=path)
+    for c in calib:
+        c.close()
+    res["source"] = "tuned now"
+    return res
+
+
+def run_mixed(args):
+    """Mixed-job workloads: batching (the same jobs one by one through
+    hasty_job_render_passes, then all at once through hasty_batch_render) or
+    serving (Poisson arrivals through hasty_server_*)."""
+    import numpy as np
+    import torch
+    from hastyrenderer_gb300 import Context, RenderJob, Server, autotune, batch_render, workloads
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if rank != 0:
+        return
+    torch.cuda.init()
+    base = os.environ.get("HASTY_BENCH_MIX", os.path.join(tempfile.gettempdir(), "hasty_bench_mix"))
+    t_gen = time.perf_counter()
+    jobs = workloads.mixed_jobs(base, n_jobs=args.jobs, seed=0)
+    gen_s = time.perf_counter() - t_gen
+    ctx = Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0)
+    tune = _tuned(args, jobs, ctx)
+    engine_args = autotune.batch_args(tune)
+    hbm, peak_kind = peaks()
+    sampler = ClockSampler(local_rank)
+
+    if args.workload == "batch":
+        total = sum(workloads.job_samples(j) for j in jobs)
+        t0 = time.perf_counter()
+        resident = [RenderJob(j["path"], ctx) for j in jobs]
+        load_s = time.perf_counter() - t0
+        spp = [j["spp"] for j in jobs]
+        plain_est = []
+        with sampler:
+            # plain drop-in, one job after another (device time from the job's own CUDA events)
+            plain_ms = 0.0
+            plain_rays = 0
+            w0 = time.perf_counter()
+            for job, p in zip(resident, spp):
+                s0 = job.stats()
+                job.render_passes(p, sync=True)
+                s1 = job.stats()
+                plain_ms += s1["kernel_ms"] - s0["kernel_ms"]
+                plain_rays += s1["rays"] - s0["rays"]
+                plain_est.append(job.compute_estimate())
+                job.release_paths()
+                job.reset()
+            plain_wall = time.perf_counter() - w0
+            for _ in range(max(args.warmup - 2, 0)):   # the autotuner's trials already warmed the engine
+                batch_render(resident[:8], [2] * 8, **engine_args)
+                for job in resident[:8]:
+                    job.reset()
+            w0 = time.perf_counter()
+            st = batch_render(resident, spp, **engine_args)
+            batch_wall = time.perf_counter() - w0
+        diffs = [_rel_diff(job.compute_estimate(), ref) for job, ref in zip(resident, plain_est)]
+        batch_sps = total / (st["device_ms"] * 1e-3)
+        plain_sps = total / (plain_ms * 1e-3)
+        line = {
+            "metric": "samples/s", "value": batch_sps, "unit": "samples/s", "n_gpus": 1, "steps": 1,
+            "warmup": args.warmup, "ms_per_step": st["device_ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
+            "config": {"workload": f"mixed_{len(jobs)}_jobs_batched", "jobs": len(jobs), "samples": total,
+                       "engine": engine_args, "l2": "working set > L2 (path pool + scenes), no flush"},
+            "mrays_per_s": st["rays"] / (st["device_ms"] * 1e-3) * 1e-6,
+            "plain": {"value": plain_sps, "unit": "samples/s", "device_ms": plain_ms, "wall_ms": plain_wall * 1e3,
+                      "mrays_per_s": plain_rays / (plain_ms * 1e-3) * 1e-6},
+            "batched_over_plain": batch_sps / plain_sps,
+            "wall": {"batched_ms": batch_wall * 1e3, "plain_ms": plain_wall * 1e3, "load_s": load_s,
+                     "scene_generation_s": gen_s},
+            "equal_estimate": {"max_rel_l2_diff_vs_plain": max(diffs), "note": "same samples; fixed-point vs FP64 sums"},
+            "engine_iterations": st["iterations"], "engine_bytes": st["engine_bytes"],
+            "autotune": {k: tune[k] for k in ("paths_in_flight", "regen_fraction", "samples_per_s", "source") if k in tune},
+            "clocks": sampler.summary(), "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
+        }
+        print(json.dumps(line), flush=True)
+        return
+
+    # serving: Poisson arrivals over a warm scene pool
+    pool = jobs[: max(1, len(jobs) // 2)]
+    reqs = workloads.poisson_requests(pool, os.path.join(base, f"requests_{args.rate:g}_{args.duration:g}"),
+                                      rate=args.rate, duration=args.duration, seed=1)
+    srv = Server(ctx, memory_budget=120 << 30, max_resident_jobs=32, max_resident_scenes=32, **engine_args)
+    t0 = time.perf_counter()
+    for j in pool:                       # warm the scene cache: one cheap request per scene
+        srv.submit(j["path"], passes=1)
+    srv.wait_idle(-1)
+    for r in srv.poll(max_results=len(pool) + 8, wait_ms=0):
+        srv.release(r["id"])
+    warm_s = time.perf_counter() - t0
+    st0 = srv.stats()
+    results = []
+    with sampler:
+        t0 = time.perf_counter()
+        k = 0
+        while k < len(reqs) or len(results) < len(reqs):
+            now = time.perf_counter() - t0
+            while k < len(reqs) and reqs[k]["t"] <= now:
+                srv.submit(reqs[k]["path"], passes=reqs[k]["spp"], seed=reqs[k]["seed"])
+                k += 1
+            wait = 0 if k >= len(reqs) else max(0, int((reqs[k]["t"] - (time.perf_counter() - t0)) * 1e3))
+            for r in srv.poll(wait_ms=max(1, min(wait, 50)) if k < len(reqs) else 200):
+                if r["status"] == 0:
+                    img = srv.read(r["id"])   # host result as a caller reads it
+                    del img
+                srv.release(r["id"])
+                results.append(r)
+        span = time.perf_counter() - t0
+    st1 = srv.stats()
+    srv.stop()
+    ok = [r for r in results if r["status"] == 0]
+    lat = np.array([r["latency_ms"] for r in ok]) if ok else np.zeros(1)
+    samples = sum(r["samples"] for r in ok)
+    dev_ms = st1["device_ms"] - st0["device_ms"]
+    line = {
+        "metric": "samples/s", "value": samples / span, "unit": "samples/s", "n_gpus": 1, "steps": len(reqs),
+        "warmup": len(pool), "ms_per_step": span * 1e3 / max(len(reqs), 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
+        "config": {"workload": f"serving_poisson_{args.rate:g}_per_s_{args.duration:g}_s", "requests": len(reqs),
+                   "scene_pool": len(pool), "engine": engine_args, "max_resident_jobs": 32, "memory_budget": 120 << 30},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                       "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+        "completed": len(ok), "failed": len(results) - len(ok),
+        "device_samples_per_s": samples / max(dev_ms * 1e-3, 1e-9),
+        "mrays_per_s": (st1["rays"] - st0["rays"]) / max(dev_ms * 1e-3, 1e-9) * 1e-6,
+        "offered_samples_per_s": sum(r["width"] * r["height"] * r["spp"] for r in reqs) / args.duration,
+        "peak_resident_bytes": st1["peak_resident_bytes"], "warm_s": warm_s, "span_s": span,
+        "autotune": {k: tune[k] for k in ("paths_in_flight", "regen_fraction", "samples_per_s", "source") if k in tune},
+        "clocks": sampler.summary(),
+    }
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

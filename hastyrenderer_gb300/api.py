@@ -104,6 +104,10 @@ class RenderJob:
     def set_paths_in_flight(self, n: int) -> None:
         check(native.lib().hasty_job_set_paths_in_flight(self._h, ctypes.c_int64(n)))
 
+    def release_paths(self) -> None:
+        """Frees the path state (about 336 B per path in flight) until the next render."""
+        check(native.lib().hasty_job_release_paths(self._h))
+
     def render_passes(self, n: int, sync: bool = False) -> None:
         check(native.lib().hasty_job_render_passes(self._h, int(n)))
         if sync:

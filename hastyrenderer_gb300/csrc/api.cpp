@@ -355,6 +355,23 @@ int hasty_job_set_paths_in_flight(hasty_job* job, int64_t paths) {
   });
 }
 
+int hasty_job_release_paths(hasty_job* job) {
+  return guarded([&] {
+    as_job(job);
+    ck(cudaSetDevice(job->ctx->device), "cudaSetDevice");
+    ck(cudaStreamSynchronize(job->stream), "sync");
+    job->collect_events();
+    PathsDev& p = job->pd;
+    void* bufs[] = {p.rng, p.thr, p.rad, p.pend_b, p.nee_c, p.nee_t, p.med, p.med_geom, p.ray_o, p.ray_d, p.hit,
+                    p.pq[0], p.pq[1], p.rq[0], p.rq[1], p.counts, p.out_color, p.out_normal, p.out_albedo};
+    for (void* b : bufs) job->release(b);
+    unsigned long long* stats = p.stats;
+    p = PathsDev{};
+    p.stats = stats;
+    return HASTY_OK;
+  });
+}
+
 int hasty_job_render_passes(hasty_job* job, int n_passes) {
   return guarded([&] {
     as_job(job);

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -44,6 +45,8 @@ void Engine::init(hasty_ctx* c, int64_t capacity, int slots, uint32_t segments, 
   md.slot_px = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * size_t(cap)));
   md.slot_pass = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * size_t(cap)));
   md.free_slots = static_cast<int32_t*>(alloc(sizeof(int32_t) * size_t(cap)));
+  md.flags = static_cast<uint8_t*>(alloc(size_t(cap)));
+  md.block_sums = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 3 * size_t(compact_blocks(int(cap)))));
   md.free_count = static_cast<uint32_t*>(alloc(sizeof(uint32_t)));
   md.next_sample = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
   md.total_samples = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
@@ -58,7 +61,9 @@ void Engine::init(hasty_ctx* c, int64_t capacity, int slots, uint32_t segments, 
   ck(cudaMemsetAsync(md.total_samples, 0, sizeof(unsigned long long), stream), "memset");
   launch_multi_init(pd, md, int(cap), stream);
   ck(cudaGetLastError(), "engine init");
-  build_graph();
+  const char* mode = std::getenv("HASTY_ENGINE_LAUNCH");
+  use_graph = !(mode && std::strcmp(mode, "stream") == 0);
+  if (use_graph) build_graph();
   ck(cudaStreamSynchronize(stream), "engine init");
 }
 
@@ -75,7 +80,7 @@ void Engine::build_graph() {
   ck(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np), "add conditional node");
   cudaGraph_t body = np.conditional.phGraph_out[0];
   ck(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "begin capture");
-  launch_multi_iteration(pd, md, int(cap), (unsigned long long)h, 1, stream);
+  launch_multi_iteration(pd, md, int(cap), (ctx->flags & HASTY_CTX_BINARY_BVH) ? 0 : 1, (unsigned long long)h, 1, stream);
   cudaGraph_t captured = nullptr;
   ck(cudaStreamEndCapture(stream, &captured), "end capture");
   ck(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
@@ -124,14 +129,28 @@ bool Engine::run_wave(uint32_t n_iter, bool* bound_hit) {
   if (!staged.empty()) publish();
   uint32_t end = iterations + std::max<uint32_t>(n_iter, 1u);
   ck(cudaMemcpyAsync(&md.ctl[7], &end, sizeof(end), cudaMemcpyHostToDevice, stream), "wave end");
-  ck(cudaGraphLaunch(exec, stream), "cudaGraphLaunch");
   uint32_t ctl[8];
   unsigned long long ns = 0;
   uint32_t counts[4];
-  ck(cudaMemcpyAsync(ctl, md.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stream), "ctl");
-  ck(cudaMemcpyAsync(&ns, md.next_sample, sizeof(ns), cudaMemcpyDeviceToHost, stream), "next");
-  ck(cudaMemcpyAsync(counts, pd.counts, sizeof(counts), cudaMemcpyDeviceToHost, stream), "counts");
-  ck(cudaStreamSynchronize(stream), "wave");
+  auto read_back = [&] {
+    ck(cudaMemcpyAsync(ctl, md.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stream), "ctl");
+    ck(cudaMemcpyAsync(&ns, md.next_sample, sizeof(ns), cudaMemcpyDeviceToHost, stream), "next");
+    ck(cudaMemcpyAsync(counts, pd.counts, sizeof(counts), cudaMemcpyDeviceToHost, stream), "counts");
+    ck(cudaStreamSynchronize(stream), "wave");
+  };
+  if (use_graph) {
+    ck(cudaGraphLaunch(exec, stream), "cudaGraphLaunch");
+    read_back();
+  } else {
+    // the loop condition of the graph's while node, evaluated on the host
+    for (;;) {
+      launch_multi_iteration(pd, md, int(cap), (ctx->flags & HASTY_CTX_BINARY_BVH) ? 0 : 1, 0ull, 0, stream);
+      ck(cudaGetLastError(), "engine iteration");
+      read_back();
+      bool more = counts[ctl[0] & 1u] > 0 || ns < total;
+      if (!more || ctl[6] != 0 || ctl[5] >= end) break;
+    }
+  }
   iterations = ctl[5];
   if (bound_hit) *bound_hit = ctl[6] != 0;
   next = ns;

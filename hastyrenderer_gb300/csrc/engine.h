@@ -33,6 +33,10 @@ struct Engine {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   uint32_t iterations = 0;
+  // false: iterations are plain stream launches issued by the host, one at a
+  // time (HASTY_ENGINE_LAUNCH=stream; profilers cannot see into graphs with
+  // conditional nodes). Same kernels, same results.
+  bool use_graph = true;
   // host view, as of the end of the last wave
   uint32_t seg_lo = 0, seg_hi = 0;
   std::deque<std::pair<unsigned long long, uint32_t>> spans;   // (begin, samples) of segments [seg_lo, seg_hi)

@@ -425,11 +425,21 @@ void launch_debug_bsdf(int which, const float* in, int n, const uint32_t* replay
 // k_multi_plan (1 thread) decides how many new camera samples to issue into
 // free slots, k_multi_regen starts them, the closest-hit kernel traces every
 // queued ray, k_shade_multi advances every queued path by one bounce (the
-// same shade_path as the single-job kernel), and k_multi_cond flips the queue
-// parity and sets the enclosing CUDA-graph while-loop's condition.
+// same shade_path as the single-job kernel) and records per slot whether the
+// path lives on and which rays it queued, three compaction kernels rebuild
+// the path queue, the ray queue and the free-slot list from those flags in
+// ascending slot order, and k_multi_cond flips the queue parity and sets the
+// enclosing CUDA-graph while-loop's condition. Keeping every list in slot
+// order keeps the structure-of-arrays path state accessed in dense runs
+// however often slots are recycled.
 namespace hasty {
 namespace {
 using namespace dev;
+
+enum : uint8_t { SF_ALIVE = 1, SF_RAY_B = 2, SF_RAY_L = 4 };
+constexpr int kCompactThreads = 256;
+constexpr int kCompactSteps = 8;
+constexpr int kCompactTile = kCompactThreads * kCompactSteps;   // slots per compaction block
 
 // Last live segment whose first sample is <= g (segments are contiguous and
 // in increasing order of `begin`).
@@ -444,7 +454,10 @@ __device__ __forceinline__ const SegDev& find_segment(const MultiDev& m, unsigne
 
 __global__ void k_multi_init(PathsDev P, MultiDev m, int cap) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < cap) m.free_slots[i] = cap - 1 - i;
+  if (i < cap) {
+    m.free_slots[i] = i;          // ascending
+    m.flags[i] = 0;
+  }
   if (i == 0) {
     *m.free_count = uint32_t(cap);
     for (int k = 0; k < 4; ++k) P.counts[k] = 0;
@@ -454,8 +467,6 @@ __global__ void k_multi_init(PathsDev P, MultiDev m, int cap) {
 
 __global__ void k_multi_plan(PathsDev P, MultiDev m) {
   uint32_t q = m.ctl[0];
-  P.counts[q ^ 1] = 0;
-  P.counts[2 + (q ^ 1)] = 0;
   uint32_t live = P.counts[q];
   uint32_t n_new = 0;
   unsigned long long next = *m.next_sample, total = *m.total_samples;
@@ -465,13 +476,11 @@ __global__ void k_multi_plan(PathsDev P, MultiDev m) {
     n_new = left < fc ? uint32_t(left) : fc;
   }
   m.ctl[1] = n_new;
-  m.ctl[2] = *m.free_count;
   m.ctl[3] = P.counts[q];
   m.ctl[4] = P.counts[2 + q];
   *m.regen_base = next;
   P.counts[q] += n_new;
   P.counts[2 + q] += n_new;
-  *m.free_count -= n_new;
   *m.next_sample = next + n_new;
 }
 
@@ -480,7 +489,7 @@ __global__ void __launch_bounds__(256) k_multi_regen(PathsDev P, MultiDev m) {
   uint32_t n_new = m.ctl[1];
   if (i >= n_new) return;
   uint32_t q = m.ctl[0];
-  int s = m.free_slots[m.ctl[2] - 1 - i];
+  int s = m.free_slots[i];        // the lowest free slots, in ascending order
   unsigned long long g = *m.regen_base + i;
   const SegDev& seg = find_segment(m, g);
   const int j = seg.job;
@@ -528,10 +537,6 @@ __device__ __forceinline__ void add_fixed(unsigned long long* acc, V3 L, float4 
 __global__ void __launch_bounds__(128) k_shade_multi(PathsDev P, MultiDev m) {
   const uint32_t q = m.ctl[0];
   const uint32_t n_in = P.counts[q];
-  uint32_t* pq_cnt = &P.counts[q ^ 1];
-  uint32_t* rq_cnt = &P.counts[2 + (q ^ 1)];
-  int32_t* pq_out = P.pq[q ^ 1];
-  int32_t* rq_out = P.rq[q ^ 1];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if ((i & ~31u) >= n_in) return;
   const bool valid = i < n_in;
@@ -550,24 +555,9 @@ __global__ void __launch_bounds__(128) k_shade_multi(PathsDev P, MultiDev m) {
       if (has_nan(res.L)) atomicAdd(&P.stats[ST_NAN], 1ull);
       else add_fixed(job.acc + 9 * int64_t(px), res.L, P.out_normal[s], P.out_albedo[s], P.stats);
     }
+    m.flags[s] = uint8_t((res.keep ? SF_ALIVE : 0) | (res.emitB ? SF_RAY_B : 0) | (res.emitL ? SF_RAY_L : 0));
   }
-  const bool keep = res.keep, emitB = res.emitB, emitL = res.emitL;
-  uint32_t lane = threadIdx.x & 31u;
-  uint32_t nrays = (emitB ? 1u : 0u) + (emitL ? 1u : 0u);
-  uint32_t roff = warp_reserve(rq_cnt, nrays);
-  if (emitB) rq_out[roff++] = 2 * s;
-  if (emitL) rq_out[roff] = 2 * s + 1;
-  unsigned kb = __ballot_sync(kFull, keep);
-  uint32_t pbase = 0;
-  if (lane == 0 && kb) pbase = atomicAdd(pq_cnt, uint32_t(__popc(kb)));
-  pbase = __shfl_sync(kFull, pbase, 0);
-  if (keep) pq_out[pbase + __popc(kb & ((1u << lane) - 1u))] = s;
-  // finished slots go back on the free stack; per-job completion counts
-  unsigned fb = __ballot_sync(kFull, finished);
-  uint32_t fbase = 0;
-  if (lane == 0 && fb) fbase = atomicAdd(m.free_count, uint32_t(__popc(fb)));
-  fbase = __shfl_sync(kFull, fbase, 0);
-  if (finished) m.free_slots[fbase + __popc(fb & ((1u << lane) - 1u))] = s;
+  const uint32_t lane = threadIdx.x & 31u;
   unsigned same = __match_any_sync(kFull, finished ? j : -1);
   if (finished && (__ffs(same) - 1) == int(lane)) atomicAdd(m.jobs[j].done, (unsigned long long)__popc(same));
   unsigned sb = __ballot_sync(kFull, res.shaded != 0);
@@ -577,6 +567,139 @@ __global__ void __launch_bounds__(128) k_shade_multi(PathsDev P, MultiDev m) {
     if (sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
     if (ob) atomicAdd(&P.stats[ST_MEDIA_OVERFLOW], (unsigned long long)__popc(ob));
     if (cb) atomicAdd(&P.stats[ST_TRIAL_CAP], (unsigned long long)__popc(cb));
+  }
+}
+
+// ---- ordered compaction of the slot flags ---------------------------------
+// Block b covers slots [b*kCompactTile, (b+1)*kCompactTile), step k of
+// thread t is slot b*kCompactTile + k*kCompactThreads + t, so slot order is
+// (block, step, thread) order. Counts per block: live paths, queued rays,
+// free slots.
+struct SlotFlags {
+  bool in, alive, rb, rl;
+};
+
+__device__ __forceinline__ SlotFlags slot_flags(const MultiDev& m, int64_t s, int cap) {
+  SlotFlags f;
+  f.in = s < cap;
+  uint8_t v = f.in ? m.flags[s] : uint8_t(0);
+  f.alive = (v & SF_ALIVE) != 0;
+  f.rb = (v & SF_RAY_B) != 0;
+  f.rl = (v & SF_RAY_L) != 0;
+  return f;
+}
+
+__global__ void __launch_bounds__(kCompactThreads) k_compact_count(MultiDev m, int cap) {
+  __shared__ uint32_t s_sum[3][kCompactThreads / 32];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint32_t na = 0, nr = 0, nf = 0;
+  for (int k = 0; k < kCompactSteps; ++k) {
+    SlotFlags f = slot_flags(m, int64_t(blockIdx.x) * kCompactTile + k * kCompactThreads + t, cap);
+    na += f.alive ? 1u : 0u;
+    nf += (f.in && !f.alive) ? 1u : 0u;
+    nr += (f.rb ? 1u : 0u) + (f.rl ? 1u : 0u);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    na += __shfl_down_sync(kFull, na, o);
+    nr += __shfl_down_sync(kFull, nr, o);
+    nf += __shfl_down_sync(kFull, nf, o);
+  }
+  if (lane == 0) { s_sum[0][warp] = na; s_sum[1][warp] = nr; s_sum[2][warp] = nf; }
+  __syncthreads();
+  if (t < 3) {
+    uint32_t v = 0;
+    for (int w = 0; w < kCompactThreads / 32; ++w) v += s_sum[t][w];
+    m.block_sums[3 * int64_t(blockIdx.x) + t] = v;
+  }
+}
+
+// One block: exclusive scan of the per-block counts (in place) and the
+// totals: next path-queue length, next ray-queue length, free slots.
+__global__ void __launch_bounds__(1024) k_compact_scan(PathsDev P, MultiDev m, int n_blocks) {
+  __shared__ uint32_t s_warp[3][32];
+  __shared__ uint32_t s_carry[3];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t < 3) s_carry[t] = 0;
+  __syncthreads();
+  for (int base = 0; base < n_blocks; base += 1024) {
+    const int i = base + t;
+    uint32_t v[3], incl[3];
+    for (int c = 0; c < 3; ++c) {
+      v[c] = i < n_blocks ? m.block_sums[3 * int64_t(i) + c] : 0u;
+      uint32_t x = v[c];
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += y;
+      }
+      incl[c] = x;
+      if (lane == 31) s_warp[c][warp] = x;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      for (int c = 0; c < 3; ++c) {
+        uint32_t x = s_warp[c][lane];
+        for (int o = 1; o < 32; o <<= 1) {
+          uint32_t y = __shfl_up_sync(kFull, x, o);
+          if (lane >= o) x += y;
+        }
+        s_warp[c][lane] = x;        // inclusive over warps
+      }
+    }
+    __syncthreads();
+    if (i < n_blocks) {
+      for (int c = 0; c < 3; ++c)
+        m.block_sums[3 * int64_t(i) + c] = s_carry[c] + (warp ? s_warp[c][warp - 1] : 0u) + incl[c] - v[c];
+    }
+    __syncthreads();
+    if (t < 3) s_carry[t] += s_warp[t][31];
+    __syncthreads();
+  }
+  if (t == 0) {
+    const uint32_t q = m.ctl[0];
+    P.counts[q ^ 1] = s_carry[0];
+    P.counts[2 + (q ^ 1)] = s_carry[1];
+    *m.free_count = s_carry[2];
+  }
+}
+
+__global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(PathsDev P, MultiDev m, int cap) {
+  __shared__ uint32_t s_w[3][kCompactThreads / 32];
+  __shared__ uint32_t s_run[3];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const uint32_t q = m.ctl[0];
+  int32_t* pq_out = P.pq[q ^ 1];
+  int32_t* rq_out = P.rq[q ^ 1];
+  if (t < 3) s_run[t] = m.block_sums[3 * int64_t(blockIdx.x) + t];
+  __syncthreads();
+  const unsigned below = (1u << lane) - 1u;
+  for (int k = 0; k < kCompactSteps; ++k) {
+    const int64_t s = int64_t(blockIdx.x) * kCompactTile + k * kCompactThreads + t;
+    SlotFlags f = slot_flags(m, s, cap);
+    const bool fr = f.in && !f.alive;
+    const unsigned ba = __ballot_sync(kFull, f.alive);
+    const unsigned bf = __ballot_sync(kFull, fr);
+    const uint32_t nr = (f.rb ? 1u : 0u) + (f.rl ? 1u : 0u);
+    uint32_t rincl = nr;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(kFull, rincl, o);
+      if (lane >= o) rincl += y;
+    }
+    if (lane == 31) { s_w[0][warp] = __popc(ba); s_w[1][warp] = rincl; s_w[2][warp] = __popc(bf); }
+    __syncthreads();
+    uint32_t oa = s_run[0], orr = s_run[1], of = s_run[2];
+    for (int w = 0; w < warp; ++w) { oa += s_w[0][w]; orr += s_w[1][w]; of += s_w[2][w]; }
+    if (f.alive) pq_out[oa + __popc(ba & below)] = int32_t(s);
+    if (fr) m.free_slots[of + __popc(bf & below)] = int32_t(s);
+    uint32_t ro = orr + rincl - nr;
+    if (f.rb) rq_out[ro++] = int32_t(2 * s);
+    if (f.rl) rq_out[ro] = int32_t(2 * s + 1);
+    __syncthreads();
+    if (t < 3) {
+      uint32_t v = 0;
+      for (int w = 0; w < kCompactThreads / 32; ++w) v += s_w[t][w];
+      s_run[t] += v;
+    }
+    __syncthreads();
   }
 }
 
@@ -607,12 +730,18 @@ void launch_multi_init(const PathsDev& p, const MultiDev& m, int cap, cudaStream
   k_multi_init<<<(cap + 255) / 256, 256, 0, st>>>(p, m, cap);
 }
 
-void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int cap, unsigned long long cond, int use_cond,
-                            cudaStream_t st) {
+int compact_blocks(int cap) { return (cap + kCompactTile - 1) / kCompactTile; }
+
+void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int cap, int bvh_kind, unsigned long long cond,
+                            int use_cond, cudaStream_t st) {
+  const int nb = compact_blocks(cap);
   k_multi_plan<<<1, 1, 0, st>>>(p, m);
   k_multi_regen<<<(cap + 255) / 256, 256, 0, st>>>(p, m);
-  launch_trace_multi(p, m, 2 * cap, st);
+  launch_trace_multi(p, m, bvh_kind, 2 * cap, st);
   k_shade_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m);
+  k_compact_count<<<nb, kCompactThreads, 0, st>>>(m, cap);
+  k_compact_scan<<<1, 1024, 0, st>>>(p, m, nb);
+  k_compact_scatter<<<nb, kCompactThreads, 0, st>>>(p, m, cap);
   k_multi_cond<<<1, 1, 0, st>>>(p, m, cudaGraphConditionalHandle(cond), use_cond);
 }
 

@@ -300,6 +300,8 @@ __global__ void k_trace_rays(SceneDev sc, const float* rays, int n, float4* hits
 }
 
 // Multi-job engine: each ray belongs to the job of its path slot (ray id / 2).
+// All jobs of one engine share the BVH layout of their context (KIND).
+template <int KIND>
 __global__ void __launch_bounds__(128) k_trace_multi(PathsDev P, MultiDev m) {
   const uint32_t q = m.ctl[0];
   uint32_t n = P.counts[2 + q];
@@ -309,15 +311,15 @@ __global__ void __launch_bounds__(128) k_trace_multi(PathsDev P, MultiDev m) {
   int rid = P.rq[q][i];
   const SceneDev& sc = m.jobs[m.slot_job[rid >> 1]].sc;
   float4 o = P.ray_o[rid], d = P.ray_d[rid];
-  Hit h = sc.bvh_kind == 1 ? trace_wide(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z)
-                           : trace_binary(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
+  Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
   P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
 }
 
 }  // namespace
 
-void launch_trace_multi(const PathsDev& p, const MultiDev& m, int max_rays, cudaStream_t st) {
-  k_trace_multi<<<(max_rays + 127) / 128, 128, 0, st>>>(p, m);
+void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t st) {
+  if (bvh_kind == 1) k_trace_multi<1><<<(max_rays + 127) / 128, 128, 0, st>>>(p, m);
+  else k_trace_multi<0><<<(max_rays + 127) / 128, 128, 0, st>>>(p, m);
 }
 
 void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cudaStream_t st) {

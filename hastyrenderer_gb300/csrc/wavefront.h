@@ -103,7 +103,9 @@ struct MultiDev {
   int32_t* slot_job;           // job of the path in each slot
   uint32_t* slot_px;           // pixel of the path's camera sample
   uint32_t* slot_pass;         // pass of the path's camera sample
-  int32_t* free_slots;         // stack of free slot ids
+  int32_t* free_slots;         // free slot ids in ascending order (rebuilt every iteration)
+  uint8_t* flags;              // per slot: path lives on / BSDF ray queued / light ray queued
+  uint32_t* block_sums;        // 3 per compaction block: counts, then exclusive offsets
   uint32_t* free_count;
   unsigned long long* next_sample;
   unsigned long long* total_samples;
@@ -122,12 +124,14 @@ enum MultiStat { MS_RAYS = ST_RAYS, MS_SHADED = ST_SHADED, MS_PATHS = ST_PATHS, 
 // One engine iteration (regenerate, trace, shade, loop condition) launched
 // into `stream`; `cond` is the CUDA-graph conditional handle of the enclosing
 // while node (0 when launched without a graph).
-void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int capacity, unsigned long long cond_handle,
-                            int use_cond, cudaStream_t stream);
+void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int capacity, int bvh_kind,
+                            unsigned long long cond_handle, int use_cond, cudaStream_t stream);
 void launch_multi_init(const PathsDev& p, const MultiDev& m, int capacity, cudaStream_t stream);
+// Compaction blocks of an engine with `capacity` slots (3 block_sums entries each).
+int compact_blocks(int capacity);
 // Adds a finished job's fixed-point sums into FP64 accumulators (sum * 2^-32).
 void launch_fixed_to_double(const unsigned long long* acc, int npix, double* c, double* n, double* a, cudaStream_t stream);
 // trace.cu: closest hit of the queued rays of the multi-job engine.
-void launch_trace_multi(const PathsDev& p, const MultiDev& m, int max_rays, cudaStream_t stream);
+void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t stream);
 
 }  // namespace hasty

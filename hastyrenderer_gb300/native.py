@@ -105,6 +105,7 @@ def lib() -> ctypes.CDLL:
         "hasty_job_reset": [P],
         "hasty_job_set_paths_in_flight": [P, I64],
         "hasty_job_render_passes": [P, I],
+        "hasty_job_release_paths": [P],
         "hasty_job_sync": [P],
         "hasty_job_stop": [P],
         "hasty_job_stats_get": [P, P],

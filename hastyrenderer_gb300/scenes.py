@@ -263,12 +263,14 @@ def sky_environment(width=2048, height=1024, sun_elevation_deg=35.0, sun_azimuth
 
 def sphere_field(out_dir, seed=0, n_spheres=800, subdiv=3, width=1920, height=1080, spp=256, max_depth=12,
                  env_size=(2048, 1024), aperture=0.15, num_blades=6, blade_rotation=0.3, box=20.0,
-                 vary_glass_ior=False, roulette_start_depth=1, roulette_q=0.3, use_mis=True):
+                 vary_glass_ior=False, roulette_start_depth=1, roulette_q=0.3, use_mis=True, sky_path=None):
     """N icospheres (radius log-uniform in [0.05, 0.5], centres uniform in a
     box of the given size above a 2-triangle ground plane). Materials: 40%
     Lambert, 40% GGX (roughness U[0.02, 1], metallic 0/1), 20% dielectric
     (transmission 1, roughness 0, IOR U[1.3, 1.7]). Procedural FP32 sky with a
-    Gaussian sun, importance sampled; thin-lens camera with aperture blades."""
+    Gaussian sun, importance sampled; thin-lens camera with aperture blades.
+    sky_path: use this existing sky PFM (it does not depend on the seed)
+    instead of writing one into out_dir."""
     rng = np.random.default_rng(seed)
     ow = _ObjWriter()
     sv, sf = icosphere(subdiv)
@@ -296,13 +298,17 @@ def sphere_field(out_dir, seed=0, n_spheres=800, subdiv=3, width=1920, height=10
         ow.add(f"sphere{i}", sv * radii[i] + centers[i], sf, name, normals=sv, smooth=True)
     os.makedirs(out_dir, exist_ok=True)
     ew, eh = env_size
-    write_pfm(os.path.join(out_dir, "sky.pfm"), sky_environment(ew, eh))
+    if sky_path is None:
+        write_pfm(os.path.join(out_dir, "sky.pfm"), sky_environment(ew, eh))
+        sky_ref = "sky.pfm"
+    else:
+        sky_ref = os.path.abspath(sky_path)
     look = np.array([0.0, box * 0.25, 0.0])
     pos = np.array([0.0, box * 0.45, box * 1.35])
     scene = {"camera": {"position": pos.tolist(), "look_at": look.tolist(), "aperture": aperture,
                         "focal_distance": float(np.linalg.norm(pos - look)), "num_blades": num_blades,
                         "blade_rotation": blade_rotation},
-             "world": {"environment_texture": "sky.pfm", "vary_glass_ior": bool(vary_glass_ior)}}
+             "world": {"environment_texture": sky_ref, "vary_glass_ior": bool(vary_glass_ior)}}
     settings = {"num_samples": spp, "num_threads": 8, "width": width, "height": height,
                 "roulette_start_depth": roulette_start_depth, "roulette_q": roulette_q,
                 "max_depth": max_depth, "use_mis": use_mis}

@@ -62,3 +62,14 @@ def test_small_pool_regeneration():
     assert st["iterations"] > 12
     for x, y in zip(_sums(a), _sums(b)):
         assert np.array_equal(x, y)
+
+
+def test_release_paths_between_renders():
+    """Freeing the path state between renders changes nothing in the result."""
+    a, b = _job("room"), _job("room")
+    a.render_passes(3, sync=True)
+    b.render_passes(1, sync=True)
+    b.release_paths()
+    b.render_passes(2, sync=True)
+    for x, y in zip(_sums(a), _sums(b)):
+        assert np.array_equal(x, y)
