@@ -29,6 +29,8 @@ NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contr
 CU_EXTRA = {"integrator.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-sign-compare"]
 CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu"]
+# Extra nvcc flags for experiments (e.g. HASTY_NVCC_FLAGS="-DHASTY_OUTLINE_MASK=3").
+EXTRA_NVCC = os.environ.get("HASTY_NVCC_FLAGS", "").split()
 CPP_SOURCES = ["api.cpp", "engine.cpp", "server.cpp", "scene_load.cpp", "bvh_build.cpp", "image_out.cpp"]
 
 
@@ -81,7 +83,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     for f in CU_SOURCES:
         src = os.path.join(CSRC, f)
         obj = os.path.join(OBJ, f + ".o")
-        cmd = [nvcc] + ARCH + NVCC_COMMON + CU_EXTRA.get(f, []) + ["-c", src, "-o", obj]
+        cmd = [nvcc] + ARCH + NVCC_COMMON + CU_EXTRA.get(f, []) + EXTRA_NVCC + ["-c", src, "-o", obj]
         tasks.append((src, cmd, obj))
     for f in CPP_SOURCES + ["cli.cpp"]:
         src = os.path.join(CSRC, f)

@@ -60,7 +60,7 @@ void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::f
   p.pq[1] = static_cast<int32_t*>(A(c * sizeof(int32_t)));
   p.rq[0] = static_cast<int32_t*>(A(2 * c * sizeof(int32_t)));
   p.rq[1] = static_cast<int32_t*>(A(2 * c * sizeof(int32_t)));
-  p.counts = static_cast<uint32_t*>(A(4 * sizeof(uint32_t)));
+  p.counts = static_cast<uint32_t*>(A(kCountSlots * sizeof(uint32_t)));
   p.out_color = static_cast<float4*>(A(c * sizeof(float4)));
   p.out_normal = static_cast<float4*>(A(c * sizeof(float4)));
   p.out_albedo = static_cast<float4*>(A(c * sizeof(float4)));
@@ -70,7 +70,7 @@ void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::f
     p.stats = static_cast<unsigned long long*>(A(size_t(n_stats) * sizeof(unsigned long long)));
     ck(cudaMemsetAsync(p.stats, 0, sizeof(unsigned long long) * size_t(n_stats), st), "memset stats");
   }
-  ck(cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * 4, st), "memset counts");
+  ck(cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * kCountSlots, st), "memset counts");
 }
 
 // Path-state buffers of the single-job path are allocated at the first

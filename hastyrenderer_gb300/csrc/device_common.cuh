@@ -12,6 +12,40 @@
 #include <cfloat>
 #include "hasty_types.h"
 
+// Which large shading routines are compiled out of line (one shared copy,
+// called) instead of inlined at every call site; bits of HASTY_OUTLINE_MASK:
+//   1 bsdf_sample, 2 bsdf_eval + bsdf_pdf, 4 make_inter, 8 environment and
+//   light densities and sampling, 16 shade_ctx. Only code placement changes;
+//   every result is the same.
+#ifndef HASTY_OUTLINE_MASK
+#define HASTY_OUTLINE_MASK 0
+#endif
+#if (HASTY_OUTLINE_MASK & 1)
+#define HFN_SAMPLE __device__ __noinline__
+#else
+#define HFN_SAMPLE __device__ __forceinline__
+#endif
+#if (HASTY_OUTLINE_MASK & 2)
+#define HFN_EVAL __device__ __noinline__
+#else
+#define HFN_EVAL __device__ __forceinline__
+#endif
+#if (HASTY_OUTLINE_MASK & 4)
+#define HFN_INTER __device__ __noinline__
+#else
+#define HFN_INTER __device__ __forceinline__
+#endif
+#if (HASTY_OUTLINE_MASK & 8)
+#define HFN_ENV __device__ __noinline__
+#else
+#define HFN_ENV __device__ __forceinline__
+#endif
+#if (HASTY_OUTLINE_MASK & 16)
+#define HFN_CTX __device__ __noinline__
+#else
+#define HFN_CTX __device__ __forceinline__
+#endif
+
 namespace hasty {
 namespace dev {
 
@@ -393,7 +427,7 @@ __device__ __forceinline__ V3 shading_normal(const SceneDev& sc, const MaterialD
 // anisotropic frame (computeAnisotropyParameters). Each quantity is computed
 // exactly as the reference computes it inside each of those calls.
 struct ShadeCtx { V3 ns, alb, tan, bit; float rough, met, alpha, at, ab, ngwo, nswo; };
-__device__ __forceinline__ ShadeCtx shade_ctx(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wo) {
+HFN_CTX ShadeCtx shade_ctx(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wo) {
   ShadeCtx c;
   c.ngwo = dot(it.ng, wo);
   c.ns = shading_normal(sc, m, it, wo, c.ngwo);
@@ -408,7 +442,7 @@ __device__ __forceinline__ ShadeCtx shade_ctx(const SceneDev& sc, const Material
 
 struct BsdfEval { V3 fD, fC; };
 // PrincipledBRDF::evaluate, BRDF.cpp:630-679
-__device__ __forceinline__ BsdfEval bsdf_eval(const ShadeCtx& c, const MaterialDev& m, const Inter& it, V3 wo, V3 wi) {
+HFN_EVAL BsdfEval bsdf_eval(const ShadeCtx& c, const MaterialDev& m, const Inter& it, V3 wo, V3 wi) {
   float nswi = dot(c.ns, wi);
   float nsc = normal_scale(wi, c.ns, it.ng);
   BsdfEval e;
@@ -419,7 +453,7 @@ __device__ __forceinline__ BsdfEval bsdf_eval(const ShadeCtx& c, const MaterialD
 }
 
 // PrincipledBRDF::evaluateSamplePDF, BRDF.cpp:702-742 (nominal IOR)
-__device__ __forceinline__ float bsdf_pdf(const ShadeCtx& c, const MaterialDev& m, V3 wo, V3 wi, float eta_out) {
+HFN_EVAL float bsdf_pdf(const ShadeCtx& c, const MaterialDev& m, V3 wo, V3 wi, float eta_out) {
   bool from_out = c.ngwo >= 0.0f;
   float eo = from_out ? eta_out : m.ior, et = from_out ? m.ior : eta_out;
   Prob p = compute_probability(c.met, m.specular, m.transmission, c.nswo, eo, et);
@@ -432,7 +466,7 @@ __device__ __forceinline__ float bsdf_pdf(const ShadeCtx& c, const MaterialDev& 
 struct BsdfSample { bool outside; V3 dir, thrD, thrC; float pdf; };
 // PrincipledBRDF::sample (member + static), BRDF.cpp:397-579, 681-700
 template <class R>
-__device__ BsdfSample bsdf_sample(const ShadeCtx& c, const MaterialDev& m, const Inter& it, V3 wo, int wl, float eta_out,
+HFN_SAMPLE BsdfSample bsdf_sample(const ShadeCtx& c, const MaterialDev& m, const Inter& it, V3 wo, int wl, float eta_out,
                                   R& r, int& capped) {
   BsdfSample res;
   const V3 ns = c.ns, alb = c.alb, tan = c.tan, bit = c.bit;
@@ -507,7 +541,7 @@ __device__ __forceinline__ V3 tri_ng_raw(const float* p) {
 }
 
 // Scene::getInteraction, Scene.cpp:202-255
-__device__ Inter make_inter(const SceneDev& sc, int tri, V3 b, V3 ng) {
+HFN_INTER Inter make_inter(const SceneDev& sc, int tri, V3 b, V3 ng) {
   Inter it;
   const TriAttr a = sc.tri_attr[tri];
   const float* p = sc.tri_pos + 9 * int64_t(tri);
@@ -579,7 +613,7 @@ __device__ __forceinline__ void sph_from_dir(V3 d, float& th, float& ph) {
   ph = ph < 0.0f ? ph + HTWOPI_F : ph;
 }
 // EnvironmentTexture::evalEmission / BackgroundColor, Environment.h:26-29,135-140
-__device__ __forceinline__ V3 env_eval(const SceneDev& sc, V3 d) {
+HFN_ENV V3 env_eval(const SceneDev& sc, V3 d) {
   const EnvDev& e = sc.env;
   if (!e.is_texture) return ld3(e.color);
   float th, ph; sph_from_dir(d, th, ph);
@@ -592,7 +626,7 @@ __device__ __forceinline__ V3 env_eval(const SceneDev& sc, V3 d) {
   return ld3(e.texels + 3 * (int64_t(row) * e.w + col));
 }
 // EnvironmentTexture::evalSamplingDensity, Environment.h:159-166
-__device__ __forceinline__ float env_density(const SceneDev& sc, V3 d) {
+HFN_ENV float env_density(const SceneDev& sc, V3 d) {
   const EnvDev& e = sc.env;
   float th, ph; sph_from_dir(d, th, ph);
   float u = ph * float(0.5 * kInvPi);
@@ -605,7 +639,7 @@ __device__ __forceinline__ float env_density(const SceneDev& sc, V3 d) {
   return dens / fmaxf(1e-7f, 2.0f * float(kPi * kPi) * s);
 }
 // EnvironmentTexture::sample + ImageDistribution::sample, Environment.h:60-79,142-153
-template <class R> __device__ __forceinline__ V3 env_sample(const SceneDev& sc, R& r, float& density, int& capped) {
+template <class R> HFN_ENV V3 env_sample(const SceneDev& sc, R& r, float& density, int& capped) {
   const EnvDev& e = sc.env;
   uint32_t n = uint32_t(e.w) * uint32_t(e.h);
   V3 dir; float sin_t = 0.f;
@@ -636,7 +670,7 @@ template <class R> __device__ __forceinline__ V3 env_sample(const SceneDev& sc, 
 
 // Scene::evalLightRayFromStartPointDensity, Scene.cpp:587-616. `tri` < 0 is
 // a miss; `x2`/`ng2` are the hit's position and unit geometric normal.
-__device__ __forceinline__ float light_density(const SceneDev& sc, V3 o, V3 d, int tri, V3 x2, V3 ng2) {
+HFN_ENV float light_density(const SceneDev& sc, V3 o, V3 d, int tri, V3 x2, V3 ng2) {
   bool surf = tri >= 0 && sc.mats[sc.tri_attr[tri].mat].is_light;
   bool inf = tri < 0;
   if (!surf && !inf) return 0.0f;

@@ -274,7 +274,21 @@ __device__ __forceinline__ ShadeRes shade_path(const SceneDev& sc, const PathsDe
   return res;
 }
 
-__global__ void __launch_bounds__(128) k_shade(SceneDev sc, PathsDev P, BatchDesc b, int q) {
+// Minimum resident blocks per SM asked of the compiler for the shading
+// kernels (0: no bound beyond the block size). Shading is latency-bound
+// (dependent loads of hit, triangle, material, texture): 16 blocks of 128
+// threads, the SM's full 2048 threads, measured fastest on GB300 although
+// the 32-register budget spills to local memory (L1).
+#ifndef HASTY_SHADE_MIN_BLOCKS
+#define HASTY_SHADE_MIN_BLOCKS 16
+#endif
+#if HASTY_SHADE_MIN_BLOCKS > 0
+#define SHADE_BOUNDS __launch_bounds__(128, HASTY_SHADE_MIN_BLOCKS)
+#else
+#define SHADE_BOUNDS __launch_bounds__(128)
+#endif
+
+__global__ void SHADE_BOUNDS k_shade(SceneDev sc, PathsDev P, BatchDesc b, int q) {
   const uint32_t n_in = P.counts[q];
   uint32_t* pq_cnt = &P.counts[q ^ 1];
   uint32_t* rq_cnt = &P.counts[2 + (q ^ 1)];
@@ -534,7 +548,7 @@ __device__ __forceinline__ void add_fixed(unsigned long long* acc, V3 L, float4 
   if (sat) atomicAdd(&stats[MS_SATURATED], 1ull);
 }
 
-__global__ void __launch_bounds__(128) k_shade_multi(PathsDev P, MultiDev m) {
+__global__ void SHADE_BOUNDS k_shade_multi(PathsDev P, MultiDev m) {
   const uint32_t q = m.ctl[0];
   const uint32_t n_in = P.counts[q];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;

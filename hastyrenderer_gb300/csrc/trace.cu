@@ -14,6 +14,7 @@
 // The traversal routines are host+device: the host build runs the same code
 // on the CPU for the loader/builder tests (hasty_debug_host_trace).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstring>
 #include "hasty_types.h"
 #include "wavefront.h"
@@ -22,6 +23,8 @@ namespace hasty {
 namespace {
 
 #define HDI __host__ __device__ __forceinline__
+
+constexpr unsigned kFullMask = 0xFFFFFFFFu;
 
 struct Hit { float t, u, v; int tri; };
 
@@ -141,29 +144,48 @@ HDI RayInv inverse_dir(float dx, float dy, float dz) {
 // ---------------------------------------------------------- binary BVH ----
 constexpr int kStack = 64;
 
-HDI Hit trace_binary(const float4* nodes, const float4* tris, float ox, float oy, float oz, float dx, float dy, float dz) {
-  Hit best; best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
-  RayInv iv = inverse_dir(dx, dy, dz);
-  int stack[kStack];
-  int sp = 0;
-  int link = 0;   // root (always an inner node)
-  while (true) {
+// Traversal state of one ray. init() sets it up; each step() walks inner
+// nodes to the next leaf, tests the leaf's triangles and pops the next
+// subtree; it returns true once the ray is finished (result in `best`).
+// Whole-ray traversal is init() + step() until true; the persistent GPU
+// kernels interleave steps of many rays, with identical results per ray.
+// The traversal stack is kept outside the struct (passed to step()) so the
+// scalar state can stay in registers.
+struct TravBinary {
+  using Entry = int;
+  static constexpr int kDepth = kStack;
+  float ox, oy, oz, dx, dy, dz;
+  RayInv iv;
+  bool neg_x, neg_y, neg_z;
+  Hit best;
+  int link, sp;
+
+  HDI void init(float ox_, float oy_, float oz_, float dx_, float dy_, float dz_) {
+    ox = ox_; oy = oy_; oz = oz_; dx = dx_; dy = dy_; dz = dz_;
+    best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
+    iv = inverse_dir(dx, dy, dz);
+    neg_x = iv.ix < 0.f; neg_y = iv.iy < 0.f; neg_z = iv.iz < 0.f;
+    sp = 0;
+    link = 0;   // root (always an inner node)
+  }
+
+  HDI bool step(const float4* nodes, const float4* tris, int* stack) {
     while (link >= 0) {
       float4 n0 = ld(&nodes[4 * link + 0]);
       float4 n1 = ld(&nodes[4 * link + 1]);
       float4 n2 = ld(&nodes[4 * link + 2]);
       float4 n3 = ld(&nodes[4 * link + 3]);
       float tlim = best.t * kPadHi;
-      float a0 = slab(n0.x, ox, iv.ix), a1 = slab(n0.y, ox, iv.ix);
-      float b0 = slab(n0.z, oy, iv.iy), b1 = slab(n0.w, oy, iv.iy);
-      float c0 = slab(n2.x, oz, iv.iz), c1 = slab(n2.y, oz, iv.iz);
-      float t0min = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f)) * kPadLo;
-      float t0max = fminf(fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fmaxf(c0, c1)) * kPadHi, tlim);
-      float d0 = slab(n1.x, ox, iv.ix), d1 = slab(n1.y, ox, iv.ix);
-      float e0 = slab(n1.z, oy, iv.iy), e1v = slab(n1.w, oy, iv.iy);
-      float f0 = slab(n2.z, oz, iv.iz), f1 = slab(n2.w, oz, iv.iz);
-      float t1min = fmaxf(fmaxf(fminf(d0, d1), fminf(e0, e1v)), fmaxf(fminf(f0, f1), 0.0f)) * kPadLo;
-      float t1max = fminf(fminf(fminf(fmaxf(d0, d1), fmaxf(e0, e1v)), fmaxf(f0, f1)) * kPadHi, tlim);
+      // near/far planes by the direction sign: (b - o) * id is monotonic in b,
+      // so this picks exactly what per-axis min/max would
+      float t0min = fmaxf(fmaxf(slab(neg_x ? n0.y : n0.x, ox, iv.ix), slab(neg_y ? n0.w : n0.z, oy, iv.iy)),
+                          fmaxf(slab(neg_z ? n2.y : n2.x, oz, iv.iz), 0.0f)) * kPadLo;
+      float t0max = fminf(fminf(fminf(slab(neg_x ? n0.x : n0.y, ox, iv.ix), slab(neg_y ? n0.z : n0.w, oy, iv.iy)),
+                                slab(neg_z ? n2.x : n2.y, oz, iv.iz)) * kPadHi, tlim);
+      float t1min = fmaxf(fmaxf(slab(neg_x ? n1.y : n1.x, ox, iv.ix), slab(neg_y ? n1.w : n1.z, oy, iv.iy)),
+                          fmaxf(slab(neg_z ? n2.w : n2.z, oz, iv.iz), 0.0f)) * kPadLo;
+      float t1max = fminf(fminf(fminf(slab(neg_x ? n1.x : n1.y, ox, iv.ix), slab(neg_y ? n1.z : n1.w, oy, iv.iy)),
+                                slab(neg_z ? n2.z : n2.w, oz, iv.iz)) * kPadHi, tlim);
       bool h0 = t0min <= t0max, h1 = t1min <= t1max;
       int l0 = int(f2u(n3.x)), l1 = int(f2u(n3.y));
       if (h0 && h1) {
@@ -176,7 +198,7 @@ HDI Hit trace_binary(const float4* nodes, const float4* tris, float ox, float oy
       } else if (h1) {
         link = l1;
       } else {
-        if (sp == 0) return best;
+        if (sp == 0) return true;
         link = stack[--sp];
       }
     }
@@ -187,9 +209,18 @@ HDI Hit trace_binary(const float4* nodes, const float4* tris, float ox, float oy
       int ti = first + k;
       tri_test(ox, oy, oz, dx, dy, dz, ld(&tris[3 * ti]), ld(&tris[3 * ti + 1]), ld(&tris[3 * ti + 2]), best);
     }
-    if (sp == 0) return best;
+    if (sp == 0) return true;
     link = stack[--sp];
+    return false;
   }
+};
+
+HDI Hit trace_binary(const float4* nodes, const float4* tris, float ox, float oy, float oz, float dx, float dy, float dz) {
+  TravBinary tr;
+  int stack[kStack];
+  tr.init(ox, oy, oz, dx, dy, dz);
+  while (!tr.step(nodes, tris, stack)) {}
+  return tr.best;
 }
 
 // ------------------------------------------------- compressed 8-wide BVH ----
@@ -203,16 +234,42 @@ constexpr int kWideStack = 32;
 
 HDI uint32_t byte_of(uint32_t w, uint32_t k) { return (w >> (8 * k)) & 0xFFu; }
 
-HDI Hit trace_wide(const float4* nodes, const float4* tris, float ox, float oy, float oz, float dx, float dy, float dz) {
-  Hit best; best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
-  RayInv iv = inverse_dir(dx, dy, dz);
-  const uint32_t oct = (iv.ix < 0.f ? 4u : 0u) | (iv.iy < 0.f ? 2u : 0u) | (iv.iz < 0.f ? 1u : 0u);
-  const uint32_t oct4 = oct * 0x01010101u;
-  uint2 stack[kWideStack];
-  int sp = 0;
-  uint2 ng = make_uint2(0u, 0x80000000u);
-  uint2 tg = make_uint2(0u, 0u);
-  while (true) {
+// Byte k of w as a float, exactly: the byte is placed in the mantissa of
+// 2^23 by one byte permute and 2^23 is subtracted (exact for 0..255).
+HDI float byte_float(uint32_t w, uint32_t k) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, k | 0x7540u)) - 8388608.0f;
+#else
+  return float(byte_of(w, k));
+#endif
+}
+
+// Same contract as TravBinary: a step tests the pending triangle group and
+// opens one node.
+struct TravWide {
+  using Entry = uint2;
+  static constexpr int kDepth = kWideStack;
+  float ox, oy, oz, dx, dy, dz;
+  RayInv iv;
+  bool neg_x, neg_y, neg_z;
+  uint32_t oct, oct4;
+  Hit best;
+  uint2 ng, tg;
+  int sp;
+
+  HDI void init(float ox_, float oy_, float oz_, float dx_, float dy_, float dz_) {
+    ox = ox_; oy = oy_; oz = oz_; dx = dx_; dy = dy_; dz = dz_;
+    best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
+    iv = inverse_dir(dx, dy, dz);
+    neg_x = iv.ix < 0.f; neg_y = iv.iy < 0.f; neg_z = iv.iz < 0.f;
+    oct = (neg_x ? 4u : 0u) | (neg_y ? 2u : 0u) | (neg_z ? 1u : 0u);
+    oct4 = oct * 0x01010101u;
+    sp = 0;
+    ng = make_uint2(0u, 0x80000000u);
+    tg = make_uint2(0u, 0u);
+  }
+
+  HDI bool step(const float4* nodes, const float4* tris, uint2* stack) {
     while (tg.y) {
       uint32_t b = lowest_bit(tg.y);
       tg.y &= tg.y - 1u;
@@ -220,7 +277,7 @@ HDI Hit trace_wide(const float4* nodes, const float4* tris, float ox, float oy, 
       tri_test(ox, oy, oz, dx, dy, dz, ld(&tris[3 * ti]), ld(&tris[3 * ti + 1]), ld(&tris[3 * ti + 2]), best);
     }
     if (ng.y <= 0x00FFFFFFu) {
-      if (sp == 0) break;
+      if (sp == 0) return true;
       ng = stack[--sp];
     }
     uint32_t bit = highest_bit(ng.y);
@@ -241,9 +298,13 @@ HDI Hit trace_wide(const float4* nodes, const float4* tris, float ox, float oy, 
     float sx = u2f(uint32_t(ex + 127) << 23), sy = u2f(uint32_t(ey + 127) << 23), sz = u2f(uint32_t(ez + 127) << 23);
     uint32_t child_base = f2u(f1.x), tri_base = f2u(f1.y);
     uint32_t meta_w[2] = {f2u(f1.z), f2u(f1.w)};
-    uint32_t qlx[2] = {f2u(f2.x), f2u(f2.y)}, qly[2] = {f2u(f2.z), f2u(f2.w)};
-    uint32_t qlz[2] = {f2u(f3.x), f2u(f3.y)}, qhx[2] = {f2u(f3.z), f2u(f3.w)};
-    uint32_t qhy[2] = {f2u(f4.x), f2u(f4.y)}, qhz[2] = {f2u(f4.z), f2u(f4.w)};
+    // near and far planes per axis, chosen once by the ray's direction sign
+    const uint32_t nx[2] = {neg_x ? f2u(f3.z) : f2u(f2.x), neg_x ? f2u(f3.w) : f2u(f2.y)};
+    const uint32_t fx[2] = {neg_x ? f2u(f2.x) : f2u(f3.z), neg_x ? f2u(f2.y) : f2u(f3.w)};
+    const uint32_t ny[2] = {neg_y ? f2u(f4.x) : f2u(f2.z), neg_y ? f2u(f4.y) : f2u(f2.w)};
+    const uint32_t fy[2] = {neg_y ? f2u(f2.z) : f2u(f4.x), neg_y ? f2u(f2.w) : f2u(f4.y)};
+    const uint32_t nz[2] = {neg_z ? f2u(f4.z) : f2u(f3.x), neg_z ? f2u(f4.w) : f2u(f3.y)};
+    const uint32_t fz[2] = {neg_z ? f2u(f3.x) : f2u(f4.z), neg_z ? f2u(f3.y) : f2u(f4.w)};
     float tlim = best.t * kPadHi;
     uint32_t hitmask = 0;
 #pragma unroll
@@ -255,21 +316,29 @@ HDI Hit trace_wide(const float4* nodes, const float4* tris, float ox, float oy, 
       uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
 #pragma unroll
       for (uint32_t k = 0; k < 4; ++k) {
-        float lx = fmaf(float(byte_of(qlx[h], k)), sx, f0.x), hx = fmaf(float(byte_of(qhx[h], k)), sx, f0.x);
-        float ly = fmaf(float(byte_of(qly[h], k)), sy, f0.y), hy = fmaf(float(byte_of(qhy[h], k)), sy, f0.y);
-        float lz = fmaf(float(byte_of(qlz[h], k)), sz, f0.z), hz = fmaf(float(byte_of(qhz[h], k)), sz, f0.z);
-        float a0 = slab(lx, ox, iv.ix), a1 = slab(hx, ox, iv.ix);
-        float b0 = slab(ly, oy, iv.iy), b1 = slab(hy, oy, iv.iy);
-        float c0 = slab(lz, oz, iv.iz), c1 = slab(hz, oz, iv.iz);
-        float tmin = fmaxf(fmaxf(fminf(a0, a1), fminf(b0, b1)), fmaxf(fminf(c0, c1), 0.0f)) * kPadLo;
-        float tmax = fminf(fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fmaxf(c0, c1)) * kPadHi, tlim);
+        float tnx = slab(fmaf(byte_float(nx[h], k), sx, f0.x), ox, iv.ix);
+        float tfx = slab(fmaf(byte_float(fx[h], k), sx, f0.x), ox, iv.ix);
+        float tny = slab(fmaf(byte_float(ny[h], k), sy, f0.y), oy, iv.iy);
+        float tfy = slab(fmaf(byte_float(fy[h], k), sy, f0.y), oy, iv.iy);
+        float tnz = slab(fmaf(byte_float(nz[h], k), sz, f0.z), oz, iv.iz);
+        float tfz = slab(fmaf(byte_float(fz[h], k), sz, f0.z), oz, iv.iz);
+        float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f)) * kPadLo;
+        float tmax = fminf(fminf(fminf(tfx, tfy), tfz) * kPadHi, tlim);
         if (tmin <= tmax) hitmask |= byte_of(child_bits4, k) << byte_of(bit_index4, k);
       }
     }
     ng = make_uint2(child_base, (hitmask & 0xFF000000u) | node_imask);
     tg = make_uint2(tri_base, hitmask & 0x00FFFFFFu);
+    return false;
   }
-  return best;
+};
+
+HDI Hit trace_wide(const float4* nodes, const float4* tris, float ox, float oy, float oz, float dx, float dy, float dz) {
+  TravWide tr;
+  uint2 stack[kWideStack];
+  tr.init(ox, oy, oz, dx, dy, dz);
+  while (!tr.step(nodes, tris, stack)) {}
+  return tr.best;
 }
 
 template <int KIND>
@@ -278,16 +347,94 @@ HDI Hit trace_any(const float4* nodes, const float4* tris, float ox, float oy, f
   return trace_binary(nodes, tris, ox, oy, oz, dx, dy, dz);
 }
 
+// Minimum resident blocks per SM for the closest-hit kernels (0: none).
+#ifndef HASTY_TRACE_MIN_BLOCKS
+#define HASTY_TRACE_MIN_BLOCKS 0
+#endif
+#if HASTY_TRACE_MIN_BLOCKS > 0
+#define TRACE_BOUNDS __launch_bounds__(128, HASTY_TRACE_MIN_BLOCKS)
+#else
+#define TRACE_BOUNDS __launch_bounds__(128)
+#endif
+
+// Persistent closest-hit kernels (Aila and Laine 2009, dynamic fetch): a
+// grid of the SMs' resident blocks loops until the ray queue is drained.
+// Whenever kRefill lanes of a warp are idle, the warp takes that many rays
+// from the queue with one atomic on the fetch counter, so lanes whose rays
+// finish early do not idle while their warp's longest ray is traversed. Each
+// ray's traversal is the same sequence of steps as trace_binary/trace_wide.
+#ifndef HASTY_TRACE_REFILL
+#define HASTY_TRACE_REFILL 8
+#endif
+constexpr int kRefill = HASTY_TRACE_REFILL;
+// Persistent traversal pays for the wide BVH (one node per step, long and
+// uneven rays); the binary BVH's leaf-to-leaf steps are too short to carry
+// the refill bookkeeping, so it runs one ray per thread.
+template <int KIND> constexpr bool kPersistent = KIND == 1;
+
+template <int KIND> struct TravOf { using T = TravBinary; };
+template <> struct TravOf<1> { using T = TravWide; };
+
+template <int KIND, class Fetch, class Done>
+__device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* next, Fetch fetch, Done done) {
+  typename TravOf<KIND>::T tr;
+  typename TravOf<KIND>::T::Entry stack[TravOf<KIND>::T::kDepth];
+  const float4* nodes = nullptr;
+  const float4* tris = nullptr;
+  int rid = 0;
+  bool active = false;
+  bool drained = false;                 // warp-uniform: the queue has been handed out
+  const uint32_t lane = threadIdx.x & 31u;
+  for (;;) {
+    if (!drained) {
+      const unsigned idle = __ballot_sync(kFullMask, !active);
+      const uint32_t n_idle = uint32_t(__popc(idle));
+      if (n_idle >= uint32_t(kRefill)) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(next, n_idle);
+        base = __shfl_sync(kFullMask, base, 0);
+        if (base >= n || n - base <= n_idle) drained = true;
+        if (!active) {
+          const uint32_t k = base + uint32_t(__popc(idle & ((1u << lane) - 1u)));
+          if (k < n) {
+            fetch(k, tr, nodes, tris, rid);
+            active = true;
+          }
+        }
+      }
+    }
+    if (__ballot_sync(kFullMask, active) == 0) break;   // drained: an all-idle warp always refills otherwise
+    if (active && tr.step(nodes, tris, stack)) {
+      done(rid, tr.best);
+      active = false;
+    }
+  }
+}
+
 template <int KIND>
-__global__ void __launch_bounds__(128) k_trace(SceneDev sc, PathsDev P, int q) {
-  uint32_t n = P.counts[2 + q];
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0 && n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
-  if (i >= n) return;
-  int rid = P.rq[q][i];
-  float4 o = P.ray_o[rid], d = P.ray_d[rid];
-  Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
-  P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+__global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
+  const uint32_t n = P.counts[2 + q];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
+  const int32_t* rq = P.rq[q];
+  if (!kPersistent<KIND>) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      int rid = rq[i];
+      float4 o = P.ray_o[rid], d = P.ray_d[rid];
+      Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
+      P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+    }
+    return;
+  }
+  persistent_trace<KIND>(
+      n, &P.counts[kFetchCounter],
+      [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
+        rid = rq[k];
+        float4 o = P.ray_o[rid], d = P.ray_d[rid];
+        tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
+        nodes = sc.nodes;
+        tris = sc.isect_tris;
+      },
+      [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
 }
 
 template <int KIND>
@@ -302,30 +449,70 @@ __global__ void k_trace_rays(SceneDev sc, const float* rays, int n, float4* hits
 // Multi-job engine: each ray belongs to the job of its path slot (ray id / 2).
 // All jobs of one engine share the BVH layout of their context (KIND).
 template <int KIND>
-__global__ void __launch_bounds__(128) k_trace_multi(PathsDev P, MultiDev m) {
+__global__ void TRACE_BOUNDS k_trace_multi(PathsDev P, MultiDev m) {
   const uint32_t q = m.ctl[0];
-  uint32_t n = P.counts[2 + q];
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0 && n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
-  if (i >= n) return;
-  int rid = P.rq[q][i];
-  const SceneDev& sc = m.jobs[m.slot_job[rid >> 1]].sc;
-  float4 o = P.ray_o[rid], d = P.ray_d[rid];
-  Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
-  P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+  const uint32_t n = P.counts[2 + q];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
+  const int32_t* rq = P.rq[q];
+  if (!kPersistent<KIND>) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      int rid = rq[i];
+      const SceneDev& sc = m.jobs[m.slot_job[rid >> 1]].sc;
+      float4 o = P.ray_o[rid], d = P.ray_d[rid];
+      Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
+      P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+    }
+    return;
+  }
+  persistent_trace<KIND>(
+      n, &P.counts[kFetchCounter],
+      [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
+        rid = rq[k];
+        const SceneDev& sc = m.jobs[m.slot_job[rid >> 1]].sc;
+        float4 o = P.ray_o[rid], d = P.ray_d[rid];
+        tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
+        nodes = sc.nodes;
+        tris = sc.isect_tris;
+      },
+      [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
+}
+
+// Resident blocks of a persistent trace kernel on the current device.
+template <class K>
+int persistent_grid(K kernel) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
+  if (sms < 1) sms = 1;
+  if (per_sm < 1) per_sm = 1;
+  return sms * per_sm;
 }
 
 }  // namespace
 
+// The persistent kernels take rays through P.counts[kFetchCounter], cleared
+// on the stream before each launch. Grids: the SMs' resident blocks, fewer
+// when the queue bound is smaller.
 void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t st) {
-  if (bvh_kind == 1) k_trace_multi<1><<<(max_rays + 127) / 128, 128, 0, st>>>(p, m);
-  else k_trace_multi<0><<<(max_rays + 127) / 128, 128, 0, st>>>(p, m);
+  static int grid[2] = {0, 0};
+  int k = bvh_kind == 1 ? 1 : 0;
+  if (!grid[k]) grid[k] = k ? persistent_grid(k_trace_multi<1>) : persistent_grid(k_trace_multi<0>);
+  // one-ray-per-thread kernels loop over the queue with a grid-sized stride
+  int blocks = std::min(k ? grid[k] : 8 * grid[k], std::max(1, (max_rays + 127) / 128));
+  cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
+  if (k) k_trace_multi<1><<<blocks, 128, 0, st>>>(p, m);
+  else k_trace_multi<0><<<blocks, 128, 0, st>>>(p, m);
 }
 
 void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cudaStream_t st) {
-  int blocks = (max_rays + 127) / 128;
-  if (blocks < 1) blocks = 1;
-  if (sc.bvh_kind == 1) k_trace<1><<<blocks, 128, 0, st>>>(sc, p, q);
+  static int grid[2] = {0, 0};
+  int k = sc.bvh_kind == 1 ? 1 : 0;
+  if (!grid[k]) grid[k] = k ? persistent_grid(k_trace<1>) : persistent_grid(k_trace<0>);
+  int blocks = k ? std::min(grid[k], std::max(1, (max_rays + 127) / 128)) : std::max(1, (max_rays + 127) / 128);
+  cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
+  if (k) k_trace<1><<<blocks, 128, 0, st>>>(sc, p, q);
   else k_trace<0><<<blocks, 128, 0, st>>>(sc, p, q);
 }
 
