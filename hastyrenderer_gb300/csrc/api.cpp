@@ -61,6 +61,8 @@ void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::f
   p.rq[0] = static_cast<int32_t*>(A(2 * c * sizeof(int32_t)));
   p.rq[1] = static_cast<int32_t*>(A(2 * c * sizeof(int32_t)));
   p.counts = static_cast<uint32_t*>(A(kCountSlots * sizeof(uint32_t)));
+  p.vtx = static_cast<float4*>(A(6 * c * sizeof(float4)));
+  p.sq = static_cast<int32_t*>(A(c * sizeof(int32_t)));
   p.out_color = static_cast<float4*>(A(c * sizeof(float4)));
   p.out_normal = static_cast<float4*>(A(c * sizeof(float4)));
   p.out_albedo = static_cast<float4*>(A(c * sizeof(float4)));
@@ -80,7 +82,7 @@ void hasty::ensure_paths(hasty_job& j) {
   if (j.pd.rng && j.pd.capacity == j.capacity) return;
   ck(cudaStreamSynchronize(j.stream), "sync");
   void* olds[] = {j.pd.rng, j.pd.thr, j.pd.rad, j.pd.pend_b, j.pd.nee_c, j.pd.nee_t, j.pd.med, j.pd.med_geom, j.pd.ray_o,
-                  j.pd.ray_d, j.pd.hit, j.pd.pq[0], j.pd.pq[1], j.pd.rq[0], j.pd.rq[1], j.pd.counts, j.pd.out_color,
+                  j.pd.ray_d, j.pd.hit, j.pd.pq[0], j.pd.pq[1], j.pd.rq[0], j.pd.rq[1], j.pd.counts, j.pd.vtx, j.pd.sq, j.pd.out_color,
                   j.pd.out_normal, j.pd.out_albedo};
   for (void* p : olds) j.release(p);
   unsigned long long* stats = j.pd.stats;
@@ -363,7 +365,7 @@ int hasty_job_release_paths(hasty_job* job) {
     job->collect_events();
     PathsDev& p = job->pd;
     void* bufs[] = {p.rng, p.thr, p.rad, p.pend_b, p.nee_c, p.nee_t, p.med, p.med_geom, p.ray_o, p.ray_d, p.hit,
-                    p.pq[0], p.pq[1], p.rq[0], p.rq[1], p.counts, p.out_color, p.out_normal, p.out_albedo};
+                    p.pq[0], p.pq[1], p.rq[0], p.rq[1], p.counts, p.vtx, p.sq, p.out_color, p.out_normal, p.out_albedo};
     for (void* b : bufs) job->release(b);
     unsigned long long* stats = p.stats;
     p = PathsDev{};

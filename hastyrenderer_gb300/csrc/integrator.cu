@@ -1,10 +1,11 @@
 // Wavefront form of the reference's recursive estimator
 // (estimateRadiance, core/src/PathTracing.cpp:21-95; strategies in
-// core/src/MIS.cpp). Per bounce, `k_shade` finishes the previous vertex's two
-// MIS samples once their rays have been traced (light sample: visibility,
+// core/src/MIS.cpp). Per bounce, `k_resolve` finishes the previous vertex's
+// two MIS samples once their rays have been traced (light sample: visibility,
 // light pdf, power-heuristic weight, emitted radiance; BSDF sample: weight and
-// the next vertex), shades the new vertex (Russian roulette, light sample,
-// BSDF sample, medium stack, dispersion band) and queues the rays it needs.
+// the next vertex) and plays Russian roulette; `k_sample` shades the
+// surviving vertices (light sample, BSDF sample, medium stack, dispersion
+// band) and queues the rays they need.
 // Random numbers are drawn in the reference's order, one PCG32 stream per
 // (job seed, pixel, pass).
 #include <cuda_runtime.h>
@@ -100,232 +101,319 @@ __global__ void __launch_bounds__(256) k_raygen(SceneDev sc, PathsDev P, BatchDe
   P.rq[0][s] = 2 * s;
 }
 
-// One bounce of one path (slot s): resolve the previous vertex's light and
-// BSDF samples, shade the vertex reached, queue its rays in the slot's ray
-// entries. `key` is the path's stream key. The caller handles a finished path
-// (res.keep false) and the queues.
-struct ShadeRes { bool keep, emitB, emitL; int shaded, overflow, capped; V3 L; };
+// One bounce of one path (slot s) is split in two kernels so that each runs
+// a smaller, more uniform body and the sampling kernel only sees paths that
+// continue:
+//  * resolve_path: resolve the previous vertex's light sample and the BSDF
+//    sample's hit (self-intersection, MIS weight, depth limit, miss, emitter,
+//    Russian roulette); a path that survives leaves its vertex record (the
+//    interaction and the transmittance-and-roulette factor) for
+//  * sample_path: the light strategy's sample and the BSDF sample of the
+//    vertex, queued as the slot's two rays.
+// The arithmetic is the single-kernel bounce's, in the same order.
+struct ResolveRes { bool sample; int shaded; V3 L; };
+struct SampleRes { bool keep, emitB, emitL; int overflow, capped; V3 L; };
 
-__device__ __forceinline__ ShadeRes shade_path(const SceneDev& sc, const PathsDev& P, int s, uint64_t key) {
-  ShadeRes res;
-  res.keep = res.emitB = res.emitL = false;
-  res.shaded = res.overflow = res.capped = 0;
-  bool& keep = res.keep;
-  bool& emitB = res.emitB;
-  bool& emitL = res.emitL;
-  int& shaded = res.shaded;
-  int& overflow = res.overflow;
-  int& capped = res.capped;
-  {
-    float4 rad = P.rad[s];
-    uint32_t flags = __float_as_uint(rad.w);
-    V3 L = xyz(rad);
-    bool done = false;
+__device__ __forceinline__ void store_vertex(const PathsDev& P, int s, const Inter& it, V3 tl) {
+  float4* v = P.vtx + 6 * int64_t(s);
+  v[0] = make_float4(it.x.x, it.x.y, it.x.z, it.h);
+  v[1] = make_float4(it.ng.x, it.ng.y, it.ng.z, it.u);
+  v[2] = make_float4(it.ns.x, it.ns.y, it.ns.z, it.v);
+  v[3] = make_float4(it.tan.x, it.tan.y, it.tan.z, __int_as_float(it.tri));
+  v[4] = make_float4(it.bit.x, it.bit.y, it.bit.z, __int_as_float(it.mat));
+  v[5] = make_float4(__uint_as_float(it.geom | (it.has_uv ? 0x80000000u : 0u)), tl.x, tl.y, tl.z);
+}
 
-    // ---- resolve the pending light sample (MIS.cpp:32-54 + PathTracing.cpp:62-81)
-    if (flags & PF_PEND_L) {
-      float4 h = P.hit[2 * s + 1];
-      float4 nc = P.nee_c[s], nt = P.nee_t[s];
-      int ltri = __float_as_int(nt.w), htri = __float_as_int(h.w);
-      bool vis = ltri >= 0 ? (htri == ltri) : (htri < 0 || sc.mats[sc.tri_attr[htri].mat].is_light);
-      if (vis) {
-        V3 o = xyz(P.ray_o[2 * s + 1]), d = xyz(P.ray_d[2 * s + 1]);
-        V3 x2, ng2;
-        if (htri >= 0) { x2 = hit_point(sc, htri, h.y, h.z); ng2 = normalize(tri_ng_raw(sc.tri_pos + 9 * int64_t(htri))); }
-        float pdfL = light_density(sc, o, d, htri, x2, ng2);
-        if (pdfL != 0.0f) {
-          float pB = nc.w;
-          float w = (pdfL * pdfL) / ((0.0f + pdfL * pdfL) + pB * pB);
-          V3 Li = htri >= 0 ? cwise(beers(xyz(nt), norm(x2 - o)), emission(sc, sc.tri_attr[htri].mat, ng2, -d))
-                            : cwise(beers(xyz(nt), 1e6f), env_eval(sc, d));
-          L = L + cwise(Li, (xyz(nc) / pdfL) * w);
-        }
+__device__ __forceinline__ void load_vertex(const PathsDev& P, int s, Inter& it, V3& tl) {
+  const float4* v = P.vtx + 6 * int64_t(s);
+  float4 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4], f = v[5];
+  it.x = xyz(a); it.h = a.w;
+  it.ng = xyz(b); it.u = b.w;
+  it.ns = xyz(c); it.v = c.w;
+  it.tan = xyz(d); it.tri = __float_as_int(d.w);
+  it.bit = xyz(e); it.mat = __float_as_int(e.w);
+  uint32_t g = __float_as_uint(f.x);
+  it.geom = g & 0x7FFFFFFFu; it.has_uv = (g & 0x80000000u) != 0;
+  tl = V3(f.y, f.z, f.w);
+}
+
+__device__ __forceinline__ ResolveRes resolve_path(const SceneDev& sc, const PathsDev& P, int s, uint64_t key) {
+  ResolveRes res;
+  res.sample = false;
+  res.shaded = 0;
+  float4 rad = P.rad[s];
+  uint32_t flags = __float_as_uint(rad.w);
+  V3 L = xyz(rad);
+  bool done = false;
+
+  // ---- resolve the pending light sample (MIS.cpp:32-54 + PathTracing.cpp:62-81)
+  if (flags & PF_PEND_L) {
+    float4 h = P.hit[2 * s + 1];
+    float4 nc = P.nee_c[s], nt = P.nee_t[s];
+    int ltri = __float_as_int(nt.w), htri = __float_as_int(h.w);
+    bool vis = ltri >= 0 ? (htri == ltri) : (htri < 0 || sc.mats[sc.tri_attr[htri].mat].is_light);
+    if (vis) {
+      V3 o = xyz(P.ray_o[2 * s + 1]), d = xyz(P.ray_d[2 * s + 1]);
+      V3 x2, ng2;
+      if (htri >= 0) { x2 = hit_point(sc, htri, h.y, h.z); ng2 = normalize(tri_ng_raw(sc.tri_pos + 9 * int64_t(htri))); }
+      float pdfL = light_density(sc, o, d, htri, x2, ng2);
+      if (pdfL != 0.0f) {
+        float pB = nc.w;
+        float w = (pdfL * pdfL) / ((0.0f + pdfL * pdfL) + pB * pB);
+        V3 Li = htri >= 0 ? cwise(beers(xyz(nt), norm(x2 - o)), emission(sc, sc.tri_attr[htri].mat, ng2, -d))
+                          : cwise(beers(xyz(nt), 1e6f), env_eval(sc, d));
+        L = L + cwise(Li, (xyz(nc) / pdfL) * w);
       }
     }
-
-    // ---- resolve the pending BSDF sample and shade the vertex it reached
-    if (!(flags & PF_PEND_B)) {
-      done = true;
-    } else {
-      float4 h = P.hit[2 * s];
-      int htri = __float_as_int(h.w);
-      V3 o = xyz(P.ray_o[2 * s]), d = xyz(P.ray_d[2 * s]);
-      float4 thr4 = P.thr[s];
-      V3 thr = xyz(thr4);
-      int depth = 0;
-      Inter it;
-      bool have_it = false;
-      if (!(flags & PF_CAMERA)) {
-        float4 pb = P.pend_b[s];
-        if (htri == __float_as_int(pb.w)) {          // isSelfIntersection, PathTracing.h:41-45
-          done = true;
-        } else {
-          float wB = 1.0f;
-          if (sc.two_strategies) {
-            V3 x2, ng2;
-            if (htri >= 0) { it = inter_from_hit(sc, htri, h.y, h.z); have_it = true; x2 = it.x; ng2 = it.ng; }
-            float pdfL = light_density(sc, o, d, htri, x2, ng2);
-            float pB = thr4.w;
-            wB = (pB * pB) / ((0.0f + pdfL * pdfL) + pB * pB);
-          }
-          thr = cwise(thr, xyz(pb) * wB);
-          depth = int(flags & PF_DEPTH_MASK) + 1;
-        }
-      }
-      if (!done && depth >= sc.max_depth) done = true;
-      if (!done) {
-        Media M; M.n = int((flags & PF_NMED_MASK) >> PF_NMED_SHIFT);
-        for (int k = 0; k < M.n; ++k) { float4 m4 = P.med[4 * s + k]; M.T[k] = xyz(m4); M.ior[k] = m4.w; M.geom[k] = P.med_geom[4 * s + k]; }
-        V3 Tp = M.transmittance();
-        if (htri < 0) {                              // miss: PathTracing.cpp:86-94
-          V3 Le = cwise(beers(Tp, 1e6f), env_eval(sc, d));
-          L = L + cwise(thr, Le);
-          if (depth == 0) { P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f); P.out_albedo[s] = f4(Le, 0.f); }
-          done = true;
-        } else {
-          if (!have_it) it = inter_from_hit(sc, htri, h.y, h.z);
-          const MaterialDev m = sc.mats[it.mat];
-          if (depth == 0) { P.out_normal[s] = f4(it.ns, 0.f); P.out_albedo[s] = f4(mat_albedo(sc, m, it), 0.f); }
-          V3 tl = beers(Tp, norm(it.x - o));
-          if (m.is_light) {                          // PathTracing.cpp:38-41
-            L = L + cwise(thr, cwise(tl, emission(sc, it.mat, it.ng, -d)));
-            done = true;
-          } else {
-            shaded = 1;
-            Rng r; r.inc = Rng::inc_of(key); r.state = P.rng[s];
-            float qrr = depth >= sc.rr_start ? sc.rr_q : 0.0f;      // PathTracing.cpp:49-56
-            if (r.u01() < qrr) {
-              done = true;
-            } else {
-              tl = tl / (1.0f - qrr);
-              V3 wo = -d;
-              const ShadeCtx cx = shade_ctx(sc, m, it, wo);
-              int wl = int((flags & PF_WL_MASK) >> PF_WL_SHIFT) - 1;
-              float eta_out = M.outside_ior(it, wo);
-              bool next_ok = depth + 1 < sc.max_depth;
-              // light strategy (Scene.cpp:538-586)
-              if (sc.two_strategies) {
-                float xi = r.u01();
-                V3 oL, dL; int ltri = -1;
-                if (xi < sc.p_surface) {
-                  uint32_t kk = sample_cdf(sc.light_cdf, uint32_t(sc.n_light_tris), r, sc.light_guide, sc.light_guide_log2);
-                  ltri = sc.light_tris[kk];
-                  V3 bb = triangle_uniform(r);
-                  const float* lp = sc.tri_pos + 9 * int64_t(ltri);
-                  V3 xl = bb.x * ld3(lp) + bb.y * ld3(lp + 3) + bb.z * ld3(lp + 6);
-                  oL = ray_x(it, dot(it.ng, xl - it.x) >= 0.0f);
-                  dL = normalize(xl - oL);
-                } else {
-                  float dens;
-                  dL = env_sample(sc, r, dens, capped);
-                  oL = ray_x(it, dot(it.ng, dL) >= 0.0f);
-                }
-                if (next_ok) {
-                  BsdfEval ev = bsdf_eval(cx, m, it, wo, dL);
-                  V3 c3 = cwise(tl, ev.fD + ev.fC) * fabsf(dot(dL, it.ng));
-                  if (!is_zero(c3)) {
-                    float pBL = bsdf_pdf(cx, m, wo, dL, eta_out);
-                    Media ML = M;
-                    overflow |= ML.update(sc, m, it, wo, dL, wl);
-                    P.nee_c[s] = f4(cwise(thr, c3), pBL);
-                    P.nee_t[s] = f4(ML.transmittance(), __int_as_float(ltri));
-                    P.ray_o[2 * s + 1] = f4(oL, 0.f);
-                    P.ray_d[2 * s + 1] = f4(dL, 0.f);
-                    emitL = true;
-                  }
-                }
-              }
-              // BSDF strategy (MIS.cpp:6-26, Scene.cpp:328-338)
-              float prob = 1.0f;
-              if (wl == -1 && m.vary_ior) {              // LightRayInfo.cpp:52-79
-                float p3 = 1.0f / 3.0f;
-                float xi = r.u01();
-                if (xi < p3) wl = 0; else if (xi < p3 + p3) wl = 1; else wl = 2;
-                prob = p3;
-              }
-              BsdfSample bs = bsdf_sample(cx, m, it, wo, wl, eta_out, r, capped);
-              if (bs.pdf != 0.0f) {
-                V3 t2 = cwise(tl, bs.thrD / prob + bs.thrC / prob);
-                if (!is_zero(t2) && next_ok) {
-                  overflow |= M.update(sc, m, it, wo, bs.dir, wl);
-                  P.thr[s] = f4(thr, bs.pdf);
-                  P.pend_b[s] = f4(t2, __int_as_float(it.tri));
-                  P.ray_o[2 * s] = f4(ray_x(it, bs.outside), 0.f);
-                  P.ray_d[2 * s] = f4(bs.dir, 0.f);
-                  for (int k = 0; k < M.n; ++k) { P.med[4 * s + k] = f4(M.T[k], M.ior[k]); P.med_geom[4 * s + k] = M.geom[k]; }
-                  emitB = true;
-                }
-              }
-              P.rng[s] = r.state;
-              uint32_t nf = uint32_t(depth) | (uint32_t(wl + 1) << PF_WL_SHIFT) | (uint32_t(M.n) << PF_NMED_SHIFT) |
-                            (emitB ? PF_PEND_B : 0u) | (emitL ? PF_PEND_L : 0u);
-              flags = nf;
-              done = !(emitB || emitL);
-            }
-          }
-        }
-      }
-    }
-    keep = !done;
-    if (keep) P.rad[s] = f4(L, __uint_as_float(flags));
-    res.L = L;
   }
 
+  // ---- resolve the pending BSDF sample and shade the vertex it reached
+  if (!(flags & PF_PEND_B)) {
+    done = true;
+  } else {
+    float4 h = P.hit[2 * s];
+    int htri = __float_as_int(h.w);
+    V3 o = xyz(P.ray_o[2 * s]), d = xyz(P.ray_d[2 * s]);
+    float4 thr4 = P.thr[s];
+    V3 thr = xyz(thr4);
+    int depth = 0;
+    Inter it;
+    bool have_it = false;
+    if (!(flags & PF_CAMERA)) {
+      float4 pb = P.pend_b[s];
+      if (htri == __float_as_int(pb.w)) {          // isSelfIntersection, PathTracing.h:41-45
+        done = true;
+      } else {
+        float wB = 1.0f;
+        if (sc.two_strategies) {
+          V3 x2, ng2;
+          if (htri >= 0) { it = inter_from_hit(sc, htri, h.y, h.z); have_it = true; x2 = it.x; ng2 = it.ng; }
+          float pdfL = light_density(sc, o, d, htri, x2, ng2);
+          float pB = thr4.w;
+          wB = (pB * pB) / ((0.0f + pdfL * pdfL) + pB * pB);
+        }
+        thr = cwise(thr, xyz(pb) * wB);
+        depth = int(flags & PF_DEPTH_MASK) + 1;
+      }
+    }
+    if (!done && depth >= sc.max_depth) done = true;
+    if (!done) {
+      Media M; M.n = int((flags & PF_NMED_MASK) >> PF_NMED_SHIFT);
+      for (int k = 0; k < M.n; ++k) { float4 m4 = P.med[4 * s + k]; M.T[k] = xyz(m4); M.ior[k] = m4.w; M.geom[k] = P.med_geom[4 * s + k]; }
+      V3 Tp = M.transmittance();
+      if (htri < 0) {                              // miss: PathTracing.cpp:86-94
+        V3 Le = cwise(beers(Tp, 1e6f), env_eval(sc, d));
+        L = L + cwise(thr, Le);
+        if (depth == 0) { P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f); P.out_albedo[s] = f4(Le, 0.f); }
+        done = true;
+      } else {
+        if (!have_it) it = inter_from_hit(sc, htri, h.y, h.z);
+        const MaterialDev m = sc.mats[it.mat];
+        if (depth == 0) { P.out_normal[s] = f4(it.ns, 0.f); P.out_albedo[s] = f4(mat_albedo(sc, m, it), 0.f); }
+        V3 tl = beers(Tp, norm(it.x - o));
+        if (m.is_light) {                          // PathTracing.cpp:38-41
+          L = L + cwise(thr, cwise(tl, emission(sc, it.mat, it.ng, -d)));
+          done = true;
+        } else {
+          res.shaded = 1;
+          Rng r; r.inc = Rng::inc_of(key); r.state = P.rng[s];
+          float qrr = depth >= sc.rr_start ? sc.rr_q : 0.0f;      // PathTracing.cpp:49-56
+          if (r.u01() < qrr) {
+            done = true;
+          } else {
+            tl = tl / (1.0f - qrr);
+            P.rng[s] = r.state;
+            P.thr[s] = f4(thr, thr4.w);
+            store_vertex(P, s, it, tl);
+            flags = (flags & (PF_WL_MASK | PF_NMED_MASK)) | uint32_t(depth);
+            res.sample = true;
+          }
+        }
+      }
+    }
+  }
+  if (res.sample) P.rad[s] = f4(L, __uint_as_float(flags));
+  res.L = L;
   return res;
 }
 
-// Minimum resident blocks per SM asked of the compiler for the shading
-// kernels (0: no bound beyond the block size). Shading is latency-bound
-// (dependent loads of hit, triangle, material, texture): 16 blocks of 128
-// threads, the SM's full 2048 threads, measured fastest on GB300 although
-// the 32-register budget spills to local memory (L1).
+__device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const PathsDev& P, int s, uint64_t key) {
+  SampleRes res;
+  res.keep = res.emitB = res.emitL = false;
+  res.overflow = res.capped = 0;
+  int& overflow = res.overflow;
+  int& capped = res.capped;
+  bool& emitB = res.emitB;
+  bool& emitL = res.emitL;
+  float4 rad = P.rad[s];
+  uint32_t flags = __float_as_uint(rad.w);
+  V3 L = xyz(rad);
+  const int depth = int(flags & PF_DEPTH_MASK);
+  Inter it;
+  V3 tl;
+  load_vertex(P, s, it, tl);
+  const MaterialDev m = sc.mats[it.mat];
+  const V3 thr = xyz(P.thr[s]);
+  const V3 d = xyz(P.ray_d[2 * s]);
+  Media M; M.n = int((flags & PF_NMED_MASK) >> PF_NMED_SHIFT);
+  for (int k = 0; k < M.n; ++k) { float4 m4 = P.med[4 * s + k]; M.T[k] = xyz(m4); M.ior[k] = m4.w; M.geom[k] = P.med_geom[4 * s + k]; }
+  Rng r; r.inc = Rng::inc_of(key); r.state = P.rng[s];
+  V3 wo = -d;
+  const ShadeCtx cx = shade_ctx(sc, m, it, wo);
+  int wl = int((flags & PF_WL_MASK) >> PF_WL_SHIFT) - 1;
+  float eta_out = M.outside_ior(it, wo);
+  bool next_ok = depth + 1 < sc.max_depth;
+  // light strategy (Scene.cpp:538-586)
+  if (sc.two_strategies) {
+    float xi = r.u01();
+    V3 oL, dL; int ltri = -1;
+    if (xi < sc.p_surface) {
+      uint32_t kk = sample_cdf(sc.light_cdf, uint32_t(sc.n_light_tris), r, sc.light_guide, sc.light_guide_log2);
+      ltri = sc.light_tris[kk];
+      V3 bb = triangle_uniform(r);
+      const float* lp = sc.tri_pos + 9 * int64_t(ltri);
+      V3 xl = bb.x * ld3(lp) + bb.y * ld3(lp + 3) + bb.z * ld3(lp + 6);
+      oL = ray_x(it, dot(it.ng, xl - it.x) >= 0.0f);
+      dL = normalize(xl - oL);
+    } else {
+      float dens;
+      dL = env_sample(sc, r, dens, capped);
+      oL = ray_x(it, dot(it.ng, dL) >= 0.0f);
+    }
+    if (next_ok) {
+      BsdfEval ev = bsdf_eval(cx, m, it, wo, dL);
+      V3 c3 = cwise(tl, ev.fD + ev.fC) * fabsf(dot(dL, it.ng));
+      if (!is_zero(c3)) {
+        float pBL = bsdf_pdf(cx, m, wo, dL, eta_out);
+        Media ML = M;
+        overflow |= ML.update(sc, m, it, wo, dL, wl);
+        P.nee_c[s] = f4(cwise(thr, c3), pBL);
+        P.nee_t[s] = f4(ML.transmittance(), __int_as_float(ltri));
+        P.ray_o[2 * s + 1] = f4(oL, 0.f);
+        P.ray_d[2 * s + 1] = f4(dL, 0.f);
+        emitL = true;
+      }
+    }
+  }
+  // BSDF strategy (MIS.cpp:6-26, Scene.cpp:328-338)
+  float prob = 1.0f;
+  if (wl == -1 && m.vary_ior) {              // LightRayInfo.cpp:52-79
+    float p3 = 1.0f / 3.0f;
+    float xi = r.u01();
+    if (xi < p3) wl = 0; else if (xi < p3 + p3) wl = 1; else wl = 2;
+    prob = p3;
+  }
+  BsdfSample bs = bsdf_sample(cx, m, it, wo, wl, eta_out, r, capped);
+  if (bs.pdf != 0.0f) {
+    V3 t2 = cwise(tl, bs.thrD / prob + bs.thrC / prob);
+    if (!is_zero(t2) && next_ok) {
+      overflow |= M.update(sc, m, it, wo, bs.dir, wl);
+      P.thr[s] = f4(thr, bs.pdf);
+      P.pend_b[s] = f4(t2, __int_as_float(it.tri));
+      P.ray_o[2 * s] = f4(ray_x(it, bs.outside), 0.f);
+      P.ray_d[2 * s] = f4(bs.dir, 0.f);
+      for (int k = 0; k < M.n; ++k) { P.med[4 * s + k] = f4(M.T[k], M.ior[k]); P.med_geom[4 * s + k] = M.geom[k]; }
+      emitB = true;
+    }
+  }
+  P.rng[s] = r.state;
+  uint32_t nf = uint32_t(depth) | (uint32_t(wl + 1) << PF_WL_SHIFT) | (uint32_t(M.n) << PF_NMED_SHIFT) |
+                (emitB ? PF_PEND_B : 0u) | (emitL ? PF_PEND_L : 0u);
+  res.keep = emitB || emitL;
+  if (res.keep) P.rad[s] = f4(L, __uint_as_float(nf));
+  res.L = L;
+  return res;
+}
+
+// Minimum resident blocks per SM asked of the compiler for the resolve and
+// sample kernels (0: no bound beyond the block size). Both are latency-bound
+// (dependent loads of hit, triangle, material, texture), so occupancy pays
+// more than the registers it costs: 8 blocks of 128 threads (64 registers)
+// measured fastest for both on GB300, ahead of 4, 6 and 12.
 #ifndef HASTY_SHADE_MIN_BLOCKS
-#define HASTY_SHADE_MIN_BLOCKS 16
+#define HASTY_SHADE_MIN_BLOCKS 8
 #endif
-#if HASTY_SHADE_MIN_BLOCKS > 0
-#define SHADE_BOUNDS __launch_bounds__(128, HASTY_SHADE_MIN_BLOCKS)
+#ifndef HASTY_RESOLVE_MIN_BLOCKS
+#define HASTY_RESOLVE_MIN_BLOCKS HASTY_SHADE_MIN_BLOCKS
+#endif
+#ifndef HASTY_SAMPLE_MIN_BLOCKS
+#define HASTY_SAMPLE_MIN_BLOCKS HASTY_SHADE_MIN_BLOCKS
+#endif
+#if HASTY_RESOLVE_MIN_BLOCKS > 0
+#define RESOLVE_BOUNDS __launch_bounds__(128, HASTY_RESOLVE_MIN_BLOCKS)
 #else
-#define SHADE_BOUNDS __launch_bounds__(128)
+#define RESOLVE_BOUNDS __launch_bounds__(128)
+#endif
+#if HASTY_SAMPLE_MIN_BLOCKS > 0
+#define SAMPLE_BOUNDS __launch_bounds__(128, HASTY_SAMPLE_MIN_BLOCKS)
+#else
+#define SAMPLE_BOUNDS __launch_bounds__(128)
 #endif
 
-__global__ void SHADE_BOUNDS k_shade(SceneDev sc, PathsDev P, BatchDesc b, int q) {
+__device__ __forceinline__ uint64_t slot_key(const BatchDesc& b, int s, int npix) {
+  return path_key(b.seed, uint32_t(s % npix), b.pass_base + uint32_t(s / npix));
+}
+
+// Paths of queue q: resolve; finished ones leave their radiance in
+// out_color, survivors are appended to the sample queue.
+__global__ void RESOLVE_BOUNDS k_resolve(SceneDev sc, PathsDev P, BatchDesc b, int q) {
   const uint32_t n_in = P.counts[q];
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((i & ~31u) >= n_in) return;                 // whole warp past the queue
+  const bool valid = i < n_in;
+  const int npix = sc.width * sc.height;
+  int s = valid ? P.pq[q][i] : 0;
+  ResolveRes res;
+  res.sample = false;
+  res.shaded = 0;
+  if (valid) {
+    res = resolve_path(sc, P, s, slot_key(b, s, npix));
+    if (!res.sample) P.out_color[s] = f4(res.L, 0.f);
+  }
+  unsigned kb = __ballot_sync(kFull, res.sample);
+  uint32_t lane = threadIdx.x & 31u;
+  uint32_t base = 0;
+  if (lane == 0 && kb) base = atomicAdd(&P.counts[kSampleCount], uint32_t(__popc(kb)));
+  base = __shfl_sync(kFull, base, 0);
+  if (res.sample) P.sq[base + __popc(kb & ((1u << lane) - 1u))] = s;
+  unsigned sb = __ballot_sync(kFull, res.shaded != 0);
+  if (lane == 0 && sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
+}
+
+// Paths of the sample queue: sample the vertex; paths with rays go to queue
+// q^1 and their rays to ray queue q^1, the rest leave their radiance.
+__global__ void SAMPLE_BOUNDS k_sample(SceneDev sc, PathsDev P, BatchDesc b, int q) {
+  const uint32_t n_in = P.counts[kSampleCount];
   uint32_t* pq_cnt = &P.counts[q ^ 1];
   uint32_t* rq_cnt = &P.counts[2 + (q ^ 1)];
   int32_t* pq_out = P.pq[q ^ 1];
   int32_t* rq_out = P.rq[q ^ 1];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if ((i & ~31u) >= n_in) return;                 // whole warp past the queue
+  if ((i & ~31u) >= n_in) return;
   const bool valid = i < n_in;
   const int npix = sc.width * sc.height;
-
-  int s = valid ? P.pq[q][i] : 0;
-  ShadeRes res;
+  int s = valid ? P.sq[i] : 0;
+  SampleRes res;
   res.keep = res.emitB = res.emitL = false;
-  res.shaded = res.overflow = res.capped = 0;
+  res.overflow = res.capped = 0;
   if (valid) {
-    res = shade_path(sc, P, s, path_key(b.seed, uint32_t(s % npix), b.pass_base + uint32_t(s / npix)));
+    res = sample_path(sc, P, s, slot_key(b, s, npix));
     if (!res.keep) P.out_color[s] = f4(res.L, 0.f);
   }
-  const bool keep = res.keep, emitB = res.emitB, emitL = res.emitL;
-  const int shaded = res.shaded, overflow = res.overflow, capped = res.capped;
-
   // warp-ballot compaction of the surviving paths and their rays
-  uint32_t nrays = (emitB ? 1u : 0u) + (emitL ? 1u : 0u);
+  uint32_t nrays = (res.emitB ? 1u : 0u) + (res.emitL ? 1u : 0u);
   uint32_t roff = warp_reserve(rq_cnt, nrays);
-  if (emitB) rq_out[roff++] = 2 * s;
-  if (emitL) rq_out[roff] = 2 * s + 1;
-  unsigned kb = __ballot_sync(kFull, keep);
+  if (res.emitB) rq_out[roff++] = 2 * s;
+  if (res.emitL) rq_out[roff] = 2 * s + 1;
+  unsigned kb = __ballot_sync(kFull, res.keep);
   uint32_t lane = threadIdx.x & 31u;
   uint32_t pbase = 0;
   if (lane == 0 && kb) pbase = atomicAdd(pq_cnt, uint32_t(__popc(kb)));
   pbase = __shfl_sync(kFull, pbase, 0);
-  if (keep) pq_out[pbase + __popc(kb & ((1u << lane) - 1u))] = s;
-  unsigned sb = __ballot_sync(kFull, shaded != 0);
-  unsigned ob = __ballot_sync(kFull, overflow != 0);
-  unsigned cb = __ballot_sync(kFull, capped != 0);
+  if (res.keep) pq_out[pbase + __popc(kb & ((1u << lane) - 1u))] = s;
+  unsigned ob = __ballot_sync(kFull, res.overflow != 0);
+  unsigned cb = __ballot_sync(kFull, res.capped != 0);
   if (lane == 0) {
-    if (sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
     if (ob) atomicAdd(&P.stats[ST_MEDIA_OVERFLOW], (unsigned long long)__popc(ob));
     if (cb) atomicAdd(&P.stats[ST_TRIAL_CAP], (unsigned long long)__popc(cb));
   }
@@ -369,7 +457,10 @@ void launch_raygen(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, cu
 
 void launch_shade(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, int q, int max_paths, cudaStream_t st) {
   int blocks = (max_paths + 127) / 128;
-  k_shade<<<blocks > 0 ? blocks : 1, 128, 0, st>>>(sc, p, b, q);
+  if (blocks < 1) blocks = 1;
+  cudaMemsetAsync(&p.counts[kSampleCount], 0, sizeof(uint32_t), st);
+  k_resolve<<<blocks, 128, 0, st>>>(sc, p, b, q);
+  k_sample<<<blocks, 128, 0, st>>>(sc, p, b, q);
 }
 
 void launch_accumulate(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, double* ac, double* an, double* aa, cudaStream_t st) {
@@ -438,9 +529,10 @@ void launch_debug_bsdf(int which, const float* in, int n, const uint32_t* replay
 // Multi-job engine kernels (see MultiDev in wavefront.h). One iteration:
 // k_multi_plan (1 thread) decides how many new camera samples to issue into
 // free slots, k_multi_regen starts them, the closest-hit kernel traces every
-// queued ray, k_shade_multi advances every queued path by one bounce (the
-// same shade_path as the single-job kernel) and records per slot whether the
-// path lives on and which rays it queued, three compaction kernels rebuild
+// queued ray, k_resolve_multi and k_sample_multi advance every queued path by
+// one bounce (the same resolve_path / sample_path as the single-job kernels)
+// and record per slot whether the path lives on and which rays it queued
+// (finished samples go to their job's sums), three compaction kernels rebuild
 // the path queue, the ray queue and the free-slot list from those flags in
 // ascending slot order, and k_multi_cond flips the queue parity and sets the
 // enclosing CUDA-graph while-loop's condition. Keeping every list in slot
@@ -489,6 +581,7 @@ __global__ void k_multi_plan(PathsDev P, MultiDev m) {
     uint32_t fc = *m.free_count;
     n_new = left < fc ? uint32_t(left) : fc;
   }
+  P.counts[kSampleCount] = 0;
   m.ctl[1] = n_new;
   m.ctl[3] = P.counts[q];
   m.ctl[4] = P.counts[2 + q];
@@ -548,7 +641,22 @@ __device__ __forceinline__ void add_fixed(unsigned long long* acc, V3 L, float4 
   if (sat) atomicAdd(&stats[MS_SATURATED], 1ull);
 }
 
-__global__ void SHADE_BOUNDS k_shade_multi(PathsDev P, MultiDev m) {
+// A finished sample of job j: fixed-point sums of its pixel (NaN radiance is
+// dropped and counted), then the per-job finished counters, one atomic per
+// distinct job in the warp.
+__device__ __forceinline__ void finish_multi(const PathsDev& P, const MultiDev& m, bool finished, int j, int s, V3 L) {
+  if (finished) {
+    const JobDev& job = m.jobs[j];
+    if (has_nan(L)) atomicAdd(&P.stats[ST_NAN], 1ull);
+    else add_fixed(job.acc + 9 * int64_t(m.slot_px[s]), L, P.out_normal[s], P.out_albedo[s], P.stats);
+    m.flags[s] = 0;
+  }
+  const uint32_t lane = threadIdx.x & 31u;
+  unsigned same = __match_any_sync(kFull, finished ? j : -1);
+  if (finished && (__ffs(same) - 1) == int(lane)) atomicAdd(m.jobs[j].done, (unsigned long long)__popc(same));
+}
+
+__global__ void RESOLVE_BOUNDS k_resolve_multi(PathsDev P, MultiDev m) {
   const uint32_t q = m.ctl[0];
   const uint32_t n_in = P.counts[q];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -556,29 +664,40 @@ __global__ void SHADE_BOUNDS k_shade_multi(PathsDev P, MultiDev m) {
   const bool valid = i < n_in;
   int s = valid ? P.pq[q][i] : 0;
   int j = valid ? m.slot_job[s] : 0;
-  ShadeRes res;
-  res.keep = res.emitB = res.emitL = false;
-  res.shaded = res.overflow = res.capped = 0;
-  bool finished = false;
-  if (valid) {
-    const JobDev& job = m.jobs[j];
-    const uint32_t px = m.slot_px[s];
-    res = shade_path(job.sc, P, s, path_key(job.seed, px, m.slot_pass[s]));
-    if (!res.keep) {
-      finished = true;
-      if (has_nan(res.L)) atomicAdd(&P.stats[ST_NAN], 1ull);
-      else add_fixed(job.acc + 9 * int64_t(px), res.L, P.out_normal[s], P.out_albedo[s], P.stats);
-    }
-    m.flags[s] = uint8_t((res.keep ? SF_ALIVE : 0) | (res.emitB ? SF_RAY_B : 0) | (res.emitL ? SF_RAY_L : 0));
-  }
+  ResolveRes res;
+  res.sample = false;
+  res.shaded = 0;
+  if (valid) res = resolve_path(m.jobs[j].sc, P, s, path_key(m.jobs[j].seed, m.slot_px[s], m.slot_pass[s]));
+  finish_multi(P, m, valid && !res.sample, j, s, res.L);
   const uint32_t lane = threadIdx.x & 31u;
-  unsigned same = __match_any_sync(kFull, finished ? j : -1);
-  if (finished && (__ffs(same) - 1) == int(lane)) atomicAdd(m.jobs[j].done, (unsigned long long)__popc(same));
+  unsigned kb = __ballot_sync(kFull, res.sample);
+  uint32_t base = 0;
+  if (lane == 0 && kb) base = atomicAdd(&P.counts[kSampleCount], uint32_t(__popc(kb)));
+  base = __shfl_sync(kFull, base, 0);
+  if (res.sample) P.sq[base + __popc(kb & ((1u << lane) - 1u))] = s;
   unsigned sb = __ballot_sync(kFull, res.shaded != 0);
+  if (lane == 0 && sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
+}
+
+__global__ void SAMPLE_BOUNDS k_sample_multi(PathsDev P, MultiDev m) {
+  const uint32_t n_in = P.counts[kSampleCount];
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if ((i & ~31u) >= n_in) return;
+  const bool valid = i < n_in;
+  int s = valid ? P.sq[i] : 0;
+  int j = valid ? m.slot_job[s] : 0;
+  SampleRes res;
+  res.keep = res.emitB = res.emitL = false;
+  res.overflow = res.capped = 0;
+  if (valid) {
+    res = sample_path(m.jobs[j].sc, P, s, path_key(m.jobs[j].seed, m.slot_px[s], m.slot_pass[s]));
+    if (res.keep) m.flags[s] = uint8_t(SF_ALIVE | (res.emitB ? SF_RAY_B : 0) | (res.emitL ? SF_RAY_L : 0));
+  }
+  finish_multi(P, m, valid && !res.keep, j, s, res.L);
+  const uint32_t lane = threadIdx.x & 31u;
   unsigned ob = __ballot_sync(kFull, res.overflow != 0);
   unsigned cb = __ballot_sync(kFull, res.capped != 0);
   if (lane == 0) {
-    if (sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
     if (ob) atomicAdd(&P.stats[ST_MEDIA_OVERFLOW], (unsigned long long)__popc(ob));
     if (cb) atomicAdd(&P.stats[ST_TRIAL_CAP], (unsigned long long)__popc(cb));
   }
@@ -752,7 +871,8 @@ void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int cap, int b
   k_multi_plan<<<1, 1, 0, st>>>(p, m);
   k_multi_regen<<<(cap + 255) / 256, 256, 0, st>>>(p, m);
   launch_trace_multi(p, m, bvh_kind, 2 * cap, st);
-  k_shade_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m);
+  k_resolve_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m);
+  k_sample_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m);
   k_compact_count<<<nb, kCompactThreads, 0, st>>>(m, cap);
   k_compact_scan<<<1, 1024, 0, st>>>(p, m, nb);
   k_compact_scatter<<<nb, kCompactThreads, 0, st>>>(p, m, cap);

@@ -11,7 +11,7 @@
 // array, g_scratch below. The call makes no cudaMalloc, cudaFree or other
 // allocating call.
 //
-// Limits. g_scratch is kStaticBytes (7 MiB), which holds the state of
+// Limits. g_scratch is kStaticBytes (8 MiB), which holds the state of
 // kStaticMaxPixels (16384) camera paths, e.g. a 128 x 128 frame; a larger
 // frame is rejected with HASTY_ERR_ARG. Each device that runs this code
 // reserves the array for the life of the process.
@@ -37,8 +37,8 @@
 namespace hasty {
 namespace {
 
-constexpr size_t kStaticBytes = size_t(7) << 20;
-constexpr int kStaticMaxPixels = 16384;   // 336 B of path state + 48 B of sums per pixel
+constexpr size_t kStaticBytes = size_t(8) << 20;
+constexpr int kStaticMaxPixels = 16384;   // 436 B of path state + 48 B of sums per pixel
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_scratch[kStaticBytes];

@@ -39,7 +39,9 @@ struct PathsDev {
   float4* hit;          // 2 per path: t, u, v, triangle (-1 miss)
   int32_t* pq[2];       // path queues
   int32_t* rq[2];       // ray queues (ray ids 2s, 2s+1)
-  uint32_t* counts;     // [pq0, pq1, rq0, rq1, trace fetch counter, 3 spare]
+  uint32_t* counts;     // [pq0, pq1, rq0, rq1, trace fetch counter, sample-queue length, 2 spare]
+  float4* vtx;          // 6 per path: vertex record from the resolve to the sample kernel
+  int32_t* sq;          // sample queue (paths that continue past resolve)
   float4* out_color;    // per slot: final radiance of the sample
   float4* out_normal;
   float4* out_albedo;
@@ -50,6 +52,7 @@ struct PathsDev {
 enum StatIndex { ST_RAYS = 0, ST_SHADED, ST_PATHS, ST_NAN, ST_MEDIA_OVERFLOW, ST_TRIAL_CAP, ST_COUNT };
 constexpr int kCountSlots = 8;
 constexpr int kFetchCounter = 4;   // counts[4]: rays handed out by the persistent trace kernels
+constexpr int kSampleCount = 5;    // counts[5]: length of the sample queue
 
 struct BatchDesc {
   uint64_t seed;

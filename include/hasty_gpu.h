@@ -101,6 +101,9 @@ int hasty_job_reset(hasty_job* job);                        /* clears accumulato
 /* Maximum camera samples in flight per batch (paths); 0 = automatic. */
 int hasty_job_set_paths_in_flight(hasty_job* job, int64_t paths);
 
+/* Frees the job's path state (re-allocated by the next render); synchronous. */
+int hasty_job_release_paths(hasty_job* job);
+
 int hasty_job_render_passes(hasty_job* job, int n_passes);  /* asynchronous */
 int hasty_job_sync(hasty_job* job);
 int hasty_job_stop(hasty_job* job);
@@ -222,7 +225,7 @@ int hasty_server_stop(hasty_server* srv);
  * overwrites. Asynchronous on the job's stream (hasty_job_sync waits). Leaves
  * the job's accumulators, pass counter and statistics untouched.
  * For callers that may not allocate device memory while rendering: the call
- * makes no cudaMalloc/cudaFree and uses one fixed 7 MiB static device array
+ * makes no cudaMalloc/cudaFree and uses one fixed 8 MiB static device array
  * as scratch, so frames above 16384 pixels (e.g. 128 x 128) are rejected
  * with HASTY_ERR_ARG. The first call on each device looks up that array's
  * address; make it before any stream capture begins. All calls share the
