@@ -39,7 +39,8 @@ B_SHADE = 2 * 96 + 92
 # over the 12 bounces of one 4,147,200-path batch, wide BVH) from one ncu
 # capture of `bench.py --steps 1 --warmup 3 --spp-per-step 2`; the default run
 # renders the same batches (profiles/dram_per_launch_sphere_field_1920x1080.md).
-MEASURED_TRAFFIC = {"wide": {"k_trace": 114.2e6, "k_shade": 273.5e6}}
+# The shading stage is one k_resolve and one k_sample launch per bounce.
+MEASURED_TRAFFIC = {"wide": {"k_trace": 115.7e6, "k_resolve+k_sample": 243.1e6 + 257.5e6}}
 
 
 def peaks():
@@ -280,7 +281,8 @@ def main():
             b_ray = 32 + 16 + 64 * bvh_costs["nodes_per_ray"] + 48 * bvh_costs["tris_per_ray"]
             traffic = MEASURED_TRAFFIC.get(args.bvh, {}) if args.spp_per_step % 2 == 0 else {}
             n_launch = max(trace_launches, 1)
-            for name, work, unit_bytes, ms in (("k_trace", rays, b_ray, trace_ms), ("k_shade", shaded, B_SHADE, shade_ms)):
+            for name, work, unit_bytes, ms in (("k_trace", rays, b_ray, trace_ms),
+                                                ("k_resolve+k_sample", shaded, B_SHADE, shade_ms)):
                 per_launch_bytes = work * unit_bytes / n_launch
                 achieved = per_launch_bytes / (ms * 1e-3 / n_launch) / 1e9
                 kernels.append({"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
