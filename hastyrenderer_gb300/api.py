@@ -23,6 +23,7 @@ class Context:
     """One CUDA device."""
 
     BINARY_BVH = 1   # HASTY_CTX_BINARY_BVH
+    HOST_BVH = 2     # HASTY_CTX_HOST_BVH: build the BVH on the host instead of the GPU
 
     def __init__(self, device: int = 0, flags: int = 0):
         self._h = ctypes.c_void_p()

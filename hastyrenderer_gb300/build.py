@@ -28,7 +28,7 @@ NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contr
                "-I" + CSRC, "--expt-relaxed-constexpr"]
 CU_EXTRA = {"integrator.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-sign-compare"]
-CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu"]
+CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu", "bvh_gpu.cu"]
 # Extra nvcc flags for experiments (e.g. HASTY_NVCC_FLAGS="-DHASTY_OUTLINE_MASK=3").
 EXTRA_NVCC = os.environ.get("HASTY_NVCC_FLAGS", "").split()
 CPP_SOURCES = ["api.cpp", "engine.cpp", "server.cpp", "scene_load.cpp", "bvh_build.cpp", "image_out.cpp"]

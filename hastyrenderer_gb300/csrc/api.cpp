@@ -99,11 +99,15 @@ void prepare_scene(hasty_job& j) {
   HostScene& h = j.host;
   std::unique_ptr<hasty_job::Prepared> p(new hasty_job::Prepared());
   bool binary = (j.ctx->flags & HASTY_CTX_BINARY_BVH) != 0;
+  bool on_host = (j.ctx->flags & HASTY_CTX_HOST_BVH) != 0;
+  if (!on_host) ck(cudaSetDevice(j.ctx->device), "cudaSetDevice");
   if (binary) {
-    build_bvh_binary(h.tri_pos.data(), h.n_tris(), 4, p->bvh);
+    if (on_host) build_bvh_binary(h.tri_pos.data(), h.n_tris(), 4, p->bvh);
+    else build_bvh_binary_gpu(h.tri_pos.data(), h.n_tris(), 4, p->bvh);
     if (p->bvh.depth > 60) throw ApiError{HASTY_ERR_LOAD, "BVH deeper than the traversal stack (64)"};
   } else {
-    build_bvh_wide(h.tri_pos.data(), h.n_tris(), p->bvh);
+    if (on_host) build_bvh_wide(h.tri_pos.data(), h.n_tris(), p->bvh);
+    else build_bvh_wide_gpu(h.tri_pos.data(), h.n_tris(), p->bvh);
     if (p->bvh.depth > 30) throw ApiError{HASTY_ERR_LOAD, "wide BVH deeper than the traversal stack (32)"};
   }
   p->binary = binary;

@@ -65,7 +65,7 @@ struct Builder {
           float sc = float(B) / ext;
           for (int32_t i = k.first; i < k.first + k.count; ++i) {
             int32_t t2 = idx[size_t(i)];
-            int b = std::min(B - 1, int((cen[3 * size_t(t2) + a] - cb.lo[a]) * sc));
+            int b = std::max(0, std::min(B - 1, int((cen[3 * size_t(t2) + a] - cb.lo[a]) * sc)));
             bc[b]++; bb[b].grow(tbox[size_t(t2)]);
           }
           float rarea[B]; int rcnt[B];
@@ -88,7 +88,7 @@ struct Builder {
         float sc = float(B) / (cb.hi[axis] - cb.lo[axis]);
         float lo = cb.lo[axis];
         auto it = std::partition(idx.begin() + k.first, idx.begin() + k.first + k.count, [&](int32_t t2) {
-          return std::min(B - 1, int((cen[3 * size_t(t2) + axis] - lo) * sc)) <= split_bin;
+          return std::max(0, std::min(B - 1, int((cen[3 * size_t(t2) + axis] - lo) * sc))) <= split_bin;
         });
         mid = int32_t(it - idx.begin());
       } else {
@@ -152,25 +152,47 @@ void leaf_ordered_tris(const float* tri_pos, const std::vector<int32_t>& order, 
 
 }  // namespace
 
-void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out) {
-  auto t0 = std::chrono::steady_clock::now();
-  Builder b;
-  run_builder(b, tri_pos, n, max_leaf);
+namespace {
 
+Box box_of(const TreeNode& t) {
+  Box b;
+  for (int a = 0; a < 3; ++a) { b.lo[a] = t.lo[a]; b.hi[a] = t.hi[a]; }
+  return b;
+}
+
+// The host builder's tree as a BinaryTree (nodes [0, used)).
+void to_tree(const Builder& b, BinaryTree& t) {
+  size_t used = size_t(b.next_node.load());
+  t.nodes.resize(used);
+  for (size_t i = 0; i < used; ++i) {
+    const BNode& s = b.nodes[i];
+    TreeNode& d = t.nodes[i];
+    for (int a = 0; a < 3; ++a) { d.lo[a] = s.box.lo[a]; d.hi[a] = s.box.hi[a]; }
+    d.child = s.child; d.first = s.first; d.count = s.count; d.pad = 0;
+  }
+  t.idx = b.idx;
+  t.depth = b.max_depth.load() + 1;
+}
+
+}  // namespace
+
+void emit_bvh_binary(const BinaryTree& t, const float* tri_pos, BvhHost& out) {
   // Emit the GPU layout breadth-first (keeps the top levels contiguous).
   // The root must be an inner node: a single leaf becomes child 0 of a root
   // whose child 1 is an empty leaf.
-  const std::vector<BNode>& nd = b.nodes;
-  struct Pending { BNode a, b; };
-  BNode empty;
+  const std::vector<TreeNode>& nd = t.nodes;
+  struct Pending { TreeNode a, b; };
+  TreeNode empty;
+  for (int a = 0; a < 3; ++a) { empty.lo[a] = FLT_MAX; empty.hi[a] = -FLT_MAX; }
+  empty.child = -1; empty.first = 0; empty.count = 0; empty.pad = 0;
   std::deque<Pending> q;
   if (nd[0].child < 0) q.push_back({nd[0], empty});
   else q.push_back({nd[size_t(nd[0].child)], nd[size_t(nd[0].child) + 1]});
   std::vector<size_t> fixups;   // float offsets of inner-child links, in push order
   out.nodes.clear();
-  auto child_fields = [](const BNode& c, float* box6, int32_t& link, int32_t& cnt) {
-    box6[0] = c.box.lo[0]; box6[1] = c.box.hi[0]; box6[2] = c.box.lo[1];
-    box6[3] = c.box.hi[1]; box6[4] = c.box.lo[2]; box6[5] = c.box.hi[2];
+  auto child_fields = [](const TreeNode& c, float* box6, int32_t& link, int32_t& cnt) {
+    box6[0] = c.lo[0]; box6[1] = c.hi[0]; box6[2] = c.lo[1];
+    box6[3] = c.hi[1]; box6[4] = c.lo[2]; box6[5] = c.hi[2];
     if (c.child < 0) { link = ~((c.first << 3) | c.count); cnt = c.count; } else { link = 0; cnt = 0; }
   };
   while (!q.empty()) {
@@ -189,10 +211,26 @@ void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out
   }
   // the k-th node pushed after the root is emitted as gpu node k+1
   for (size_t k = 0; k < fixups.size(); ++k) { int32_t v = int32_t(k + 1); std::memcpy(&out.nodes[fixups[k]], &v, 4); }
-
-  out.order = b.idx;
+  out.order = t.idx;
   leaf_ordered_tris(tri_pos, out.order, out.tris);
-  out.depth = b.max_depth.load() + 1;
+  out.depth = t.depth;
+}
+
+void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out) {
+  auto t0 = std::chrono::steady_clock::now();
+  Builder b;
+  run_builder(b, tri_pos, n, max_leaf);
+  BinaryTree t;
+  to_tree(b, t);
+  emit_bvh_binary(t, tri_pos, out);
+  out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void build_bvh_binary_gpu(const float* tri_pos, size_t n, int max_leaf, BvhHost& out) {
+  auto t0 = std::chrono::steady_clock::now();
+  BinaryTree t;
+  build_tree_gpu(tri_pos, n, max_leaf, t);
+  emit_bvh_binary(t, tri_pos, out);
   out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
@@ -221,8 +259,9 @@ int grid_exponent(float extent) {
   return std::max(-100, std::min(127, e));
 }
 
-void emit_wide(const Builder& b, WideOut& out) {
-  const std::vector<BNode>& nd = b.nodes;
+void emit_wide(const BinaryTree& b, WideOut& out) {
+  const std::vector<TreeNode>& nd = b.nodes;
+  auto area = [&](int32_t k) { return box_of(nd[size_t(k)]).area(); };
   struct Job { int32_t bnode; uint32_t wide; int depth; };
   std::deque<Job> q;
   out.nodes.assign(80, 0);
@@ -234,14 +273,14 @@ void emit_wide(const Builder& b, WideOut& out) {
     out.depth = std::max(out.depth, jb.depth);
     // gather up to 8 children
     std::vector<int32_t> kids;
-    const BNode& root = nd[size_t(jb.bnode)];
+    const TreeNode& root = nd[size_t(jb.bnode)];
     if (root.child < 0) kids.push_back(jb.bnode);
     else { kids.push_back(root.child); kids.push_back(root.child + 1); }
     while (kids.size() < 8) {
-      int best = -1; float area = -1.f;
+      int best = -1; float best_area = -1.f;
       for (size_t i = 0; i < kids.size(); ++i) {
-        const BNode& c = nd[size_t(kids[i])];
-        if (c.child >= 0 && c.box.area() > area) { area = c.box.area(); best = int(i); }
+        const TreeNode& c = nd[size_t(kids[i])];
+        if (c.child >= 0 && area(kids[i]) > best_area) { best_area = area(kids[i]); best = int(i); }
       }
       if (best < 0) break;
       int32_t c = kids[size_t(best)];
@@ -250,7 +289,7 @@ void emit_wide(const Builder& b, WideOut& out) {
     }
     // node box
     Box nb;
-    for (int32_t k : kids) nb.grow(nd[size_t(k)].box);
+    for (int32_t k : kids) nb.grow(box_of(nd[size_t(k)]));
     float ctr[3] = {0.5f * (nb.lo[0] + nb.hi[0]), 0.5f * (nb.lo[1] + nb.hi[1]), 0.5f * (nb.lo[2] + nb.hi[2])};
     // slot assignment: slot s is entered first by rays whose direction signs
     // are ((s&4)?+:-, (s&2)?+:-, (s&1)?+:-); it takes the child that lies
@@ -258,7 +297,7 @@ void emit_wide(const Builder& b, WideOut& out) {
     struct Cand { float cost; int kid, slot; };
     std::vector<Cand> cands;
     for (size_t i = 0; i < kids.size(); ++i) {
-      const Box& cb = nd[size_t(kids[i])].box;
+      const Box cb = box_of(nd[size_t(kids[i])]);
       float c[3] = {0.5f * (cb.lo[0] + cb.hi[0]) - ctr[0], 0.5f * (cb.lo[1] + cb.hi[1]) - ctr[1], 0.5f * (cb.lo[2] + cb.hi[2]) - ctr[2]};
       for (int s = 0; s < 8; ++s) {
         float d[3] = {(s & 4) ? 1.f : -1.f, (s & 2) ? 1.f : -1.f, (s & 1) ? 1.f : -1.f};
@@ -286,17 +325,17 @@ void emit_wide(const Builder& b, WideOut& out) {
       uint8_t* qlo[3] = {node + 32 + s, node + 40 + s, node + 48 + s};
       uint8_t* qhi[3] = {node + 56 + s, node + 64 + s, node + 72 + s};
       if (kid_in[s] < 0) { *meta = 0; for (int a = 0; a < 3; ++a) { *qlo[a] = 255; *qhi[a] = 0; } continue; }
-      const BNode& c = nd[size_t(kids[size_t(kid_in[s])])];
+      const TreeNode& c = nd[size_t(kids[size_t(kid_in[s])])];
       for (int a = 0; a < 3; ++a) {
         float sc = pow2f(ex[a]);
         float lo = nb.lo[a];
-        double ql = std::floor((double(c.box.lo[a]) - double(lo)) / double(sc));
-        double qh = std::ceil((double(c.box.hi[a]) - double(lo)) / double(sc));
+        double ql = std::floor((double(c.lo[a]) - double(lo)) / double(sc));
+        double qh = std::ceil((double(c.hi[a]) - double(lo)) / double(sc));
         int il = int(std::max(0.0, std::min(255.0, ql)));
         int ih = int(std::max(0.0, std::min(255.0, qh)));
         // the device decodes fma(q, 2^e, p) rounded once; widen until conservative
-        while (il > 0 && std::fma(float(il), sc, lo) > c.box.lo[a]) --il;
-        while (ih < 255 && std::fma(float(ih), sc, lo) < c.box.hi[a]) ++ih;
+        while (il > 0 && std::fma(float(il), sc, lo) > c.lo[a]) --il;
+        while (ih < 255 && std::fma(float(ih), sc, lo) < c.hi[a]) ++ih;
         *qlo[a] = uint8_t(il); *qhi[a] = uint8_t(ih);
       }
       if (c.child >= 0) {
@@ -324,17 +363,31 @@ void emit_wide(const Builder& b, WideOut& out) {
 
 }  // namespace
 
-void build_bvh_wide(const float* tri_pos, size_t n, BvhHost& out) {
-  auto t0 = std::chrono::steady_clock::now();
-  Builder b;
-  run_builder(b, tri_pos, n, 3);
+void emit_bvh_wide(const BinaryTree& t, const float* tri_pos, BvhHost& out) {
   WideOut w;
-  emit_wide(b, w);
+  emit_wide(t, w);
   out.nodes.resize(w.nodes.size() / 4);
   std::memcpy(out.nodes.data(), w.nodes.data(), w.nodes.size());
   out.order = w.order;
   leaf_ordered_tris(tri_pos, out.order, out.tris);
   out.depth = w.depth;
+}
+
+void build_bvh_wide(const float* tri_pos, size_t n, BvhHost& out) {
+  auto t0 = std::chrono::steady_clock::now();
+  Builder b;
+  run_builder(b, tri_pos, n, 3);
+  BinaryTree t;
+  to_tree(b, t);
+  emit_bvh_wide(t, tri_pos, out);
+  out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void build_bvh_wide_gpu(const float* tri_pos, size_t n, BvhHost& out) {
+  auto t0 = std::chrono::steady_clock::now();
+  BinaryTree t;
+  build_tree_gpu(tri_pos, n, 3, t);
+  emit_bvh_wide(t, tri_pos, out);
   out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 

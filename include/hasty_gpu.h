@@ -45,6 +45,7 @@ extern "C" {
 
 /* hasty_ctx_create flags */
 #define HASTY_CTX_BINARY_BVH 1u   /* binary BVH instead of the compressed 8-wide one */
+#define HASTY_CTX_HOST_BVH 2u     /* build the BVH on the host instead of the GPU */
 
 #define HASTY_AOV_COLOR 0
 #define HASTY_AOV_NORMAL 1
