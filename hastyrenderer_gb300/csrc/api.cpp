@@ -125,7 +125,7 @@ int64_t upload_bytes(const hasty_job& j) {
   const hasty_job::Prepared& p = *j.prep;
   return vec_bytes(h.tri_pos) + vec_bytes(h.tri_attr) + vec_bytes(h.normals) + vec_bytes(h.texcoords) +
          vec_bytes(p.bvh.nodes) + vec_bytes(p.bvh.tris) + vec_bytes(h.mats) + vec_bytes(h.textures) +
-         vec_bytes(h.tex_pool) + vec_bytes(h.light_tris) + vec_bytes(h.light_cdf) + vec_bytes(p.light_guide) +
+         vec_bytes(h.tex_pool) + vec_bytes(h.tex_pool8) + vec_bytes(h.light_tris) + vec_bytes(h.light_cdf) + vec_bytes(p.light_guide) +
          vec_bytes(h.env_texels) + vec_bytes(h.env_weights) + vec_bytes(h.env_cdf) + vec_bytes(p.env_guide);
 }
 
@@ -147,6 +147,7 @@ void upload_scene(hasty_job& j) {
   s.mats = j.upload(h.mats);
   s.textures = j.upload(h.textures);
   s.tex_pool = j.upload(h.tex_pool);
+  s.tex_pool8 = j.upload(h.tex_pool8);
   s.n_light_tris = int32_t(h.light_tris.size());
   s.light_tris = j.upload(h.light_tris);
   s.light_cdf = j.upload(h.light_cdf);
@@ -258,6 +259,7 @@ void hasty::finish_job_load(hasty_job& job, bool plain) {
   std::vector<float>().swap(j->host.tri_pos);
   std::vector<float>().swap(j->host.env_texels);
   std::vector<float>().swap(j->host.tex_pool);
+  std::vector<uint8_t>().swap(j->host.tex_pool8);
 }
 
 std::unique_ptr<hasty_job> hasty::load_job(hasty_ctx* ctx, const std::string& path, bool plain) {

@@ -382,7 +382,18 @@ __device__ __forceinline__ void tex_lookup(const SceneDev& sc, int ti, float u0,
   int col = int(u * float(td.w)), row = int(omv * float(td.h));
   col = col >= td.w ? td.w - 1 : (col < 0 ? 0 : col);
   row = row >= td.h ? td.h - 1 : (row < 0 ? 0 : row);
-  const float* p = sc.tex_pool + td.offset + (int64_t(row) * td.w + col) * td.ch;
+  const int64_t texel = int64_t(row) * td.w + col;
+  if (td.fmt == 1) {
+    const float* lut = sc.tex_pool + td.lut;
+    if (td.ch == 1) {
+      out[0] = lut[sc.tex_pool8[td.offset + texel]];
+    } else {
+      uint32_t w = *reinterpret_cast<const uint32_t*>(sc.tex_pool8 + td.offset + 4 * texel);
+      out[0] = lut[w & 0xFFu]; out[1] = lut[(w >> 8) & 0xFFu]; out[2] = lut[(w >> 16) & 0xFFu];
+    }
+    return;
+  }
+  const float* p = sc.tex_pool + td.offset + texel * td.ch;
   for (int c = 0; c < td.ch; ++c) out[c] = p[c];
 }
 __device__ __forceinline__ V3 mat_albedo(const SceneDev& sc, const MaterialDev& m, const Inter& it) {
@@ -400,9 +411,7 @@ __device__ __forceinline__ float mat_scalar(const SceneDev& sc, float val, int t
 // BRDF.cpp:589-603
 __device__ __forceinline__ float mat_ior(const MaterialDev& m, int wl) {
   if (!m.vary_ior) return m.ior;
-  if (wl == 0) return m.ior * (1.43f / 1.45f);
-  if (wl == 1) return m.ior * (1.45f / 1.45f);
-  if (wl == 2) return m.ior * (1.47f / 1.45f);
+  if (wl >= 0 && wl < 3) return m.ior_band[wl];    // precomputed on the host (MaterialDev::ior_band)
   return __int_as_float(0x7fc00000);
 }
 // BRDF.cpp:604-628

@@ -22,11 +22,18 @@ struct MaterialDev {
   float specular, ior, anisotropy, transmission;
   int32_t normal_tex; int32_t vary_ior;
   float emission[3]; int32_t is_light;
+  // IOR of the three dispersion bands (used when vary_ior): the reference's
+  // ratios ior * {1.43, 1.45, 1.47} / 1.45 (core/src/BRDF.cpp:589-603), or
+  // Cauchy's ior + b / lambda^2 when the world asks for it (extension).
+  float ior_band[3]; int32_t pad_band;
 };
 
-// Nearest-neighbour texture: `ch` floats per texel at `offset` in the float
-// pool, row 0 = top of the picture (core/include/Hasty/Texture.h:119-139).
-struct TextureDev { int32_t w, h, ch; int32_t clamp_u, clamp_v; int64_t offset; };
+// Nearest-neighbour texture, row 0 = top of the picture
+// (core/include/Hasty/Texture.h:119-139). fmt 0: `ch` floats per texel at
+// `offset` in the float pool; fmt 1: bytes at `offset` in the 8-bit pool (4
+// per texel for ch 3, 1 for ch 1), each mapped through the 256 floats at
+// `lut` in the float pool.
+struct TextureDev { int32_t w, h, ch; int32_t clamp_u, clamp_v; int32_t fmt; int64_t offset; int64_t lut; };
 
 // Per-triangle shading record, indexed by the global triangle id (shapes in
 // file order, faces in shape order): vertex, normal and texcoord indices,
@@ -83,6 +90,7 @@ struct SceneDev {
   const MaterialDev* mats;
   const TextureDev* textures;
   const float* tex_pool;
+  const uint8_t* tex_pool8;
   // lights
   int32_t n_light_tris;
   const int32_t* light_tris;

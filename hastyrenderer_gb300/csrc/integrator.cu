@@ -496,6 +496,9 @@ __global__ void k_debug_bsdf(int which, const float* in, int n, const uint32_t* 
   m.albedo_tex = m.roughness_tex = m.metallic_tex = m.normal_tex = -1;
   m.metallic = p[18]; m.specular = p[19]; m.roughness = p[20]; m.anisotropy = p[21];
   m.transmission = p[22]; m.ior = p[23]; m.vary_ior = p[24] != 0.0f;
+  m.ior_band[0] = m.ior * (1.43f / 1.45f);
+  m.ior_band[1] = m.ior * (1.45f / 1.45f);
+  m.ior_band[2] = m.ior * (1.47f / 1.45f);
   V3 wo = ld3(p + 25), wi = ld3(p + 28);
   int wl = int(p[31]);
   float eta = p[32];

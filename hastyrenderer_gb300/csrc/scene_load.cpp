@@ -125,9 +125,12 @@ void vec3_of(const JNode& n, float* out) {
 }
 
 // ---------------------------------------------------------------- images --
-struct Img { int w = 0, h = 0, ch = 0; std::vector<float> px; };
+// px: values as floats (PNM/PAM: v / maxval); u8: the raw bytes when the
+// file stores 8-bit samples (maxval 255), for 8-bit device textures.
+struct Img { int w = 0, h = 0, ch = 0; std::vector<float> px; std::vector<uint8_t> u8; };
 
-// PFM (scanlines bottom-up in the file, returned top-down) and binary PNM.
+// PFM (scanlines bottom-up in the file, returned top-down), binary PNM and
+// PAM (P7: WIDTH/HEIGHT/DEPTH/MAXVAL header, e.g. RGB_ALPHA for RGBA8).
 Img read_image(const std::string& path) {
   std::string data = slurp(path);
   const char* p = data.c_str(); const char* e = p + data.size();
@@ -163,11 +166,26 @@ Img read_image(const std::string& path) {
     }
     return im;
   }
-  if (magic == "P6" || magic == "P5") {
-    im.w = std::atoi(token().c_str()); im.h = std::atoi(token().c_str());
-    int maxv = std::atoi(token().c_str());
+  if (magic == "P6" || magic == "P5" || magic == "P7") {
+    int maxv = 0;
+    if (magic == "P7") {
+      for (int guard = 0; guard < 64; ++guard) {
+        std::string key = token();
+        if (key == "ENDHDR") break;
+        if (key.empty()) throw LoadError("truncated PAM header " + path);
+        std::string val = token();
+        if (key == "WIDTH") im.w = std::atoi(val.c_str());
+        else if (key == "HEIGHT") im.h = std::atoi(val.c_str());
+        else if (key == "DEPTH") im.ch = std::atoi(val.c_str());
+        else if (key == "MAXVAL") maxv = std::atoi(val.c_str());
+      }
+      if (im.ch < 1 || im.ch > 4) throw LoadError("PAM depth must be 1..4: " + path);
+    } else {
+      im.w = std::atoi(token().c_str()); im.h = std::atoi(token().c_str());
+      maxv = std::atoi(token().c_str());
+      im.ch = magic == "P6" ? 3 : 1;
+    }
     ++p;
-    im.ch = magic == "P6" ? 3 : 1;
     size_t n = size_t(im.w) * im.h * im.ch;
     size_t bps = maxv < 256 ? 1 : 2;
     if (im.w <= 0 || im.h <= 0 || maxv <= 0 || size_t(e - p) < n * bps) throw LoadError("truncated PNM " + path);
@@ -177,9 +195,10 @@ Img read_image(const std::string& path) {
       unsigned v = bps == 1 ? q[i] : (unsigned(q[2 * i]) << 8 | q[2 * i + 1]);
       im.px[i] = float(v) / float(maxv);
     }
+    if (maxv == 255) im.u8.assign(q, q + n);
     return im;
   }
-  throw LoadError("unsupported image format: " + path + " (PFM, PPM, PGM are accepted)");
+  throw LoadError("unsupported image format: " + path + " (PFM, PPM, PGM, PAM are accepted)");
 }
 
 // ----------------------------------------------------------------- OBJ ----
@@ -303,10 +322,35 @@ ObjFile read_obj(const std::string& path, const std::string& mtl_dir) {
   return o;
 }
 
+// The value of texel sample x after loading: sRGB albedo maps are raised to
+// 2.2 (clampAndPowInplace(image, 0, FLT_MAX, 2.2), core/src/Texture.cpp:43).
+float texel_value(float x, bool srgb) { return srgb ? std::pow(std::max(0.0f, std::min(FLT_MAX, x)), 2.2f) : x; }
+
 int add_texture(HostScene& sc, const std::string& path, int want, bool srgb) {
   Img im = read_image(path);
   TextureDev t{};
   t.w = im.w; t.h = im.h;
+  if (!im.u8.empty() && (want == 1 ? im.ch == 1 : (im.ch == 3 || im.ch == 4))) {
+    // 8-bit texture: bytes on the device (4 per colour texel, 1 per scalar
+    // texel) and a 256-entry table of the float each byte loads as, so a
+    // lookup returns exactly what the float texture would hold.
+    t.fmt = 1;
+    t.ch = want == 1 ? 1 : 3;
+    t.lut = int64_t(sc.tex_pool.size());
+    for (int b = 0; b < 256; ++b) sc.tex_pool.push_back(texel_value(float(b) / float(255), srgb));
+    t.offset = int64_t(sc.tex_pool8.size());
+    size_t n = size_t(im.w) * im.h;
+    if (want == 1) {
+      sc.tex_pool8.insert(sc.tex_pool8.end(), im.u8.begin(), im.u8.end());
+    } else {
+      for (size_t i = 0; i < n; ++i) {
+        for (int c = 0; c < 3; ++c) sc.tex_pool8.push_back(im.u8[i * size_t(im.ch) + size_t(c)]);
+        sc.tex_pool8.push_back(0);
+      }
+    }
+    sc.textures.push_back(t);
+    return int(sc.textures.size() - 1);
+  }
   t.offset = int64_t(sc.tex_pool.size());
   if (want == 1) {
     if (im.ch != 1) throw LoadError("could not read " + path + ", wrong number of channels, expected 1, found " + std::to_string(im.ch));
@@ -319,10 +363,8 @@ int add_texture(HostScene& sc, const std::string& path, int want, bool srgb) {
     for (size_t i = 0; i < n; ++i)
       for (int c = 0; c < 3; ++c) sc.tex_pool.push_back(im.px[i * size_t(im.ch) + size_t(c)]);
   }
-  if (srgb) {  // clampAndPowInplace(image, 0, FLT_MAX, 2.2), core/src/Texture.cpp:43
-    for (size_t i = size_t(t.offset); i < sc.tex_pool.size(); ++i)
-      sc.tex_pool[i] = std::pow(std::max(0.0f, std::min(FLT_MAX, sc.tex_pool[i])), 2.2f);
-  }
+  if (srgb)
+    for (size_t i = size_t(t.offset); i < sc.tex_pool.size(); ++i) sc.tex_pool[i] = texel_value(sc.tex_pool[i], true);
   sc.textures.push_back(t);
   return int(sc.textures.size() - 1);
 }
@@ -459,6 +501,19 @@ void load_scene_file(const std::string& scene_path, HostScene& sc) {
     if (!(vs > 0.f)) throw LoadError("environment texture is black; it cannot be importance sampled");
   }
   if (const JNode* v = world.get("vary_glass_ior")) sc.vary_glass_ior = v->boolean();
+  if (const JNode* dj = world.get("dispersion")) {      // extension: Cauchy bands
+    const JNode& model = dj->req("model");
+    if (model.str() == "cauchy") sc.cauchy = true;
+    else if (model.str() != "ratio") throw LoadError("world.dispersion.model: expected \"cauchy\" or \"ratio\"");
+    if (const JNode* b = dj->get("b")) sc.cauchy_b = float(b->number());
+    if (const JNode* wv = dj->get("wavelengths")) {
+      if (wv->t != JNode::ARR || wv->items.size() != 3) throw LoadError("world.dispersion.wavelengths: expected 3 values (um)");
+      for (int k = 0; k < 3; ++k) {
+        sc.band_um[k] = float(wv->items[size_t(k)].number());
+        if (!(sc.band_um[k] > 0.0f)) throw LoadError("world.dispersion.wavelengths must be positive");
+      }
+    }
+  }
 
   ObjFile obj = read_obj(resolve(folder, scene.req("mesh").str()), folder);
   sc.vertices = std::move(obj.v); sc.normals = std::move(obj.vn); sc.texcoords = std::move(obj.vt);
@@ -478,6 +533,11 @@ void load_scene_file(const std::string& scene_path, HostScene& sc) {
     d.ior = m.Ni;
     d.anisotropy = m.aniso;
     d.is_light = (m.Ke[0] > 0.0f || m.Ke[1] > 0.0f || m.Ke[2] > 0.0f) ? 1 : 0;
+    for (int k = 0; k < 3; ++k) {
+      const float ratio[3] = {1.43f / 1.45f, 1.45f / 1.45f, 1.47f / 1.45f};
+      float lam = sc.band_um[k];
+      d.ior_band[k] = sc.cauchy ? d.ior + sc.cauchy_b / (lam * lam) : d.ior * ratio[k];
+    }
     // A transmissive surface with a rough lobe makes the reference throw
     // "not implemented" at the first shade (BRDF.cpp:386-389); refuse it here.
     if (d.transmission > 0.0f) {

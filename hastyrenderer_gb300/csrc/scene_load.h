@@ -47,12 +47,18 @@ struct HostScene {
   // materials / textures
   std::vector<MaterialDev> mats;
   std::vector<TextureDev> textures;
-  std::vector<float> tex_pool;
+  std::vector<float> tex_pool;      // float texels and the 8-bit textures' tables
+  std::vector<uint8_t> tex_pool8;   // 8-bit texels
   // lights
   std::vector<int32_t> light_tris;
   std::vector<double> light_cdf;
   float total_light_area = 0.f;
   bool vary_glass_ior = false;
+  // world "dispersion": {"model": "cauchy", "b": um^2, "wavelengths": [3 x um]}
+  // (extension; default: the reference's fixed band ratios)
+  bool cauchy = false;
+  float cauchy_b = 0.0042f;
+  float band_um[3] = {0.65f, 0.55f, 0.45f};
 
   size_t n_tris() const { return tri_attr.size(); }
   bool has_light() const {

@@ -24,7 +24,7 @@ import os
 import numpy as np
 
 __all__ = [
-    "write_pfm", "write_pnm", "icosphere", "cornell_box", "sphere_field", "textured_room",
+    "write_pfm", "write_pnm", "write_pam", "icosphere", "cornell_box", "sphere_field", "textured_room",
     "sky_environment", "roughness_to_ns",
 ]
 
@@ -47,6 +47,17 @@ def write_pnm(path: str, img: np.ndarray) -> None:
     tag = b"P6" if a.ndim == 3 else b"P5"
     with open(path, "wb") as f:
         f.write(tag + b"\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(a).tobytes())
+
+
+def write_pam(path: str, img: np.ndarray) -> None:
+    """Write an 8-bit HxWx4 RGBA (or HxWx3, alpha 255 added) PAM (P7, RGB_ALPHA), values in [0,1]."""
+    a = np.clip(np.rint(np.asarray(img, dtype=np.float64) * 255.0), 0, 255).astype(np.uint8)
+    if a.shape[-1] == 3:
+        a = np.concatenate([a, np.full(a.shape[:2] + (1,), 255, np.uint8)], -1)
+    h, w = a.shape[:2]
+    with open(path, "wb") as f:
+        f.write(b"P7\nWIDTH %d\nHEIGHT %d\nDEPTH 4\nMAXVAL 255\nTUPLTYPE RGB_ALPHA\nENDHDR\n" % (w, h))
         f.write(np.ascontiguousarray(a).tobytes())
 
 
@@ -331,22 +342,26 @@ def _value_noise(rng, size, cells):
 
 
 def textured_room(out_dir, seed=0, width=64, height=48, spp=16, max_depth=8, tex_size=64, use_mis=True,
-                  roulette_start_depth=2, roulette_q=0.3):
+                  roulette_start_depth=2, roulette_q=0.3, rgba8=False, dispersion=None):
     """Textured quads (albedo map in sRGB, roughness/metallic maps, normal map),
     a smooth sphere without UVs (magenta fallback for its albedo map), an
-    anisotropic GGX panel and an area light over a dim constant background."""
+    anisotropic GGX panel and an area light over a dim constant background.
+    rgba8: write the albedo and normal maps as RGBA8 PAM files (same texel
+    values as the PPM ones). dispersion: the world's "dispersion" object
+    (e.g. {"model": "cauchy", "b": 0.0042}) for the dispersive glass."""
     rng = np.random.default_rng(seed)
     os.makedirs(out_dir, exist_ok=True)
     n = tex_size
     alb = np.stack([_value_noise(rng, n, 4) * 0.8 + 0.1 for _ in range(3)], -1)
-    write_pnm(os.path.join(out_dir, "albedo.ppm"), alb)
+    alb_name, nrm_name = ("albedo.pam", "normal.pam") if rgba8 else ("albedo.ppm", "normal.ppm")
+    (write_pam if rgba8 else write_pnm)(os.path.join(out_dir, alb_name), alb)
     write_pnm(os.path.join(out_dir, "rough.pgm"), _value_noise(rng, n, 3) * 0.8 + 0.1)
     write_pnm(os.path.join(out_dir, "metal.pgm"), (_value_noise(rng, n, 2) > 0.6).astype(np.float64))
     h = _value_noise(rng, n, 6)
     gy, gx = np.gradient(h)
     nm = np.stack([-gx * 4.0, -gy * 4.0, np.ones_like(h)], -1)
     nm /= np.linalg.norm(nm, axis=-1, keepdims=True)
-    write_pnm(os.path.join(out_dir, "normal.ppm"), nm * 0.5 + 0.5)
+    (write_pam if rgba8 else write_pnm)(os.path.join(out_dir, nrm_name), nm * 0.5 + 0.5)
     ow = _ObjWriter()
     uv = np.array([[0, 0], [2, 0], [2, 2], [0, 2]], dtype=np.float64)
     v, f = _quad((-2, 0, -2), (-2, 0, 2), (2, 0, 2), (2, 0, -2))
@@ -361,16 +376,18 @@ def textured_room(out_dir, seed=0, width=64, height=48, spp=16, max_depth=8, tex
     ow.add("glass", gv * 0.4 + np.array([0.7, 0.4, 0.6]), gf, "glass", normals=gv, smooth=True)
     v, f = _quad((-0.5, 2.9, -0.5), (0.5, 2.9, -0.5), (0.5, 2.9, 0.5), (-0.5, 2.9, 0.5))
     ow.add("light", v, f, "light")
-    mtl = (_mtl_entry("tex_floor", kd=(1, 1, 1), ks=0.5, map_kd="albedo.ppm", map_ns="rough.pgm",
-                      map_pm="metal.pgm", map_bump="normal.ppm")
-           + _mtl_entry("tex_wall", kd=(1, 1, 1), ks=0.3, roughness=0.6, map_kd="albedo.ppm", map_bump="normal.ppm")
+    mtl = (_mtl_entry("tex_floor", kd=(1, 1, 1), ks=0.5, map_kd=alb_name, map_ns="rough.pgm",
+                      map_pm="metal.pgm", map_bump=nrm_name)
+           + _mtl_entry("tex_wall", kd=(1, 1, 1), ks=0.3, roughness=0.6, map_kd=alb_name, map_bump=nrm_name)
            + _mtl_entry("aniso", kd=(0.9, 0.6, 0.3), ks=0.5, roughness=0.35, metallic=1.0, aniso=0.8)
-           + _mtl_entry("ball", kd=(0.9, 0.9, 0.9), ks=0.5, roughness=0.3, map_kd="albedo.ppm")
+           + _mtl_entry("ball", kd=(0.9, 0.9, 0.9), ks=0.5, roughness=0.3, map_kd=alb_name)
            + _mtl_entry("glass", kd=(0.95, 0.97, 1.0), ks=0.5, roughness=0.0, ior=1.5, dissolve=0.0)
            + _mtl_entry("light", kd=(0, 0, 0), ke=(40.0, 38.0, 34.0)))
     scene = {"camera": {"position": [0.3, 1.6, 4.2], "look_at": [0.0, 0.8, 0.0], "aperture": 0.05,
                         "focal_distance": 4.0, "num_blades": 5},
              "world": {"background_color": [0.05, 0.06, 0.08], "vary_glass_ior": True}}
+    if dispersion is not None:
+        scene["world"]["dispersion"] = dict(dispersion)
     settings = {"num_samples": spp, "num_threads": 8, "width": width, "height": height,
                 "roulette_start_depth": roulette_start_depth, "roulette_q": roulette_q,
                 "max_depth": max_depth, "use_mis": use_mis}

@@ -372,11 +372,26 @@ inline bool read_image(const std::string& path, ImageF& img, std::string& err) {
       std::memcpy(&img.data[size_t(y) * w * ch], &raw[size_t(h - 1 - y) * w * ch], sizeof(float) * w * ch);
     return true;
   }
-  if (m == "P6" || m == "P5") {
-    int w, h, maxv;
-    if (!read_int(w) || !read_int(h) || !read_int(maxv)) { std::fclose(fp); err = "bad PNM header " + path; return false; }
+  if (m == "P6" || m == "P5" || m == "P7") {
+    int w = 0, h = 0, maxv = 0, ch = 0;
+    if (m == "P7") {             // PAM: KEY value lines up to ENDHDR
+      char key[64], val[64];
+      for (int guard = 0;; ++guard) {
+        if (guard > 64 || std::fscanf(fp, "%63s", key) != 1) { std::fclose(fp); err = "bad PAM header " + path; return false; }
+        if (std::string(key) == "ENDHDR") break;
+        if (std::fscanf(fp, "%63s", val) != 1) { std::fclose(fp); err = "bad PAM header " + path; return false; }
+        std::string k(key);
+        if (k == "WIDTH") w = std::atoi(val);
+        else if (k == "HEIGHT") h = std::atoi(val);
+        else if (k == "DEPTH") ch = std::atoi(val);
+        else if (k == "MAXVAL") maxv = std::atoi(val);
+      }
+      if (ch < 1 || ch > 4 || w <= 0 || h <= 0 || maxv <= 0) { std::fclose(fp); err = "bad PAM header " + path; return false; }
+    } else {
+      if (!read_int(w) || !read_int(h) || !read_int(maxv)) { std::fclose(fp); err = "bad PNM header " + path; return false; }
+      ch = (m == "P6") ? 3 : 1;
+    }
     std::fgetc(fp);
-    int ch = (m == "P6") ? 3 : 1;
     size_t n = size_t(w) * h * ch;
     img.width = w; img.height = h; img.channels = ch; img.data.resize(n);
     if (maxv < 256) {
@@ -392,7 +407,7 @@ inline bool read_image(const std::string& path, ImageF& img, std::string& err) {
     return true;
   }
   std::fclose(fp);
-  err = "unsupported image format " + path + " (PFM, PPM and PGM are read)";
+  err = "unsupported image format " + path + " (PFM, PPM, PGM and PAM are read)";
   return false;
 }
 

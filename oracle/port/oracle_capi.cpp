@@ -30,6 +30,7 @@ Material kat_material(const float* in) {
   m.albedo = V3(in[15], in[16], in[17]);
   m.metallic = in[18]; m.specular = in[19]; m.roughness = in[20];
   m.anisotropy = in[21]; m.transmission = in[22]; m.ior = in[23]; m.vary_ior = in[24] != 0.0f;
+  { const float um[3] = {0.65f, 0.55f, 0.45f}; set_ior_bands(m, false, 0.0f, um); }
   return m;
 }
 void put3(float* o, const V3& v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; }

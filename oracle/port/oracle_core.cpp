@@ -403,13 +403,17 @@ float MaterialCtx::metallic(const Interaction& it) const {
   float c; (*tex)[mat->metallic_tex].lookup(it.uv[0], it.uv[1], &c);
   return c;
 }
-float MaterialCtx::ior(int wl) const {
+float MaterialCtx::ior(int wl) const {       // BRDF.cpp:589-603 (bands precomputed at load)
   if (!mat->vary_ior) return mat->ior;
-  switch (wl) {
-    case 0: return mat->ior * (1.43f / 1.45f);
-    case 1: return mat->ior * (1.45f / 1.45f);
-    case 2: return mat->ior * (1.47f / 1.45f);
-    default: return std::numeric_limits<float>::quiet_NaN();
+  if (wl >= 0 && wl < 3) return mat->ior_band[wl];
+  return std::numeric_limits<float>::quiet_NaN();
+}
+
+void set_ior_bands(Material& m, bool cauchy, float b, const float* band_um) {
+  const float ratio[3] = {1.43f / 1.45f, 1.45f / 1.45f, 1.47f / 1.45f};
+  for (int k = 0; k < 3; ++k) {
+    float lam = band_um[k];
+    m.ior_band[k] = cauchy ? m.ior + b / (lam * lam) : m.ior * ratio[k];
   }
 }
 V3 MaterialCtx::shading_normal(const Interaction& it, const V3& wo, float ngwo) const {
@@ -637,6 +641,15 @@ void Scene::load_scene(const std::string& scene_path) {
   }
   bool vary = false;
   if (w.contains("vary_glass_ior")) vary = w.at("vary_glass_ior").as_bool();
+  // extension (not in the reference): "dispersion": {"model": "cauchy", "b", "wavelengths"}
+  bool cauchy = false;
+  float cauchy_b = 0.0042f, band_um[3] = {0.65f, 0.55f, 0.45f};
+  if (w.contains("dispersion")) {
+    const Json& dj = w.at("dispersion");
+    cauchy = dj.at("model").as_string() == "cauchy";
+    if (dj.contains("b")) cauchy_b = float(dj.at("b").as_number());
+    if (dj.contains("wavelengths")) for (int k = 0; k < 3; ++k) band_um[k] = float(dj.at("wavelengths").at(size_t(k)).as_number());
+  }
 
   std::string mesh = join_path(folder, j.at("mesh").as_string());
   ObjData obj; std::string err;
@@ -656,6 +669,7 @@ void Scene::load_scene(const std::string& scene_path) {
     else m.metallic = om.ambient[0];
     m.specular = om.specular[0];
     m.ior = om.ior;
+    set_ior_bands(m, cauchy, cauchy_b, band_um);
     m.anisotropy = om.anisotropy;
     m.emission = V3(om.emission[0], om.emission[1], om.emission[2]);
     m.is_light = om.emission[0] > 0.0f || om.emission[1] > 0.0f || om.emission[2] > 0.0f;

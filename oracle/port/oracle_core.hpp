@@ -166,7 +166,11 @@ struct Material {               // PrincipledBRDF members, BRDF.h:161-171 + MTL 
   bool vary_ior = false;
   V3 emission;
   bool is_light = false;
+  float ior_band[3] = {1, 1, 1};   // band IORs (reference ratios, or the Cauchy extension)
 };
+
+// Band IORs of a material: the reference's ratios, or Cauchy's ior + b / lambda^2.
+void set_ior_bands(Material& m, bool cauchy, float b, const float* band_um);
 
 struct SampleResult { bool outside; V3 dir, thrD, thrC; float pdf; };     // BRDF.h:58-70
 struct EvalResult { V3 fD, fC, ns; };                                      // BRDF.h:46-56
