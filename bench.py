@@ -175,14 +175,16 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--bvh", default="wide", choices=["wide", "binary"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "stress"],
                     help="plain: the large single job (default); batch: the 64-job mix batched vs one by one; "
-                         "serve: Poisson arrivals over the server")
+                         "serve: Poisson arrivals over the server; stress: 10.36M-triangle 4K scene, one pass per step")
     ap.add_argument("--jobs", type=int, default=64, help="batch/serve: jobs in the mix (serve: scene pool = half)")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: arrivals per second")
     ap.add_argument("--duration", type=float, default=120.0, help="serve: seconds of arrivals")
     ap.add_argument("--no-tune", action="store_true", help="batch/serve: skip the autotuner (engine defaults)")
     args = ap.parse_args()
+    if args.workload == "stress":
+        return run_stress(args)
     if args.workload != "plain":
         return run_mixed(args)
 
@@ -317,6 +319,64 @@ def main():
     job.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+STRESS_WORKLOAD = "stress_8000x_icosphere3_10000_cuboids_10360018tri_3840x2160_rgba8tex4096_cauchy_depth32"
+
+
+def run_stress(args):
+    """The stress scene through the plain drop-in: one pass (8.29M camera
+    samples) per step, FP64 cross-pass accumulation, device-timed."""
+    import numpy as np
+    import torch
+    from hastyrenderer_gb300 import Context, RenderJob, scenes
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    torch.cuda.init()
+    base = os.environ.get("HASTY_BENCH_STRESS", os.path.join(tempfile.gettempdir(), "hasty_bench_stress"))
+    path = os.path.join(base, "renderJob.json")
+    t0 = time.perf_counter()
+    if not os.path.exists(path):
+        scenes.stress_scene(base, seed=4)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    job = RenderJob(path, Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0))
+    load_s = time.perf_counter() - t0
+    info = job.info
+    job.set_stage_timing(True)
+    for _ in range(args.warmup):
+        job.render_passes(1)
+    job.sync()
+    s0 = job.stats()
+    sampler = ClockSampler(local_rank)
+    with sampler:
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            job.render_passes(1)
+        job.sync()
+        wall = time.perf_counter() - w0
+    s1 = job.stats()
+    ms = s1["kernel_ms"] - s0["kernel_ms"]
+    samples = args.steps * info.width * info.height
+    est = job.compute_estimate()
+    line = {
+        "metric": "samples/s", "value": samples / (ms * 1e-3), "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": STRESS_WORKLOAD, "width": info.width, "height": info.height, "max_depth": info.max_depth,
+                   "triangles": info.n_triangles, "bvh": args.bvh, "accumulation": "fp64 across passes",
+                   "l2": "working set > L2, no flush"},
+        "mrays_per_s": (s1["rays"] - s0["rays"]) / (ms * 1e-3) * 1e-6,
+        "stage_ms_per_step": {"trace": (s1["trace_ms"] - s0["trace_ms"]) / args.steps,
+                              "shade": (s1["shade_ms"] - s0["shade_ms"]) / args.steps},
+        "wall_ms_per_step": wall / args.steps * 1e3, "bvh_build_ms": info.bvh_build_ms, "bvh_depth": info.bvh_depth,
+        "load_s": load_s, "scene_generation_s": gen_s, "device_bytes": info.device_bytes,
+        "estimate_finite": bool(np.isfinite(est).all()), "media_overflow": s1["media_overflow"],
+        "trial_cap": s1["trial_cap"], "clocks": sampler.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    job.close()
 
 
 def _rel_diff(a, b):

@@ -24,7 +24,7 @@ import os
 import numpy as np
 
 __all__ = [
-    "write_pfm", "write_pnm", "write_pam", "icosphere", "cornell_box", "sphere_field", "textured_room",
+    "write_pfm", "write_pnm", "write_pam", "icosphere", "cornell_box", "sphere_field", "textured_room", "stress_scene",
     "sky_environment", "roughness_to_ns",
 ]
 
@@ -323,6 +323,76 @@ def sphere_field(out_dir, seed=0, n_spheres=800, subdiv=3, width=1920, height=10
     settings = {"num_samples": spp, "num_threads": 8, "width": width, "height": height,
                 "roulette_start_depth": roulette_start_depth, "roulette_q": roulette_q,
                 "max_depth": max_depth, "use_mis": use_mis}
+    return _write_job(out_dir, scene, settings, seed, "".join(mtl), ow)
+
+
+def stress_scene(out_dir, seed=0, n_spheres=8000, n_cuboids=10000, tex_size=4096, width=3840, height=2160,
+                 spp=1024, max_depth=32, box=60.0, roulette_start_depth=3, roulette_q=0.3):
+    """Stress workload: n_spheres subdivision-3 icospheres (1280 tris each;
+    10.24M at 8000) plus n_cuboids rotated cuboids (12 tris each) on a ground
+    plane; 50% dispersive glass (Cauchy n = 1.5 + 0.0042 / lambda^2, um) and
+    50% GGX (roughness U[0.01, 0.3]); four quads with tex_size^2 RGBA8
+    value-noise albedo and normal maps; the procedural sky plus three area
+    lights; thin lens; depth max_depth."""
+    rng = np.random.default_rng(seed)
+    os.makedirs(out_dir, exist_ok=True)
+    ow = _ObjWriter()
+    mtl = [_mtl_entry("ground", kd=(0.45, 0.45, 0.42))]
+    g = box
+    v, f = _quad((-g, 0, -g), (-g, 0, g), (g, 0, g), (g, 0, -g))
+    ow.add("ground", v, f, "ground")
+
+    def material(name):
+        if rng.uniform() < 0.5:
+            tint = 1.0 - rng.uniform(0.0, 0.2, 3)
+            return _mtl_entry(name, kd=tint, ks=0.5, roughness=0.0, ior=1.5, dissolve=0.0)
+        return _mtl_entry(name, kd=rng.uniform(0.1, 0.9, 3), ks=0.5, roughness=float(rng.uniform(0.01, 0.3)),
+                          metallic=float(rng.integers(0, 2)))
+
+    sv, sf = icosphere(3)
+    half = box / 2.0
+    for i in range(n_spheres):
+        r = math.exp(rng.uniform(math.log(0.1), math.log(0.8)))
+        c = np.array([rng.uniform(-half, half), rng.uniform(r, box * 0.4), rng.uniform(-half, half)])
+        mtl.append(material(f"s{i}"))
+        ow.add(f"sphere{i}", sv * r + c, sf, f"s{i}", normals=sv, smooth=True)
+    for i in range(n_cuboids):
+        size = rng.uniform(0.2, 1.5, 3)
+        c = np.array([rng.uniform(-half, half), size[1] / 2.0, rng.uniform(-half, half)])
+        cv, cf = _cuboid(c, size, float(rng.uniform(0.0, math.pi)))
+        mtl.append(material(f"c{i}"))
+        ow.add(f"cuboid{i}", cv, cf, f"c{i}")
+    n = tex_size
+    uv = np.array([[0, 0], [1, 0], [1, 1], [0, 1]], dtype=np.float64)
+    for k in range(4):
+        alb = np.stack([_value_noise(rng, n, 32) * 0.8 + 0.1 for _ in range(3)], -1)
+        h = _value_noise(rng, n, 64)
+        gy, gx = np.gradient(h)
+        nm = np.stack([-gx * 40.0, -gy * 40.0, np.ones_like(h)], -1)
+        nm /= np.linalg.norm(nm, axis=-1, keepdims=True)
+        write_pam(os.path.join(out_dir, f"albedo{k}.pam"), alb)
+        write_pam(os.path.join(out_dir, f"normal{k}.pam"), nm * 0.5 + 0.5)
+        x0 = -half + k * box / 4.0
+        v, f = _quad((x0, 0.0, -half), (x0 + box / 4.5, 0.0, -half), (x0 + box / 4.5, box / 5.0, -half),
+                     (x0, box / 5.0, -half))
+        ow.add(f"panel{k}", v, f, f"tex{k}", uvs=uv)
+        mtl.append(_mtl_entry(f"tex{k}", kd=(1, 1, 1), ks=0.4, roughness=0.4, map_kd=f"albedo{k}.pam",
+                              map_bump=f"normal{k}.pam"))
+    for k in range(3):
+        x = (k - 1) * box / 3.0
+        v, f = _quad((x - 2, box * 0.6, -2), (x + 2, box * 0.6, -2), (x + 2, box * 0.6, 2), (x - 2, box * 0.6, 2))
+        ow.add(f"light{k}", v, f, f"light{k}")       # Ng = (p1 - p0) x (p2 - p0) points down, at the scene
+        mtl.append(_mtl_entry(f"light{k}", kd=(0, 0, 0), ke=(60.0, 55.0, 50.0)))
+    write_pfm(os.path.join(out_dir, "sky.pfm"), sky_environment(2048, 1024))
+    look = np.array([0.0, box * 0.1, 0.0])
+    pos = np.array([0.0, box * 0.35, box * 0.9])
+    scene = {"camera": {"position": pos.tolist(), "look_at": look.tolist(), "aperture": 0.1,
+                        "focal_distance": float(np.linalg.norm(pos - look)), "num_blades": 6},
+             "world": {"environment_texture": "sky.pfm", "vary_glass_ior": True,
+                       "dispersion": {"model": "cauchy", "b": 0.0042}}}
+    settings = {"num_samples": spp, "num_threads": 8, "width": width, "height": height,
+                "roulette_start_depth": roulette_start_depth, "roulette_q": roulette_q,
+                "max_depth": max_depth, "use_mis": True}
     return _write_job(out_dir, scene, settings, seed, "".join(mtl), ow)
 
 
