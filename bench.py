@@ -321,7 +321,7 @@ def main():
         dist.destroy_process_group()
 
 
-STRESS_WORKLOAD = "stress_8000x_icosphere3_10000_cuboids_10360018tri_3840x2160_rgba8tex4096_cauchy_depth32"
+STRESS_WORKLOAD = "stress_8000x_icosphere3_10000_cuboids_10360016tri_3840x2160_rgba8tex4096_cauchy_depth32"
 
 
 def run_stress(args):
@@ -370,7 +370,7 @@ def run_stress(args):
         "mrays_per_s": (s1["rays"] - s0["rays"]) / (ms * 1e-3) * 1e-6,
         "stage_ms_per_step": {"trace": (s1["trace_ms"] - s0["trace_ms"]) / args.steps,
                               "shade": (s1["shade_ms"] - s0["shade_ms"]) / args.steps},
-        "wall_ms_per_step": wall / args.steps * 1e3, "bvh_build_ms": info.bvh_build_ms, "bvh_depth": info.bvh_depth,
+        "wall_ms_per_step": wall / args.steps * 1e3, "bvh_build_ms": info.bvh_build_ms, "bvh_tree_ms": info.bvh_tree_ms, "bvh_depth": info.bvh_depth,
         "load_s": load_s, "scene_generation_s": gen_s, "device_bytes": info.device_bytes,
         "estimate_finite": bool(np.isfinite(est).all()), "media_overflow": s1["media_overflow"],
         "trial_cap": s1["trial_cap"], "clocks": sampler.summary(),

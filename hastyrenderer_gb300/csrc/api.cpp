@@ -134,7 +134,7 @@ void upload_scene(hasty_job& j) {
   HostScene& h = j.host;
   SceneDev& s = j.sd;
   hasty_job::Prepared& p = *j.prep;
-  j.bvh_depth = p.bvh.depth; j.bvh_ms = p.bvh.build_ms;
+  j.bvh_depth = p.bvh.depth; j.bvh_ms = p.bvh.build_ms; j.bvh_tree_ms = p.bvh.tree_ms;
   s.n_tris = int32_t(h.n_tris());
   s.tri_pos = j.upload(h.tri_pos);
   s.tri_attr = j.upload(h.tri_attr);
@@ -330,6 +330,7 @@ int hasty_job_info_get(hasty_job* job, hasty_job_info* out) {
     out->env_is_texture = h.env_texture ? 1 : 0; out->exposure = h.cam.exposure;
     out->samples_done = job->samples_done; out->bvh_depth = job->bvh_depth; out->bvh_build_ms = job->bvh_ms;
     out->device_bytes = job->bytes;
+    out->bvh_tree_ms = job->bvh_tree_ms;
     return HASTY_OK;
   });
 }

@@ -222,6 +222,7 @@ void build_bvh_binary(const float* tri_pos, size_t n, int max_leaf, BvhHost& out
   run_builder(b, tri_pos, n, max_leaf);
   BinaryTree t;
   to_tree(b, t);
+  out.tree_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   emit_bvh_binary(t, tri_pos, out);
   out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -230,6 +231,7 @@ void build_bvh_binary_gpu(const float* tri_pos, size_t n, int max_leaf, BvhHost&
   auto t0 = std::chrono::steady_clock::now();
   BinaryTree t;
   build_tree_gpu(tri_pos, n, max_leaf, t);
+  out.tree_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   emit_bvh_binary(t, tri_pos, out);
   out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -379,6 +381,7 @@ void build_bvh_wide(const float* tri_pos, size_t n, BvhHost& out) {
   run_builder(b, tri_pos, n, 3);
   BinaryTree t;
   to_tree(b, t);
+  out.tree_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   emit_bvh_wide(t, tri_pos, out);
   out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }

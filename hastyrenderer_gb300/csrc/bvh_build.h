@@ -19,6 +19,7 @@ struct BvhHost {
   std::vector<int32_t> order;     // leaf position -> global triangle id
   int32_t depth = 0;
   double build_ms = 0;
+  double tree_ms = 0;             // of which: the binary tree (device or host)
 };
 
 // Binary build tree: node 0 is the root; an inner node's children are the

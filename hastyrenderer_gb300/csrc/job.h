@@ -65,7 +65,7 @@ struct hasty_job {
   hasty_ctx* ctx = nullptr;
   HostScene host;
   int32_t bvh_depth = 0;
-  double bvh_ms = 0;
+  double bvh_ms = 0, bvh_tree_ms = 0;
   SceneDev sd{};
   PathsDev pd{};
   cudaStream_t stream = nullptr;

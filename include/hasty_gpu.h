@@ -72,6 +72,7 @@ typedef struct hasty_job_info {
   int32_t bvh_depth;
   double bvh_build_ms;
   int64_t device_bytes;        /* device memory held by the job */
+  double bvh_tree_ms;          /* part of bvh_build_ms spent building the binary tree */
 } hasty_job_info;
 
 typedef struct hasty_stats {
