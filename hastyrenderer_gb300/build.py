@@ -4,7 +4,8 @@
     python -m hastyrenderer_gb300.build --oracle   # also the CPU checker under oracle/
 
 CUDA sources are compiled for sm_103a only; `integrator.cu` without FMA
-contraction (products and sums round like the reference's scalar C++).
+contraction (products and sums round like the reference's scalar C++), and
+`bvh_gpu.cu` likewise (its layout writer matches the host writer's bytes).
 Outputs: hastyrenderer_gb300/lib/libhasty_gb300.so, lib/hasty_gpu_render.
 """
 from __future__ import annotations
@@ -26,7 +27,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE,
                "-I" + CSRC, "--expt-relaxed-constexpr"]
-CU_EXTRA = {"integrator.cu": ["--fmad=false"]}
+CU_EXTRA = {"integrator.cu": ["--fmad=false"], "bvh_gpu.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-sign-compare"]
 CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu", "bvh_gpu.cu"]
 # Extra nvcc flags for experiments (e.g. HASTY_NVCC_FLAGS="-DHASTY_OUTLINE_MASK=3").

@@ -515,6 +515,17 @@ int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* 
   });
 }
 
+int hasty_debug_wide_emit_check(int device, const char* job_path, int64_t* info, int32_t* identical) {
+  return guarded([&] {
+    if (!job_path || !identical) throw ApiError{HASTY_ERR_ARG, "null argument"};
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    HostScene h;
+    load_render_job(job_path, h);
+    *identical = check_wide_emit_gpu(h.tri_pos.data(), h.n_tris(), info) ? 1 : 0;
+    return HASTY_OK;
+  });
+}
+
 int hasty_debug_host_trace(const char* job_path, int kind, const float* rays, size_t n, int32_t* tri, float* t, float* u,
                            float* v, int64_t* info) {
   return guarded([&] {

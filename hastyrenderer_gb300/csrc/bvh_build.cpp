@@ -254,10 +254,15 @@ struct WideOut {
 
 float pow2f(int e) { return std::ldexp(1.0f, e); }
 
+// Smallest e with 255 * 2^e >= extent (exact comparisons; the log2 estimate
+// only picks the start), clamped to [-100, 127]. The device writer in
+// bvh_gpu.cu computes the same value.
 int grid_exponent(float extent) {
   if (!(extent > 0.f)) return -100;
   int e = int(std::ceil(std::log2(double(extent) / 255.0)));
+  e = std::max(-110, std::min(140, e));
   while (255.0 * std::ldexp(1.0, e) < double(extent)) ++e;
+  while (255.0 * std::ldexp(1.0, e - 1) >= double(extent)) --e;
   return std::max(-100, std::min(127, e));
 }
 
@@ -306,7 +311,7 @@ void emit_wide(const BinaryTree& b, WideOut& out) {
         cands.push_back({c[0] * d[0] + c[1] * d[1] + c[2] * d[2], int(i), s});
       }
     }
-    std::sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& c) { return a.cost < c.cost; });
+    std::stable_sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& c) { return a.cost < c.cost; });
     int slot_of[8]; int kid_in[8];
     for (int i = 0; i < 8; ++i) { slot_of[i] = -1; kid_in[i] = -1; }
     for (const Cand& c : cands)
@@ -388,10 +393,37 @@ void build_bvh_wide(const float* tri_pos, size_t n, BvhHost& out) {
 
 void build_bvh_wide_gpu(const float* tri_pos, size_t n, BvhHost& out) {
   auto t0 = std::chrono::steady_clock::now();
-  BinaryTree t;
-  build_tree_gpu(tri_pos, n, 3, t);
-  emit_bvh_wide(t, tri_pos, out);
+  build_wide_gpu(tri_pos, n, out);       // tree and layout on the device
   out.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+namespace {
+template <class T>
+bool same_bytes(const std::vector<T>& a, const std::vector<T>& b) {
+  return a.size() == b.size() && (a.empty() || std::memcmp(a.data(), b.data(), a.size() * sizeof(T)) == 0);
+}
+}  // namespace
+
+bool check_wide_emit_gpu(const float* tri_pos, size_t n, int64_t* info) {
+  BvhHost dev, dev2;
+  build_wide_gpu(tri_pos, n, dev);
+  build_wide_gpu(tri_pos, n, dev2);
+  BinaryTree t;
+  build_tree_gpu(tri_pos, n, 3, t);       // the same device tree, laid out on the host
+  BvhHost host;
+  emit_bvh_wide(t, tri_pos, host);
+  int64_t first = -1;
+  size_t m = std::min(dev.nodes.size(), host.nodes.size());
+  for (size_t i = 0; i < m; ++i)
+    if (std::memcmp(&dev.nodes[i], &host.nodes[i], 4) != 0) { first = int64_t(i); break; }
+  bool nodes_eq = same_bytes(dev.nodes, host.nodes), tris_eq = same_bytes(dev.tris, host.tris);
+  bool order_eq = same_bytes(dev.order, host.order);
+  if (info) {
+    info[0] = int64_t(dev.nodes.size() / 20); info[1] = int64_t(host.nodes.size() / 20); info[2] = first;
+    info[3] = dev.depth; info[4] = host.depth; info[5] = tris_eq; info[6] = order_eq;
+    info[7] = same_bytes(dev.nodes, dev2.nodes) && same_bytes(dev.order, dev2.order);
+  }
+  return nodes_eq && tris_eq && order_eq && dev.depth == host.depth;
 }
 
 }  // namespace hasty

@@ -46,6 +46,14 @@ void emit_bvh_wide(const BinaryTree& t, const float* tri_pos, BvhHost& out);
 // builder (32 bins per axis, leaf when no split beats the leaf cost), on the
 // current CUDA device. Triangles are uploaded from tri_pos (host).
 void build_tree_gpu(const float* tri_pos, size_t n, int max_leaf, BinaryTree& out);
+// Tree and compressed 8-wide layout both on the device; byte-identical to
+// build_tree_gpu + emit_bvh_wide (tree_ms set to the tree part).
+void build_wide_gpu(const float* tri_pos, size_t n, BvhHost& out);
+// True when the device layout equals the host layout of the same device
+// tree, compared as bytes. info (8 values, may be null): device and host
+// node counts, first differing node word (-1: none), device and host depth,
+// triangles equal, order equal, two device builds equal.
+bool check_wide_emit_gpu(const float* tri_pos, size_t n, int64_t* info);
 
 // tri_pos: 9 floats per triangle (v0, v1, v2). max_leaf: triangles per leaf.
 // Host builds; the _gpu variants build the tree on the device and write the

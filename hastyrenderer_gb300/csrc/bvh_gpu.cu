@@ -19,7 +19,9 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <chrono>
 #include <climits>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -505,19 +507,242 @@ struct DevBuf {
   DevBuf& operator=(const DevBuf&) = delete;
 };
 
-}  // namespace
+// ---- compressed 8-wide layout on the device ---------------------------------
+// The host writer (bvh_build.cpp, emit_wide) processes wide nodes breadth
+// first: a node opens binary nodes greedily (largest surface area first) up to
+// 8 children, assigns them to octant slots, quantises their boxes, and gives
+// its inner children consecutive node indices and its leaves' triangles
+// consecutive positions, both in slot order. Here one level of that queue is
+// processed at once (one thread per wide node) and the indices come from
+// exclusive scans over the level, which reproduces the host's numbering. The
+// float arithmetic is the host's (this file is built without FMA
+// contraction; fmaf where the host calls std::fma).
 
-void build_tree_gpu(const float* tri_pos, size_t n, int max_leaf, BinaryTree& out) {
+struct WideJob { int32_t bnode; uint32_t wide; int32_t depth; int32_t pad; };
+
+__device__ __forceinline__ float area_of(const TreeNode& t) { return box_area(t.lo, t.hi); }
+
+__device__ int grid_exponent_dev(float extent) {
+  if (!(extent > 0.f)) return -100;
+  int e = int(ceil(log2(double(extent) / 255.0)));
+  e = max(-110, min(140, e));
+  for (int g = 0; g < 300 && 255.0 * ldexp(1.0, e) < double(extent); ++g) ++e;
+  for (int g = 0; g < 300 && 255.0 * ldexp(1.0, e - 1) >= double(extent); ++g) --e;
+  return max(-100, min(127, e));
+}
+
+// One wide node per thread: children, slots, quantised boxes. Writes the
+// node's 20 words except child base (word 4) and triangle base (word 5),
+// the binary node in each slot (-1: empty) and the node's counts of inner
+// children and leaf triangles.
+__global__ void k_wide_collapse(const WideJob* jobs, int m, const TreeNode* tree, uint32_t* wide, int32_t* slot_kid,
+                                int32_t* n_inner, int32_t* n_tris) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  const WideJob jb = jobs[k];
+  int kids[8];
+  int nk = 0;
+  const TreeNode& root = tree[jb.bnode];
+  if (root.child < 0) { kids[nk++] = jb.bnode; }
+  else { kids[nk++] = root.child; kids[nk++] = root.child + 1; }
+  while (nk < 8) {
+    int best = -1;
+    float barea = -1.f;
+    for (int i = 0; i < nk; ++i) {
+      const TreeNode& c = tree[kids[i]];
+      if (c.child >= 0 && area_of(c) > barea) { barea = area_of(c); best = i; }
+    }
+    if (best < 0) break;
+    int c = kids[best];
+    kids[best] = tree[c].child;
+    kids[nk++] = tree[c].child + 1;
+  }
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int i = 0; i < nk; ++i)
+    for (int a = 0; a < 3; ++a) {
+      // std::min / std::max order of the host's Box::grow
+      float l = tree[kids[i]].lo[a], h = tree[kids[i]].hi[a];
+      lo[a] = l < lo[a] ? l : lo[a];
+      hi[a] = hi[a] < h ? h : hi[a];
+    }
+  float ctr[3] = {0.5f * (lo[0] + hi[0]), 0.5f * (lo[1] + hi[1]), 0.5f * (lo[2] + hi[2])};
+  // candidates (kid, slot) with cost, generated kid-major like the host and
+  // sorted stably by cost (insertion sort)
+  float cost[64];
+  int8_t ckid[64], cslot[64];
+  int nc = 0;
+  for (int i = 0; i < nk; ++i) {
+    const TreeNode& cb = tree[kids[i]];
+    float c[3] = {0.5f * (cb.lo[0] + cb.hi[0]) - ctr[0], 0.5f * (cb.lo[1] + cb.hi[1]) - ctr[1],
+                  0.5f * (cb.lo[2] + cb.hi[2]) - ctr[2]};
+    for (int sl = 0; sl < 8; ++sl) {
+      float d[3] = {(sl & 4) ? 1.f : -1.f, (sl & 2) ? 1.f : -1.f, (sl & 1) ? 1.f : -1.f};
+      float v = c[0] * d[0] + c[1] * d[1] + c[2] * d[2];
+      int j = nc++;
+      while (j > 0 && cost[j - 1] > v) { cost[j] = cost[j - 1]; ckid[j] = ckid[j - 1]; cslot[j] = cslot[j - 1]; --j; }
+      cost[j] = v; ckid[j] = int8_t(i); cslot[j] = int8_t(sl);
+    }
+  }
+  int slot_of[8], kid_in[8];
+  for (int i = 0; i < 8; ++i) { slot_of[i] = -1; kid_in[i] = -1; }
+  for (int q = 0; q < nc; ++q)
+    if (slot_of[ckid[q]] < 0 && kid_in[cslot[q]] < 0) { slot_of[ckid[q]] = cslot[q]; kid_in[cslot[q]] = ckid[q]; }
+  int ex[3];
+  for (int a = 0; a < 3; ++a) ex[a] = grid_exponent_dev(hi[a] - lo[a]);
+  uint8_t bytes[80];
+  for (int i = 0; i < 80; ++i) bytes[i] = 0;
+  for (int a = 0; a < 3; ++a) {
+    uint32_t w = __float_as_uint(lo[a]);
+    for (int b = 0; b < 4; ++b) bytes[4 * a + b] = uint8_t(w >> (8 * b));
+  }
+  bytes[12] = uint8_t(int8_t(ex[0])); bytes[13] = uint8_t(int8_t(ex[1])); bytes[14] = uint8_t(int8_t(ex[2]));
+  uint8_t imask = 0;
+  int inner = 0, tri_off = 0;
+  int32_t* sk = slot_kid + 8 * int64_t(k);
+  for (int sl = 0; sl < 8; ++sl) {
+    if (kid_in[sl] < 0) {
+      sk[sl] = -1;
+      bytes[24 + sl] = 0;
+      for (int a = 0; a < 3; ++a) { bytes[32 + 8 * a + sl] = 255; bytes[56 + 8 * a + sl] = 0; }
+      continue;
+    }
+    const int kb = kids[kid_in[sl]];
+    sk[sl] = kb;
+    const TreeNode& c = tree[kb];
+    for (int a = 0; a < 3; ++a) {
+      float sc = ldexpf(1.0f, ex[a]);
+      float l0 = lo[a];
+      double ql = floor((double(c.lo[a]) - double(l0)) / double(sc));
+      double qh = ceil((double(c.hi[a]) - double(l0)) / double(sc));
+      int il = int(fmax(0.0, fmin(255.0, ql)));
+      int ih = int(fmax(0.0, fmin(255.0, qh)));
+      while (il > 0 && fmaf(float(il), sc, l0) > c.lo[a]) --il;
+      while (ih < 255 && fmaf(float(ih), sc, l0) < c.hi[a]) ++ih;
+      bytes[32 + 8 * a + sl] = uint8_t(il);
+      bytes[56 + 8 * a + sl] = uint8_t(ih);
+    }
+    if (c.child >= 0) {
+      imask |= uint8_t(1u << sl);
+      bytes[24 + sl] = uint8_t((1u << 5) | uint32_t(24 + sl));
+      ++inner;
+    } else {
+      int cnt = c.count;          // 0..3
+      uint8_t unary = cnt == 0 ? 0 : (cnt == 1 ? 1 : (cnt == 2 ? 3 : 7));
+      bytes[24 + sl] = cnt == 0 ? 0 : uint8_t((unary << 5) | uint32_t(tri_off));
+      tri_off += cnt;
+    }
+  }
+  bytes[15] = imask;
+  uint32_t* out = wide + 20 * int64_t(jb.wide);
+  for (int i = 0; i < 20; ++i)
+    if (i != 4 && i != 5)
+      out[i] = uint32_t(bytes[4 * i]) | uint32_t(bytes[4 * i + 1]) << 8 | uint32_t(bytes[4 * i + 2]) << 16 |
+               uint32_t(bytes[4 * i + 3]) << 24;
+  n_inner[k] = inner;
+  n_tris[k] = tri_off;
+}
+
+// Exclusive scans of two arrays of m counts (one block); totals at tot[0..1].
+__global__ void __launch_bounds__(1024) k_scan2(int32_t* a, int32_t* b, int m, int32_t* tot) {
+  __shared__ int32_t s_w[2][32];
+  __shared__ int32_t s_carry[2];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t < 2) s_carry[t] = 0;
+  __syncthreads();
+  for (int base = 0; base < m; base += 1024) {
+    int i = base + t;
+    int32_t v[2] = {i < m ? a[i] : 0, i < m ? b[i] : 0}, incl[2];
+    for (int c = 0; c < 2; ++c) {
+      int32_t x = v[c];
+      for (int o = 1; o < 32; o <<= 1) { int32_t y = __shfl_up_sync(kAll, x, o); if (lane >= o) x += y; }
+      incl[c] = x;
+      if (lane == 31) s_w[c][warp] = x;
+    }
+    __syncthreads();
+    if (warp == 0)
+      for (int c = 0; c < 2; ++c) {
+        int32_t x = s_w[c][lane];
+        for (int o = 1; o < 32; o <<= 1) { int32_t y = __shfl_up_sync(kAll, x, o); if (lane >= o) x += y; }
+        s_w[c][lane] = x;
+      }
+    __syncthreads();
+    if (i < m) {
+      a[i] = s_carry[0] + (warp ? s_w[0][warp - 1] : 0) + incl[0] - v[0];
+      b[i] = s_carry[1] + (warp ? s_w[1][warp - 1] : 0) + incl[1] - v[1];
+    }
+    __syncthreads();
+    if (t < 2) s_carry[t] += s_w[t][31];
+    __syncthreads();
+  }
+  if (t < 2) tot[t] = s_carry[t];
+}
+
+// Child and triangle bases of each wide node; the next level's jobs; the
+// triangle order of the leaves.
+__global__ void k_wide_assign(const WideJob* jobs, int m, const int32_t* slot_kid, const int32_t* inner_off,
+                              const int32_t* tri_off, uint32_t node_base, uint32_t tri_base, const TreeNode* tree,
+                              const int32_t* idx, uint32_t* wide, int32_t* order, WideJob* next) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  const WideJob jb = jobs[k];
+  uint32_t cb = node_base + uint32_t(inner_off[k]);
+  uint32_t tb = tri_base + uint32_t(tri_off[k]);
+  uint32_t* out = wide + 20 * int64_t(jb.wide);
+  out[4] = cb;
+  out[5] = tb;
+  int r = 0;
+  uint32_t t = tb;
+  for (int sl = 0; sl < 8; ++sl) {
+    int kb = slot_kid[8 * int64_t(k) + sl];
+    if (kb < 0) continue;
+    const TreeNode& c = tree[kb];
+    if (c.child >= 0) {
+      next[inner_off[k] + r] = WideJob{kb, cb + uint32_t(r), jb.depth + 1, 0};
+      ++r;
+    } else {
+      for (int q = 0; q < c.count; ++q) order[t++] = idx[c.first + q];
+    }
+  }
+}
+
+// Leaf-ordered triangles: v0 (w = global id), v0 - v1, v2 - v0.
+__global__ void k_wide_tris(const float* pos, const int32_t* order, int n, float4* tris) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int t = order[i];
+  const float* p = pos + 9 * int64_t(t);
+  tris[3 * int64_t(i)] = make_float4(p[0], p[1], p[2], __int_as_float(t));
+  tris[3 * int64_t(i) + 1] = make_float4(p[0] - p[3], p[1] - p[4], p[2] - p[5], 0.f);
+  tris[3 * int64_t(i) + 2] = make_float4(p[6] - p[0], p[7] - p[1], p[8] - p[2], 0.f);
+}
+
+// A binary tree built on the device, kept there.
+struct DeviceTree {
+  cudaStream_t st = nullptr;
+  std::unique_ptr<DevBuf<float>> pos;
+  std::unique_ptr<DevBuf<int32_t>> idx;
+  std::unique_ptr<DevBuf<TreeNode>> nodes;
+  int n_nodes = 0, depth = 0;
+  DeviceTree() = default;
+  DeviceTree(const DeviceTree&) = delete;
+  DeviceTree& operator=(const DeviceTree&) = delete;
+  ~DeviceTree() { if (st) { cudaStreamSynchronize(st); cudaStreamDestroy(st); } }
+};
+
+void build_tree_device(const float* tri_pos, size_t n, int max_leaf, DeviceTree& dt) {
   if (n == 0) throw std::runtime_error("GPU BVH build: no triangles");
   if (n > size_t(INT32_MAX / 2)) throw std::runtime_error("GPU BVH build: too many triangles");
   const int ni = int(n);
-  cudaStream_t st;
-  ck(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
-  struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); } } guard{st};
-  DevBuf<float> d_pos(9 * n);
+  ck(cudaStreamCreateWithFlags(&dt.st, cudaStreamNonBlocking), "stream");
+  cudaStream_t st = dt.st;
+  dt.pos.reset(new DevBuf<float>(9 * n));
+  dt.idx.reset(new DevBuf<int32_t>(n));
+  dt.nodes.reset(new DevBuf<TreeNode>(2 * n + 1));
+  DevBuf<float>& d_pos = *dt.pos;
+  DevBuf<int32_t>& idx = *dt.idx;
+  DevBuf<TreeNode>& nodes = *dt.nodes;
   DevBuf<float4> tlo(n), thi(n), cen(n);
-  DevBuf<int32_t> idx(n), tmp(n);
-  DevBuf<TreeNode> nodes(2 * n + 1);
+  DevBuf<int32_t> tmp(n);
   DevBuf<int> counters(3);                       // next node, max depth, warp-stack overflow
   ck(cudaMemcpyAsync(d_pos.p, tri_pos, 9 * n * sizeof(float), cudaMemcpyHostToDevice, st), "upload triangles");
   k_prims<<<(ni + 255) / 256, 256, 0, st>>>(d_pos.p, ni, tlo.p, thi.p, cen.p, idx.p);
@@ -572,12 +797,71 @@ void build_tree_gpu(const float* tri_pos, size_t n, int max_leaf, BinaryTree& ou
   ck(cudaMemcpyAsync(cnt, counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, st), "counters");
   ck(cudaStreamSynchronize(st), "build");
   if (cnt[2] != 0) throw std::runtime_error("GPU BVH build: subtree stack overflow");
-  out.nodes.resize(size_t(cnt[0]));
+  dt.n_nodes = cnt[0];
+  dt.depth = cnt[1] + 1;
+}
+
+}  // namespace
+
+void build_tree_gpu(const float* tri_pos, size_t n, int max_leaf, BinaryTree& out) {
+  DeviceTree dt;
+  build_tree_device(tri_pos, n, max_leaf, dt);
+  out.nodes.resize(size_t(dt.n_nodes));
   out.idx.resize(n);
-  ck(cudaMemcpyAsync(out.nodes.data(), nodes.p, out.nodes.size() * sizeof(TreeNode), cudaMemcpyDeviceToHost, st), "nodes");
-  ck(cudaMemcpyAsync(out.idx.data(), idx.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "order");
+  ck(cudaMemcpyAsync(out.nodes.data(), dt.nodes->p, out.nodes.size() * sizeof(TreeNode), cudaMemcpyDeviceToHost, dt.st),
+     "nodes");
+  ck(cudaMemcpyAsync(out.idx.data(), dt.idx->p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, dt.st), "order");
+  ck(cudaStreamSynchronize(dt.st), "download");
+  out.depth = dt.depth;
+}
+
+void build_wide_gpu(const float* tri_pos, size_t n, BvhHost& out) {
+  auto t0 = std::chrono::steady_clock::now();
+  DeviceTree dt;
+  build_tree_device(tri_pos, n, 3, dt);
+  out.tree_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  cudaStream_t st = dt.st;
+  const size_t max_wide = size_t(dt.n_nodes) + 1;
+  DevBuf<uint32_t> wide(20 * max_wide);
+  DevBuf<int32_t> order(n);
+  DevBuf<int32_t> tot(2);
+  std::unique_ptr<DevBuf<WideJob>> jobs(new DevBuf<WideJob>(1));
+  WideJob root{0, 0u, 1, 0};
+  ck(cudaMemcpyAsync(jobs->p, &root, sizeof(root), cudaMemcpyHostToDevice, st), "root job");
+  int m = 1, depth = 0;
+  uint32_t node_base = 1, tri_base = 0;
+  while (m > 0) {
+    depth += 1;
+    const size_t mm = size_t(m);
+    DevBuf<int32_t> slot_kid{8 * mm}, n_inner{mm}, n_tri{mm};
+    k_wide_collapse<<<(m + 127) / 128, 128, 0, st>>>(jobs->p, m, dt.nodes->p, wide.p, slot_kid.p, n_inner.p, n_tri.p);
+    k_scan2<<<1, 1024, 0, st>>>(n_inner.p, n_tri.p, m, tot.p);
+    int32_t t2[2];
+    ck(cudaMemcpyAsync(t2, tot.p, sizeof(t2), cudaMemcpyDeviceToHost, st), "level totals");
+    ck(cudaStreamSynchronize(st), "wide level");
+    if (size_t(node_base) + size_t(t2[0]) > max_wide) throw std::runtime_error("GPU BVH build: wide node count out of range");
+    std::unique_ptr<DevBuf<WideJob>> next(new DevBuf<WideJob>(size_t(std::max(t2[0], 1))));
+    k_wide_assign<<<(m + 127) / 128, 128, 0, st>>>(jobs->p, m, slot_kid.p, n_inner.p, n_tri.p, node_base, tri_base,
+                                                   dt.nodes->p, dt.idx->p, wide.p, order.p, next->p);
+    ck(cudaGetLastError(), "wide level");
+    node_base += uint32_t(t2[0]);
+    tri_base += uint32_t(t2[1]);
+    m = t2[0];
+    ck(cudaStreamSynchronize(st), "wide level");
+    jobs = std::move(next);
+  }
+  if (tri_base != uint32_t(n)) throw std::runtime_error("GPU BVH build: leaves do not hold every triangle");
+  DevBuf<float4> tris(3 * n);
+  k_wide_tris<<<(int(n) + 255) / 256, 256, 0, st>>>(dt.pos->p, order.p, int(n), tris.p);
+  ck(cudaGetLastError(), "wide triangles");
+  out.nodes.resize(20 * size_t(node_base));
+  out.order.resize(n);
+  out.tris.resize(12 * n);
+  ck(cudaMemcpyAsync(out.nodes.data(), wide.p, out.nodes.size() * sizeof(float), cudaMemcpyDeviceToHost, st), "wide nodes");
+  ck(cudaMemcpyAsync(out.order.data(), order.p, n * sizeof(int32_t), cudaMemcpyDeviceToHost, st), "order");
+  ck(cudaMemcpyAsync(out.tris.data(), tris.p, out.tris.size() * sizeof(float), cudaMemcpyDeviceToHost, st), "triangles");
   ck(cudaStreamSynchronize(st), "download");
-  out.depth = cnt[1] + 1;
+  out.depth = depth;
 }
 
 }  // namespace hasty

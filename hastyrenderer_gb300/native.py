@@ -118,6 +118,7 @@ def lib() -> ctypes.CDLL:
         "hasty_debug_tri_ids": [P, P, P, SZ],
         "hasty_debug_host_trace": [ctypes.c_char_p, I, P, SZ, P, P, P, P, P],
         "hasty_debug_bsdf": [I, P, SZ, P, SZ, P],
+        "hasty_debug_wide_emit_check": [I, ctypes.c_char_p, P, P],
         "hasty_batch_render": [P, P, P, SZ, P, P],
         "hasty_job_render_pass_static": [P, I, P],
         "hasty_server_start": [P, P, P],

@@ -243,6 +243,13 @@ int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* 
  * answers n rays. info (may be NULL): triangles, nodes, tree depth. */
 int hasty_debug_host_trace(const char* render_job_path, int kind, const float* rays, size_t n, int32_t* tri, float* t,
                            float* u, float* v, int64_t* info);
+/* Builds the BVH tree of a job on `device`, writes the compressed 8-wide
+ * layout on the device and on the host from that same tree, and reports
+ * whether the two are byte-identical (identical = 1). info (8 values, may be
+ * NULL): device and host node counts, first differing node word (-1 none),
+ * device and host depth, triangles equal, order equal, two device builds
+ * equal. */
+int hasty_debug_wide_emit_check(int device, const char* render_job_path, int64_t* info, int32_t* identical);
 /* Triangle index -> (OBJ shape = Embree geomID, face = primID). */
 int hasty_debug_tri_ids(hasty_job* job, int32_t* geom, int32_t* prim, size_t n);
 /* BSDF known-answer evaluation on the device. which: 0 sample, 1 evaluate, 2 pdf.

@@ -69,3 +69,25 @@ def test_device_tree_full_size():
     print(f"wide BVH build: device {g[4].bvh_build_ms:.0f} ms, host {h[4].bvh_build_ms:.0f} ms; "
           f"depth {g[4].bvh_depth} / {h[4].bvh_depth}")
     assert g[4].bvh_depth <= 30
+
+
+@pytest.mark.parametrize("name", ["cornell", "field", "room", "full"])
+def test_device_layout_equals_host_layout(name):
+    """The compressed 8-wide layout written on the device is byte-identical
+    to the host writer's for the same device-built tree, and two device
+    builds are identical."""
+    import ctypes
+    from hastyrenderer_gb300 import native
+    if name == "full":
+        import bench
+        base = os.path.join(tempfile.gettempdir(), "hasty_bench_c1")
+        os.makedirs(base, exist_ok=True)
+        path = bench.make_job(base)
+    else:
+        path = os.path.join(GOLDEN, "scenes", name, "renderJob.json")
+    info = (ctypes.c_int64 * 8)()
+    same = ctypes.c_int32()
+    native.check(native.lib().hasty_debug_wide_emit_check(0, path.encode(), info, ctypes.byref(same)))
+    assert info[0] > 0
+    assert same.value == 1, list(info)
+    assert info[7] == 1, list(info)
