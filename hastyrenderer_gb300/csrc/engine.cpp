@@ -51,7 +51,7 @@ void Engine::init(hasty_ctx* c, int64_t capacity, int slots, uint32_t segments, 
   md.next_sample = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
   md.total_samples = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
   md.regen_base = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long)));
-  md.ctl = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 8));
+  md.ctl = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * kCtlWords));
   md.regen_below = regen_below;
   md.max_iter = max_iter;
   ck(cudaMemsetAsync(d_window, 0, sizeof(uint32_t) * 2, stream), "memset");
@@ -191,6 +191,11 @@ Engine::~Engine() {
 
 int64_t engine_pool_size(int64_t requested) { return requested > 0 ? requested : (int64_t(1) << 22); }
 
+uint32_t engine_lanes(int64_t cap, uint32_t npix) {
+  int64_t l = cap / (4 * int64_t(std::max<uint32_t>(npix, 1u)));
+  return uint32_t(std::max<int64_t>(1, std::min<int64_t>(16, l)));
+}
+
 uint32_t engine_regen_threshold(float fraction, int64_t cap) {
   float f = fraction > 0.f ? fraction : 0.9f;
   if (f >= 1.0f) return uint32_t(cap) + 1u;
@@ -224,17 +229,21 @@ int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, 
     e.init(ctx, cap, int(std::max<size_t>(n_jobs, 1)), uint32_t(std::max<uint64_t>(n_segments, 1)),
            engine_regen_threshold(cfg ? cfg->regen_fraction : 0.f, cap), max_iter);
     std::vector<unsigned long long*> accs(n_jobs);
+    std::vector<uint32_t> lanes(n_jobs, 1u);
     for (size_t i = 0; i < n_jobs; ++i) {
       hasty_job* j = jobs[i];
       uint32_t npix = uint32_t(j->sd.width) * uint32_t(j->sd.height);
-      accs[i] = static_cast<unsigned long long*>(e.alloc(sizeof(unsigned long long) * 9 * size_t(npix)));
-      ck(cudaMemsetAsync(accs[i], 0, sizeof(unsigned long long) * 9 * size_t(npix), e.stream), "memset acc");
+      lanes[i] = engine_lanes(cap, npix);
+      const size_t acc_bytes = sizeof(unsigned long long) * 9 * size_t(npix) * lanes[i];
+      accs[i] = static_cast<unsigned long long*>(e.alloc(acc_bytes));
+      ck(cudaMemsetAsync(accs[i], 0, acc_bytes, e.stream), "memset acc");
       JobDev d;
       std::memset(&d, 0, sizeof(d));
       d.sc = j->sd;
       d.acc = accs[i];
       d.seed = j->seed;
       d.npix = npix;
+      d.lanes = lanes[i];
       e.set_job(int(i), d);
       // jobs in order, each job's passes in order
       for (int32_t p = 0; p < passes[i]; ++p) e.append(int(i), uint32_t(j->samples_done + p), npix);
@@ -254,6 +263,7 @@ int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, 
     // fold the fixed-point sums into each job's FP64 accumulators
     for (size_t i = 0; i < n_jobs; ++i) {
       hasty_job* j = jobs[i];
+      launch_fold_lanes(accs[i], j->sd.width * j->sd.height, int(lanes[i]), e.stream);
       launch_fixed_to_double(accs[i], j->sd.width * j->sd.height, j->acc[0], j->acc[1], j->acc[2], e.stream);
       j->samples_done += passes[i];
     }

@@ -76,6 +76,9 @@ struct Engine {
 };
 
 int64_t engine_pool_size(int64_t requested);
+// Accumulator lanes of a job of npix pixels in a pool of cap paths: about
+// four samples of a pixel in flight per lane, 1..16 lanes.
+uint32_t engine_lanes(int64_t cap, uint32_t npix);
 uint32_t engine_regen_threshold(float fraction, int64_t cap);
 
 }  // namespace hasty

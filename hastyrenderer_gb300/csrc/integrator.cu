@@ -550,15 +550,14 @@ constexpr int kCompactThreads = 256;
 constexpr int kCompactSteps = 8;
 constexpr int kCompactTile = kCompactThreads * kCompactSteps;   // slots per compaction block
 
-// Last live segment whose first sample is <= g (segments are contiguous and
-// in increasing order of `begin`).
-__device__ __forceinline__ const SegDev& find_segment(const MultiDev& m, unsigned long long g) {
-  uint32_t lo = m.seg_window[0], hi = m.seg_window[1] - 1u;
+// Logical index of the last segment in [lo, hi] whose first sample is <= g
+// (segments are contiguous and in increasing order of `begin`).
+__device__ __forceinline__ uint32_t segment_index(const MultiDev& m, unsigned long long g, uint32_t lo, uint32_t hi) {
   while (lo < hi) {
     uint32_t mid = lo + ((hi - lo + 1u) >> 1);
     if (m.segs[mid & m.seg_mask].begin <= g) lo = mid; else hi = mid - 1u;
   }
-  return m.segs[lo & m.seg_mask];
+  return lo;
 }
 
 __global__ void k_multi_init(PathsDev P, MultiDev m, int cap) {
@@ -570,7 +569,7 @@ __global__ void k_multi_init(PathsDev P, MultiDev m, int cap) {
   if (i == 0) {
     *m.free_count = uint32_t(cap);
     for (int k = 0; k < 4; ++k) P.counts[k] = 0;
-    for (int k = 0; k < 8; ++k) m.ctl[k] = 0;
+    for (int k = 0; k < kCtlWords; ++k) m.ctl[k] = 0;
   }
 }
 
@@ -583,6 +582,11 @@ __global__ void k_multi_plan(PathsDev P, MultiDev m) {
     unsigned long long left = total - next;
     uint32_t fc = *m.free_count;
     n_new = left < fc ? uint32_t(left) : fc;
+  }
+  if (n_new > 0) {   // segments this regeneration draws from: narrows every thread's search
+    uint32_t lo = segment_index(m, next, m.seg_window[0], m.seg_window[1] - 1u);
+    m.ctl[8] = lo;
+    m.ctl[9] = segment_index(m, next + n_new - 1u, lo, m.seg_window[1] - 1u);
   }
   P.counts[kSampleCount] = 0;
   m.ctl[1] = n_new;
@@ -601,7 +605,7 @@ __global__ void __launch_bounds__(256) k_multi_regen(PathsDev P, MultiDev m) {
   uint32_t q = m.ctl[0];
   int s = m.free_slots[i];        // the lowest free slots, in ascending order
   unsigned long long g = *m.regen_base + i;
-  const SegDev& seg = find_segment(m, g);
+  const SegDev& seg = m.segs[segment_index(m, g, m.ctl[8], m.ctl[9]) & m.seg_mask];
   const int j = seg.job;
   const uint32_t pass = seg.pass;
   const uint32_t px = uint32_t(g - seg.begin);
@@ -651,7 +655,8 @@ __device__ __forceinline__ void finish_multi(const PathsDev& P, const MultiDev& 
   if (finished) {
     const JobDev& job = m.jobs[j];
     if (has_nan(L)) atomicAdd(&P.stats[ST_NAN], 1ull);
-    else add_fixed(job.acc + 9 * int64_t(m.slot_px[s]), L, P.out_normal[s], P.out_albedo[s], P.stats);
+    else add_fixed(job.acc + 9 * (int64_t(m.slot_pass[s] % job.lanes) * job.npix + m.slot_px[s]), L, P.out_normal[s],
+                   P.out_albedo[s], P.stats);
     m.flags[s] = 0;
   }
   const uint32_t lane = threadIdx.x & 31u;
@@ -849,6 +854,16 @@ __global__ void k_multi_cond(PathsDev P, MultiDev m, cudaGraphConditionalHandle 
   if (use_cond) cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
+__global__ void k_fold_lanes(unsigned long long* acc, int npix, int lanes) {
+  int px = blockIdx.x * blockDim.x + threadIdx.x;
+  if (px >= npix) return;
+  for (int k = 0; k < 9; ++k) {
+    unsigned long long v = acc[9 * int64_t(px) + k];
+    for (int l = 1; l < lanes; ++l) v += acc[9 * (int64_t(l) * npix + px) + k];
+    acc[9 * int64_t(px) + k] = v;
+  }
+}
+
 __global__ void k_fixed_to_double(const unsigned long long* acc, int npix, double* c, double* n, double* a) {
   int px = blockIdx.x * blockDim.x + threadIdx.x;
   if (px >= npix) return;
@@ -880,6 +895,10 @@ void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int cap, int b
   k_compact_scan<<<1, 1024, 0, st>>>(p, m, nb);
   k_compact_scatter<<<nb, kCompactThreads, 0, st>>>(p, m, cap);
   k_multi_cond<<<1, 1, 0, st>>>(p, m, cudaGraphConditionalHandle(cond), use_cond);
+}
+
+void launch_fold_lanes(unsigned long long* acc, int npix, int lanes, cudaStream_t st) {
+  if (lanes > 1) k_fold_lanes<<<(npix + 255) / 256, 256, 0, st>>>(acc, npix, lanes);
 }
 
 void launch_fixed_to_double(const unsigned long long* acc, int npix, double* c, double* n, double* a, cudaStream_t st) {

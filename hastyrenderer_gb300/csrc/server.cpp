@@ -61,6 +61,7 @@ struct Request {
   unsigned long long* d_acc = nullptr;
   int64_t acc_bytes = 0;
   uint32_t npix = 0;
+  uint32_t lanes = 1;                 // accumulator lanes (engine_lanes)
   int32_t passes_issued = 0;
   float exposure = 0.f;
   std::vector<long long> acc;         // 9 fixed-point sums per pixel, after completion
@@ -177,7 +178,8 @@ struct hasty_server {
       int slot = -1;
       for (size_t k = 0; k < slots.size(); ++k) if (!slots[k]) { slot = int(k); break; }
       if (slot < 0) return;
-      int64_t need = int64_t(r->npix) * 9 * 8;
+      const uint32_t lanes = engine_lanes(cfg.paths_in_flight, r->npix);
+      int64_t need = int64_t(r->npix) * 9 * 8 * lanes;
       if (engine.bytes + e->bytes + need > cfg.memory_budget) {
         it = pending.erase(it);
         finish_locked(r, Request::kFailed, HASTY_ERR_MEMORY, "request does not fit the server's memory budget");
@@ -202,6 +204,7 @@ struct hasty_server {
       r->slot = slot;
       r->t_admit = now_ms();
       r->acc_bytes = need;
+      r->lanes = lanes;
       r->exposure = e->job->host.cam.exposure;
       acc_bytes += need;
       note_peak();
@@ -269,17 +272,24 @@ void hasty_server::engine_loop() {
         d.acc = r->d_acc;
         d.seed = r->seed;
         d.npix = r->npix;
+        d.lanes = r->lanes;
         engine.set_job(r->slot, d);
       }
-      // queue passes round-robin over the resident requests
+      // queue passes round-robin over the resident requests; a turn issues
+      // consecutive passes of one request up to quantum_samples camera samples
+      // (one pass at least), so small frames do not alternate pass by pass
       const size_t n = slots.size();
       while (engine.unissued() < uint64_t(cfg.lookahead_samples) && engine.free_segments() > 0) {
         bool any = false;
         for (size_t k = 0; k < n && engine.free_segments() > 0; ++k) {
           Request* r = slots[(rr + k) % n];
           if (!r || r->state != Request::kActive || r->passes_issued >= r->passes) continue;
-          engine.append(r->slot, uint32_t(r->passes_issued), r->npix);
-          r->passes_issued++;
+          int64_t turn = 0;
+          do {
+            engine.append(r->slot, uint32_t(r->passes_issued), r->npix);
+            r->passes_issued++;
+            turn += int64_t(r->npix);
+          } while (r->passes_issued < r->passes && turn < cfg.quantum_samples && engine.free_segments() > 0);
           any = true;
           if (engine.unissued() >= uint64_t(cfg.lookahead_samples)) { rr = (rr + k + 1) % n; break; }
         }
@@ -306,7 +316,9 @@ void hasty_server::engine_loop() {
         }
         for (Request* r : retire) {
           r->acc.resize(size_t(r->npix) * 9);
-          ck(cudaMemcpyAsync(r->acc.data(), r->d_acc, size_t(r->acc_bytes), cudaMemcpyDeviceToHost, engine.stream), "copy sums");
+          launch_fold_lanes(r->d_acc, int(r->npix), int(r->lanes), engine.stream);
+          ck(cudaMemcpyAsync(r->acc.data(), r->d_acc, r->acc.size() * sizeof(r->acc[0]), cudaMemcpyDeviceToHost,
+                             engine.stream), "copy sums");
           ck(cudaFreeAsync(r->d_acc, engine.stream), "cudaFreeAsync (sums)");
           r->d_acc = nullptr;
         }
@@ -448,6 +460,7 @@ void clamp_config(hasty_server_config& c) {
   if (c.memory_budget <= 0) c.memory_budget = kDefaultBudget;
   if (c.lookahead_samples <= 0) c.lookahead_samples = 4 * c.paths_in_flight;
   if (c.loader_threads <= 0) c.loader_threads = 2;
+  if (c.quantum_samples <= 0) c.quantum_samples = c.paths_in_flight / 2;
 }
 
 }  // namespace

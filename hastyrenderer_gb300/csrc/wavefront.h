@@ -86,10 +86,11 @@ constexpr double kFixedScale = 4294967296.0;   // 2^32
 
 struct JobDev {
   SceneDev sc;
-  unsigned long long* acc;     // 9 int64 per pixel: colour, normal, albedo (two's complement)
+  unsigned long long* acc;     // lanes x npix x 9 int64: colour, normal, albedo (two's complement)
   unsigned long long* done;    // finished camera samples
   uint64_t seed;
   uint32_t npix;
+  uint32_t lanes;              // a sample of pass p goes to lane p % lanes (spreads the atomics of small frames)
 };
 
 // One pass of one job: global samples [begin, begin + npix) of the job table
@@ -115,12 +116,15 @@ struct MultiDev {
   unsigned long long* next_sample;
   unsigned long long* total_samples;
   unsigned long long* regen_base;   // first global sample of the current regeneration
-  uint32_t* ctl;               // [0] queue parity, [1] regen count, [2] free-stack top before regen,
+  uint32_t* ctl;               // kCtlWords: [0] queue parity, [1] regen count, [2] unused,
                                // [3] path-queue base, [4] ray-queue base, [5] iterations, [6] bound hit,
-                               // [7] iteration at which the current wave ends
+                               // [7] iteration at which the current wave ends, [8], [9] first and last
+                               // segment (logical index) of the current regeneration
   uint32_t regen_below;        // regenerate only when fewer live paths than this
   uint32_t max_iter;           // iteration bound of one run (device-side loop guard)
 };
+
+constexpr int kCtlWords = 16;
 
 enum MultiStat { MS_RAYS = ST_RAYS, MS_SHADED = ST_SHADED, MS_PATHS = ST_PATHS, MS_NAN = ST_NAN,
                  MS_MEDIA_OVERFLOW = ST_MEDIA_OVERFLOW, MS_TRIAL_CAP = ST_TRIAL_CAP, MS_SATURATED = ST_COUNT,
@@ -134,7 +138,10 @@ void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int capacity, 
 void launch_multi_init(const PathsDev& p, const MultiDev& m, int capacity, cudaStream_t stream);
 // Compaction blocks of an engine with `capacity` slots (3 block_sums entries each).
 int compact_blocks(int capacity);
-// Adds a finished job's fixed-point sums into FP64 accumulators (sum * 2^-32).
+// Sums lanes 1.. of a job's fixed-point sums into lane 0 (integer adds:
+// exact, so the result does not depend on the lane count).
+void launch_fold_lanes(unsigned long long* acc, int npix, int lanes, cudaStream_t stream);
+// Adds a finished job's fixed-point sums (lane 0) into FP64 accumulators (sum * 2^-32).
 void launch_fixed_to_double(const unsigned long long* acc, int npix, double* c, double* n, double* a, cudaStream_t stream);
 // trace.cu: closest hit of the queued rays of the multi-job engine.
 void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t stream);

@@ -58,7 +58,8 @@ class ServerConfig(ctypes.Structure):
     _fields_ = [("paths_in_flight", ctypes.c_int64), ("regen_fraction", ctypes.c_float),
                 ("max_resident_jobs", ctypes.c_int32), ("max_resident_scenes", ctypes.c_int32),
                 ("wave_iterations", ctypes.c_int32), ("memory_budget", ctypes.c_int64),
-                ("lookahead_samples", ctypes.c_int64), ("loader_threads", ctypes.c_int32)]
+                ("lookahead_samples", ctypes.c_int64), ("loader_threads", ctypes.c_int32),
+                ("quantum_samples", ctypes.c_int64)]
 
 
 class ServerResult(ctypes.Structure):

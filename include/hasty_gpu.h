@@ -155,12 +155,15 @@ int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, 
 /* ---- Serving: a request loop over the multi-job engine ---------------------
  * Requests (a renderJob.json, a pass count, a seed) are admitted while job
  * slots and the device-memory budget allow: scene + BVH + textures of each
- * resident scene, 72 B per pixel of fixed-point sums per resident request,
- * plus the engine's path pool. Scenes are cached by scene file and shared by
+ * resident scene, 72 B per pixel and accumulator lane of fixed-point sums per
+ * resident request (1..16 lanes: about four samples of a pixel in flight per
+ * lane, so small frames do not serialise on their pixels' atomics), plus the
+ * engine's path pool. Scenes are cached by scene file and shared by
  * the requests that use them; a scene no request uses is evicted when room is
  * needed. Loader threads parse scenes and build BVHs on the host while the
- * engine renders. Resident requests' passes are interleaved round-robin in one
- * continuously running engine, so requests that arrive while others render
+ * engine renders. Resident requests' passes are interleaved round-robin (a
+ * turn issues consecutive passes of one request up to quantum_samples camera
+ * samples) in one continuously running engine, so requests that arrive while others render
  * start as soon as path slots free up. A request's result is bit-identical to
  * hasty_batch_render of the same job, seed and pass count, alone or in any mix.
  * The server's functions are internally synchronised (any host thread).
@@ -176,6 +179,7 @@ typedef struct hasty_server_config {
   int64_t memory_budget;       /* device bytes; 0 = 120 GB */
   int64_t lookahead_samples;   /* samples queued ahead of the engine; 0 = 4 x paths_in_flight */
   int32_t loader_threads;      /* 0 = 2 */
+  int64_t quantum_samples;     /* camera samples of one request's round-robin turn; 0 = paths_in_flight / 2 */
 } hasty_server_config;
 
 typedef struct hasty_server_result {
