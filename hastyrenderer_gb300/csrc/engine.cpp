@@ -25,7 +25,7 @@ void Engine::init(hasty_ctx* c, int64_t capacity, int slots, uint32_t segments, 
   if (capacity < 1 || capacity > int64_t(INT32_MAX) / 2) throw ApiError{HASTY_ERR_ARG, "bad paths-in-flight value"};
   if (slots < 1) throw ApiError{HASTY_ERR_ARG, "engine needs at least one job slot"};
   ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "stream");
-  cap = capacity;
+  cap = (capacity + kGroup - 1) / kGroup * kGroup;
   job_slots = slots;
   seg_cap = 64;
   while (seg_cap < segments) {
@@ -41,9 +41,7 @@ void Engine::init(hasty_ctx* c, int64_t capacity, int slots, uint32_t segments, 
   md.segs = d_segs;
   md.seg_mask = seg_cap - 1u;
   md.seg_window = d_window;
-  md.slot_job = static_cast<int32_t*>(alloc(sizeof(int32_t) * size_t(cap)));
-  md.slot_px = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * size_t(cap)));
-  md.slot_pass = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * size_t(cap)));
+  md.slot_meta = static_cast<uint4*>(alloc(sizeof(uint4) * size_t(cap)));
   md.free_slots = static_cast<int32_t*>(alloc(sizeof(int32_t) * size_t(cap)));
   md.flags = static_cast<uint8_t*>(alloc(size_t(cap)));
   md.block_sums = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 3 * size_t(compact_blocks(int(cap)))));
@@ -192,7 +190,11 @@ Engine::~Engine() {
 int64_t engine_pool_size(int64_t requested) { return requested > 0 ? requested : (int64_t(1) << 22); }
 
 uint32_t engine_lanes(int64_t cap, uint32_t npix) {
-  int64_t l = cap / (4 * int64_t(std::max<uint32_t>(npix, 1u)));
+  if (const char* v = std::getenv("HASTY_ENGINE_LANES")) {   // fixed lane count (tuning)
+    long l = std::strtol(v, nullptr, 10);
+    if (l >= 1 && l <= 64) return uint32_t(l);
+  }
+  int64_t l = cap / (256 * int64_t(std::max<uint32_t>(npix, 1u)));
   return uint32_t(std::max<int64_t>(1, std::min<int64_t>(16, l)));
 }
 

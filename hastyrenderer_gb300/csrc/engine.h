@@ -76,8 +76,10 @@ struct Engine {
 };
 
 int64_t engine_pool_size(int64_t requested);
-// Accumulator lanes of a job of npix pixels in a pool of cap paths: about
-// four samples of a pixel in flight per lane, 1..16 lanes.
+// Accumulator lanes of a job of npix pixels in a pool of cap paths: one lane
+// per 256 samples of a pixel that can be in flight, 1..16 lanes. Only tiny
+// frames get more than one: lanes multiply the job's accumulator footprint,
+// and sums that fall out of L2 cost more than contended atomics.
 uint32_t engine_lanes(int64_t cap, uint32_t npix);
 uint32_t engine_regen_threshold(float fraction, int64_t cap);
 

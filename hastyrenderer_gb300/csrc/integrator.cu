@@ -536,11 +536,15 @@ void launch_debug_bsdf(int which, const float* in, int n, const uint32_t* replay
 // one bounce (the same resolve_path / sample_path as the single-job kernels)
 // and record per slot whether the path lives on and which rays it queued
 // (finished samples go to their job's sums), three compaction kernels rebuild
-// the path queue, the ray queue and the free-slot list from those flags in
+// the path queue, the ray queue and the free-group list from those flags in
 // ascending slot order, and k_multi_cond flips the queue parity and sets the
 // enclosing CUDA-graph while-loop's condition. Keeping every list in slot
 // order keeps the structure-of-arrays path state accessed in dense runs
-// however often slots are recycled.
+// however often slots are recycled. New samples only go into groups of
+// kGroup slots whose paths have all ended: the 32 samples of a group are
+// adjacent pixels of one pass that start together, so a warp's paths stay at
+// one depth and write and read whole runs of path state, as in a plain batch,
+// while the pool as a whole never drains (no per-batch tail).
 namespace hasty {
 namespace {
 using namespace dev;
@@ -563,11 +567,11 @@ __device__ __forceinline__ uint32_t segment_index(const MultiDev& m, unsigned lo
 __global__ void k_multi_init(PathsDev P, MultiDev m, int cap) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < cap) {
-    m.free_slots[i] = i;          // ascending
+    if (i % kGroup == 0) m.free_slots[i / kGroup] = i;   // ascending
     m.flags[i] = 0;
   }
   if (i == 0) {
-    *m.free_count = uint32_t(cap);
+    *m.free_count = uint32_t(cap);                     // cap is a multiple of kGroup
     for (int k = 0; k < 4; ++k) P.counts[k] = 0;
     for (int k = 0; k < kCtlWords; ++k) m.ctl[k] = 0;
   }
@@ -598,22 +602,20 @@ __global__ void k_multi_plan(PathsDev P, MultiDev m) {
   *m.next_sample = next + n_new;
 }
 
-__global__ void __launch_bounds__(256) k_multi_regen(PathsDev P, MultiDev m) {
+__global__ void __launch_bounds__(256) k_multi_regen(PathsDev P, MultiDev m, const JobDev* __restrict__ jobs) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t n_new = m.ctl[1];
   if (i >= n_new) return;
   uint32_t q = m.ctl[0];
-  int s = m.free_slots[i];        // the lowest free slots, in ascending order
+  int s = m.free_slots[i / kGroup] + int(i % kGroup);   // the lowest free groups, in ascending order
   unsigned long long g = *m.regen_base + i;
   const SegDev& seg = m.segs[segment_index(m, g, m.ctl[8], m.ctl[9]) & m.seg_mask];
   const int j = seg.job;
   const uint32_t pass = seg.pass;
   const uint32_t px = uint32_t(g - seg.begin);
-  const JobDev& job = m.jobs[j];
+  const JobDev& job = jobs[j];
   const SceneDev& sc = job.sc;
-  m.slot_job[s] = j;
-  m.slot_px[s] = px;
-  m.slot_pass[s] = pass;
+  m.slot_meta[s] = make_uint4(uint32_t(j), px, pass, pass % job.lanes);
   int x = int(px % uint32_t(sc.width)), y = int(px / uint32_t(sc.width));
   Rng r; r.seed(path_key(job.seed, px, pass));
   float ox = halton(2, pass), oy = halton(3, pass);
@@ -634,8 +636,10 @@ __global__ void __launch_bounds__(256) k_multi_regen(PathsDev P, MultiDev m) {
 
 // Fixed-point addition of one finished sample (NaN radiance drops the sample
 // and its AOVs, core/src/PathTracing.cpp:132-142). Values beyond +/-2^30 are
-// clamped and counted.
-__device__ __forceinline__ void add_fixed(unsigned long long* acc, V3 L, float4 n, float4 a, unsigned long long* stats) {
+// clamped and counted. Component k of the pixel is acc[k * stride]: a warp's
+// adjacent pixels then add into adjacent words.
+__device__ __forceinline__ void add_fixed(unsigned long long* acc, int64_t stride, V3 L, float4 n, float4 a,
+                                          unsigned long long* stats) {
   float v[9] = {L.x, L.y, L.z, n.x, n.y, n.z, a.x, a.y, a.z};
   bool sat = false;
 #pragma unroll
@@ -643,7 +647,7 @@ __device__ __forceinline__ void add_fixed(unsigned long long* acc, V3 L, float4 
     float x = v[k];
     if (fabsf(x) > 1073741824.0f) { x = copysignf(1073741824.0f, x); sat = true; }
     long long qv = __float2ll_rn(x * 4294967296.0f);
-    if (qv) atomicAdd(&acc[k], (unsigned long long)qv);
+    if (qv) atomicAdd(&acc[k * stride], (unsigned long long)qv);
   }
   if (sat) atomicAdd(&stats[MS_SATURATED], 1ull);
 }
@@ -651,32 +655,37 @@ __device__ __forceinline__ void add_fixed(unsigned long long* acc, V3 L, float4 
 // A finished sample of job j: fixed-point sums of its pixel (NaN radiance is
 // dropped and counted), then the per-job finished counters, one atomic per
 // distinct job in the warp.
-__device__ __forceinline__ void finish_multi(const PathsDev& P, const MultiDev& m, bool finished, int j, int s, V3 L) {
+__device__ __forceinline__ void finish_multi(const PathsDev& P, const MultiDev& m, const JobDev* __restrict__ jobs,
+                                             bool finished, int j, int s, uint4 meta, V3 L) {
   if (finished) {
-    const JobDev& job = m.jobs[j];
+    const JobDev& job = jobs[j];
     if (has_nan(L)) atomicAdd(&P.stats[ST_NAN], 1ull);
-    else add_fixed(job.acc + 9 * (int64_t(m.slot_pass[s] % job.lanes) * job.npix + m.slot_px[s]), L, P.out_normal[s],
-                   P.out_albedo[s], P.stats);
+    else add_fixed(job.acc + int64_t(meta.w) * 9 * job.npix + meta.y, job.npix, L, P.out_normal[s], P.out_albedo[s],
+                   P.stats);
     m.flags[s] = 0;
   }
   const uint32_t lane = threadIdx.x & 31u;
   unsigned same = __match_any_sync(kFull, finished ? j : -1);
-  if (finished && (__ffs(same) - 1) == int(lane)) atomicAdd(m.jobs[j].done, (unsigned long long)__popc(same));
+  if (finished && (__ffs(same) - 1) == int(lane)) atomicAdd(jobs[j].done, (unsigned long long)__popc(same));
 }
 
-__global__ void RESOLVE_BOUNDS k_resolve_multi(PathsDev P, MultiDev m) {
+// The job table is passed as a restrict pointer of its own: no store of the
+// kernel writes it, so its scene fields are loaded once rather than again after
+// every path-state store.
+__global__ void RESOLVE_BOUNDS k_resolve_multi(PathsDev P, MultiDev m, const JobDev* __restrict__ jobs) {
   const uint32_t q = m.ctl[0];
   const uint32_t n_in = P.counts[q];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if ((i & ~31u) >= n_in) return;
   const bool valid = i < n_in;
   int s = valid ? P.pq[q][i] : 0;
-  int j = valid ? m.slot_job[s] : 0;
+  const uint4 meta = valid ? m.slot_meta[s] : make_uint4(0u, 0u, 0u, 0u);
+  const int j = int(meta.x);
   ResolveRes res;
   res.sample = false;
   res.shaded = 0;
-  if (valid) res = resolve_path(m.jobs[j].sc, P, s, path_key(m.jobs[j].seed, m.slot_px[s], m.slot_pass[s]));
-  finish_multi(P, m, valid && !res.sample, j, s, res.L);
+  if (valid) res = resolve_path(jobs[j].sc, P, s, path_key(jobs[j].seed, meta.y, meta.z));
+  finish_multi(P, m, jobs, valid && !res.sample, j, s, meta, res.L);
   const uint32_t lane = threadIdx.x & 31u;
   unsigned kb = __ballot_sync(kFull, res.sample);
   uint32_t base = 0;
@@ -687,21 +696,22 @@ __global__ void RESOLVE_BOUNDS k_resolve_multi(PathsDev P, MultiDev m) {
   if (lane == 0 && sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
 }
 
-__global__ void SAMPLE_BOUNDS k_sample_multi(PathsDev P, MultiDev m) {
+__global__ void SAMPLE_BOUNDS k_sample_multi(PathsDev P, MultiDev m, const JobDev* __restrict__ jobs) {
   const uint32_t n_in = P.counts[kSampleCount];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if ((i & ~31u) >= n_in) return;
   const bool valid = i < n_in;
   int s = valid ? P.sq[i] : 0;
-  int j = valid ? m.slot_job[s] : 0;
+  const uint4 meta = valid ? m.slot_meta[s] : make_uint4(0u, 0u, 0u, 0u);
+  const int j = int(meta.x);
   SampleRes res;
   res.keep = res.emitB = res.emitL = false;
   res.overflow = res.capped = 0;
   if (valid) {
-    res = sample_path(m.jobs[j].sc, P, s, path_key(m.jobs[j].seed, m.slot_px[s], m.slot_pass[s]));
+    res = sample_path(jobs[j].sc, P, s, path_key(jobs[j].seed, meta.y, meta.z));
     if (res.keep) m.flags[s] = uint8_t(SF_ALIVE | (res.emitB ? SF_RAY_B : 0) | (res.emitL ? SF_RAY_L : 0));
   }
-  finish_multi(P, m, valid && !res.keep, j, s, res.L);
+  finish_multi(P, m, jobs, valid && !res.keep, j, s, meta, res.L);
   const uint32_t lane = threadIdx.x & 31u;
   unsigned ob = __ballot_sync(kFull, res.overflow != 0);
   unsigned cb = __ballot_sync(kFull, res.capped != 0);
@@ -714,8 +724,8 @@ __global__ void SAMPLE_BOUNDS k_sample_multi(PathsDev P, MultiDev m) {
 // ---- ordered compaction of the slot flags ---------------------------------
 // Block b covers slots [b*kCompactTile, (b+1)*kCompactTile), step k of
 // thread t is slot b*kCompactTile + k*kCompactThreads + t, so slot order is
-// (block, step, thread) order. Counts per block: live paths, queued rays,
-// free slots.
+// (block, step, thread) order, and each warp's step is one group of kGroup
+// slots. Counts per block: live paths, queued rays, free groups.
 struct SlotFlags {
   bool in, alive, rb, rl;
 };
@@ -737,7 +747,8 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_count(MultiDev m, i
   for (int k = 0; k < kCompactSteps; ++k) {
     SlotFlags f = slot_flags(m, int64_t(blockIdx.x) * kCompactTile + k * kCompactThreads + t, cap);
     na += f.alive ? 1u : 0u;
-    nf += (f.in && !f.alive) ? 1u : 0u;
+    const bool gfree = __ballot_sync(kFull, f.alive) == 0u && __shfl_sync(kFull, f.in ? 1 : 0, 0) != 0;
+    nf += (gfree && lane == 0) ? 1u : 0u;
     nr += (f.rb ? 1u : 0u) + (f.rl ? 1u : 0u);
   }
   for (int o = 16; o > 0; o >>= 1) {
@@ -755,7 +766,8 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_count(MultiDev m, i
 }
 
 // One block: exclusive scan of the per-block counts (in place) and the
-// totals: next path-queue length, next ray-queue length, free slots.
+// totals: next path-queue length, next ray-queue length, free slots (whole
+// free groups).
 __global__ void __launch_bounds__(1024) k_compact_scan(PathsDev P, MultiDev m, int n_blocks) {
   __shared__ uint32_t s_warp[3][32];
   __shared__ uint32_t s_carry[3];
@@ -799,7 +811,7 @@ __global__ void __launch_bounds__(1024) k_compact_scan(PathsDev P, MultiDev m, i
     const uint32_t q = m.ctl[0];
     P.counts[q ^ 1] = s_carry[0];
     P.counts[2 + (q ^ 1)] = s_carry[1];
-    *m.free_count = s_carry[2];
+    *m.free_count = s_carry[2] * uint32_t(kGroup);
   }
 }
 
@@ -816,21 +828,20 @@ __global__ void __launch_bounds__(kCompactThreads) k_compact_scatter(PathsDev P,
   for (int k = 0; k < kCompactSteps; ++k) {
     const int64_t s = int64_t(blockIdx.x) * kCompactTile + k * kCompactThreads + t;
     SlotFlags f = slot_flags(m, s, cap);
-    const bool fr = f.in && !f.alive;
     const unsigned ba = __ballot_sync(kFull, f.alive);
-    const unsigned bf = __ballot_sync(kFull, fr);
+    const bool gfree = ba == 0u && __shfl_sync(kFull, f.in ? 1 : 0, 0) != 0;
     const uint32_t nr = (f.rb ? 1u : 0u) + (f.rl ? 1u : 0u);
     uint32_t rincl = nr;
     for (int o = 1; o < 32; o <<= 1) {
       uint32_t y = __shfl_up_sync(kFull, rincl, o);
       if (lane >= o) rincl += y;
     }
-    if (lane == 31) { s_w[0][warp] = __popc(ba); s_w[1][warp] = rincl; s_w[2][warp] = __popc(bf); }
+    if (lane == 31) { s_w[0][warp] = __popc(ba); s_w[1][warp] = rincl; s_w[2][warp] = gfree ? 1u : 0u; }
     __syncthreads();
     uint32_t oa = s_run[0], orr = s_run[1], of = s_run[2];
     for (int w = 0; w < warp; ++w) { oa += s_w[0][w]; orr += s_w[1][w]; of += s_w[2][w]; }
     if (f.alive) pq_out[oa + __popc(ba & below)] = int32_t(s);
-    if (fr) m.free_slots[of + __popc(bf & below)] = int32_t(s);
+    if (gfree && lane == 0) m.free_slots[of] = int32_t(s);
     uint32_t ro = orr + rincl - nr;
     if (f.rb) rq_out[ro++] = int32_t(2 * s);
     if (f.rl) rq_out[ro] = int32_t(2 * s + 1);
@@ -858,9 +869,9 @@ __global__ void k_fold_lanes(unsigned long long* acc, int npix, int lanes) {
   int px = blockIdx.x * blockDim.x + threadIdx.x;
   if (px >= npix) return;
   for (int k = 0; k < 9; ++k) {
-    unsigned long long v = acc[9 * int64_t(px) + k];
-    for (int l = 1; l < lanes; ++l) v += acc[9 * (int64_t(l) * npix + px) + k];
-    acc[9 * int64_t(px) + k] = v;
+    unsigned long long v = acc[int64_t(k) * npix + px];
+    for (int l = 1; l < lanes; ++l) v += acc[(int64_t(l) * 9 + k) * npix + px];
+    acc[int64_t(k) * npix + px] = v;
   }
 }
 
@@ -869,9 +880,9 @@ __global__ void k_fixed_to_double(const unsigned long long* acc, int npix, doubl
   if (px >= npix) return;
   const double inv = 1.0 / kFixedScale;
   for (int k = 0; k < 3; ++k) {
-    c[3 * px + k] += double((long long)acc[9 * int64_t(px) + k]) * inv;
-    n[3 * px + k] += double((long long)acc[9 * int64_t(px) + 3 + k]) * inv;
-    a[3 * px + k] += double((long long)acc[9 * int64_t(px) + 6 + k]) * inv;
+    c[3 * px + k] += double((long long)acc[int64_t(k) * npix + px]) * inv;
+    n[3 * px + k] += double((long long)acc[int64_t(3 + k) * npix + px]) * inv;
+    a[3 * px + k] += double((long long)acc[int64_t(6 + k) * npix + px]) * inv;
   }
 }
 
@@ -887,10 +898,10 @@ void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int cap, int b
                             int use_cond, cudaStream_t st) {
   const int nb = compact_blocks(cap);
   k_multi_plan<<<1, 1, 0, st>>>(p, m);
-  k_multi_regen<<<(cap + 255) / 256, 256, 0, st>>>(p, m);
+  k_multi_regen<<<(cap + 255) / 256, 256, 0, st>>>(p, m, m.jobs);
   launch_trace_multi(p, m, bvh_kind, 2 * cap, st);
-  k_resolve_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m);
-  k_sample_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m);
+  k_resolve_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m, m.jobs);
+  k_sample_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m, m.jobs);
   k_compact_count<<<nb, kCompactThreads, 0, st>>>(m, cap);
   k_compact_scan<<<1, 1024, 0, st>>>(p, m, nb);
   k_compact_scatter<<<nb, kCompactThreads, 0, st>>>(p, m, cap);

@@ -560,7 +560,7 @@ int hasty_server_read_sums(hasty_server* s, int64_t id, int aov, double* host, s
     Request* r = finished_request(s, id, aov, w, h);
     const double inv = 1.0 / kFixedScale;
     for (size_t px = 0; px < size_t(r->npix); ++px)
-      for (int c = 0; c < 3; ++c) host[3 * px + size_t(c)] = 0.0 + double(r->acc[9 * px + size_t(3 * aov + c)]) * inv;
+      for (int c = 0; c < 3; ++c) host[3 * px + size_t(c)] = 0.0 + double(r->acc[size_t(3 * aov + c) * r->npix + px]) * inv;
     return HASTY_OK;
   });
 }
@@ -575,7 +575,7 @@ int hasty_server_read(hasty_server* s, int64_t id, int aov, float* host, size_t 
     const float scale = aov == HASTY_AOV_COLOR ? std::pow(2.0f, r->exposure) : 1.0f;
     for (size_t px = 0; px < size_t(r->npix); ++px)
       for (int c = 0; c < 3; ++c) {
-        double sum = 0.0 + double(r->acc[9 * px + size_t(3 * aov + c)]) * inv;
+        double sum = 0.0 + double(r->acc[size_t(3 * aov + c) * r->npix + px]) * inv;
         host[3 * px + size_t(c)] = (float(sum) / den) * scale;
       }
     return HASTY_OK;

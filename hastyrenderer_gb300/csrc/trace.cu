@@ -457,7 +457,7 @@ __global__ void TRACE_BOUNDS k_trace_multi(PathsDev P, MultiDev m) {
   if (!kPersistent<KIND>) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
       int rid = rq[i];
-      const SceneDev& sc = m.jobs[m.slot_job[rid >> 1]].sc;
+      const SceneDev& sc = m.jobs[m.slot_meta[rid >> 1].x].sc;
       float4 o = P.ray_o[rid], d = P.ray_d[rid];
       Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
       P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
@@ -468,7 +468,7 @@ __global__ void TRACE_BOUNDS k_trace_multi(PathsDev P, MultiDev m) {
       n, &P.counts[kFetchCounter],
       [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
         rid = rq[k];
-        const SceneDev& sc = m.jobs[m.slot_job[rid >> 1]].sc;
+        const SceneDev& sc = m.jobs[m.slot_meta[rid >> 1].x].sc;
         float4 o = P.ray_o[rid], d = P.ray_d[rid];
         tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
         nodes = sc.nodes;

@@ -86,7 +86,7 @@ constexpr double kFixedScale = 4294967296.0;   // 2^32
 
 struct JobDev {
   SceneDev sc;
-  unsigned long long* acc;     // lanes x npix x 9 int64: colour, normal, albedo (two's complement)
+  unsigned long long* acc;     // [lane][9][npix] int64: colour, normal, albedo components (two's complement)
   unsigned long long* done;    // finished camera samples
   uint64_t seed;
   uint32_t npix;
@@ -106,10 +106,10 @@ struct MultiDev {
   const SegDev* segs;          // ring of segments, power-of-two capacity
   uint32_t seg_mask;
   const uint32_t* seg_window;  // [lo, hi): logical indices of the live segments (device-resident)
-  int32_t* slot_job;           // job of the path in each slot
-  uint32_t* slot_px;           // pixel of the path's camera sample
-  uint32_t* slot_pass;         // pass of the path's camera sample
-  int32_t* free_slots;         // free slot ids in ascending order (rebuilt every iteration)
+  uint4* slot_meta;            // per slot: job, pixel and pass of the path's camera sample, accumulator
+                               // lane (one 16-byte load in the shading kernels)
+  int32_t* free_slots;         // first slot of each free group (kGroup slots, no live path), ascending
+                               // (rebuilt every iteration)
   uint8_t* flags;              // per slot: path lives on / BSDF ray queued / light ray queued
   uint32_t* block_sums;        // 3 per compaction block: counts, then exclusive offsets
   uint32_t* free_count;
@@ -125,6 +125,8 @@ struct MultiDev {
 };
 
 constexpr int kCtlWords = 16;
+constexpr int kGroup = 32;     // slots regenerated together (one warp); the engine's capacity is a multiple
+static_assert(kGroup == 32, "a group is one warp of the compaction kernels");
 
 enum MultiStat { MS_RAYS = ST_RAYS, MS_SHADED = ST_SHADED, MS_PATHS = ST_PATHS, MS_NAN = ST_NAN,
                  MS_MEDIA_OVERFLOW = ST_MEDIA_OVERFLOW, MS_TRIAL_CAP = ST_TRIAL_CAP, MS_SATURATED = ST_COUNT,

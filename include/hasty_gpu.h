@@ -156,9 +156,9 @@ int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, 
  * Requests (a renderJob.json, a pass count, a seed) are admitted while job
  * slots and the device-memory budget allow: scene + BVH + textures of each
  * resident scene, 72 B per pixel and accumulator lane of fixed-point sums per
- * resident request (1..16 lanes: about four samples of a pixel in flight per
- * lane, so small frames do not serialise on their pixels' atomics), plus the
- * engine's path pool. Scenes are cached by scene file and shared by
+ * resident request (one lane per 256 samples of a pixel that can be in
+ * flight, 1..16: only tiny frames get several, so their pixels' atomics do not
+ * serialise), plus the engine's path pool. Scenes are cached by scene file and shared by
  * the requests that use them; a scene no request uses is evicted when room is
  * needed. Loader threads parse scenes and build BVHs on the host while the
  * engine renders. Resident requests' passes are interleaved round-robin (a
