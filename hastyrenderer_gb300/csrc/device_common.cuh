@@ -411,7 +411,11 @@ __device__ __forceinline__ float mat_scalar(const SceneDev& sc, float val, int t
 // BRDF.cpp:589-603
 __device__ __forceinline__ float mat_ior(const MaterialDev& m, int wl) {
   if (!m.vary_ior) return m.ior;
-  if (wl >= 0 && wl < 3) return m.ior_band[wl];    // precomputed on the host (MaterialDev::ior_band)
+  // precomputed on the host (MaterialDev::ior_band); selected with constant
+  // indices so that a material copy can stay in registers
+  if (wl == 0) return m.ior_band[0];
+  if (wl == 1) return m.ior_band[1];
+  if (wl == 2) return m.ior_band[2];
   return __int_as_float(0x7fc00000);
 }
 // BRDF.cpp:604-628

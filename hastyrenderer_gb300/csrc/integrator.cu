@@ -37,34 +37,61 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t cnt
 
 // Medium stack of one path (LightRayInfo, core/src/LightRayInfo.cpp:8-126),
 // bounded to kMaxMedia entries; a push beyond that is dropped and counted.
+// Medium stack of a path, read and updated in place in the path state
+// (P.med / P.med_geom, kMaxMedia entries per slot): only the depth n is held
+// in a register, so paths outside any medium never touch the stack.
 struct Media {
   int n;
-  V3 T[kMaxMedia];
-  float ior[kMaxMedia];
-  int geom[kMaxMedia];
-  __device__ V3 transmittance() const { return n > 0 ? T[0] : V3(1.f, 1.f, 1.f); }
+  float4* med;
+  int32_t* geom;
+  __device__ Media(const PathsDev& P, int s, int count)
+      : n(count), med(P.med + kMaxMedia * int64_t(s)), geom(P.med_geom + kMaxMedia * int64_t(s)) {}
+  // first entry of medium g, -1 when absent
+  __device__ int find(int g) const {
+    for (int i = 0; i < n; ++i) if (geom[i] == g) return i;
+    return -1;
+  }
+  __device__ V3 T(int k) const { return xyz(med[k]); }
+  __device__ V3 transmittance() const { return n > 0 ? T(0) : V3(1.f, 1.f, 1.f); }
   __device__ float outside_ior(const Inter& it, V3 wfrom) const {
     if (dot(wfrom, it.ng) < 0.0f) {
-      int idx = -1;
-      for (int i = 0; i < n; ++i) if (geom[i] == int(it.geom)) { idx = i; break; }
+      int idx = find(int(it.geom));
       if (idx == -1 || n == 1) return 1.0f;
-      return idx == 0 ? ior[1] : ior[0];
+      return idx == 0 ? med[1].w : med[0].w;
     }
-    return n == 0 ? 1.0f : ior[0];
+    return n == 0 ? 1.0f : med[0].w;
   }
-  // returns 1 when a push overflowed
+  // Transmittance() of the stack that update(sc, m, it, wfrom, wto, wl)
+  // would leave, without changing it (the light sample's stack is only
+  // needed for that); overflow as update's return value.
+  __device__ V3 transmittance_after(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wfrom, V3 wto,
+                                    int& overflow) const {
+    float nf = dot(it.ng, wfrom), nt = dot(it.ng, wto);
+    if (nf >= 0.0f && nt < 0.0f) {
+      if (n >= kMaxMedia) { overflow = 1; return T(0); }
+      return n == 0 ? mat_albedo(sc, m, it) : T(0);
+    }
+    if (nf < 0.0f && nt >= 0.0f) {
+      int idx = find(int(it.geom));
+      if (idx > 0) return T(0);
+      if (idx == 0) return n > 1 ? T(1) : V3(1.f, 1.f, 1.f);
+    }
+    return transmittance();
+  }
+  // Push or pop for a direction change at `it` (in place); returns 1 when a
+  // push overflowed.
   __device__ int update(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wfrom, V3 wto, int wl) {
     float nf = dot(it.ng, wfrom), nt = dot(it.ng, wto);
     if (nf >= 0.0f && nt < 0.0f) {
       if (n >= kMaxMedia) return 1;
-      T[n] = mat_albedo(sc, m, it); ior[n] = mat_ior(m, wl); geom[n] = int(it.geom); ++n;
+      med[n] = f4(mat_albedo(sc, m, it), mat_ior(m, wl));
+      geom[n] = int(it.geom);
+      ++n;
     } else if (nf < 0.0f && nt >= 0.0f) {
-      for (int i = 0; i < n; ++i) {
-        if (geom[i] == int(it.geom)) {
-          for (int j = i; j < n - 1; ++j) { T[j] = T[j + 1]; ior[j] = ior[j + 1]; geom[j] = geom[j + 1]; }
-          --n;
-          break;
-        }
+      int idx = find(int(it.geom));
+      if (idx >= 0) {
+        for (int j = idx; j < n - 1; ++j) { med[j] = med[j + 1]; geom[j] = geom[j + 1]; }
+        --n;
       }
     }
     return 0;
@@ -198,9 +225,8 @@ __device__ __forceinline__ ResolveRes resolve_path(const SceneDev& sc, const Pat
     }
     if (!done && depth >= sc.max_depth) done = true;
     if (!done) {
-      Media M; M.n = int((flags & PF_NMED_MASK) >> PF_NMED_SHIFT);
-      for (int k = 0; k < M.n; ++k) { float4 m4 = P.med[4 * s + k]; M.T[k] = xyz(m4); M.ior[k] = m4.w; M.geom[k] = P.med_geom[4 * s + k]; }
-      V3 Tp = M.transmittance();
+      // transmittance of the medium stack: its first entry (Media::transmittance)
+      V3 Tp = (flags & PF_NMED_MASK) ? xyz(P.med[4 * int64_t(s)]) : V3(1.f, 1.f, 1.f);
       if (htri < 0) {                              // miss: PathTracing.cpp:86-94
         V3 Le = cwise(beers(Tp, 1e6f), env_eval(sc, d));
         L = L + cwise(thr, Le);
@@ -208,7 +234,7 @@ __device__ __forceinline__ ResolveRes resolve_path(const SceneDev& sc, const Pat
         done = true;
       } else {
         if (!have_it) it = inter_from_hit(sc, htri, h.y, h.z);
-        const MaterialDev m = sc.mats[it.mat];
+        const MaterialDev& m = sc.mats[it.mat];
         if (depth == 0) { P.out_normal[s] = f4(it.ns, 0.f); P.out_albedo[s] = f4(mat_albedo(sc, m, it), 0.f); }
         V3 tl = beers(Tp, norm(it.x - o));
         if (m.is_light) {                          // PathTracing.cpp:38-41
@@ -252,11 +278,10 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
   Inter it;
   V3 tl;
   load_vertex(P, s, it, tl);
-  const MaterialDev m = sc.mats[it.mat];
+  const MaterialDev& m = sc.mats[it.mat];
   const V3 thr = xyz(P.thr[s]);
   const V3 d = xyz(P.ray_d[2 * s]);
-  Media M; M.n = int((flags & PF_NMED_MASK) >> PF_NMED_SHIFT);
-  for (int k = 0; k < M.n; ++k) { float4 m4 = P.med[4 * s + k]; M.T[k] = xyz(m4); M.ior[k] = m4.w; M.geom[k] = P.med_geom[4 * s + k]; }
+  Media M(P, s, int((flags & PF_NMED_MASK) >> PF_NMED_SHIFT));
   Rng r; r.inc = Rng::inc_of(key); r.state = P.rng[s];
   V3 wo = -d;
   const ShadeCtx cx = shade_ctx(sc, m, it, wo);
@@ -285,10 +310,11 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
       V3 c3 = cwise(tl, ev.fD + ev.fC) * fabsf(dot(dL, it.ng));
       if (!is_zero(c3)) {
         float pBL = bsdf_pdf(cx, m, wo, dL, eta_out);
-        Media ML = M;
-        overflow |= ML.update(sc, m, it, wo, dL, wl);
+        int ovL = 0;
+        const V3 TL = M.transmittance_after(sc, m, it, wo, dL, ovL);
+        overflow |= ovL;
         P.nee_c[s] = f4(cwise(thr, c3), pBL);
-        P.nee_t[s] = f4(ML.transmittance(), __int_as_float(ltri));
+        P.nee_t[s] = f4(TL, __int_as_float(ltri));
         P.ray_o[2 * s + 1] = f4(oL, 0.f);
         P.ray_d[2 * s + 1] = f4(dL, 0.f);
         emitL = true;
@@ -312,7 +338,6 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
       P.pend_b[s] = f4(t2, __int_as_float(it.tri));
       P.ray_o[2 * s] = f4(ray_x(it, bs.outside), 0.f);
       P.ray_d[2 * s] = f4(bs.dir, 0.f);
-      for (int k = 0; k < M.n; ++k) { P.med[4 * s + k] = f4(M.T[k], M.ior[k]); P.med_geom[4 * s + k] = M.geom[k]; }
       emitB = true;
     }
   }
