@@ -246,6 +246,34 @@ HDI float byte_float(uint32_t w, uint32_t k) {
 
 // Same contract as TravBinary: a step tests the pending triangle group and
 // opens one node.
+// Per-node, per-axis terms of the child slab test t = fma(q, a, b). A child
+// plane is x = fma(q, s, p0) rounded once (the float plane the layout writer
+// makes conservative), and the exact test computes t_old = ((x - o) * inv)
+// with two roundings: t_old = T (1 + th), |th| <= gamma(3), T = (x - o) inv
+// taken exactly, which the kPadLo / kPadHi factors absorb. Here a = s * inv
+// is exact (s is a power of two) and b = (p0 - o) * inv, so
+//   fma(q, a, b) = T (1 + th'), |th'| <= gamma(2),  plus  R,
+//   |R| <= u |inv| (|p0| + 255 s + 2 |p0 - o|) (1 + 4u),  u = 2^-24,
+// R coming from x's own rounding (which this form skips) and from b's two
+// roundings. eps = 2^-22 |inv| (|p0| + 256 s + 2 |p0 - o|) + 1e-37 covers R
+// and the rounding of b -/+ eps with a factor of two to spare (the constant
+// covers products in the subnormal range); near planes use b - eps and far
+// planes b + eps, so each near value is at most, and each far value at
+// least, a value t_old can take: the test culls nothing the exact one keeps.
+// (Coordinates and grid steps are assumed below 2^120, far beyond any scene.)
+struct PlaneTerms { float a, b_near, b_far; };
+HDI PlaneTerms plane_terms(float p0, float o, float inv, float s) {
+  PlaneTerms t;
+  const float d = subr(p0, o);
+  const float b = mulr(d, inv);
+  const float mag = fmaf(2.0f, fabsf(d), fmaf(256.0f, s, fabsf(p0)));
+  const float eps = fmaf(mulr(mag, fabsf(inv)), 2.384185791015625e-07f, 1e-37f);   // 2^-22
+  t.a = mulr(s, inv);
+  t.b_near = subr(b, eps);
+  t.b_far = addr(b, eps);
+  return t;
+}
+
 struct TravWide {
   using Entry = uint2;
   static constexpr int kDepth = kWideStack;
@@ -296,6 +324,11 @@ struct TravWide {
     int ex = int(int8_t(eword & 0xFFu)), ey = int(int8_t((eword >> 8) & 0xFFu)), ez = int(int8_t((eword >> 16) & 0xFFu));
     uint32_t node_imask = eword >> 24;
     float sx = u2f(uint32_t(ex + 127) << 23), sy = u2f(uint32_t(ey + 127) << 23), sz = u2f(uint32_t(ez + 127) << 23);
+    // Child plane t = q * A + B per axis (one FMA per plane), A = 2^e * inv
+    // (exact), B = (p0 - o) * inv moved by eps to the conservative side.
+    const PlaneTerms px = plane_terms(f0.x, ox, iv.ix, sx);
+    const PlaneTerms py = plane_terms(f0.y, oy, iv.iy, sy);
+    const PlaneTerms pz = plane_terms(f0.z, oz, iv.iz, sz);
     uint32_t child_base = f2u(f1.x), tri_base = f2u(f1.y);
     uint32_t meta_w[2] = {f2u(f1.z), f2u(f1.w)};
     // near and far planes per axis, chosen once by the ray's direction sign
@@ -316,12 +349,12 @@ struct TravWide {
       uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
 #pragma unroll
       for (uint32_t k = 0; k < 4; ++k) {
-        float tnx = slab(fmaf(byte_float(nx[h], k), sx, f0.x), ox, iv.ix);
-        float tfx = slab(fmaf(byte_float(fx[h], k), sx, f0.x), ox, iv.ix);
-        float tny = slab(fmaf(byte_float(ny[h], k), sy, f0.y), oy, iv.iy);
-        float tfy = slab(fmaf(byte_float(fy[h], k), sy, f0.y), oy, iv.iy);
-        float tnz = slab(fmaf(byte_float(nz[h], k), sz, f0.z), oz, iv.iz);
-        float tfz = slab(fmaf(byte_float(fz[h], k), sz, f0.z), oz, iv.iz);
+        float tnx = fmaf(byte_float(nx[h], k), px.a, px.b_near);
+        float tfx = fmaf(byte_float(fx[h], k), px.a, px.b_far);
+        float tny = fmaf(byte_float(ny[h], k), py.a, py.b_near);
+        float tfy = fmaf(byte_float(fy[h], k), py.a, py.b_far);
+        float tnz = fmaf(byte_float(nz[h], k), pz.a, pz.b_near);
+        float tfz = fmaf(byte_float(fz[h], k), pz.a, pz.b_far);
         float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f)) * kPadLo;
         float tmax = fminf(fminf(fminf(tfx, tfy), tfz) * kPadHi, tlim);
         if (tmin <= tmax) hitmask |= byte_of(child_bits4, k) << byte_of(bit_index4, k);
