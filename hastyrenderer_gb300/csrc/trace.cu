@@ -8,8 +8,11 @@
 // and the chosen triangle are the ones the CPU checker computes. The far
 // limit is applied to the divided distance and ties at equal t go to the
 // smaller triangle id, so the answer does not depend on traversal order.
-// Box tests round each step once and are padded by 1 +/- 2*gamma(3), so no
-// box that holds the closest hit is culled by rounding (Ize 2013).
+// Binary-BVH box tests round each step once and are padded by
+// 1 +/- 2*gamma(3), so no box that holds the closest hit is culled by
+// rounding (Ize 2013); the wide BVH's one-FMA child planes carry an absolute
+// error bound instead (plane_terms). The far limit at the current closest
+// hit is padded by 1 + 2*gamma(3) in both.
 //
 // The traversal routines are host+device: the host build runs the same code
 // on the CPU for the loader/builder tests (hasty_debug_host_trace).
@@ -248,25 +251,25 @@ HDI float byte_float(uint32_t w, uint32_t k) {
 // opens one node.
 // Per-node, per-axis terms of the child slab test t = fma(q, a, b). A child
 // plane is x = fma(q, s, p0) rounded once (the float plane the layout writer
-// makes conservative), and the exact test computes t_old = ((x - o) * inv)
-// with two roundings: t_old = T (1 + th), |th| <= gamma(3), T = (x - o) inv
-// taken exactly, which the kPadLo / kPadHi factors absorb. Here a = s * inv
-// is exact (s is a power of two) and b = (p0 - o) * inv, so
-//   fma(q, a, b) = T (1 + th'), |th'| <= gamma(2),  plus  R,
+// makes conservative); the slab parameter is T = (x - o) / d. Here a = s * inv
+// is exact (s is a power of two, inv = fl(1/d)) and b = (p0 - o) * inv, so
+//   fma(q, a, b) = T (1 + th), |th| <= gamma(2),  plus  R,
 //   |R| <= u |inv| (|p0| + 255 s + 2 |p0 - o|) (1 + 4u),  u = 2^-24,
 // R coming from x's own rounding (which this form skips) and from b's two
-// roundings. eps = 2^-22 |inv| (|p0| + 256 s + 2 |p0 - o|) + 1e-37 covers R
-// and the rounding of b -/+ eps with a factor of two to spare (the constant
-// covers products in the subnormal range); near planes use b - eps and far
-// planes b + eps, so each near value is at most, and each far value at
-// least, a value t_old can take: the test culls nothing the exact one keeps.
+// roundings; and |T| <= (|p0 - o| + 255 s) |inv| (1 + u). With the rounding
+// of b -/+ eps, the total error is below u |inv| (|p0| + 765 s + 5 |p0 - o|)
+// to first order; eps = 2^-22 |inv| (|p0| + 1024 s + 6 |p0 - o|) + 1e-37
+// covers it at least twice over (the constant covers products in the
+// subnormal range). Near planes use b - eps and far planes b + eps, so each
+// near value is at most, and each far value at least, the exact T: the box
+// test needs no further padding and culls no box the ray enters.
 // (Coordinates and grid steps are assumed below 2^120, far beyond any scene.)
 struct PlaneTerms { float a, b_near, b_far; };
 HDI PlaneTerms plane_terms(float p0, float o, float inv, float s) {
   PlaneTerms t;
   const float d = subr(p0, o);
   const float b = mulr(d, inv);
-  const float mag = fmaf(2.0f, fabsf(d), fmaf(256.0f, s, fabsf(p0)));
+  const float mag = fmaf(6.0f, fabsf(d), fmaf(1024.0f, s, fabsf(p0)));
   const float eps = fmaf(mulr(mag, fabsf(inv)), 2.384185791015625e-07f, 1e-37f);   // 2^-22
   t.a = mulr(s, inv);
   t.b_near = subr(b, eps);
@@ -355,8 +358,8 @@ struct TravWide {
         float tfy = fmaf(byte_float(fy[h], k), py.a, py.b_far);
         float tnz = fmaf(byte_float(nz[h], k), pz.a, pz.b_near);
         float tfz = fmaf(byte_float(fz[h], k), pz.a, pz.b_far);
-        float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f)) * kPadLo;
-        float tmax = fminf(fminf(fminf(tfx, tfy), tfz) * kPadHi, tlim);
+        float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+        float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
         if (tmin <= tmax) hitmask |= byte_of(child_bits4, k) << byte_of(bit_index4, k);
       }
     }
