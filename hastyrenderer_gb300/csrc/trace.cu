@@ -237,13 +237,13 @@ constexpr int kWideStack = 32;
 
 HDI uint32_t byte_of(uint32_t w, uint32_t k) { return (w >> (8 * k)) & 0xFFu; }
 
-// Byte k of w as a float, exactly: the byte is placed in the mantissa of
-// 2^23 by one byte permute and 2^23 is subtracted (exact for 0..255).
-HDI float byte_float(uint32_t w, uint32_t k) {
+// 2^23 + byte k of w as a float, exactly: one byte permute places the byte
+// in the mantissa of 2^23 (the offset is folded into the planes' b terms).
+HDI float byte_biased(uint32_t w, uint32_t k) {
 #ifdef __CUDA_ARCH__
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, k | 0x7540u)) - 8388608.0f;
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, k | 0x7540u));
 #else
-  return float(byte_of(w, k));
+  return 8388608.0f + float(byte_of(w, k));
 #endif
 }
 
@@ -272,8 +272,16 @@ HDI PlaneTerms plane_terms(float p0, float o, float inv, float s) {
   const float mag = fmaf(6.0f, fabsf(d), fmaf(1024.0f, s, fabsf(p0)));
   const float eps = fmaf(mulr(mag, fabsf(inv)), 2.384185791015625e-07f, 1e-37f);   // 2^-22
   t.a = mulr(s, inv);
-  t.b_near = subr(b, eps);
-  t.b_far = addr(b, eps);
+  // The child loop evaluates fma(2^23 + q, a, b') with b' = b -/+ eps - 2^23 a
+  // (2^23 a is exact; the FMA forms (2^23 + q) a exactly). The one extra
+  // rounding, of b' itself, is at most u (2^23 |a| + |b| + eps) = s |inv| / 2
+  // + u (|b| + eps): half a grid step, added to eps with a relative margin
+  // of 1e-6; the u |b| part is inside eps's factor-two margin.
+  const float half = mulr(mulr(0.5000005f, s), fabsf(inv));
+  const float e = addr(eps, half);
+  const float a23 = mulr(-8388608.0f, t.a);
+  t.b_near = addr(subr(b, e), a23);
+  t.b_far = addr(addr(b, e), a23);
   return t;
 }
 
@@ -352,12 +360,12 @@ struct TravWide {
       uint32_t child_bits4 = (meta4 >> 5) & 0x07070707u;
 #pragma unroll
       for (uint32_t k = 0; k < 4; ++k) {
-        float tnx = fmaf(byte_float(nx[h], k), px.a, px.b_near);
-        float tfx = fmaf(byte_float(fx[h], k), px.a, px.b_far);
-        float tny = fmaf(byte_float(ny[h], k), py.a, py.b_near);
-        float tfy = fmaf(byte_float(fy[h], k), py.a, py.b_far);
-        float tnz = fmaf(byte_float(nz[h], k), pz.a, pz.b_near);
-        float tfz = fmaf(byte_float(fz[h], k), pz.a, pz.b_far);
+        float tnx = fmaf(byte_biased(nx[h], k), px.a, px.b_near);
+        float tfx = fmaf(byte_biased(fx[h], k), px.a, px.b_far);
+        float tny = fmaf(byte_biased(ny[h], k), py.a, py.b_near);
+        float tfy = fmaf(byte_biased(fy[h], k), py.a, py.b_far);
+        float tnz = fmaf(byte_biased(nz[h], k), pz.a, pz.b_near);
+        float tfz = fmaf(byte_biased(fz[h], k), pz.a, pz.b_far);
         float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
         float tmax = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
         if (tmin <= tmax) hitmask |= byte_of(child_bits4, k) << byte_of(bit_index4, k);
