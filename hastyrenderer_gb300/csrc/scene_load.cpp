@@ -3,6 +3,8 @@
 #include "scene_load.h"
 
 #include <algorithm>
+#include <cctype>
+#include <charconv>
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
@@ -12,6 +14,7 @@
 #include <map>
 #include <memory>
 #include <sstream>
+#include <thread>
 #include <unordered_map>
 
 namespace hasty {
@@ -109,10 +112,18 @@ class JReader {
 };
 
 std::string slurp(const std::string& path) {
-  std::ifstream f(path, std::ios::binary);
-  if (!f) throw LoadError("could not open " + path + " for reading");
-  std::ostringstream ss; ss << f.rdbuf();
-  return ss.str();
+  std::FILE* fp = std::fopen(path.c_str(), "rb");
+  if (!fp) throw LoadError("could not open " + path + " for reading");
+  std::string data;
+  long size = std::fseek(fp, 0, SEEK_END) == 0 ? std::ftell(fp) : -1;
+  if (size > 0 && std::fseek(fp, 0, SEEK_SET) == 0) {
+    data.resize(size_t(size));
+    data.resize(std::fread(&data[0], 1, size_t(size), fp));
+  }
+  char chunk[1 << 16];     // whatever follows (or a stream without a size)
+  for (size_t got; (got = std::fread(chunk, 1, sizeof(chunk), fp)) > 0;) data.append(chunk, got);
+  std::fclose(fp);
+  return data;
 }
 JNode read_json(const std::string& path) { return JReader(slurp(path)).parse(); }
 
@@ -222,10 +233,22 @@ std::string word(const char*& s) {
   while (*s && *s != ' ' && *s != '\t' && *s != '\r' && *s != '\n') ++s;
   return std::string(b, s);
 }
+// A number as strtof reads it. Plain decimals go through std::from_chars
+// (also correctly rounded, so the same float, but several times faster);
+// the forms where the two differ (a leading '+' or extra whitespace, hex,
+// out-of-range values) take strtof itself.
 float num(const char*& s) {
-  s = ws(s); char* e = nullptr; float f = std::strtof(s, &e);
-  if (e == s) return 0.0f;
-  s = e; return f;
+  s = ws(s);
+  const char* e = s;
+  while (*e && !std::isspace(static_cast<unsigned char>(*e))) ++e;
+  if (e > s && *s != '+') {
+    float f = 0.0f;
+    std::from_chars_result r = std::from_chars(s, e, f);
+    if (r.ec == std::errc() && *r.ptr != 'x' && *r.ptr != 'X') { s = r.ptr; return f; }
+  }
+  char* se = nullptr; float f = std::strtof(s, &se);
+  if (se == s) return 0.0f;
+  s = se; return f;
 }
 void num3(const char*& s, float* o) { for (int i = 0; i < 3; ++i) o[i] = num(s); }
 std::string last_word(const char* s) { std::string l; for (std::string t = word(s); !t.empty(); t = word(s)) l = t; return l; }
@@ -264,59 +287,175 @@ int rel_index(long idx, size_t count) {
   return -1;
 }
 
-ObjFile read_obj(const std::string& path, const std::string& mtl_dir) {
-  std::ifstream f(path);
-  if (!f) throw LoadError("TinyObjReader error Cannot open file [" + path + "]");
+// One chunk of an OBJ file, parsed on its own thread. Faces keep their raw
+// indices (0 where absent, which resolves to -1 like an index of 0) and the
+// chunk-local v/vt/vn counts at the face, so that relative (negative) indices
+// can be resolved once the counts of the earlier chunks are known.
+// Directives are kept in order with the number of faces before them.
+struct ObjChunk {
+  std::vector<float> v, vn, vt;
+  struct Face { uint32_t first, n, lv, lvt, lvn; };
+  struct RawCorner { long v, vt, vn; };
+  std::vector<Face> faces;
+  std::vector<RawCorner> corners;
+  enum Kind { kFlush, kUseMtl, kMtlLib, kSmooth };
+  struct Directive { size_t face_pos; Kind kind; std::string arg; uint32_t sg; };
+  std::vector<Directive> directives;
+};
+
+// The line-by-line grammar of the reader, applied to the lines in
+// [begin, end) (whole lines). Each line is copied to a NUL-terminated buffer
+// first, so the scanning functions see exactly what a getline would give.
+void parse_obj_lines(const char* begin, const char* end, ObjChunk& c) {
+  std::string line;
+  const char* p = begin;
+  while (p < end) {
+    const char* le = static_cast<const char*>(std::memchr(p, '\n', size_t(end - p)));
+    if (!le) le = end;
+    line.assign(p, le);
+    p = le < end ? le + 1 : end;
+    char* s0 = &line[0];
+    const char* s = ws(s0);
+    if (!*s || *s == '#') continue;
+    if (s[0] == 'v' && (s[1] == ' ' || s[1] == '\t')) { s += 1; for (int i = 0; i < 3; ++i) c.v.push_back(num(s)); continue; }
+    if (s[0] == 'v' && s[1] == 'n' && (s[2] == ' ' || s[2] == '\t')) { s += 2; for (int i = 0; i < 3; ++i) c.vn.push_back(num(s)); continue; }
+    if (s[0] == 'v' && s[1] == 't' && (s[2] == ' ' || s[2] == '\t')) { s += 2; c.vt.push_back(num(s)); c.vt.push_back(num(s)); continue; }
+    if (s[0] == 'f' && (s[1] == ' ' || s[1] == '\t')) {
+      ObjChunk::Face f;
+      f.first = uint32_t(c.corners.size());
+      f.lv = uint32_t(c.v.size() / 3); f.lvt = uint32_t(c.vt.size() / 2); f.lvn = uint32_t(c.vn.size() / 3);
+      char* q0 = s0 + (s - s0) + 1;
+      for (;;) {
+        // token = next run of non-blank characters, NUL-terminated in place
+        while (*q0 == ' ' || *q0 == '\t') ++q0;
+        char* te = q0;
+        while (*te && *te != ' ' && *te != '\t' && *te != '\r' && *te != '\n') ++te;
+        if (te == q0) break;
+        const char saved = *te;
+        *te = '\0';
+        ObjChunk::RawCorner rc{0, 0, 0};
+        const char* q = q0;
+        char* e = nullptr;
+        rc.v = std::strtol(q, &e, 10);
+        if (*e == '/') {
+          q = e + 1;
+          if (*q != '/') { long b = std::strtol(q, &e, 10); if (e != q) rc.vt = b; q = e; }
+          if (*q == '/') { ++q; long cc = std::strtol(q, &e, 10); if (e != q) rc.vn = cc; }
+        }
+        c.corners.push_back(rc);
+        *te = saved;
+        q0 = te;
+      }
+      f.n = uint32_t(c.corners.size()) - f.first;
+      c.faces.push_back(f);
+      continue;
+    }
+    std::string k = word(s);
+    ObjChunk::Directive d{c.faces.size(), ObjChunk::kFlush, std::string(), 0u};
+    if (k == "o" || k == "g") { c.directives.push_back(d); }
+    else if (k == "usemtl") { d.kind = ObjChunk::kUseMtl; d.arg = word(s); c.directives.push_back(d); }
+    else if (k == "mtllib") { d.kind = ObjChunk::kMtlLib; d.arg = word(s); c.directives.push_back(d); }
+    else if (k == "s") {
+      std::string v = word(s);
+      d.kind = ObjChunk::kSmooth;
+      d.sg = v == "off" ? 0u : uint32_t(std::strtoul(v.c_str(), nullptr, 10));
+      c.directives.push_back(d);
+    }
+  }
+}
+
+// Wavefront OBJ with tinyobjloader's conventions (the reference's reader):
+// polygons are fanned, quads split along the shorter diagonal, shapes cut at
+// o/g, usemtl by name in the mtllib libraries read so far. The file is read
+// at once and its lines are parsed on all host threads in chunks; a
+// sequential merge then resolves indices and assembles shapes in file order,
+// so the result is the one a single pass over the lines gives.
+ObjFile read_obj(const std::string& path, const std::string& mtl_dir, size_t force_chunks = 0) {
+  std::string buf;
+  try {
+    buf = slurp(path);
+  } catch (const LoadError&) {
+    throw LoadError("TinyObjReader error Cannot open file [" + path + "]");
+  }
+  const char* b0 = buf.data();
+  const char* b1 = b0 + buf.size();
+  unsigned hw = std::thread::hardware_concurrency();
+  size_t n_chunks = std::max<size_t>(1, std::min<size_t>(hw ? hw : 4, buf.size() / (1u << 20) + 1));
+  n_chunks = std::min<size_t>(n_chunks, 64);
+  if (force_chunks) n_chunks = force_chunks;
+  std::vector<const char*> cut(n_chunks + 1, b1);
+  cut[0] = b0;
+  for (size_t k = 1; k < n_chunks; ++k) {
+    const char* t = b0 + buf.size() * k / n_chunks;
+    if (t < cut[k - 1]) t = cut[k - 1];
+    const char* nl = static_cast<const char*>(std::memchr(t, '\n', size_t(b1 - t)));
+    cut[k] = nl ? nl + 1 : b1;
+  }
+  std::vector<ObjChunk> chunks(n_chunks);
+  {
+    std::vector<std::thread> th;
+    for (size_t k = 1; k < n_chunks; ++k) th.emplace_back(parse_obj_lines, cut[k], cut[k + 1], std::ref(chunks[k]));
+    parse_obj_lines(cut[0], cut[1], chunks[0]);
+    for (std::thread& t : th) t.join();
+  }
   ObjFile o;
+  size_t nv = 0, nvn = 0, nvt = 0;
+  for (const ObjChunk& c : chunks) { nv += c.v.size(); nvn += c.vn.size(); nvt += c.vt.size(); }
+  o.v.reserve(nv); o.vn.reserve(nvn); o.vt.reserve(nvt);
+  for (const ObjChunk& c : chunks) {
+    o.v.insert(o.v.end(), c.v.begin(), c.v.end());
+    o.vn.insert(o.vn.end(), c.vn.begin(), c.vn.end());
+    o.vt.insert(o.vt.end(), c.vt.begin(), c.vt.end());
+  }
   std::map<std::string, int> mindex;
   ObjShapeRec cur;
   int mat = -1; uint32_t sg = 0;
   auto flush = [&]() { if (!cur.corners.empty()) o.shapes.push_back(std::move(cur)); cur = ObjShapeRec(); };
-  std::string line;
+  auto apply = [&](const ObjChunk::Directive& d) {
+    switch (d.kind) {
+      case ObjChunk::kFlush: flush(); break;
+      case ObjChunk::kUseMtl: { auto it = mindex.find(d.arg); mat = it == mindex.end() ? -1 : it->second; break; }
+      case ObjChunk::kMtlLib: read_mtl(resolve(mtl_dir, d.arg), o.mtls, mindex); break;
+      case ObjChunk::kSmooth: sg = d.sg; break;
+    }
+  };
   std::vector<Corner> poly;
-  while (std::getline(f, line)) {
-    const char* s = ws(line.c_str());
-    if (!*s || *s == '#') continue;
-    if (s[0] == 'v' && (s[1] == ' ' || s[1] == '\t')) { s += 1; for (int i = 0; i < 3; ++i) o.v.push_back(num(s)); continue; }
-    if (s[0] == 'v' && s[1] == 'n' && (s[2] == ' ' || s[2] == '\t')) { s += 2; for (int i = 0; i < 3; ++i) o.vn.push_back(num(s)); continue; }
-    if (s[0] == 'v' && s[1] == 't' && (s[2] == ' ' || s[2] == '\t')) { s += 2; o.vt.push_back(num(s)); o.vt.push_back(num(s)); continue; }
-    if (s[0] == 'f' && (s[1] == ' ' || s[1] == '\t')) {
-      s += 1; poly.clear();
-      for (std::string t = word(s); !t.empty(); t = word(s)) {
-        Corner c{-1, -1, -1};
-        const char* q = t.c_str();
-        char* e = nullptr;
-        long a = std::strtol(q, &e, 10);
-        c.v = rel_index(a, o.v.size() / 3);
-        if (*e == '/') {
-          q = e + 1;
-          if (*q != '/') { long b = std::strtol(q, &e, 10); if (e != q) c.vt = rel_index(b, o.vt.size() / 2); q = e; }
-          if (*q == '/') { ++q; long cc = std::strtol(q, &e, 10); if (e != q) c.vn = rel_index(cc, o.vn.size() / 3); }
-        }
-        poly.push_back(c);
+  size_t base_v = 0, base_vt = 0, base_vn = 0;
+  for (const ObjChunk& c : chunks) {
+    size_t di = 0;
+    for (size_t fi = 0; fi < c.faces.size(); ++fi) {
+      while (di < c.directives.size() && c.directives[di].face_pos == fi) apply(c.directives[di++]);
+      const ObjChunk::Face& f = c.faces[fi];
+      poly.clear();
+      for (uint32_t k = 0; k < f.n; ++k) {
+        const ObjChunk::RawCorner& r = c.corners[size_t(f.first) + k];
+        Corner cr;
+        cr.v = rel_index(r.v, base_v + f.lv);
+        cr.vt = rel_index(r.vt, base_vt + f.lvt);
+        cr.vn = rel_index(r.vn, base_vn + f.lvn);
+        poly.push_back(cr);
       }
       if (poly.size() < 3) continue;
-      auto tri = [&](size_t a, size_t b, size_t c) {
-        cur.corners.push_back(poly[a]); cur.corners.push_back(poly[b]); cur.corners.push_back(poly[c]);
+      auto tri = [&](size_t a, size_t b, size_t cc) {
+        cur.corners.push_back(poly[a]); cur.corners.push_back(poly[b]); cur.corners.push_back(poly[cc]);
         cur.mat.push_back(mat); cur.sg.push_back(sg);
       };
       if (poly.size() == 3) tri(0, 1, 2);
       else if (poly.size() == 4) {
         // tinyobjloader splits a quad along its shorter diagonal
-        auto P = [&](size_t k, int a) { return o.v[3 * size_t(poly[k].v) + size_t(a)]; };
+        auto P = [&](size_t k, int a) {
+          const size_t i = 3 * size_t(poly[k].v) + size_t(a);
+          return poly[k].v >= 0 && i < o.v.size() ? o.v[i] : 0.0f;
+        };
         float d02 = 0, d13 = 0;
         for (int a = 0; a < 3; ++a) { float x = P(2, a) - P(0, a), y = P(3, a) - P(1, a); d02 += x * x; d13 += y * y; }
         if (d02 < d13) { tri(0, 1, 2); tri(0, 2, 3); } else { tri(0, 1, 3); tri(1, 2, 3); }
       } else {
         for (size_t k = 1; k + 1 < poly.size(); ++k) tri(0, k, k + 1);
       }
-      continue;
     }
-    std::string k = word(s);
-    if (k == "o" || k == "g") flush();
-    else if (k == "usemtl") { auto it = mindex.find(word(s)); mat = it == mindex.end() ? -1 : it->second; }
-    else if (k == "mtllib") read_mtl(resolve(mtl_dir, word(s)), o.mtls, mindex);
-    else if (k == "s") { std::string v = word(s); sg = v == "off" ? 0u : uint32_t(std::strtoul(v.c_str(), nullptr, 10)); }
+    while (di < c.directives.size()) apply(c.directives[di++]);
+    base_v += c.v.size() / 3; base_vt += c.vt.size() / 2; base_vn += c.vn.size() / 3;
   }
   flush();
   return o;
@@ -549,6 +688,10 @@ void load_scene_file(const std::string& scene_path, HostScene& sc) {
   }
 
   std::vector<float> areas;
+  size_t n_tris = 0;
+  for (const ObjShapeRec& sh : obj.shapes) n_tris += sh.mat.size();
+  sc.tri_attr.reserve(n_tris);
+  sc.tri_pos.reserve(9 * n_tris);
   for (size_t s = 0; s < obj.shapes.size(); ++s) {         // Scene.cpp:122-189
     const ObjShapeRec& sh = obj.shapes[s];
     size_t nf = sh.mat.size();
