@@ -78,17 +78,44 @@ void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::f
 // Path-state buffers of the single-job path are allocated at the first
 // render (jobs that only feed the multi-job engine never need them) and
 // re-allocated when the paths-in-flight setting changes.
+namespace {
+// Frees the path buffers of p (not the statistics it points to).
+void release_path_buffers(hasty_job& j, PathsDev& p) {
+  void* bufs[] = {p.rng, p.thr, p.rad, p.pend_b, p.nee_c, p.nee_t, p.med, p.med_geom, p.ray_o, p.ray_d, p.hit,
+                  p.pq[0], p.pq[1], p.rq[0], p.rq[1], p.counts, p.vtx, p.sq, p.out_color, p.out_normal, p.out_albedo};
+  for (void* b : bufs) j.release(b);
+  unsigned long long* stats = p.stats;
+  p = PathsDev{};
+  p.stats = stats;
+}
+}  // namespace
+
 void hasty::ensure_paths(hasty_job& j) {
+  for (int k = 0; k < 2; ++k) {
+    if (!j.lane_stream[k]) ck(cudaStreamCreateWithFlags(&j.lane_stream[k], cudaStreamNonBlocking), "lane stream");
+    if (!j.lane_done[k]) ck(cudaEventCreateWithFlags(&j.lane_done[k], cudaEventDisableTiming), "lane event");
+    if (!j.lane_free[k]) ck(cudaEventCreateWithFlags(&j.lane_free[k], cudaEventDisableTiming), "lane event");
+  }
+  if (!j.main_ready) ck(cudaEventCreateWithFlags(&j.main_ready, cudaEventDisableTiming), "lane event");
   if (j.pd.rng && j.pd.capacity == j.capacity) return;
   ck(cudaStreamSynchronize(j.stream), "sync");
-  void* olds[] = {j.pd.rng, j.pd.thr, j.pd.rad, j.pd.pend_b, j.pd.nee_c, j.pd.nee_t, j.pd.med, j.pd.med_geom, j.pd.ray_o,
-                  j.pd.ray_d, j.pd.hit, j.pd.pq[0], j.pd.pq[1], j.pd.rq[0], j.pd.rq[1], j.pd.counts, j.pd.vtx, j.pd.sq, j.pd.out_color,
-                  j.pd.out_normal, j.pd.out_albedo};
-  for (void* p : olds) j.release(p);
+  release_path_buffers(j, j.pd);
+  release_path_buffers(j, j.pd2);       // lane 1 is allocated again when next used
   unsigned long long* stats = j.pd.stats;
-  j.pd = PathsDev{};
   alloc_paths_into(j.pd, j.capacity, ST_COUNT, [&](size_t b) { return static_cast<void*>(j.alloc<uint8_t>(b)); }, j.stream,
                    stats);
+  j.lane_free_valid[0] = j.lane_free_valid[1] = false;
+  j.lanes_wait_main = true;             // counters were cleared on `stream`
+}
+
+// Lane 1's path buffers, sharing lane 0's statistics.
+void ensure_lane2(hasty_job& j) {
+  if (j.pd2.rng && j.pd2.capacity == j.capacity) return;
+  release_path_buffers(j, j.pd2);
+  alloc_paths_into(j.pd2, j.capacity, ST_COUNT, [&](size_t b) { return static_cast<void*>(j.alloc<uint8_t>(b)); }, j.stream,
+                   j.pd.stats);
+  j.lane_free_valid[1] = false;
+  j.lanes_wait_main = true;
 }
 
 namespace {
@@ -179,6 +206,7 @@ void clear_accumulators(hasty_job& j) {
   size_t n = size_t(j.sd.width) * size_t(j.sd.height) * 3;
   for (double* a : j.acc) ck(cudaMemsetAsync(a, 0, n * sizeof(double), j.stream), "memset acc");
   ck(cudaMemsetAsync(j.pd.stats, 0, sizeof(unsigned long long) * ST_COUNT, j.stream), "memset stats");
+  j.lanes_wait_main = true;
   j.samples_done = 0;
   j.kernel_ms = j.trace_ms = j.shade_ms = 0.0;
   j.trace_launches = j.kernel_launches = 0;
@@ -190,37 +218,42 @@ int64_t default_capacity(int64_t npix) {
   return (cap / npix) * npix;
 }
 
-void render_batch(hasty_job& j, int n_passes) {
+// One batch of passes on render lane `lane` (the two lanes alternate; see
+// hasty_job): ray generation and the bounces on the lane's stream, then the
+// accumulation on the job's stream.
+void render_batch(hasty_job& j, int n_passes, int lane) {
   BatchDesc b;
   b.seed = j.seed;
   b.pass_base = uint32_t(j.samples_done);
   b.n_passes = n_passes;
   b.n_paths = n_passes * j.sd.width * j.sd.height;
-  cudaEvent_t e0, e1;
-  ck(cudaEventCreate(&e0), "event"); ck(cudaEventCreate(&e1), "event");
-  ck(cudaEventRecord(e0, j.stream), "event record");
-  launch_raygen(j.sd, j.pd, b, j.stream);
+  PathsDev& pd = lane ? j.pd2 : j.pd;
+  cudaStream_t ls = j.lane_stream[lane];
+  if (j.lane_free_valid[lane]) ck(cudaStreamWaitEvent(ls, j.lane_free[lane], 0), "lane wait");
+  launch_raygen(j.sd, pd, b, ls);
   int max_paths = b.n_paths;
   auto timed = [&](int stage, auto&& fn) {
     if (!j.stage_timing) { fn(); return; }
     cudaEvent_t a, c;
     ck(cudaEventCreate(&a), "event"); ck(cudaEventCreate(&c), "event");
-    ck(cudaEventRecord(a, j.stream), "event record");
+    ck(cudaEventRecord(a, ls), "event record");
     fn();
-    ck(cudaEventRecord(c, j.stream), "event record");
+    ck(cudaEventRecord(c, ls), "event record");
     j.pending_events.push_back({a, c, stage});
   };
   for (int bounce = 0; bounce < j.sd.max_depth; ++bounce) {
     int q = bounce & 1;
-    timed(1, [&] { launch_trace(j.sd, j.pd, q, 2 * max_paths, j.stream); });
-    ck(cudaMemsetAsync(&j.pd.counts[q ^ 1], 0, sizeof(uint32_t), j.stream), "memset count");
-    ck(cudaMemsetAsync(&j.pd.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), j.stream), "memset count");
-    timed(2, [&] { launch_shade(j.sd, j.pd, b, q, max_paths, j.stream); });
+    timed(1, [&] { launch_trace(j.sd, pd, q, 2 * max_paths, ls); });
+    ck(cudaMemsetAsync(&pd.counts[q ^ 1], 0, sizeof(uint32_t), ls), "memset count");
+    ck(cudaMemsetAsync(&pd.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), ls), "memset count");
+    timed(2, [&] { launch_shade(j.sd, pd, b, q, max_paths, ls); });
   }
-  launch_accumulate(j.sd, j.pd, b, j.acc[0], j.acc[1], j.acc[2], j.stream);
+  ck(cudaEventRecord(j.lane_done[lane], ls), "lane event");
+  ck(cudaStreamWaitEvent(j.stream, j.lane_done[lane], 0), "lane wait");
+  launch_accumulate(j.sd, pd, b, j.acc[0], j.acc[1], j.acc[2], j.stream);
   ck(cudaGetLastError(), "kernel launch");
-  ck(cudaEventRecord(e1, j.stream), "event record");
-  j.pending_events.push_back({e0, e1, 0});
+  ck(cudaEventRecord(j.lane_free[lane], j.stream), "lane event");
+  j.lane_free_valid[lane] = true;
   j.trace_launches += uint64_t(j.sd.max_depth);
   j.kernel_launches += uint64_t(2 + 2 * j.sd.max_depth);
   j.samples_done += n_passes;
@@ -370,13 +403,9 @@ int hasty_job_release_paths(hasty_job* job) {
     ck(cudaSetDevice(job->ctx->device), "cudaSetDevice");
     ck(cudaStreamSynchronize(job->stream), "sync");
     job->collect_events();
-    PathsDev& p = job->pd;
-    void* bufs[] = {p.rng, p.thr, p.rad, p.pend_b, p.nee_c, p.nee_t, p.med, p.med_geom, p.ray_o, p.ray_d, p.hit,
-                    p.pq[0], p.pq[1], p.rq[0], p.rq[1], p.counts, p.vtx, p.sq, p.out_color, p.out_normal, p.out_albedo};
-    for (void* b : bufs) job->release(b);
-    unsigned long long* stats = p.stats;
-    p = PathsDev{};
-    p.stats = stats;
+    release_path_buffers(*job, job->pd);
+    release_path_buffers(*job, job->pd2);
+    job->lane_free_valid[0] = job->lane_free_valid[1] = false;
     return HASTY_OK;
   });
 }
@@ -391,12 +420,36 @@ int hasty_job_render_passes(hasty_job* job, int n_passes) {
     int64_t npix = int64_t(job->sd.width) * job->sd.height;
     int per_batch = int(std::max<int64_t>(1, job->capacity / npix));
     int left = n_passes;
+    if (left == 0) return HASTY_OK;
+    // Device time of this call: from its first launch to its last
+    // accumulation (consecutive calls chain on `stream`, so overlapped
+    // batches are counted once).
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "event"); ck(cudaEventCreate(&e1), "event");
+    ck(cudaEventRecord(e0, job->stream), "event record");
+    if (job->lanes_wait_main) {
+      ck(cudaEventRecord(job->main_ready, job->stream), "lane event");
+      for (cudaStream_t ls : job->lane_stream) ck(cudaStreamWaitEvent(ls, job->main_ready, 0), "lane wait");
+      job->lanes_wait_main = false;
+    }
     while (left > 0) {
-      if (job->stop.load()) throw ApiError{HASTY_ERR_STOPPED, "job stopped"};
+      if (job->stop.load()) break;
       int k = std::min(left, per_batch);
-      render_batch(*job, k);
+      // stage timing keeps one lane, so per-kernel times are not shared
+      int lane = job->stage_timing ? 0 : job->next_lane;
+      if (lane == 1) ensure_lane2(*job);
+      if (job->lanes_wait_main) {          // lane 1 was just allocated on `stream`
+        ck(cudaEventRecord(job->main_ready, job->stream), "lane event");
+        ck(cudaStreamWaitEvent(job->lane_stream[1], job->main_ready, 0), "lane wait");
+        job->lanes_wait_main = false;
+      }
+      render_batch(*job, k, lane);
+      job->next_lane = lane ^ 1;
       left -= k;
     }
+    ck(cudaEventRecord(e1, job->stream), "event record");
+    job->pending_events.push_back({e0, e1, 0});
+    if (job->stop.load()) throw ApiError{HASTY_ERR_STOPPED, "job stopped"};
     return HASTY_OK;
   });
 }

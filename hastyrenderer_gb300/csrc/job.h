@@ -67,8 +67,22 @@ struct hasty_job {
   int32_t bvh_depth = 0;
   double bvh_ms = 0, bvh_tree_ms = 0;
   SceneDev sd{};
-  PathsDev pd{};
-  cudaStream_t stream = nullptr;
+  PathsDev pd{};                      // lane 0's path buffers (and the job's statistics)
+  cudaStream_t stream = nullptr;      // uploads, accumulation (in batch order), read-back
+  // Two render lanes: consecutive batches alternate between lane 0 (paths
+  // `pd`) and lane 1 (paths `pd2`, allocated when first used), each on its
+  // own stream, so that one batch's tracing overlaps the other's shading.
+  // A batch's accumulation runs on `stream` after the batch (event
+  // lane_done), so everything later on `stream` sees the rendering done; a
+  // lane starts its next batch after the accumulation that read its
+  // buffers (event lane_free). Lanes wait for `stream` (event main_ready)
+  // only after it cleared state they use (statistics, counters).
+  PathsDev pd2{};
+  cudaStream_t lane_stream[2] = {nullptr, nullptr};
+  cudaEvent_t lane_done[2] = {nullptr, nullptr}, lane_free[2] = {nullptr, nullptr}, main_ready = nullptr;
+  bool lane_free_valid[2] = {false, false};
+  bool lanes_wait_main = true;
+  int next_lane = 0;
   // host-side scene data between prepare and upload (BVH, guide tables)
   struct Prepared {
     hasty::BvhHost bvh;
@@ -133,8 +147,15 @@ struct hasty_job {
   }
   ~hasty_job() {
     if (stream) cudaStreamSynchronize(stream);
+    for (cudaStream_t s : lane_stream) if (s) cudaStreamSynchronize(s);
     collect_events();
     for (const Block& b : allocs) cudaFree(b.p);
+    for (int k = 0; k < 2; ++k) {
+      if (lane_done[k]) cudaEventDestroy(lane_done[k]);
+      if (lane_free[k]) cudaEventDestroy(lane_free[k]);
+      if (lane_stream[k]) cudaStreamDestroy(lane_stream[k]);
+    }
+    if (main_ready) cudaEventDestroy(main_ready);
     if (stream) cudaStreamDestroy(stream);
   }
 };

@@ -18,6 +18,7 @@
 // on the CPU for the loader/builder tests (hasty_debug_host_trace).
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include "hasty_types.h"
 #include "wavefront.h"
@@ -531,6 +532,10 @@ int persistent_grid(K kernel) {
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
   if (sms < 1) sms = 1;
   if (per_sm < 1) per_sm = 1;
+  if (const char* v = std::getenv("HASTY_TRACE_BLOCKS_PER_SM")) {   // tuning: fewer resident blocks
+    int b = std::atoi(v);
+    if (b >= 1 && b < per_sm) per_sm = b;
+  }
   return sms * per_sm;
 }
 
