@@ -523,43 +523,53 @@ __global__ void TRACE_BOUNDS k_trace_multi(PathsDev P, MultiDev m) {
 }
 
 // Resident blocks of a persistent trace kernel on the current device.
+struct PersistentShape { int sms, per_sm; };
 template <class K>
-int persistent_grid(K kernel) {
+PersistentShape persistent_shape(K kernel) {
   int dev = 0;
   cudaGetDevice(&dev);
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
-  if (sms < 1) sms = 1;
-  if (per_sm < 1) per_sm = 1;
-  if (const char* v = std::getenv("HASTY_TRACE_BLOCKS_PER_SM")) {   // tuning: fewer resident blocks
+  return {sms < 1 ? 1 : sms, per_sm < 1 ? 1 : per_sm};
+}
+
+// Persistent grid: all resident blocks, or at most cap_per_sm per SM (to leave
+// room for kernels of another stream); HASTY_TRACE_BLOCKS_PER_SM overrides
+// both (tuning).
+int persistent_blocks(PersistentShape s, int cap_per_sm) {
+  int per = s.per_sm;
+  if (cap_per_sm > 0 && cap_per_sm < per) per = cap_per_sm;
+  if (const char* v = std::getenv("HASTY_TRACE_BLOCKS_PER_SM")) {
     int b = std::atoi(v);
-    if (b >= 1 && b < per_sm) per_sm = b;
+    if (b >= 1 && b < s.per_sm) per = b;
   }
-  return sms * per_sm;
+  return s.sms * per;
 }
 
 }  // namespace
 
 // The persistent kernels take rays through P.counts[kFetchCounter], cleared
-// on the stream before each launch. Grids: the SMs' resident blocks, fewer
-// when the queue bound is smaller.
+// on the stream before each launch. Grids: the SMs' resident blocks (at most
+// blocks_per_sm per SM when given), fewer when the queue bound is smaller.
 void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t st) {
-  static int grid[2] = {0, 0};
+  static PersistentShape shape[2] = {{0, 0}, {0, 0}};
   int k = bvh_kind == 1 ? 1 : 0;
-  if (!grid[k]) grid[k] = k ? persistent_grid(k_trace_multi<1>) : persistent_grid(k_trace_multi<0>);
+  if (!shape[k].sms) shape[k] = k ? persistent_shape(k_trace_multi<1>) : persistent_shape(k_trace_multi<0>);
+  const int grid = persistent_blocks(shape[k], 0);
   // one-ray-per-thread kernels loop over the queue with a grid-sized stride
-  int blocks = std::min(k ? grid[k] : 8 * grid[k], std::max(1, (max_rays + 127) / 128));
+  int blocks = std::min(k ? grid : 8 * grid, std::max(1, (max_rays + 127) / 128));
   cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
   if (k) k_trace_multi<1><<<blocks, 128, 0, st>>>(p, m);
   else k_trace_multi<0><<<blocks, 128, 0, st>>>(p, m);
 }
 
-void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cudaStream_t st) {
-  static int grid[2] = {0, 0};
+void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cudaStream_t st, int blocks_per_sm) {
+  static PersistentShape shape[2] = {{0, 0}, {0, 0}};
   int k = sc.bvh_kind == 1 ? 1 : 0;
-  if (!grid[k]) grid[k] = k ? persistent_grid(k_trace<1>) : persistent_grid(k_trace<0>);
-  int blocks = k ? std::min(grid[k], std::max(1, (max_rays + 127) / 128)) : std::max(1, (max_rays + 127) / 128);
+  if (!shape[k].sms) shape[k] = k ? persistent_shape(k_trace<1>) : persistent_shape(k_trace<0>);
+  int blocks = k ? std::min(persistent_blocks(shape[k], blocks_per_sm), std::max(1, (max_rays + 127) / 128))
+                 : std::max(1, (max_rays + 127) / 128);
   cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
   if (k) k_trace<1><<<blocks, 128, 0, st>>>(sc, p, q);
   else k_trace<0><<<blocks, 128, 0, st>>>(sc, p, q);

@@ -63,7 +63,9 @@ struct BatchDesc {
 
 // Kernel launchers (integrator.cu / trace.cu). All launches go to `stream`.
 void launch_raygen(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, cudaStream_t stream);
-void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cudaStream_t stream);
+// blocks_per_sm > 0 caps the persistent wide-BVH grid at that many resident
+// blocks per SM (room for another stream's kernels); 0: all that fit.
+void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cudaStream_t stream, int blocks_per_sm = 0);
 void launch_shade(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, int q, int max_paths, cudaStream_t stream);
 void launch_accumulate(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, double* acc_color, double* acc_normal,
                        double* acc_albedo, cudaStream_t stream);
