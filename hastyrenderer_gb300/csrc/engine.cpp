@@ -78,7 +78,8 @@ void Engine::build_graph() {
   ck(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np), "add conditional node");
   cudaGraph_t body = np.conditional.phGraph_out[0];
   ck(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "begin capture");
-  launch_multi_iteration(pd, md, int(cap), (ctx->flags & HASTY_CTX_BINARY_BVH) ? 0 : 1, (unsigned long long)h, 1, stream);
+  launch_multi_iteration(pd, md, int(cap), (ctx->flags & HASTY_CTX_BINARY_BVH) ? 0 : 1, (unsigned long long)h, 1, stream,
+                         trace_blocks_per_sm);
   cudaGraph_t captured = nullptr;
   ck(cudaStreamEndCapture(stream, &captured), "end capture");
   ck(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
@@ -124,31 +125,43 @@ void Engine::publish() {
 }
 
 bool Engine::run_wave(uint32_t n_iter, bool* bound_hit) {
+  launch_wave(n_iter);
+  return finish_wave(bound_hit);
+}
+
+void Engine::launch_wave(uint32_t n_iter) {
   if (!staged.empty()) publish();
-  uint32_t end = iterations + std::max<uint32_t>(n_iter, 1u);
-  ck(cudaMemcpyAsync(&md.ctl[7], &end, sizeof(end), cudaMemcpyHostToDevice, stream), "wave end");
-  uint32_t ctl[8];
-  unsigned long long ns = 0;
-  uint32_t counts[4];
-  auto read_back = [&] {
+  wave_end = iterations + std::max<uint32_t>(n_iter, 1u);
+  ck(cudaMemcpyAsync(&md.ctl[7], &wave_end, sizeof(wave_end), cudaMemcpyHostToDevice, stream), "wave end");
+  if (use_graph) {
+    ck(cudaGraphLaunch(exec, stream), "cudaGraphLaunch");
+    return;
+  }
+  // the loop condition of the graph's while node, evaluated on the host
+  for (;;) {
+    launch_multi_iteration(pd, md, int(cap), (ctx->flags & HASTY_CTX_BINARY_BVH) ? 0 : 1, 0ull, 0, stream,
+                           trace_blocks_per_sm);
+    ck(cudaGetLastError(), "engine iteration");
+    uint32_t ctl[8];
+    unsigned long long ns = 0;
+    uint32_t counts[4];
     ck(cudaMemcpyAsync(ctl, md.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stream), "ctl");
     ck(cudaMemcpyAsync(&ns, md.next_sample, sizeof(ns), cudaMemcpyDeviceToHost, stream), "next");
     ck(cudaMemcpyAsync(counts, pd.counts, sizeof(counts), cudaMemcpyDeviceToHost, stream), "counts");
     ck(cudaStreamSynchronize(stream), "wave");
-  };
-  if (use_graph) {
-    ck(cudaGraphLaunch(exec, stream), "cudaGraphLaunch");
-    read_back();
-  } else {
-    // the loop condition of the graph's while node, evaluated on the host
-    for (;;) {
-      launch_multi_iteration(pd, md, int(cap), (ctx->flags & HASTY_CTX_BINARY_BVH) ? 0 : 1, 0ull, 0, stream);
-      ck(cudaGetLastError(), "engine iteration");
-      read_back();
-      bool more = counts[ctl[0] & 1u] > 0 || ns < total;
-      if (!more || ctl[6] != 0 || ctl[5] >= end) break;
-    }
+    bool more = counts[ctl[0] & 1u] > 0 || ns < total;
+    if (!more || ctl[6] != 0 || ctl[5] >= wave_end) break;
   }
+}
+
+bool Engine::finish_wave(bool* bound_hit) {
+  uint32_t ctl[8];
+  unsigned long long ns = 0;
+  uint32_t counts[4];
+  ck(cudaMemcpyAsync(ctl, md.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stream), "ctl");
+  ck(cudaMemcpyAsync(&ns, md.next_sample, sizeof(ns), cudaMemcpyDeviceToHost, stream), "next");
+  ck(cudaMemcpyAsync(counts, pd.counts, sizeof(counts), cudaMemcpyDeviceToHost, stream), "counts");
+  ck(cudaStreamSynchronize(stream), "wave");
   iterations = ctl[5];
   if (bound_hit) *bound_hit = ctl[6] != 0;
   next = ns;
@@ -198,6 +211,10 @@ uint32_t engine_lanes(int64_t cap, uint32_t npix) {
   return uint32_t(std::max<int64_t>(1, std::min<int64_t>(16, l)));
 }
 
+// Resident closest-hit blocks per SM for an engine that shares the GPU with
+// another (the plain path's lanes use the same bound).
+constexpr int kSharedTraceBlocksPerSM = 5;
+
 uint32_t engine_regen_threshold(float fraction, int64_t cap) {
   float f = fraction > 0.f ? fraction : 0.9f;
   if (f >= 1.0f) return uint32_t(cap) + 1u;
@@ -225,61 +242,100 @@ int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, 
     }
     if (n_segments >= (uint64_t(1) << 30)) throw ApiError{HASTY_ERR_ARG, "too many passes in one batch"};
     auto t0 = std::chrono::steady_clock::now();
-    Engine e;
+    // Two engines on two streams, each with half the pool, take alternate
+    // passes of every job, so that one engine's tracing overlaps the other's
+    // shading. Each job's fixed-point sums have 2 x L lanes (L per engine);
+    // the integer fold at the end makes the result the one engine's.
+    int n_eng = n_segments >= 2 ? 2 : 1;
+    if (const char* v = std::getenv("HASTY_BATCH_ENGINES")) n_eng = std::atoi(v) == 1 ? 1 : n_eng;   // tuning
     int64_t cap = engine_pool_size(cfg ? cfg->paths_in_flight : 0);
+    const int64_t cap_each = std::max<int64_t>(kGroup, cap / n_eng);
     uint32_t max_iter = (cfg && cfg->max_iterations > 0) ? uint32_t(cfg->max_iterations) : 50000000u;
-    e.init(ctx, cap, int(std::max<size_t>(n_jobs, 1)), uint32_t(std::max<uint64_t>(n_segments, 1)),
-           engine_regen_threshold(cfg ? cfg->regen_fraction : 0.f, cap), max_iter);
+    Engine engines[2];
+    for (int k = 0; k < n_eng; ++k) {
+      engines[k].trace_blocks_per_sm = n_eng > 1 ? kSharedTraceBlocksPerSM : 0;
+      engines[k].init(ctx, cap_each, int(std::max<size_t>(n_jobs, 1)),
+                      uint32_t(std::max<uint64_t>(n_segments / uint64_t(n_eng) + 1, 1)),
+                      engine_regen_threshold(cfg ? cfg->regen_fraction : 0.f, cap_each), max_iter);
+    }
+    Engine& e = engines[0];
     std::vector<unsigned long long*> accs(n_jobs);
     std::vector<uint32_t> lanes(n_jobs, 1u);
     for (size_t i = 0; i < n_jobs; ++i) {
       hasty_job* j = jobs[i];
       uint32_t npix = uint32_t(j->sd.width) * uint32_t(j->sd.height);
-      lanes[i] = engine_lanes(cap, npix);
-      const size_t acc_bytes = sizeof(unsigned long long) * 9 * size_t(npix) * lanes[i];
+      lanes[i] = engine_lanes(cap_each, npix);
+      const size_t lane_words = 9 * size_t(npix);
+      const size_t acc_bytes = sizeof(unsigned long long) * lane_words * lanes[i] * size_t(n_eng);
       accs[i] = static_cast<unsigned long long*>(e.alloc(acc_bytes));
       ck(cudaMemsetAsync(accs[i], 0, acc_bytes, e.stream), "memset acc");
-      JobDev d;
-      std::memset(&d, 0, sizeof(d));
-      d.sc = j->sd;
-      d.acc = accs[i];
-      d.seed = j->seed;
-      d.npix = npix;
-      d.lanes = lanes[i];
-      e.set_job(int(i), d);
-      // jobs in order, each job's passes in order
-      for (int32_t p = 0; p < passes[i]; ++p) e.append(int(i), uint32_t(j->samples_done + p), npix);
+      for (int k = 0; k < n_eng; ++k) {
+        JobDev d;
+        std::memset(&d, 0, sizeof(d));
+        d.sc = j->sd;
+        d.acc = accs[i] + lane_words * lanes[i] * size_t(k);
+        d.seed = j->seed;
+        d.npix = npix;
+        d.lanes = lanes[i];
+        engines[k].set_job(int(i), d);
+      }
+      // jobs in order, each job's passes in order, alternating engines
+      for (int32_t p = 0; p < passes[i]; ++p) engines[p % n_eng].append(int(i), uint32_t(j->samples_done + p), npix);
     }
-    e.publish();
+    ck(cudaStreamSynchronize(e.stream), "memset acc");   // the other engine's kernels add into these sums
+    for (int k = 0; k < n_eng; ++k) engines[k].publish();
     cudaEvent_t a, b;
     ck(cudaEventCreate(&a), "event"); ck(cudaEventCreate(&b), "event");
     ck(cudaEventRecord(a, e.stream), "event");
+    for (int k = 1; k < n_eng; ++k) ck(cudaStreamWaitEvent(engines[k].stream, a, 0), "event wait");
+    cudaEvent_t ends[2] = {b, nullptr};
+    if (n_eng > 1) ck(cudaEventCreate(&ends[1]), "event");
+    for (int k = 0; k < n_eng; ++k) {
+      engines[k].launch_wave(max_iter);
+      ck(cudaEventRecord(ends[k], engines[k].stream), "event");
+    }
     bool bound = false;
-    e.run_wave(max_iter, &bound);
-    ck(cudaEventRecord(b, e.stream), "event");
-    ck(cudaEventSynchronize(b), "event");
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
+    for (int k = 0; k < n_eng; ++k) {
+      bool bk = false;
+      engines[k].finish_wave(&bk);
+      bound = bound || bk;
+    }
+    float ms = 0.f;   // device time: from the common start to the last engine's end
+    for (int k = 0; k < n_eng; ++k) {
+      float mk = 0.f;
+      ck(cudaEventSynchronize(ends[k]), "event");
+      cudaEventElapsedTime(&mk, a, ends[k]);
+      ms = std::max(ms, mk);
+    }
     cudaEventDestroy(a); cudaEventDestroy(b);
+    if (ends[1]) cudaEventDestroy(ends[1]);
     if (bound) throw ApiError{HASTY_ERR_CUDA, "batch stopped at its iteration bound"};
     // fold the fixed-point sums into each job's FP64 accumulators
     for (size_t i = 0; i < n_jobs; ++i) {
       hasty_job* j = jobs[i];
-      launch_fold_lanes(accs[i], j->sd.width * j->sd.height, int(lanes[i]), e.stream);
+      launch_fold_lanes(accs[i], j->sd.width * j->sd.height, int(lanes[i]) * n_eng, e.stream);
       launch_fixed_to_double(accs[i], j->sd.width * j->sd.height, j->acc[0], j->acc[1], j->acc[2], e.stream);
       j->samples_done += passes[i];
     }
     ck(cudaGetLastError(), "fold");
-    unsigned long long st[MS_COUNT];
-    e.stats(st);
+    unsigned long long st[MS_COUNT] = {};
+    for (int k = 0; k < n_eng; ++k) {
+      unsigned long long sk[MS_COUNT];
+      engines[k].stats(sk);
+      for (int c = 0; c < MS_COUNT; ++c) st[c] += sk[c];
+    }
     if (out) {
       std::memset(out, 0, sizeof(*out));
       out->device_ms = ms;
       out->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-      out->samples = e.total;
+      for (int k = 0; k < n_eng; ++k) {
+        out->samples += engines[k].total;
+        out->iterations = std::max<uint64_t>(out->iterations, engines[k].iterations);
+        out->paths_in_flight += engines[k].cap;
+        out->engine_bytes += engines[k].bytes;
+      }
       out->rays = st[MS_RAYS]; out->shaded = st[MS_SHADED]; out->nan_samples = st[MS_NAN];
-      out->saturated = st[MS_SATURATED]; out->iterations = e.iterations; out->paths_in_flight = e.cap;
-      out->engine_bytes = e.bytes;
+      out->saturated = st[MS_SATURATED];
     }
     return HASTY_OK;
   });

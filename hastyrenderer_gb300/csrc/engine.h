@@ -65,6 +65,15 @@ struct Engine {
   // One graph launch of up to n_iter iterations; synchronous. Returns true
   // while work remains.
   bool run_wave(uint32_t n_iter, bool* bound_hit);
+  // run_wave in two halves, so that waves of several engines (one stream
+  // each) run at the same time: launch_wave returns once the wave is queued
+  // (graph mode; the host-driven stream mode runs it to the end), and
+  // finish_wave waits for it and reads the engine's state back.
+  void launch_wave(uint32_t n_iter);
+  bool finish_wave(bool* bound_hit);
+  // Resident blocks per SM of the persistent closest-hit kernel (0: all that
+  // fit); set before init, for engines that share the GPU with another.
+  int trace_blocks_per_sm = 0;
   bool busy() const { return live > 0 || next < total; }
   unsigned long long unissued() const { return total - next; }
   void read_done(std::vector<unsigned long long>& out);
@@ -72,6 +81,7 @@ struct Engine {
 
  private:
   std::vector<SegDev> staged;
+  uint32_t wave_end = 0;
   void build_graph();
 };
 

@@ -920,11 +920,11 @@ void launch_multi_init(const PathsDev& p, const MultiDev& m, int cap, cudaStream
 int compact_blocks(int cap) { return (cap + kCompactTile - 1) / kCompactTile; }
 
 void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int cap, int bvh_kind, unsigned long long cond,
-                            int use_cond, cudaStream_t st) {
+                            int use_cond, cudaStream_t st, int trace_blocks_per_sm) {
   const int nb = compact_blocks(cap);
   k_multi_plan<<<1, 1, 0, st>>>(p, m);
   k_multi_regen<<<(cap + 255) / 256, 256, 0, st>>>(p, m, m.jobs);
-  launch_trace_multi(p, m, bvh_kind, 2 * cap, st);
+  launch_trace_multi(p, m, bvh_kind, 2 * cap, st, trace_blocks_per_sm);
   k_resolve_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m, m.jobs);
   k_sample_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m, m.jobs);
   k_compact_count<<<nb, kCompactThreads, 0, st>>>(m, cap);

@@ -552,11 +552,12 @@ int persistent_blocks(PersistentShape s, int cap_per_sm) {
 // The persistent kernels take rays through P.counts[kFetchCounter], cleared
 // on the stream before each launch. Grids: the SMs' resident blocks (at most
 // blocks_per_sm per SM when given), fewer when the queue bound is smaller.
-void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t st) {
+void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t st,
+                        int blocks_per_sm) {
   static PersistentShape shape[2] = {{0, 0}, {0, 0}};
   int k = bvh_kind == 1 ? 1 : 0;
   if (!shape[k].sms) shape[k] = k ? persistent_shape(k_trace_multi<1>) : persistent_shape(k_trace_multi<0>);
-  const int grid = persistent_blocks(shape[k], 0);
+  const int grid = persistent_blocks(shape[k], blocks_per_sm);
   // one-ray-per-thread kernels loop over the queue with a grid-sized stride
   int blocks = std::min(k ? grid : 8 * grid, std::max(1, (max_rays + 127) / 128));
   cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);

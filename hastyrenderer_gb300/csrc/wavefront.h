@@ -138,7 +138,7 @@ enum MultiStat { MS_RAYS = ST_RAYS, MS_SHADED = ST_SHADED, MS_PATHS = ST_PATHS, 
 // into `stream`; `cond` is the CUDA-graph conditional handle of the enclosing
 // while node (0 when launched without a graph).
 void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int capacity, int bvh_kind,
-                            unsigned long long cond_handle, int use_cond, cudaStream_t stream);
+                            unsigned long long cond_handle, int use_cond, cudaStream_t stream, int trace_blocks_per_sm = 0);
 void launch_multi_init(const PathsDev& p, const MultiDev& m, int capacity, cudaStream_t stream);
 // Compaction blocks of an engine with `capacity` slots (3 block_sums entries each).
 int compact_blocks(int capacity);
@@ -148,6 +148,7 @@ void launch_fold_lanes(unsigned long long* acc, int npix, int lanes, cudaStream_
 // Adds a finished job's fixed-point sums (lane 0) into FP64 accumulators (sum * 2^-32).
 void launch_fixed_to_double(const unsigned long long* acc, int npix, double* c, double* n, double* a, cudaStream_t stream);
 // trace.cu: closest hit of the queued rays of the multi-job engine.
-void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t stream);
+void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t stream,
+                        int blocks_per_sm = 0);
 
 }  // namespace hasty

@@ -124,11 +124,14 @@ int hasty_job_write_outputs(hasty_job* job, const char* out_dir, int write_pfm);
  * Path slots are shared by all jobs and refilled with new camera samples as
  * paths finish (regeneration); one CUDA graph launch whose conditional
  * while-node repeats regenerate/trace/shade on the device runs the whole batch.
- * Each job's samples are accumulated in int64 fixed point (2^-32), which is
- * order-independent: a job's result is bit-identical alone or in any mix.
+ * Two such engines, each with half the pool and its own stream, take
+ * alternate passes of every job so that one's tracing overlaps the other's
+ * shading. Each job's samples are accumulated in int64 fixed point (2^-32),
+ * which is order-independent: a job's result is bit-identical alone or in
+ * any mix, on one engine or two.
  * No counterpart in the reference (its jobs run one at a time). */
 typedef struct hasty_batch_config {
-  int64_t paths_in_flight;     /* path-slot pool; 0 = 4M */
+  int64_t paths_in_flight;     /* path-slot pool (both engines together); 0 = 4M */
   float regen_fraction;        /* refill when live paths < fraction * pool; 0 = 0.9, >= 1 every iteration */
   int32_t max_iterations;      /* device-side loop bound; 0 = 50M */
 } hasty_batch_config;
@@ -141,8 +144,8 @@ typedef struct hasty_batch_stats {
   uint64_t shaded;
   uint64_t nan_samples;
   uint64_t saturated;          /* samples clamped to +/-2^30 in fixed point */
-  uint64_t iterations;         /* engine iterations (one bounce of every live path each) */
-  int64_t paths_in_flight;
+  uint64_t iterations;         /* engine iterations (one bounce of every live path each; the longer engine) */
+  int64_t paths_in_flight;     /* both engines together */
   int64_t engine_bytes;        /* device memory of the engine (path pool, fixed-point sums) */
 } hasty_batch_stats;
 
