@@ -120,6 +120,60 @@ class ReferenceBuild(_Base):
         return os.path.exists(REF_LIB)
 
 
+class PhotonMapper:
+    """Photon mapper of the CPU checker (oracle/port/oracle_pm.cpp) or of the
+    reference build (oracle/ref_pm_harness.cpp): `iterate(n)` runs n more
+    progressive iterations and returns the current images (H, W, 3), the
+    radii (H, W) and {emitted, stored, iteration} of the last iteration."""
+
+    def __init__(self, job_path: str, reference: bool = False):
+        self.reference = reference
+        P, I = ctypes.c_void_p, ctypes.c_int
+        if reference:
+            self.L = _load(REF_LIB, "ref")
+            self.L.ref_pm_load.restype = P
+            self.L.ref_pm_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, I]
+            self.L.ref_pm_free.argtypes = [P]
+            self.L.ref_pm_iterate.argtypes = [P, I, P, P, P, P, P]
+            err = ctypes.create_string_buffer(1024)
+            self.h = self.L.ref_pm_load(job_path.encode(), err, 1024)
+            if not self.h:
+                raise RuntimeError("reference load failed: " + err.value.decode())
+            self.scene = None
+        else:
+            self.scene = Oracle(job_path)
+            self.L = self.scene.L
+            self.L.hor_pm_new.restype = P
+            self.L.hor_pm_new.argtypes = [P]
+            self.L.hor_pm_free.argtypes = [P]
+            self.L.hor_pm_iterate.argtypes = [P, P, I, P, P, P, P, P]
+            self.h = self.L.hor_pm_new(self.scene.h)
+        info = Oracle(job_path).info() if reference else self.scene.info()
+        self.W, self.H = info["width"], info["height"]
+
+    def iterate(self, n: int) -> dict:
+        c = np.zeros((self.H, self.W, 3), np.float32); nn = np.zeros_like(c); a = np.zeros_like(c)
+        r = np.zeros((self.H, self.W), np.float32)
+        info = np.zeros(4, np.int64)
+        if self.reference:
+            rc = self.L.ref_pm_iterate(self.h, n, c.ctypes.data, nn.ctypes.data, a.ctypes.data, r.ctypes.data,
+                                       info.ctypes.data)
+        else:
+            rc = self.L.hor_pm_iterate(self.scene.h, self.h, n, c.ctypes.data, nn.ctypes.data, a.ctypes.data,
+                                       r.ctypes.data, info.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("photon mapper iteration failed")
+        return {"color": c, "normal": nn, "albedo": a, "radii": r, "emitted": int(info[0]), "stored": int(info[1]),
+                "iteration": int(info[2])}
+
+    def close(self):
+        if self.h:
+            (self.L.ref_pm_free if self.reference else self.L.hor_pm_free)(self.h)
+            self.h = None
+        if self.scene is not None:
+            self.scene.close()
+
+
 def kat(which: int, inputs: np.ndarray, replay: np.ndarray, reference: bool = False) -> np.ndarray:
     """Known-answer call of one routine per row of `inputs` with the matching
     row of `replay` as its uniform stream. Output rows have 12 floats."""

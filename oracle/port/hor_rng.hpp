@@ -29,6 +29,14 @@ inline uint64_t path_key(uint64_t seed, uint32_t pixel, uint32_t pass) {
   return splitmix64(splitmix64(seed) ^ ((uint64_t(pass) << 32) | uint64_t(pixel)));
 }
 
+// Photon mapper streams: photon i of iteration t, and the initial radius
+// footprint of pixel p (pass value no render reaches).
+constexpr uint64_t kPhotonKeyMix = 0x50484F544F4E5321ull;
+constexpr uint32_t kFootprintPass = 0xFFFFFFFFu;
+inline uint64_t photon_key(uint64_t seed, uint32_t photon, uint32_t iteration) {
+  return path_key(seed ^ kPhotonKeyMix, photon, iteration);
+}
+
 constexpr uint64_t kPcgMult = 6364136223846793005ull;
 
 // PCG32 (XSH-RR output, 64-bit LCG state), O'Neill 2014.

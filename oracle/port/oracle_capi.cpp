@@ -2,6 +2,7 @@
 // loaded with ctypes by tests/, __graft_entry__.smoke() and bench.py's
 // CPU-baseline leg. Nothing in the product links against this library.
 #include "oracle_core.hpp"
+#include "oracle_pm.hpp"
 #include <atomic>
 #include <cstring>
 #include <thread>
@@ -317,6 +318,44 @@ int hor_kat(int which, const float* in, const uint32_t* replay, int nreplay, flo
   } catch (const std::exception&) {
     return -2;
   }
+}
+
+// ---- photon mapper (oracle_pm.hpp) ----------------------------------------
+void* hor_pm_new(void* p) {
+  auto* st = new PmState();
+  return st;
+}
+void hor_pm_free(void* s) { delete static_cast<PmState*>(s); }
+// Runs n more iterations; writes the current colour / normal / albedo images
+// (W*H*3 floats), the radii (W*H) and info = {emitted, stored, iteration} +
+// the cell size (as float bits in info[3]) of the last iteration.
+int hor_pm_iterate(void* p, void* s, int n, float* color, float* normal, float* albedo, float* radii, int64_t* info) {
+  const Scene& sc = static_cast<Handle*>(p)->sc;
+  PmState& st = *static_cast<PmState*>(s);
+  try {
+    if (!st.initialised) pm_init(sc, st);
+    for (int k = 0; k < n; ++k) pm_iteration(sc, st);
+  } catch (const std::exception&) {
+    return -1;
+  }
+  const size_t np = size_t(st.W) * st.H;
+  if (color) std::memcpy(color, st.color.data(), 3 * np * sizeof(float));
+  if (normal) std::memcpy(normal, st.normal.data(), 3 * np * sizeof(float));
+  if (albedo) std::memcpy(albedo, st.albedo.data(), 3 * np * sizeof(float));
+  if (radii) std::memcpy(radii, st.radii.data(), np * sizeof(float));
+  if (info) {
+    info[0] = int64_t(st.emitted); info[1] = int64_t(st.stored); info[2] = st.iteration;
+    uint32_t cb; std::memcpy(&cb, &st.cell, 4); info[3] = cb;
+  }
+  return 0;
+}
+// Initial radii only (before the first iteration).
+int hor_pm_init_radii(void* p, void* s, float* radii) {
+  const Scene& sc = static_cast<Handle*>(p)->sc;
+  PmState& st = *static_cast<PmState*>(s);
+  pm_init(sc, st);
+  std::memcpy(radii, st.radii.data(), size_t(st.W) * st.H * sizeof(float));
+  return 0;
 }
 
 }  // extern "C"

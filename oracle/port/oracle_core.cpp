@@ -241,7 +241,7 @@ float compute_alpha(float rough) {
   return a;
 }
 
-ProbResult compute_probability(float m, float s, float t, float cos_o, float eo, float er) {
+ProbResult compute_probability(float m, float s, float t, float cos_o, float eo, float er, int flags) {
   ProbResult p;
   p.cosT = 0.0f;
   p.refr = refraction_cos_t(cos_o, eo, er, p.cosT);
@@ -249,6 +249,8 @@ ProbResult compute_probability(float m, float s, float t, float cos_o, float eo,
   float mD = (1.0f - t) * (1.0f - m) * (1.0f - 0.5f * s);
   float mS = mixf(mixf(0.5f * s, p.FD, t), 1.0f, m);
   float mR = (1.0 - p.FD) * t * (1.0 - m);
+  if (!(flags & kEvalDiffuse)) mD = 0.0f;
+  if (!(flags & kEvalConcentrated)) { mS = 0.0f; mR = 0.0f; }
   float sum = mD + mS + mR;
   p.none = sum == 0.0f;
   if (p.none) { p.pD = p.pS = p.pR = 0.0f; }
@@ -298,7 +300,7 @@ V3 evaluate_concentrated(float nsWi, const V3& albedo, float m, float s, float t
 
 SampleResult principled_sample(Rng& r, const Interaction& it, const V3& wo, const V3& ns, const V3& albedo,
                                float m, float s, float rough, float aniso, float t, int wavelength,
-                               float eta_out, float eta_mat) {
+                               float eta_out, float eta_mat, int flags, bool adjoint) {
   SampleResult res;
   float ngwo = dot(it.ng, wo);
   float nswo = dot(ns, wo);
@@ -306,7 +308,7 @@ SampleResult principled_sample(Rng& r, const Interaction& it, const V3& wo, cons
   res.outside = ngwo >= 0.0f;
   float eo = res.outside ? eta_out : eta_mat;
   float er = res.outside ? eta_mat : eta_out;
-  ProbResult p = compute_probability(m, s, t, nswo, eo, er);
+  ProbResult p = compute_probability(m, s, t, nswo, eo, er, flags);
   if (p.none) {
     res.dir = V3(1, 0, 0); res.thrD = V3(0, 0, 0); res.thrC = V3(0, 0, 0); res.pdf = 0.0f;
     return res;
@@ -358,7 +360,7 @@ SampleResult principled_sample(Rng& r, const Interaction& it, const V3& wo, cons
     } else {
       float ratio = eo / er;
       res.dir = refraction_direction_from_angles(wo, ns, ratio, nswo, p.cosT);
-      float scale = sq(ratio);
+      float scale = adjoint ? 1.0f : sq(ratio);
       float fc = res.pdf / p.pR * scale * (1.0f - p.FD) / std::fabs(dot(res.dir, it.ng));
       fC = fc * mask;
     }
@@ -431,7 +433,7 @@ V3 MaterialCtx::shading_normal(const Interaction& it, const V3& wo, float ngwo) 
   if (side != side_s) ns = it.ng;
   return ns * side;
 }
-EvalResult MaterialCtx::evaluate(const Interaction& it, const V3& wo, const V3& wi, float eta_out) const {
+EvalResult MaterialCtx::evaluate(const Interaction& it, const V3& wo, const V3& wi, float eta_out, int flags) const {
   (void)eta_out;
   float ngwo = dot(it.ng, wo);
   V3 ns = shading_normal(it, wo, ngwo);
@@ -443,20 +445,30 @@ EvalResult MaterialCtx::evaluate(const Interaction& it, const V3& wo, const V3& 
   float m = metallic(it);
   float s = mat->specular, an = mat->anisotropy, t = mat->transmission;
   float nsc = normal_scale(wi, ns, it.ng);
-  r.fD = evaluate_diffuse(nswi, alb, nsc, m, s, t);
-  float nan = std::numeric_limits<float>::quiet_NaN();
-  float at, ab; V3 tan, bit;
-  anisotropy_params(it, ns, alpha, an, at, ab, tan, bit);
-  r.fC = evaluate_concentrated(nswi, alb, m, s, t, wo, wi, alpha, at, ab, tan, bit, ns, nsc, false, V3(nan, nan, nan));
+  r.fD = V3(0, 0, 0); r.fC = V3(0, 0, 0);
+  if (flags & kEvalDiffuse) r.fD = evaluate_diffuse(nswi, alb, nsc, m, s, t);
+  if (flags & kEvalConcentrated) {
+    float nan = std::numeric_limits<float>::quiet_NaN();
+    float at, ab; V3 tan, bit;
+    anisotropy_params(it, ns, alpha, an, at, ab, tan, bit);
+    r.fC = evaluate_concentrated(nswi, alb, m, s, t, wo, wi, alpha, at, ab, tan, bit, ns, nsc, false, V3(nan, nan, nan));
+  }
   return r;
 }
-SampleResult MaterialCtx::sample(Rng& r, const Interaction& it, const V3& wo, int wl, float eta_out) const {
+SampleResult MaterialCtx::sample(Rng& r, const Interaction& it, const V3& wo, int wl, float eta_out, int flags,
+                                 bool adjoint) const {
   V3 alb = albedo(it);
   float rough = roughness(it);
   float m = metallic(it);
   V3 ns = shading_normal(it, wo, dot(it.ng, wo));
   float eta_mat = ior(wl);
-  return principled_sample(r, it, wo, ns, alb, m, mat->specular, rough, mat->anisotropy, mat->transmission, wl, eta_out, eta_mat);
+  return principled_sample(r, it, wo, ns, alb, m, mat->specular, rough, mat->anisotropy, mat->transmission, wl, eta_out, eta_mat,
+                           flags, adjoint);
+}
+bool MaterialCtx::has_diffuse_lobe(const Interaction& it) const {
+  float m = metallic(it);
+  float s = mat->specular, t = mat->transmission;
+  return (1.0f - 0.5f * s) * (1.0 - t) * (1.0 - m) > 0.0f;
 }
 float MaterialCtx::sample_pdf(const Interaction& it, const V3& wo, const V3& wi, float eta_out) const {
   float ngwo = dot(it.ng, wo);
@@ -504,6 +516,18 @@ void Camera::compute_ray(Rng& r, float x, float y, float W, float H, V3& o, V3& 
   } else {
     o = pos; d = dir;
   }
+}
+
+float Camera::ray_angle(float x, float y, float W, float H) const {
+  float fov = float(kPi) * fov_deg / 180.0f;
+  float q = std::tan(fov * 0.5f);
+  float lx1 = (x + 0.5f - 0.5f * W) / W * 2.0f;
+  float ly1 = (y + 0.5f - 0.5f * H) / W * 2.0f;
+  float lx2 = (x - 0.5f - 0.5f * W) / W * 2.0f;
+  float ly2 = (y - 0.5f - 0.5f * H) / W * 2.0f;
+  float ax = std::fabs(std::atan(q * lx1) - std::atan(q * lx2));
+  float ay = std::fabs(std::atan(q * ly1) - std::atan(q * ly2));
+  return 0.5f * ax + 0.5f * ay;
 }
 
 // ========================================================= environment ====
@@ -794,6 +818,16 @@ Interaction Scene::sample_light_position(Rng& r, float& pdfA) const {
   return interaction(ti, b, n);
 }
 
+void Scene::sample_emission_ray(Rng& r, V3& flux, V3& o, V3& d) const {
+  float pPos, pDir;
+  Interaction it = sample_light_position(r, pPos);
+  V3 dir = sample_hemisphere_cos(r, it.ng, pDir);
+  V3 L = mats[it.material].emission * float(kInvPi);      // Scene.cpp:460-470 (no side test)
+  flux = L * (std::fabs(dot(it.ng, dir)) / (pPos * pDir));
+  o = ray_x(it, true);
+  d = dir;
+}
+
 void Scene::sample_light_ray(Rng& r, const Interaction& p, float& pdf, V3& o, V3& d, Hit& h, bool& visible, BvhStats* st) const {
   float psurf = !env.is_texture ? 1.0f : (!light_tris.empty() ? 0.5f : 0.0f);
   float xi = r.uniform01f();
@@ -875,7 +909,7 @@ float LightRayInfo::outside_ior(const Hit& h) const {
 }
 
 // ============================================================ integrator ====
-static V3 beers_law(const V3& T, float d) {       // core/include/Hasty/PathTracing.h:46-59
+V3 beers_law(const V3& T, float d) {              // core/include/Hasty/PathTracing.h:46-59
   if (T == V3(1, 1, 1)) return V3(1, 1, 1);
   V3 r;
   for (int i = 0; i < 3; ++i) r[i] = T[i] <= 0.0f ? 0.0f : std::pow(T[i], 1.0f * d);

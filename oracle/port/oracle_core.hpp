@@ -176,8 +176,12 @@ struct SampleResult { bool outside; V3 dir, thrD, thrC; float pdf; };     // BRD
 struct EvalResult { V3 fD, fC, ns; };                                      // BRDF.h:46-56
 struct ProbResult { bool none; float pD, pS, pR; bool refr; float FD, cosT; };  // BRDF.h:102-111
 
+// ShaderEvalFlag (BRDF.h): which lobes a sample or an evaluation covers.
+enum : int { kEvalDiffuse = 1, kEvalConcentrated = 2, kEvalAll = 3 };
+
 float compute_alpha(float roughness);                                                          // BRDF.cpp:253-263
-ProbResult compute_probability(float m, float s, float t, float cos_o, float eta_o, float eta_r);  // BRDF.cpp:264-307
+ProbResult compute_probability(float m, float s, float t, float cos_o, float eta_o, float eta_r,
+                               int flags = kEvalAll);                                          // BRDF.cpp:264-307
 void anisotropy_params(const Interaction& it, const V3& ns, float alpha, float aniso, float& at, float& ab, V3& t, V3& b);  // :308-316
 V3 evaluate_diffuse(float nsWi, const V3& albedo, float nscale, float m, float s, float t);   // :319-326
 V3 evaluate_concentrated(float nsWi, const V3& albedo, float m, float s, float t, const V3& wo, const V3& wi,
@@ -185,7 +189,8 @@ V3 evaluate_concentrated(float nsWi, const V3& albedo, float m, float s, float t
                          float nscale, bool force, const V3& FD);                              // :328-394
 SampleResult principled_sample(Rng& r, const Interaction& it, const V3& wo, const V3& ns, const V3& albedo,
                                float m, float s, float rough, float aniso, float t, int wavelength,
-                               float eta_out, float eta_mat);                                  // :397-579
+                               float eta_out, float eta_mat, int flags = kEvalAll,
+                               bool adjoint = false);                                          // :397-579
 
 struct MaterialCtx {            // evaluation of a PrincipledBRDF at a hit (texture lookups)
   const Material* mat;
@@ -195,8 +200,11 @@ struct MaterialCtx {            // evaluation of a PrincipledBRDF at a hit (text
   float metallic(const Interaction& it) const;
   float ior(int wavelength) const;                                          // BRDF.cpp:589-603
   V3 shading_normal(const Interaction& it, const V3& wo, float ngwo) const;  // BRDF.cpp:604-628
-  EvalResult evaluate(const Interaction& it, const V3& wo, const V3& wi, float eta_out) const;  // :630-679
-  SampleResult sample(Rng& r, const Interaction& it, const V3& wo, int wavelength, float eta_out) const;  // :681-700
+  EvalResult evaluate(const Interaction& it, const V3& wo, const V3& wi, float eta_out,
+                      int flags = kEvalAll) const;                                          // :630-679
+  SampleResult sample(Rng& r, const Interaction& it, const V3& wo, int wavelength, float eta_out,
+                      int flags = kEvalAll, bool adjoint = false) const;                    // :681-700
+  bool has_diffuse_lobe(const Interaction& it) const;                                       // :743-750
   float sample_pdf(const Interaction& it, const V3& wo, const V3& wi, float eta_out) const;  // :702-742
 };
 
@@ -207,6 +215,7 @@ struct Camera {                 // core/include/Hasty/Camera.h:36-46, Camera.cpp
   int blades = 8; float blade_rot = 0;
   void look_at(const V3& p, const V3& target);
   void compute_ray(Rng& r, float px, float py, float W, float H, V3& o, V3& d) const;  // Camera.cpp:41-81
+  float ray_angle(float px, float py, float W, float H) const;                          // Camera.cpp:83-98
 };
 
 struct Settings {               // RenderSettings defaults, RenderJob.h:15-30
@@ -267,6 +276,8 @@ struct Scene {
   V3 albedo(const Interaction& it) const { return ctx(it).albedo(it); }
   MaterialCtx ctx(const Interaction& it) const { return MaterialCtx{&mats[it.material], &textures}; }
   Interaction sample_light_position(Rng& r, float& pdfA) const;               // Scene.cpp:506-526
+  void sample_emission_ray(Rng& r, V3& flux, V3& o, V3& d) const;              // sampleLightRay, Scene.cpp:527-537
+  bool has_surface_light() const { return !light_tris.empty(); }
   void sample_light_ray(Rng& r, const Interaction& p, float& pdf, V3& o, V3& d, Hit& h, bool& visible, BvhStats* st) const;  // :538-586
   float light_ray_density(const Interaction& p, const V3& o, const V3& d, const Hit& h) const;  // :587-616
 };
@@ -281,6 +292,8 @@ struct LightRayInfo {           // core/src/LightRayInfo.cpp, LightRayInfo.h:30-
   int sample_wavelength(Rng& r, bool sample, float& prob);
   float outside_ior(const Hit& h) const;
 };
+
+V3 beers_law(const V3& T, float d);              // core/include/Hasty/PathTracing.h:46-59
 
 struct RenderStats { uint64_t rays = 0, nan = 0, nodes = 0, tris = 0, shaded = 0, paths = 0; };
 

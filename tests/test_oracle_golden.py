@@ -114,3 +114,22 @@ def test_sample_ggx_vndf_expectation():             # Tests.cpp:188-210
 def test_refraction_roundtrip_and_fresnel_reciprocity():   # Tests.cpp:212-232
     d, f = property_test(9, 1)
     assert d <= 1e-5 * np.sqrt(3) and f <= 1e-5
+
+
+@pytest.mark.parametrize("name", ["cornell", "room", "field"])
+def test_photon_mapper_matches_reference(name):
+    """The restated photon mapper (oracle/port/oracle_pm.cpp) against the
+    reference's own (PhotonMapping.cpp through oracle/ref_pm_harness.cpp):
+    every progressive iteration's colour, normal, albedo and radius images and
+    photon counts, bit for bit."""
+    from oracle.oracle import PhotonMapper
+    g = np.load(os.path.join(GOLDEN, f"pm_{name}.npz"))
+    pm = PhotonMapper(os.path.join(GOLDEN, "scenes", name, "renderJob.json"))
+    try:
+        for it in range(g["color"].shape[0]):
+            r = pm.iterate(1)
+            assert r["emitted"] == g["emitted"][it] and r["stored"] == g["stored"][it], it
+            for k in ("color", "normal", "albedo", "radii"):
+                assert np.array_equal(r[k], g[k][it], equal_nan=True), (k, it)
+    finally:
+        pm.close()
