@@ -175,9 +175,10 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--bvh", default="wide", choices=["wide", "binary"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "stress"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "stress", "photon"],
                     help="plain: the large single job (default); batch: the 64-job mix batched vs one by one; "
-                         "serve: Poisson arrivals over the server; stress: 10.36M-triangle 4K scene, one pass per step")
+                         "serve: Poisson arrivals over the server; stress: 10.36M-triangle 4K scene, one pass per step; "
+                         "photon: the photon mapper on the textured room, one progressive iteration per step")
     ap.add_argument("--jobs", type=int, default=64, help="batch/serve: jobs in the mix (serve: scene pool = half)")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: arrivals per second")
     ap.add_argument("--duration", type=float, default=120.0, help="serve: seconds of arrivals")
@@ -185,6 +186,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "stress":
         return run_stress(args)
+    if args.workload == "photon":
+        return run_photon(args)
     if args.workload != "plain":
         return run_mixed(args)
 
@@ -335,6 +338,75 @@ def main():
     job.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+PHOTON_WORKLOAD = "photon_mapping_textured_room_640x480_tex256_depth8_caustics_map"
+
+
+def run_photon(args):
+    """The photon mapper (hasty_pm_render) on the textured room (area light,
+    smooth glass sphere, glossy and anisotropic metal, texture maps) at
+    640x480, depth 8: one stochastic progressive iteration per step (photon
+    tracing until 0.5*W*H caustic photons are stored, photon-map build, gather
+    of every pixel). value = pixels gathered per second by the wall clock (the
+    host part of an iteration is real work); the CPU baseline is the checker's
+    photon mapper (one thread, as one reference render thread) on the same
+    scene at 160x120."""
+    import numpy as np
+    import torch
+    from hastyrenderer_gb300 import Context, RenderJob, scenes
+    torch.cuda.init()
+    base = os.environ.get("HASTY_BENCH_PHOTON", os.path.join(tempfile.gettempdir(), "hasty_bench_photon"))
+    path = os.path.join(base, "renderJob.json")
+    if not os.path.exists(path):
+        scenes.textured_room(base, seed=5, width=640, height=480, spp=64, max_depth=8, tex_size=256)
+    job = RenderJob(path, Context(0))
+    info = job.info
+    W, H = info.width, info.height
+    for _ in range(args.warmup):
+        job.pm_render(1)
+    s0 = job.pm_stats()
+    sampler = ClockSampler(0)
+    with sampler:
+        t0 = time.perf_counter()
+        job.pm_render(args.steps)
+        wall = time.perf_counter() - t0
+    s1 = job.pm_stats()
+    est = job.pm_read(0)
+    dev_ms = s1["device_ms"] - s0["device_ms"]
+    host_ms = s1["host_ms"] - s0["host_ms"]
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle.oracle import PhotonMapper
+        small = os.path.join(base + "_small", "renderJob.json")
+        if not os.path.exists(small):
+            scenes.textured_room(os.path.dirname(small), seed=5, width=160, height=120, spp=64, max_depth=8, tex_size=256)
+        pm = PhotonMapper(small)
+        pm.iterate(1)
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < min(args.cpu_budget, 10.0) or k == 0:
+            pm.iterate(1)
+            k += 1
+        dt = time.perf_counter() - t0
+        pm.close()
+        cpu = {"value": k * 160 * 120 / dt, "unit": "pixels/s", "cores": 1, "kind": "port",
+               "sample": f"{k} iterations of the same scene at 160x120 after one warm-up iteration, {dt:.1f} s"}
+    line = {
+        "metric": "pixels/s", "value": args.steps * W * H / wall, "unit": "pixels/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": PHOTON_WORKLOAD, "width": W, "height": H, "max_depth": info.max_depth,
+                   "triangles": info.n_triangles, "step": "one progressive photon-mapping iteration",
+                   "l2": "working set < L2 (small scene); no flush"},
+        "device_ms_per_step": dev_ms / args.steps, "host_ms_per_step": host_ms / args.steps,
+        "photons_emitted_per_step": s1["photons_emitted"], "photons_stored_per_step": s1["photons_stored"],
+        "photons_traced_per_s": s1["photons_emitted"] * args.steps / wall,
+        "estimate_finite": bool(np.isfinite(est).all()), "media_overflow": s1["media_overflow"],
+        "cpu_baseline": cpu, "clocks": sampler.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    job.close()
 
 
 STRESS_WORKLOAD = "stress_8000x_icosphere3_10000_cuboids_10360016tri_3840x2160_rgba8tex4096_cauchy_depth32"

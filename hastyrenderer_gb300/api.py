@@ -142,6 +142,32 @@ class RenderJob:
         check(native.lib().hasty_job_read_sums(self._h, aov, out.ctypes.data, i.width, i.height, ctypes.byref(n)))
         return out, n.value
 
+    # ---- photon mapping (hasty_pm_*): the reference's second integrator ----
+    def pm_render(self, iterations: int = 1) -> None:
+        """Renders more stochastic progressive photon-mapping iterations."""
+        check(native.lib().hasty_pm_render(self._h, int(iterations)))
+
+    def pm_reset(self) -> None:
+        check(native.lib().hasty_pm_reset(self._h))
+
+    def pm_read(self, aov: int = AOV_COLOR) -> np.ndarray:
+        """The photon mapper's current image (colour with exposure, normal, albedo)."""
+        i = self.info
+        out = np.empty((i.height, i.width, 3), dtype=np.float32)
+        check(native.lib().hasty_pm_read(self._h, aov, out.ctypes.data, i.width, i.height))
+        return out
+
+    def pm_radii(self) -> np.ndarray:
+        i = self.info
+        out = np.empty((i.height, i.width), dtype=np.float32)
+        check(native.lib().hasty_pm_read_radii(self._h, out.ctypes.data, i.width, i.height))
+        return out
+
+    def pm_stats(self) -> dict:
+        s = native.PmStats()
+        check(native.lib().hasty_pm_stats_get(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in native.PmStats._fields_}
+
     def write_outputs(self, out_dir: str, write_pfm: bool = False) -> None:
         check(native.lib().hasty_job_write_outputs(self._h, out_dir.encode(), 1 if write_pfm else 0))
 

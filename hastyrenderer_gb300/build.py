@@ -5,7 +5,8 @@
 
 CUDA sources are compiled for sm_103a only; `integrator.cu` without FMA
 contraction (products and sums round like the reference's scalar C++), and
-`bvh_gpu.cu` likewise (its layout writer matches the host writer's bytes).
+`bvh_gpu.cu` likewise (its layout writer matches the host writer's bytes), and
+`photon.cu` (the photon mapper's shading, like the integrator's).
 Outputs: hastyrenderer_gb300/lib/libhasty_gb300.so, lib/hasty_gpu_render.
 """
 from __future__ import annotations
@@ -27,12 +28,12 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE,
                "-I" + CSRC, "--expt-relaxed-constexpr"]
-CU_EXTRA = {"integrator.cu": ["--fmad=false"], "bvh_gpu.cu": ["--fmad=false"]}
+CU_EXTRA = {"integrator.cu": ["--fmad=false"], "bvh_gpu.cu": ["--fmad=false"], "photon.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-sign-compare"]
-CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu", "bvh_gpu.cu"]
+CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu", "bvh_gpu.cu", "photon.cu"]
 # Extra nvcc flags for experiments (e.g. HASTY_NVCC_FLAGS="-DHASTY_OUTLINE_MASK=3").
 EXTRA_NVCC = os.environ.get("HASTY_NVCC_FLAGS", "").split()
-CPP_SOURCES = ["api.cpp", "engine.cpp", "server.cpp", "scene_load.cpp", "bvh_build.cpp", "image_out.cpp"]
+CPP_SOURCES = ["api.cpp", "engine.cpp", "server.cpp", "scene_load.cpp", "bvh_build.cpp", "image_out.cpp", "photon_map.cpp"]
 
 
 def cuda_home() -> str:

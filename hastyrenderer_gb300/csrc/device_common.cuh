@@ -318,14 +318,19 @@ __device__ __forceinline__ float normal_scale(V3 wi, V3 ns, V3 ng) { return fabs
 __device__ __forceinline__ float compute_alpha(float r) { float a = r * r; return (a < 1e-2f && a != 0.0f) ? 1e-2f : a; }
 
 struct Prob { bool none, refr; float pD, pS, pR, FD, cosT; };
+// ShaderEvalFlag (BRDF.h): the lobes a sample covers.
+enum : int { kLobeDiffuse = 1, kLobeConcentrated = 2, kLobeAll = 3 };
 // BRDF.cpp:264-307
-__device__ __forceinline__ Prob compute_probability(float m, float s, float t, float cos_o, float eo, float er) {
+__device__ __forceinline__ Prob compute_probability(float m, float s, float t, float cos_o, float eo, float er,
+                                                    int lobes = kLobeAll) {
   Prob p; p.cosT = 0.0f;
   p.refr = refraction_cos_t(cos_o, eo, er, p.cosT);
   p.FD = p.refr ? fresnel_dielectric(cos_o, p.cosT, eo, er) : 1.0f;
   float mD = (1.0f - t) * (1.0f - m) * (1.0f - 0.5f * s);
   float mS = mixf(mixf(0.5f * s, p.FD, t), 1.0f, m);
   float mR = float((1.0 - double(p.FD)) * double(t) * (1.0 - double(m)));
+  if (!(lobes & kLobeDiffuse)) mD = 0.0f;
+  if (!(lobes & kLobeConcentrated)) { mS = 0.0f; mR = 0.0f; }
   float sum = mD + mS + mR;
   p.none = sum == 0.0f;
   if (p.none) { p.pD = p.pS = p.pR = 0.0f; }
@@ -477,10 +482,12 @@ HFN_EVAL float bsdf_pdf(const ShadeCtx& c, const MaterialDev& m, V3 wo, V3 wi, f
 }
 
 struct BsdfSample { bool outside; V3 dir, thrD, thrC; float pdf; };
-// PrincipledBRDF::sample (member + static), BRDF.cpp:397-579, 681-700
+// PrincipledBRDF::sample (member + static), BRDF.cpp:397-579, 681-700;
+// `lobes` restricts the strategies (ShaderEvalFlag), `adjoint` drops the
+// (eta_o / eta_t)^2 radiance scaling of refraction (importance transport).
 template <class R>
 HFN_SAMPLE BsdfSample bsdf_sample(const ShadeCtx& c, const MaterialDev& m, const Inter& it, V3 wo, int wl, float eta_out,
-                                  R& r, int& capped) {
+                                  R& r, int& capped, int lobes = kLobeAll, bool adjoint = false) {
   BsdfSample res;
   const V3 ns = c.ns, alb = c.alb, tan = c.tan, bit = c.bit;
   const float met = c.met, alpha = c.alpha, at = c.at, ab = c.ab, nswo = c.nswo;
@@ -489,7 +496,7 @@ HFN_SAMPLE BsdfSample bsdf_sample(const ShadeCtx& c, const MaterialDev& m, const
   res.outside = c.ngwo >= 0.0f;
   float eo = res.outside ? eta_out : eta_mat;
   float er = res.outside ? eta_mat : eta_out;
-  Prob p = compute_probability(met, s, t, nswo, eo, er);
+  Prob p = compute_probability(met, s, t, nswo, eo, er, lobes);
   if (p.none) { res.dir = V3(1.f, 0.f, 0.f); res.pdf = 0.0f; return res; }
   V3 fD, fC;
   float xi = r.u01();
@@ -533,7 +540,7 @@ HFN_SAMPLE BsdfSample bsdf_sample(const ShadeCtx& c, const MaterialDev& m, const
     } else {
       float ratio = eo / er;
       res.dir = normalize((-ratio) * wo + (ratio * nswo - p.cosT) * ns);
-      float fc = res.pdf / p.pR * sq(ratio) * (1.0f - p.FD) / fabsf(dot(res.dir, it.ng));
+      float fc = res.pdf / p.pR * (adjoint ? 1.0f : sq(ratio)) * (1.0f - p.FD) / fabsf(dot(res.dir, it.ng));
       V3 mask = wl < 0 ? V3(1.f, 1.f, 1.f) : V3(wl == 0 ? 1.f : 0.f, wl == 1 ? 1.f : 0.f, wl == 2 ? 1.f : 0.f);
       fC = fc * mask;
     }

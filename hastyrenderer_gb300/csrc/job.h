@@ -55,6 +55,11 @@ using hasty::HostScene;
 using hasty::SceneDev;
 using hasty::PathsDev;
 
+namespace hasty {
+struct PmDev;                    // photon-mapper state (photon_map.cpp)
+void destroy_pm(PmDev* pm);
+}  // namespace hasty
+
 struct hasty_ctx {
   int device = 0;
   int sm_count = 0;
@@ -83,6 +88,7 @@ struct hasty_job {
   bool lane_free_valid[2] = {false, false};
   bool lanes_wait_main = true;
   int next_lane = 0;
+  hasty::PmDev* pm = nullptr;         // photon mapper (device buffers are in `allocs`)
   // host-side scene data between prepare and upload (BVH, guide tables)
   struct Prepared {
     hasty::BvhHost bvh;
@@ -149,6 +155,7 @@ struct hasty_job {
     if (stream) cudaStreamSynchronize(stream);
     for (cudaStream_t s : lane_stream) if (s) cudaStreamSynchronize(s);
     collect_events();
+    hasty::destroy_pm(pm);
     for (const Block& b : allocs) cudaFree(b.p);
     for (int k = 0; k < 2; ++k) {
       if (lane_done[k]) cudaEventDestroy(lane_done[k]);

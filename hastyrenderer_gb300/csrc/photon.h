@@ -1,0 +1,69 @@
+// Photon mapper (stochastic progressive photon mapping with a caustics map):
+// device data and kernel launchers (photon.cu); the host side and the C ABI
+// are in photon_map.cpp.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "hasty_types.h"
+
+namespace hasty {
+
+// Random-stream keys of the photon mapper: photon i of iteration t, and the
+// initial radius footprint of a pixel (a pass value no render reaches).
+constexpr uint64_t kPhotonKeyMix = 0x50484F544F4E5321ull;
+constexpr uint32_t kFootprintPass = 0xFFFFFFFFu;
+// Deepest path the gather walks (its per-depth frames live in registers /
+// local memory); jobs with a larger max_depth are refused.
+constexpr int kPmMaxDepth = 32;
+
+// One stored photon: position + n_g . w_from, incoming direction (towards
+// where it came from) + emission index, flux + depth.
+struct PhotonRec { float4 xn, wi, flux; };
+
+struct PmEmitOut {
+  PhotonRec* photons;      // append buffer
+  uint32_t* count;         // photons appended (may exceed cap: those beyond are dropped)
+  uint32_t cap;
+  uint8_t* stored;         // per emitted photon of the launch: photons it stored
+  unsigned long long* stats;   // [0] media overflow, [1] trial cap
+};
+
+// Photon map of one iteration: photons sorted by (cell x, y, z, emission
+// index, depth); cells sorted lexicographically with the first photon and
+// the count of each.
+struct PmMapDev {
+  const PhotonRec* photons;
+  const int4* cells;       // x, y, z, first photon
+  const int32_t* cell_count;
+  int32_t n_cells;
+  float cell;
+};
+
+// Per-pixel statistics (PMRenderJobPixel) and the thread's images.
+struct PmPixelsDev {
+  float* radius;           // -1 until first set
+  float* N;
+  float* Ne;
+  float4* flux;
+  float4* lsum;            // xyz: sum of L, w: number of samples (int bits)
+  float* radii;            // the radius image of the render thread
+  float* color;            // 3 per pixel
+  float* normal;
+  float* albedo;
+};
+
+// Distance from the camera to the first surface with a diffuse lobe along
+// each pixel centre's ray (through up to max_depth concentrated bounces), or
+// -1 where the reference's footprint falls back to its default.
+void launch_pm_footprint(const SceneDev& sc, uint64_t seed, float* dist, cudaStream_t st);
+// Emits photons [first, first + n) of iteration `iter` and traces them;
+// min_q = 1 - 0.1^(1 / max_depth), the least absorption probability per
+// bounce (evaluated on the host with the reference's std::pow).
+void launch_pm_emit(const SceneDev& sc, uint64_t seed, uint32_t iter, uint32_t first, uint32_t n, float min_q,
+                    const PmEmitOut& out, cudaStream_t st);
+// Gathers every pixel of iteration `iter` (camera offset ox, oy) and updates
+// the pixel statistics; `emitted` photons were emitted this iteration.
+void launch_pm_gather(const SceneDev& sc, const PmMapDev& map, const PmPixelsDev& px, uint64_t seed, uint32_t iter,
+                      float ox, float oy, int emitted, unsigned long long* stats, cudaStream_t st);
+
+}  // namespace hasty

@@ -54,6 +54,12 @@ class BatchStats(ctypes.Structure):
                 ("engine_bytes", ctypes.c_int64)]
 
 
+class PmStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("photons_emitted", ctypes.c_int64), ("photons_stored", ctypes.c_int64),
+                ("cell_size", ctypes.c_float), ("device_ms", ctypes.c_double), ("host_ms", ctypes.c_double),
+                ("media_overflow", ctypes.c_uint64), ("trial_cap", ctypes.c_uint64)]
+
+
 class ServerConfig(ctypes.Structure):
     _fields_ = [("paths_in_flight", ctypes.c_int64), ("regen_fraction", ctypes.c_float),
                 ("max_resident_jobs", ctypes.c_int32), ("max_resident_scenes", ctypes.c_int32),
@@ -121,6 +127,11 @@ def lib() -> ctypes.CDLL:
         "hasty_debug_bsdf": [I, P, SZ, P, SZ, P],
         "hasty_debug_wide_emit_check": [I, ctypes.c_char_p, P, P],
         "hasty_batch_render": [P, P, P, SZ, P, P],
+        "hasty_pm_render": [P, I],
+        "hasty_pm_reset": [P],
+        "hasty_pm_read": [P, I, P, SZ, SZ],
+        "hasty_pm_read_radii": [P, P, SZ, SZ],
+        "hasty_pm_stats_get": [P, P],
         "hasty_job_render_pass_static": [P, I, P],
         "hasty_server_start": [P, P, P],
         "hasty_server_submit": [P, ctypes.c_char_p, ctypes.c_int32, P, P],

@@ -120,6 +120,41 @@ int hasty_job_read_sums(hasty_job* job, int aov, double* host_rgb, size_t w, siz
 /* output.exr, outputNormal.exr, outputAlbedo.exr (+ .pfm copies when write_pfm != 0). */
 int hasty_job_write_outputs(hasty_job* job, const char* out_dir, int write_pfm);
 
+/* ---- Photon mapping (the reference's second integrator) ------------------
+ * Stochastic progressive photon mapping with a caustics map, as one render
+ * thread of the reference runs it (core/src/PhotonMapping.cpp:814-935,
+ * renderPhotonThread; PMRenderJob, core/include/Hasty/PhotonMapping.h): per
+ * iteration, photons from the area lights (sampleLightRay) are traced until
+ * 0.5*W*H caustic photons (L S+ D, stored at diffuse surfaces after the first
+ * bounce) are stored or 10*W*H were emitted; every pixel then path-traces
+ * with both MIS strategies, adds photon estimates at diffuse vertices (hash
+ * cells, per-pixel radius) and updates its radius/flux statistics (alpha
+ * 0.4). Initial radii: 10x the pixel footprint with a surface light, else 1.
+ * Random streams are keyed per photon and per pixel (the reference shares
+ * one stream per thread), so results do not depend on threads. Replaces the
+ * render threads of apps/PhotonMappingViewer.cpp:48-57. max_depth <= 32. */
+typedef struct hasty_pm_stats {
+  int32_t iterations;          /* iterations rendered */
+  int64_t photons_emitted;     /* last iteration */
+  int64_t photons_stored;      /* last iteration */
+  float cell_size;             /* hash-cell size of the last iteration */
+  double device_ms;            /* photon tracing + gather kernels, all iterations */
+  double host_ms;              /* host work (cell size, photon sort, copies), all iterations */
+  uint64_t media_overflow;     /* medium-stack pushes beyond 4 (dropped) */
+  uint64_t trial_cap;          /* rejection loops that hit their bound */
+} hasty_pm_stats;
+
+/* Renders `iterations` more progressive iterations (synchronous). */
+int hasty_pm_render(hasty_job* job, int iterations);
+/* Restarts from the initial radii and empty statistics at the next render. */
+int hasty_pm_reset(hasty_job* job);
+/* Current estimate (w*h*3 floats): colour (x 2^exposure), normal or albedo
+ * of the last iteration, as the reference's thread image buffers. */
+int hasty_pm_read(hasty_job* job, int aov, float* host_rgb, size_t w, size_t h);
+/* Per-pixel gather radii after the last iteration (w*h floats). */
+int hasty_pm_read_radii(hasty_job* job, float* host, size_t w, size_t h);
+int hasty_pm_stats_get(hasty_job* job, hasty_pm_stats* stats);
+
 /* ---- Batching: many jobs in one persistent multi-job wavefront ------------
  * Path slots are shared by all jobs and refilled with new camera samples as
  * paths finish (regeneration); one CUDA graph launch whose conditional
