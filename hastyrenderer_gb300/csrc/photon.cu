@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(128) k_pm_emit(SceneDev sc, uint64_t seed, uin
           PhotonRec rec;
           rec.xn = make_float4(it.x.x, it.x.y, it.x.z, dot(it.ng, wo));
           rec.wi = make_float4(wo.x, wo.y, wo.z, __uint_as_float(idx));
-          rec.flux = make_float4(flux.x, flux.y, flux.z, __uint_as_float(uint32_t(depth)));
+          rec.flux = make_float4(flux.x, flux.y, flux.z, __uint_as_float(stored));   // k-th photon of this emission
           out.photons[slot] = rec;
         }
         ++stored;

@@ -17,7 +17,8 @@ constexpr uint32_t kFootprintPass = 0xFFFFFFFFu;
 constexpr int kPmMaxDepth = 32;
 
 // One stored photon: position + n_g . w_from, incoming direction (towards
-// where it came from) + emission index, flux + depth.
+// where it came from) + emission index, flux + its index among the photons
+// its emission stored (in depth order).
 struct PhotonRec { float4 xn, wi, flux; };
 
 struct PmEmitOut {

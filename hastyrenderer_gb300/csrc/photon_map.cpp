@@ -10,6 +10,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "job.h"
@@ -97,16 +98,36 @@ float cell_size_for(const std::vector<float>& radii, uint32_t W, uint32_t H) {
       }
     return s;
   };
-  float best = cost(cs);
-  for (int k = 0; k < 10; k++) {
-    float trial = cs * 1.5f, tc = cost(trial);
-    if (!(tc < best)) break;
-    cs = trial; best = tc;
+  // The reference evaluates cost(cs), then up to 10 trials cs *= 1.5 while
+  // they improve, then up to 10 trials cs *= 0.6666. The trial values along
+  // that path are fixed in advance, so their costs are evaluated at once on
+  // several threads and the same decisions are taken afterwards.
+  auto costs_of = [&](const std::vector<float>& c) {
+    std::vector<float> out(c.size());
+    std::vector<std::thread> th;
+    for (size_t k = 1; k < c.size(); ++k) th.emplace_back([&, k] { out[k] = cost(c[k]); });
+    if (!c.empty()) out[0] = cost(c[0]);
+    for (std::thread& t : th) t.join();
+    return out;
+  };
+  std::vector<float> up(11);
+  up[0] = cs;
+  for (int k = 1; k <= 10; ++k) up[size_t(k)] = up[size_t(k) - 1] * 1.5f;
+  std::vector<float> cu = costs_of(up);
+  float best = cu[0];
+  size_t at = 0;
+  for (size_t k = 1; k <= 10; ++k) {
+    if (!(cu[k] < best)) break;
+    best = cu[k]; at = k;
   }
-  for (int k = 0; k < 10; k++) {
-    float trial = cs * 0.6666f, tc = cost(trial);
-    if (!(tc < best)) break;
-    cs = trial; best = tc;
+  cs = up[at];
+  std::vector<float> down(10);
+  down[0] = cs * 0.6666f;
+  for (int k = 1; k < 10; ++k) down[size_t(k)] = down[size_t(k) - 1] * 0.6666f;
+  std::vector<float> cd = costs_of(down);
+  for (size_t k = 0; k < 10; ++k) {
+    if (!(cd[k] < best)) break;
+    best = cd[k]; cs = down[k];
   }
   return cs;
 }
@@ -190,8 +211,6 @@ void pm_init(hasty_job& j, PmDev& pm) {
   pm.iteration = 0;
 }
 
-struct SortKey { int32_t x, y, z; uint32_t emit, depth, idx; };
-
 // One iteration of renderPhotonThread's loop (PhotonMapping.cpp:848-931).
 void pm_iteration(hasty_job& j, PmDev& pm) {
   const uint32_t W = pm.W, H = pm.H, t = pm.iteration;
@@ -209,7 +228,8 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
     dev_ms += ms;
   };
   const float cell = cell_size_for(pm.radii, W, H);
-  uint64_t emitted = 0;
+  uint64_t emitted = 0, kept = 0;
+  std::vector<uint64_t> base;          // first emission-order slot of each emitted photon
   std::vector<PhotonRec> host_ph;
   if (j.sd.n_light_tris > 0) {
     const int trace_threshold = int(10.f * float(H) * float(W));
@@ -218,6 +238,7 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
     const float min_q = 1.0f - std::pow(0.1f, 1.0f / j.sd.max_depth);
     uint64_t first = 0, cum = 0;
     uint32_t appended = 0;
+    base.clear();
     size_t chunk = std::max<size_t>(size_t(1) << 16, 2 * size_t(count_threshold));
     ck(cudaMemsetAsync(pm.append_count, 0, sizeof(uint32_t), j.stream), "photon count");
     bool done = count_threshold <= 0;
@@ -238,9 +259,11 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
       if (appended > pm.append_cap) throw ApiError{HASTY_ERR_CUDA, "photon buffer overflow"};
       // the reference emits photon i while fewer than count_threshold are stored
       for (uint32_t k = 0; k < n && !done; ++k) {
+        base.push_back(cum);
         cum += stored[k];
         if (cum >= uint64_t(count_threshold)) { emitted = first + k + 1; done = true; }
       }
+      kept = cum;
       if (!done) { first += n; emitted = first; }
       chunk *= 2;
     }
@@ -249,32 +272,66 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
       ck(cudaMemcpyAsync(host_ph.data(), pm.append, appended * sizeof(PhotonRec), cudaMemcpyDeviceToHost, j.stream), "photons");
     ck(cudaStreamSynchronize(j.stream), "photons");
   }
-  // hash cells: keep the photons of the emitted range, order them by cell,
-  // then by emission index and depth
-  std::vector<SortKey> keys;
-  keys.reserve(host_ph.size());
-  for (uint32_t i = 0; i < host_ph.size(); ++i) {
-    const PhotonRec& r = host_ph[i];
-    uint32_t emit, depth;
+  // Photon map: the photons of the emitted range in emission order (slot =
+  // the emission's first slot + the photon's index within it), then a stable
+  // radix sort by hash cell, so each cell lists its photons in the order the
+  // reference stored them.
+  std::vector<PhotonRec> ordered(kept);
+  for (const PhotonRec& r : host_ph) {
+    uint32_t emit, k;
     std::memcpy(&emit, &r.wi.w, 4);
-    std::memcpy(&depth, &r.flux.w, 4);
-    if (emit >= emitted) continue;
-    keys.push_back(SortKey{floor_i32(r.xn.x / cell), floor_i32(r.xn.y / cell), floor_i32(r.xn.z / cell), emit, depth, i});
+    std::memcpy(&k, &r.flux.w, 4);
+    if (emit < emitted) ordered[base[emit] + k] = r;
   }
-  std::sort(keys.begin(), keys.end(), [](const SortKey& a, const SortKey& b) {
-    if (a.x != b.x) return a.x < b.x;
-    if (a.y != b.y) return a.y < b.y;
-    if (a.z != b.z) return a.z < b.z;
-    if (a.emit != b.emit) return a.emit < b.emit;
-    return a.depth < b.depth;
-  });
-  std::vector<PhotonRec> sorted(keys.size());
+  const size_t np = ordered.size();
+  std::vector<int32_t> cxyz(3 * np);
+  int32_t lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (size_t q = 0; q < np; ++q) {
+    const float* x = &ordered[q].xn.x;
+    for (int a = 0; a < 3; ++a) {
+      int32_t c = floor_i32(x[a] / cell);
+      cxyz[3 * q + a] = c;
+      if (q == 0 || c < lo[a]) lo[a] = c;
+      if (q == 0 || c > hi[a]) hi[a] = c;
+    }
+  }
+  const uint64_t nx = uint64_t(int64_t(hi[0]) - lo[0] + 1), ny = uint64_t(int64_t(hi[1]) - lo[1] + 1),
+                 nz = uint64_t(int64_t(hi[2]) - lo[2] + 1);
+  const bool fits = double(nx) * double(ny) * double(nz) < 9.0e18;      // linear cell key fits 64 bits
+  std::vector<uint64_t> key(np);
+  std::vector<uint32_t> perm(np), tmp(np);
+  for (size_t q = 0; q < np; ++q) perm[q] = uint32_t(q);
+  if (fits) {
+    for (size_t q = 0; q < np; ++q)
+      key[q] = (uint64_t(int64_t(cxyz[3 * q]) - lo[0]) * ny + uint64_t(int64_t(cxyz[3 * q + 1]) - lo[1])) * nz +
+               uint64_t(int64_t(cxyz[3 * q + 2]) - lo[2]);
+    uint64_t maxkey = 0;
+    for (uint64_t k : key) maxkey = std::max(maxkey, k);
+    for (int shift = 0; shift < 64 && (maxkey >> shift) != 0; shift += 16) {     // LSD radix, stable
+      std::vector<uint32_t> hist(65537, 0);
+      for (size_t q = 0; q < np; ++q) hist[((key[perm[q]] >> shift) & 0xFFFFu) + 1]++;
+      for (size_t b = 1; b < hist.size(); ++b) hist[b] += hist[b - 1];
+      for (size_t q = 0; q < np; ++q) tmp[hist[(key[perm[q]] >> shift) & 0xFFFFu]++] = perm[q];
+      perm.swap(tmp);
+    }
+  } else {                                                 // huge cell ranges: compare the coordinates
+    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
+      for (int c = 0; c < 3; ++c)
+        if (cxyz[3 * a + c] != cxyz[3 * b + c]) return cxyz[3 * a + c] < cxyz[3 * b + c];
+      return false;
+    });
+    for (size_t q = 0; q < np; ++q)   // equal coordinates <=> equal key (cell boundaries below)
+      key[perm[q]] = q > 0 && std::equal(&cxyz[3 * perm[q]], &cxyz[3 * perm[q]] + 3, &cxyz[3 * perm[q - 1]])
+                         ? key[perm[q - 1]] : uint64_t(q);
+  }
+  std::vector<PhotonRec> sorted(np);
   std::vector<int4> cells;
   std::vector<int32_t> counts;
-  for (size_t k = 0; k < keys.size(); ++k) {
-    sorted[k] = host_ph[keys[k].idx];
-    if (k == 0 || keys[k].x != keys[k - 1].x || keys[k].y != keys[k - 1].y || keys[k].z != keys[k - 1].z) {
-      cells.push_back(make_int4(keys[k].x, keys[k].y, keys[k].z, int(k)));
+  for (size_t q = 0; q < np; ++q) {
+    const uint32_t src = perm[q];
+    sorted[q] = ordered[src];
+    if (q == 0 || key[src] != key[perm[q - 1]]) {
+      cells.push_back(make_int4(cxyz[3 * src], cxyz[3 * src + 1], cxyz[3 * src + 2], int(q)));
       counts.push_back(0);
     }
     counts.back() += 1;
@@ -299,7 +356,7 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
   ck(cudaStreamSynchronize(j.stream), "radii");
   cudaEventDestroy(e0); cudaEventDestroy(e1);
   pm.emitted = emitted;
-  pm.photons = keys.size();
+  pm.photons = np;
   pm.cell = cell;
   pm.iteration = t + 1;
   pm.device_ms += dev_ms;
