@@ -41,7 +41,8 @@ struct PmDev {
   // last iteration
   uint64_t emitted = 0, photons = 0;
   float cell = 0.0f;
-  double device_ms = 0.0, host_ms = 0.0;
+  double device_ms = 0.0, host_ms = 0.0, photon_ms = 0.0, gather_ms = 0.0;
+  uint64_t last_emitted = 0;               // sizes the next iteration's first photon batch
 };
 
 void destroy_pm(PmDev* pm) { delete pm; }
@@ -218,7 +219,8 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
   double dev_ms = 0.0;
   cudaEvent_t e0, e1;
   ck(cudaEventCreate(&e0), "event"); ck(cudaEventCreate(&e1), "event");
-  auto time_device = [&](auto&& fn) {
+  double photon_ms = 0.0, gather_ms = 0.0;
+  auto time_device = [&](double& part, auto&& fn) {
     ck(cudaEventRecord(e0, j.stream), "event");
     fn();
     ck(cudaEventRecord(e1, j.stream), "event");
@@ -226,6 +228,7 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     dev_ms += ms;
+    part += ms;
   };
   const float cell = cell_size_for(pm.radii, W, H);
   uint64_t emitted = 0, kept = 0;
@@ -239,7 +242,9 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
     uint64_t first = 0, cum = 0;
     uint32_t appended = 0;
     base.clear();
-    size_t chunk = std::max<size_t>(size_t(1) << 16, 2 * size_t(count_threshold));
+    // first batch: what the previous iteration needed (+10%), else 2x the stored target
+    size_t chunk = std::max<size_t>(size_t(1) << 16, pm.last_emitted ? size_t(pm.last_emitted * 1.1) + 1024
+                                                                     : 2 * size_t(count_threshold));
     ck(cudaMemsetAsync(pm.append_count, 0, sizeof(uint32_t), j.stream), "photon count");
     bool done = count_threshold <= 0;
     std::vector<uint8_t> stored;
@@ -248,7 +253,7 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
       pm.append = grow(j, pm.append, pm.append_cap, size_t(appended) + size_t(n) * depth_slots, appended);
       pm.stored = grow(j, pm.stored, pm.stored_cap, n, 0);
       PmEmitOut out{pm.append, pm.append_count, uint32_t(pm.append_cap), pm.stored, pm.stats};
-      time_device([&] {
+      time_device(photon_ms, [&] {
         launch_pm_emit(j.sd, j.seed, t, uint32_t(first), n, min_q, out, j.stream);
         ck(cudaGetLastError(), "photon launch");
       });
@@ -347,7 +352,7 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
   }
   PmMapDev map{pm.sorted, pm.cells, pm.cell_count, int32_t(cells.size()), cell};
   const float ox = halton_value(2, t), oy = halton_value(3, t);
-  time_device([&] {
+  time_device(gather_ms, [&] {
     launch_pm_gather(j.sd, map, pm.px, j.seed, t, ox, oy, int(emitted), pm.stats, j.stream);
     ck(cudaGetLastError(), "gather launch");
   });
@@ -360,6 +365,9 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
   pm.cell = cell;
   pm.iteration = t + 1;
   pm.device_ms += dev_ms;
+  pm.photon_ms += photon_ms;
+  pm.gather_ms += gather_ms;
+  pm.last_emitted = emitted;
   pm.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count() - dev_ms;
 }
 
@@ -449,6 +457,8 @@ int hasty_pm_stats_get(hasty_job* job, hasty_pm_stats* out) {
     }
     out->media_overflow = st[0];
     out->trial_cap = st[1];
+    out->photon_ms = pm.photon_ms;
+    out->gather_ms = pm.gather_ms;
     return HASTY_OK;
   });
 }

@@ -57,7 +57,8 @@ class BatchStats(ctypes.Structure):
 class PmStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("photons_emitted", ctypes.c_int64), ("photons_stored", ctypes.c_int64),
                 ("cell_size", ctypes.c_float), ("device_ms", ctypes.c_double), ("host_ms", ctypes.c_double),
-                ("media_overflow", ctypes.c_uint64), ("trial_cap", ctypes.c_uint64)]
+                ("media_overflow", ctypes.c_uint64), ("trial_cap", ctypes.c_uint64), ("photon_ms", ctypes.c_double),
+                ("gather_ms", ctypes.c_double)]
 
 
 class ServerConfig(ctypes.Structure):

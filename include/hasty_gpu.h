@@ -142,6 +142,8 @@ typedef struct hasty_pm_stats {
   double host_ms;              /* host work (cell size, photon sort, copies), all iterations */
   uint64_t media_overflow;     /* medium-stack pushes beyond 4 (dropped) */
   uint64_t trial_cap;          /* rejection loops that hit their bound */
+  double photon_ms;            /* of device_ms: photon emission and tracing */
+  double gather_ms;            /* of device_ms: per-pixel gather */
 } hasty_pm_stats;
 
 /* Renders `iterations` more progressive iterations (synchronous). */
