@@ -13,7 +13,8 @@ Prints one JSON line (rank 0). `value` is camera samples per second over all
 ranks (each rank renders its own pass range of the same job: weak scaling);
 `e2e` is the same metric through the C ABI including the job load (host
 parse, BVH build, host->device upload) and a device->host read of the colour
-estimate after every step. `cpu_baseline` times the CPU checker (oracle/)
+estimate of every step (hasty_job_snapshot: copied while the next step
+renders, as a progressive viewer reads it). `cpu_baseline` times the CPU checker (oracle/)
 on this host's cores on a bounded crop of the same job.
 """
 from __future__ import annotations
@@ -227,10 +228,18 @@ def main():
     job = RenderJob(job_path, ctx)
     info = job.info
     W, H = info.width, info.height
+    # each step's colour estimate is read back while the next step renders
+    # (hasty_job_snapshot: estimate behind the step, copy on a copy stream)
+    est_sum = 0.0
     for k in range(args.steps):
         job.render_passes(args.spp_per_step)
-        est = job.compute_estimate()
+        if k:
+            est, _ = job.snapshot_get()
+            est_sum += float(est[0, 0, 0])
+        job.snapshot()
+    est, n_est = job.snapshot_get()
     e2e_s = time.perf_counter() - t0
+    assert n_est == args.steps * args.spp_per_step
     e2e_bytes_up = info.device_bytes
     del est
 
@@ -331,7 +340,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": args.steps * args.spp_per_step * W * H * world / e2e_s, "unit": "samples/s",
                     "h2d_bytes_per_step": int(e2e_bytes_up // args.steps), "d2h_bytes_per_step": W * H * 3 * 4,
-                    "includes": "job load (parse, BVH build, upload) + steps + colour read-back"},
+                    "includes": "job load (parse, BVH build, upload) + steps + a colour read-back per step, each copied while the next step renders"},
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

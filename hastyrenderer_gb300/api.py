@@ -171,6 +171,36 @@ class RenderJob:
     def write_outputs(self, out_dir: str, write_pfm: bool = False) -> None:
         check(native.lib().hasty_job_write_outputs(self._h, out_dir.encode(), 1 if write_pfm else 0))
 
+    # ---- progressive read-back (the viewer's display loop) while rendering continues ----
+    def snapshot(self, aovs=(AOV_COLOR,)) -> None:
+        """Enqueues the estimates of `aovs` behind the passes enqueued so far
+        and their copy to host memory; returns without waiting."""
+        mask = 0
+        for a in aovs:
+            mask |= 1 << int(a)
+        check(native.lib().hasty_job_snapshot(self._h, mask))
+
+    def snapshot_ready(self) -> bool:
+        r = ctypes.c_int()
+        check(native.lib().hasty_job_snapshot_query(self._h, ctypes.byref(r)))
+        return bool(r.value)
+
+    def snapshot_get(self, aov: int = AOV_COLOR) -> tuple[np.ndarray, int]:
+        """Waits for the last snapshot; returns a copy of `aov` and the passes it covers."""
+        i = self.info
+        p = ctypes.c_void_p()
+        n = ctypes.c_int32()
+        check(native.lib().hasty_job_snapshot_get(self._h, aov, ctypes.byref(p), ctypes.byref(n)))
+        buf = (ctypes.c_float * (i.height * i.width * 3)).from_address(p.value)
+        return np.frombuffer(buf, dtype=np.float32).reshape(i.height, i.width, 3).copy(), n.value
+
+    def write_outputs_async(self, out_dir: str, write_pfm: bool = False) -> None:
+        """write_outputs of this moment, written by a host thread while rendering continues."""
+        check(native.lib().hasty_job_write_outputs_async(self._h, out_dir.encode(), 1 if write_pfm else 0))
+
+    def outputs_wait(self) -> None:
+        check(native.lib().hasty_job_outputs_wait(self._h))
+
     def intersect(self, rays: np.ndarray):
         """Closest hits of rays (n x 6: origin, direction) -> (tri, t, u, v)."""
         r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)

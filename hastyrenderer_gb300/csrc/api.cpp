@@ -559,6 +559,142 @@ int hasty_job_write_outputs(hasty_job* job, const char* out_dir, int write_pfm) 
   });
 }
 
+// Enqueues snapshot slot k of the AOVs in `mask`: the estimates on the job's
+// stream behind every pass enqueued so far, their copy to pinned memory on
+// the copy stream. Returns without waiting.
+static void enqueue_snapshot(hasty_job& j, int k, uint32_t mask) {
+  if (!j.acc[0]) throw ApiError{HASTY_ERR_ARG, "job was loaded for the multi-job engine only"};
+  ck(cudaSetDevice(j.ctx->device), "cudaSetDevice");
+  const size_t n = size_t(j.sd.width) * size_t(j.sd.height) * 3;
+  hasty_job::Snapshot& s = j.snap[k];
+  if (!s.dev) {
+    s.dev = j.alloc<float>(3 * n);
+    ck(cudaHostAlloc(reinterpret_cast<void**>(&s.host), 3 * n * sizeof(float), cudaHostAllocDefault), "cudaHostAlloc");
+    ck(cudaEventCreateWithFlags(&s.copied, cudaEventDisableTiming), "event");
+  }
+  if (!j.copy_stream) {
+    ck(cudaStreamCreateWithFlags(&j.copy_stream, cudaStreamNonBlocking), "stream");
+    ck(cudaEventCreateWithFlags(&j.snap_est, cudaEventDisableTiming), "event");
+  }
+  // the slot's previous copy reads `dev`: the new estimates wait for it
+  if (s.pending) ck(cudaStreamWaitEvent(j.stream, s.copied, 0), "snapshot wait");
+  const float den = 1e-7f + float(j.samples_done);
+  for (int a = 0; a < 3; ++a) {
+    if (!(mask & (1u << a))) continue;
+    const float scale = a == HASTY_AOV_COLOR ? std::pow(2.0f, j.host.cam.exposure) : 1.0f;
+    launch_estimate(j.acc[a], int(n), den, scale, s.dev + size_t(a) * n, j.stream);
+  }
+  ck(cudaGetLastError(), "estimate launch");
+  ck(cudaEventRecord(j.snap_est, j.stream), "event record");
+  ck(cudaStreamWaitEvent(j.copy_stream, j.snap_est, 0), "snapshot wait");
+  for (int a = 0; a < 3; ++a) {
+    if (!(mask & (1u << a))) continue;
+    ck(cudaMemcpyAsync(s.host + size_t(a) * n, s.dev + size_t(a) * n, n * sizeof(float), cudaMemcpyDeviceToHost,
+                       j.copy_stream), "copy snapshot");
+  }
+  ck(cudaEventRecord(s.copied, j.copy_stream), "event record");
+  s.pending = true;
+  s.mask = mask;
+  s.samples = j.samples_done;
+}
+
+static void check_out_dir(const char* out_dir) {
+  if (!out_dir) throw ApiError{HASTY_ERR_ARG, "null directory"};
+  struct stat sb;
+  if (stat(out_dir, &sb) != 0 || !S_ISDIR(sb.st_mode)) throw ApiError{HASTY_ERR_IO, std::string("not a directory: ") + out_dir};
+}
+
+int hasty_job_snapshot(hasty_job* job, uint32_t aov_mask) {
+  return guarded([&] {
+    as_job(job);
+    if (aov_mask == 0 || aov_mask > 7u) throw ApiError{HASTY_ERR_ARG, "bad aov mask"};
+    enqueue_snapshot(*job, 0, aov_mask);
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_snapshot_query(hasty_job* job, int* ready) {
+  return guarded([&] {
+    as_job(job);
+    if (!ready) throw ApiError{HASTY_ERR_ARG, "null output"};
+    const hasty_job::Snapshot& s = job->snap[0];
+    if (!s.pending) throw ApiError{HASTY_ERR_ARG, "no snapshot was taken"};
+    const cudaError_t e = cudaEventQuery(s.copied);
+    if (e == cudaErrorNotReady) {
+      (void)cudaGetLastError();        // "not ready" is an answer, not an error to report later
+      *ready = 0;
+    } else {
+      ck(e, "snapshot query");
+      *ready = 1;
+    }
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_snapshot_get(hasty_job* job, int aov, const float** out, int32_t* num_samples) {
+  return guarded([&] {
+    as_job(job);
+    if (aov < 0 || aov > 2 || !out) throw ApiError{HASTY_ERR_ARG, "bad aov or output"};
+    const hasty_job::Snapshot& s = job->snap[0];
+    if (!s.pending) throw ApiError{HASTY_ERR_ARG, "no snapshot was taken"};
+    if (!(s.mask & (1u << aov))) throw ApiError{HASTY_ERR_ARG, "aov not in the snapshot"};
+    ck(cudaEventSynchronize(s.copied), "snapshot wait");
+    *out = s.host + size_t(aov) * size_t(job->sd.width) * size_t(job->sd.height) * 3;
+    if (num_samples) *num_samples = s.samples;
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_write_outputs_async(hasty_job* job, const char* out_dir, int write_pfm) {
+  return guarded([&] {
+    as_job(job);
+    check_out_dir(out_dir);
+    if (job->writer.joinable()) job->writer.join();   // the previous write reads slot 1
+    enqueue_snapshot(*job, 1, 7u);
+    job->writer_rc = HASTY_OK;
+    job->writer_err.clear();
+    const int device = job->ctx->device;
+    const int w = job->sd.width, h = job->sd.height;
+    hasty_job::Snapshot* s = &job->snap[1];
+    hasty_job* j = job;
+    std::string dir(out_dir);
+    job->writer = std::thread([j, s, device, w, h, dir, write_pfm] {
+      const char* names[3] = {"output", "outputNormal", "outputAlbedo"};
+      cudaError_t e = cudaSetDevice(device);
+      if (e == cudaSuccess) e = cudaEventSynchronize(s->copied);
+      if (e != cudaSuccess) {
+        j->writer_rc = HASTY_ERR_CUDA;
+        j->writer_err = std::string("snapshot wait: ") + cudaGetErrorString(e);
+        return;
+      }
+      const size_t n = size_t(w) * size_t(h) * 3;
+      for (int a = 0; a < 3; ++a) {
+        const float* img = s->host + size_t(a) * n;
+        const std::string base = dir + "/" + names[a];
+        if (!write_exr_rgb(base + ".exr", img, w, h) || (write_pfm && !write_pfm_rgb(base + ".pfm", img, w, h))) {
+          j->writer_rc = HASTY_ERR_IO;
+          j->writer_err = "could not write " + base;
+          return;
+        }
+      }
+    });
+    return HASTY_OK;
+  });
+}
+
+int hasty_job_outputs_wait(hasty_job* job) {
+  return guarded([&] {
+    as_job(job);
+    if (job->writer.joinable()) job->writer.join();
+    if (job->writer_rc != HASTY_OK) {
+      const int rc = job->writer_rc;
+      job->writer_rc = HASTY_OK;
+      throw ApiError{rc, job->writer_err};
+    }
+    return HASTY_OK;
+  });
+}
+
 int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* tri, float* t, float* u, float* v) {
   return guarded([&] {
     as_job(job);

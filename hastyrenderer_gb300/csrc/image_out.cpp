@@ -46,13 +46,20 @@ bool write_exr_rgb(const std::string& path, const float* rgb, int w, int h) {
   FILE* f = std::fopen(path.c_str(), "wb");
   if (!f) return false;
   bool ok = std::fwrite(hd.data(), 1, hd.size(), f) == hd.size();
-  std::vector<uint8_t> line;
+  // one chunk per line: y, byte count, then the B, G and R planes
+  // (little-endian floats: the host's own layout on the supported machines)
+  static_assert(__BYTE_ORDER__ == __ORDER_LITTLE_ENDIAN__, "EXR lines are written from host floats");
+  std::vector<uint8_t> line(static_cast<size_t>(line_bytes));
+  const uint32_t nbytes = uint32_t(w * 3 * 4);
+  std::memcpy(line.data() + 4, &nbytes, 4);
   for (int y = 0; y < h && ok; ++y) {
-    line.clear();
-    put_u32(line, uint32_t(y));
-    put_u32(line, uint32_t(w * 3 * 4));
-    for (int c = 2; c >= 0; --c)
-      for (int x = 0; x < w; ++x) put_f32(line, rgb[3 * (size_t(y) * w + x) + size_t(c)]);
+    const uint32_t yy = uint32_t(y);
+    std::memcpy(line.data(), &yy, 4);
+    const float* row = rgb + 3 * size_t(y) * size_t(w);
+    for (int c = 2; c >= 0; --c) {
+      uint8_t* plane = line.data() + 8 + size_t(2 - c) * size_t(w) * 4;
+      for (int x = 0; x < w; ++x) std::memcpy(plane + 4 * size_t(x), row + 3 * size_t(x) + size_t(c), 4);
+    }
     ok = std::fwrite(line.data(), 1, line.size(), f) == line.size();
   }
   return std::fclose(f) == 0 && ok;

@@ -9,6 +9,7 @@
 #include <functional>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bvh_build.h"
@@ -102,6 +103,25 @@ struct hasty_job {
   int64_t bytes = 0;
   double* acc[3] = {nullptr, nullptr, nullptr};
   float* est = nullptr;
+  // Progressive read-back: the estimates of the captured AOVs are computed
+  // on `stream` behind the passes enqueued so far into `dev`, then copied on
+  // `copy_stream` into pinned host memory, so rendering enqueued afterwards
+  // does not wait for the copy. Slot 0 serves hasty_job_snapshot, slot 1
+  // hasty_job_write_outputs_async. Buffers are allocated on first use.
+  struct Snapshot {
+    float* dev = nullptr;           // 3 AOVs x npix x 3 floats
+    float* host = nullptr;          // pinned
+    cudaEvent_t copied = nullptr;   // recorded on copy_stream after the copies
+    bool pending = false;           // a snapshot was enqueued (its copy may still run)
+    uint32_t mask = 0;              // AOVs captured (1 << HASTY_AOV_*)
+    int32_t samples = 0;            // passes it covers
+  };
+  Snapshot snap[2];
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t snap_est = nullptr;     // estimates written (recorded on `stream`)
+  std::thread writer;                 // hasty_job_write_outputs_async
+  int writer_rc = HASTY_OK;
+  std::string writer_err;
   int64_t capacity = 0;
   int32_t samples_done = 0;
   uint64_t seed = 0;
@@ -152,9 +172,17 @@ struct hasty_job {
     pending_events.clear();
   }
   ~hasty_job() {
+    if (writer.joinable()) writer.join();
     if (stream) cudaStreamSynchronize(stream);
     for (cudaStream_t s : lane_stream) if (s) cudaStreamSynchronize(s);
+    if (copy_stream) cudaStreamSynchronize(copy_stream);
     collect_events();
+    for (Snapshot& s : snap) {
+      if (s.host) cudaFreeHost(s.host);
+      if (s.copied) cudaEventDestroy(s.copied);
+    }
+    if (snap_est) cudaEventDestroy(snap_est);
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     hasty::destroy_pm(pm);
     for (const Block& b : allocs) cudaFree(b.p);
     for (int k = 0; k < 2; ++k) {

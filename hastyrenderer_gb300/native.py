@@ -122,6 +122,11 @@ def lib() -> ctypes.CDLL:
         "hasty_job_read": [P, I, P, SZ, SZ, P],
         "hasty_job_read_sums": [P, I, P, SZ, SZ, P],
         "hasty_job_write_outputs": [P, ctypes.c_char_p, I],
+        "hasty_job_snapshot": [P, ctypes.c_uint32],
+        "hasty_job_snapshot_query": [P, P],
+        "hasty_job_snapshot_get": [P, I, P, P],
+        "hasty_job_write_outputs_async": [P, ctypes.c_char_p, I],
+        "hasty_job_outputs_wait": [P],
         "hasty_debug_intersect": [P, P, SZ, P, P, P, P],
         "hasty_debug_tri_ids": [P, P, P, SZ],
         "hasty_debug_host_trace": [ctypes.c_char_p, I, P, SZ, P, P, P, P, P],

@@ -120,6 +120,31 @@ int hasty_job_read_sums(hasty_job* job, int aov, double* host_rgb, size_t w, siz
 /* output.exr, outputNormal.exr, outputAlbedo.exr (+ .pfm copies when write_pfm != 0). */
 int hasty_job_write_outputs(hasty_job* job, const char* out_dir, int write_pfm);
 
+/* ---- Progressive read-back while rendering continues ---------------------
+ * The reference's viewer shows computeEstimate of the colour buffers every
+ * ~20 ms while its render threads run (apps/PathTracingViewer.cpp:88-139,
+ * apps/ViewerUtils.cpp:95-121) and saves the three estimates at the end
+ * (:157-172). Here a snapshot computes the estimates of the AOVs in aov_mask
+ * (bit 1 << HASTY_AOV_*) behind every pass enqueued so far and copies them
+ * into pinned host memory on a copy stream; the call returns at once and
+ * passes enqueued afterwards do not wait for the copy.
+ *
+ *   hasty_job_snapshot        enqueue a snapshot (replaces the previous one)
+ *   hasty_job_snapshot_query  *ready = 1 once its copy has landed (no wait)
+ *   hasty_job_snapshot_get    wait for it; *out = w*h*3 floats of `aov`
+ *                             (colour x 2^exposure), valid until the next
+ *                             hasty_job_snapshot; *num_samples = passes covered
+ *   hasty_job_write_outputs_async  the files of hasty_job_write_outputs from
+ *                             a snapshot of this moment, written by a host
+ *                             thread (a previous write is waited for first)
+ *   hasty_job_outputs_wait    wait for that write and return its status
+ */
+int hasty_job_snapshot(hasty_job* job, uint32_t aov_mask);
+int hasty_job_snapshot_query(hasty_job* job, int* ready);
+int hasty_job_snapshot_get(hasty_job* job, int aov, const float** out, int32_t* num_samples);
+int hasty_job_write_outputs_async(hasty_job* job, const char* out_dir, int write_pfm);
+int hasty_job_outputs_wait(hasty_job* job);
+
 /* ---- Photon mapping (the reference's second integrator) ------------------
  * Stochastic progressive photon mapping with a caustics map, as one render
  * thread of the reference runs it (core/src/PhotonMapping.cpp:814-935,

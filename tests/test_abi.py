@@ -33,6 +33,12 @@ def test_errors_are_status_codes():
     assert b"null" in buf.value
     assert lib.hasty_job_stop(None) == -1
     assert lib.hasty_debug_bsdf(7, None, 0, None, 0, None) == -1
+    # progressive read-back entry points
+    assert lib.hasty_job_snapshot(None, 1) == -1
+    assert lib.hasty_job_snapshot_query(None, None) == -1
+    assert lib.hasty_job_snapshot_get(None, 0, None, None) == -1
+    assert lib.hasty_job_write_outputs_async(None, b".", 0) == -1
+    assert lib.hasty_job_outputs_wait(None) == -1
 
 
 def test_cli_argument_errors(tmp_path):
