@@ -411,6 +411,8 @@ def run_photon(args):
         "device_ms_per_step": dev_ms / args.steps, "host_ms_per_step": host_ms / args.steps,
         "photon_ms_per_step": (s1["photon_ms"] - s0["photon_ms"]) / args.steps,
         "gather_ms_per_step": (s1["gather_ms"] - s0["gather_ms"]) / args.steps,
+        "cell_size_host_ms_per_step": (s1["cell_ms"] - s0["cell_ms"]) / args.steps,
+        "map_build_ms_per_step": (s1["map_ms"] - s0["map_ms"]) / args.steps,
         "photons_emitted_per_step": s1["photons_emitted"], "photons_stored_per_step": s1["photons_stored"],
         "photons_traced_per_s": s1["photons_emitted"] * args.steps / wall,
         "estimate_finite": bool(np.isfinite(est).all()), "media_overflow": s1["media_overflow"],

@@ -168,6 +168,21 @@ class RenderJob:
         check(native.lib().hasty_pm_stats_get(self._h, ctypes.byref(s)))
         return {k: getattr(s, k) for k, _ in native.PmStats._fields_}
 
+    def pm_map(self) -> dict:
+        """Photon map of the last iteration (test hook): photons in map order
+        and the cell table (x, y, z, first, count)."""
+        L = native.lib()
+        n_ph, n_c, cell = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_float()
+        check(L.hasty_debug_pm_map(self._h, None, None, None, None, ctypes.byref(n_ph), ctypes.byref(n_c),
+                                   ctypes.byref(cell)))
+        xyz = np.empty((n_ph.value, 3), np.float32)
+        em = np.empty(n_ph.value, np.uint32)
+        ix = np.empty(n_ph.value, np.uint32)
+        cells = np.empty((n_c.value, 5), np.int32)
+        check(L.hasty_debug_pm_map(self._h, xyz.ctypes.data, em.ctypes.data, ix.ctypes.data, cells.ctypes.data,
+                                   ctypes.byref(n_ph), ctypes.byref(n_c), ctypes.byref(cell)))
+        return {"xyz": xyz, "emission": em, "index": ix, "cells": cells, "cell": cell.value}
+
     def write_outputs(self, out_dir: str, write_pfm: bool = False) -> None:
         check(native.lib().hasty_job_write_outputs(self._h, out_dir.encode(), 1 if write_pfm else 0))
 

@@ -28,9 +28,9 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE,
                "-I" + CSRC, "--expt-relaxed-constexpr"]
-CU_EXTRA = {"integrator.cu": ["--fmad=false"], "bvh_gpu.cu": ["--fmad=false"], "photon.cu": ["--fmad=false"]}
+CU_EXTRA = {"integrator.cu": ["--fmad=false"], "bvh_gpu.cu": ["--fmad=false"], "photon.cu": ["--fmad=false"], "photon_build.cu": ["--fmad=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-sign-compare"]
-CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu", "bvh_gpu.cu", "photon.cu"]
+CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu", "bvh_gpu.cu", "photon.cu", "photon_build.cu"]
 # Extra nvcc flags for experiments (e.g. HASTY_NVCC_FLAGS="-DHASTY_OUTLINE_MASK=3").
 EXTRA_NVCC = os.environ.get("HASTY_NVCC_FLAGS", "").split()
 CPP_SOURCES = ["api.cpp", "engine.cpp", "server.cpp", "scene_load.cpp", "bvh_build.cpp", "image_out.cpp", "photon_map.cpp"]

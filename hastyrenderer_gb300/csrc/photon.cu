@@ -196,15 +196,15 @@ struct PmRes { V3 pf, ll, lr, ls; int M; };
 struct PmFrame { V3 pf, lr, ls, tD, tC; int M; };
 
 // Cell of the photon map holding (x, y, z), or -1.
-__device__ __forceinline__ int find_cell(const PmMapDev& map, int x, int y, int z) {
-  int lo = 0, hi = map.n_cells;
+__device__ __forceinline__ int find_cell(const PmMapDev& map, int n_cells, int x, int y, int z) {
+  int lo = 0, hi = n_cells;
   while (lo < hi) {
     int mid = (lo + hi) >> 1;
     int4 c = map.cells[mid];
     bool less = c.x < x || (c.x == x && (c.y < y || (c.y == y && c.z < z)));
     if (less) lo = mid + 1; else hi = mid;
   }
-  if (lo < map.n_cells) {
+  if (lo < n_cells) {
     int4 c = map.cells[lo];
     if (c.x == x && c.y == y && c.z == z) return lo;
   }
@@ -222,10 +222,11 @@ __device__ V3 photon_estimate(const SceneDev& sc, const PmMapDev& map, const Mat
   const int lx = floor_int32(lo.x / map.cell), ly = floor_int32(lo.y / map.cell), lz = floor_int32(lo.z / map.cell);
   const int hx = floor_int32(hi.x / map.cell), hy = floor_int32(hi.y / map.cell), hz = floor_int32(hi.z / map.cell);
   const ShadeCtx cx = shade_ctx(sc, m, it, wo);
+  const int n_cells = *map.n_cells;
   for (int i = lx; i <= hx; i++)
     for (int j = ly; j <= hy; j++)
       for (int k = lz; k <= hz; k++) {
-        int c = find_cell(map, i, j, k);
+        int c = find_cell(map, n_cells, i, j, k);
         if (c < 0) continue;
         const int first = map.cells[c].w, cnt = map.cell_count[c];
         for (int q = first; q < first + cnt; ++q) {

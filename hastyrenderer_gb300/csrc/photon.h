@@ -36,8 +36,18 @@ struct PmMapDev {
   const PhotonRec* photons;
   const int4* cells;       // x, y, z, first photon
   const int32_t* cell_count;
-  int32_t n_cells;
+  const int32_t* n_cells;  // in device memory (written by the map build)
   float cell;
+};
+
+// Device status of one iteration's photon map build (photon_build.cu).
+struct PmStatus {
+  uint32_t cum;            // photons stored by the emissions scanned so far
+  uint32_t done;           // the stored count reached the threshold
+  uint32_t emitted;        // emissions up to and including the cutoff (when done)
+  uint32_t kept;           // photons stored by those
+  uint32_t appended;       // photons in the append buffer (a copy of its counter)
+  int32_t lo[3], hi[3];    // cell bounds of the kept photons
 };
 
 // Per-pixel statistics (PMRenderJobPixel) and the thread's images.
@@ -64,6 +74,30 @@ void launch_pm_emit(const SceneDev& sc, uint64_t seed, uint32_t iter, uint32_t f
                     const PmEmitOut& out, cudaStream_t st);
 // Gathers every pixel of iteration `iter` (camera offset ox, oy) and updates
 // the pixel statistics; `emitted` photons were emitted this iteration.
+// Photon map build on the device (photon_build.cu).
+// Exclusive scan of the store counts of emissions [first, first + n) into
+// base[first..] continuing status->cum; the emission that takes the count to
+// `threshold` sets status->done / emitted / kept. scratch: one word per
+// 2048 counts.
+void launch_pm_emit_scan(const uint8_t* stored, uint32_t n, uint32_t first, uint32_t threshold, uint32_t* base,
+                         uint32_t* scratch, PmStatus* status, cudaStream_t st);
+// Slots of the photons of emissions [0, emitted) in emission order
+// (src[slot] = append index), their hash cells (coords[axis * cap + slot])
+// and the cell bounds (status->lo / hi).
+void launch_pm_place(const PhotonRec* app, uint32_t appended, const uint32_t* base, uint32_t emitted,
+                     PmStatus* status, float cell, uint32_t* src, int32_t* coords, uint32_t cap, cudaStream_t st);
+// One stable LSD pass over n slots by the byte (coord - lo) >> shift of one
+// axis (perm_in null: slots in order). hist: 256 words per 2048 slots;
+// scratch as for the scan of hist.
+uint32_t pm_sort_tiles(uint32_t n);
+void launch_pm_sort_pass(const int32_t* coord, int32_t lo, int shift, uint32_t n, const uint32_t* perm_in,
+                         uint32_t* perm_out, uint32_t* hist, uint32_t* scratch, cudaStream_t st);
+// Photons in sorted order, the cell table (x, y, z, first) with counts and
+// the cell count in device memory.
+void launch_pm_cells(const PhotonRec* app, const uint32_t* src, const int32_t* coords, uint32_t cap, uint32_t n,
+                     const uint32_t* perm, PhotonRec* sorted, uint32_t* flag, uint32_t* cell_of, uint32_t* scratch,
+                     int4* cells, int32_t* counts, int32_t* n_cells, cudaStream_t st);
+
 void launch_pm_gather(const SceneDev& sc, const PmMapDev& map, const PmPixelsDev& px, uint64_t seed, uint32_t iter,
                       float ox, float oy, int emitted, unsigned long long* stats, cudaStream_t st);
 

@@ -37,11 +37,32 @@ struct PmDev {
   size_t cells_cap = 0;
   int32_t* cell_count = nullptr;
   size_t counts_cap = 0;
+  int32_t* n_cells = nullptr;
+  // map build (photon_build.cu)
+  PmStatus* status = nullptr;              // device
+  PmStatus* status_host = nullptr;         // pinned
+  uint32_t* base = nullptr;                // first slot of each emission
+  size_t base_cap = 0;
+  uint32_t* scratch = nullptr;
+  size_t scratch_cap = 0;
+  uint32_t* src = nullptr;                 // append index of each slot
+  size_t src_cap = 0;
+  int32_t* coords = nullptr;               // hash cell of each slot, three planes
+  size_t coords_cap = 0;
+  uint32_t* perm[2] = {nullptr, nullptr};
+  size_t perm_cap[2] = {0, 0};
+  uint32_t* flag = nullptr;
+  size_t flag_cap = 0;
+  uint32_t* cell_of = nullptr;
+  size_t cell_of_cap = 0;
+  uint32_t* hist = nullptr;
+  size_t hist_cap = 0;
+  ~PmDev() { if (status_host) cudaFreeHost(status_host); }
   std::vector<float> radii;                // host copy of the radius image
   // last iteration
   uint64_t emitted = 0, photons = 0;
   float cell = 0.0f;
-  double device_ms = 0.0, host_ms = 0.0, photon_ms = 0.0, gather_ms = 0.0;
+  double device_ms = 0.0, host_ms = 0.0, photon_ms = 0.0, gather_ms = 0.0, cell_ms = 0.0, map_ms = 0.0;
   uint64_t last_emitted = 0;               // sizes the next iteration's first photon batch
 };
 
@@ -49,7 +70,6 @@ void destroy_pm(PmDev* pm) { delete pm; }
 
 namespace {
 
-int32_t floor_i32(double x) { int i = (int)x; return i - (i > x); }     // VMath.h floor_int32
 
 // Camera::computeRayAngle (Camera.cpp:83-98); q = tan(fov / 2) as the camera
 // evaluates it.
@@ -162,6 +182,9 @@ PmDev& pm_state(hasty_job& j) {
     pm->px.albedo = j.alloc<float>(3 * n);
     pm->stats = j.alloc<unsigned long long>(2);
     pm->append_count = j.alloc<uint32_t>(1);
+    pm->n_cells = j.alloc<int32_t>(1);
+    pm->status = j.alloc<PmStatus>(1);
+    ck(cudaHostAlloc(reinterpret_cast<void**>(&pm->status_host), sizeof(PmStatus), cudaHostAllocDefault), "cudaHostAlloc");
   }
   return *j.pm;
 }
@@ -213,160 +236,135 @@ void pm_init(hasty_job& j, PmDev& pm) {
 }
 
 // One iteration of renderPhotonThread's loop (PhotonMapping.cpp:848-931).
+// The GPU traces photon batches and scans their store counts; the hash-cell
+// size is computed on the host meanwhile (it needs only the radii of the
+// previous iteration); then the photon map is built and gathered on the GPU.
 void pm_iteration(hasty_job& j, PmDev& pm) {
   const uint32_t W = pm.W, H = pm.H, t = pm.iteration;
   const auto h0 = std::chrono::steady_clock::now();
-  double dev_ms = 0.0;
-  cudaEvent_t e0, e1;
-  ck(cudaEventCreate(&e0), "event"); ck(cudaEventCreate(&e1), "event");
-  double photon_ms = 0.0, gather_ms = 0.0;
-  auto time_device = [&](double& part, auto&& fn) {
-    ck(cudaEventRecord(e0, j.stream), "event");
-    fn();
-    ck(cudaEventRecord(e1, j.stream), "event");
-    ck(cudaEventSynchronize(e1), "event");
+  cudaEvent_t ev[6];
+  for (cudaEvent_t& e : ev) ck(cudaEventCreate(&e), "event");
+  auto elapsed = [&](int a, int b) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    dev_ms += ms;
-    part += ms;
+    ck(cudaEventElapsedTime(&ms, ev[a], ev[b]), "event time");
+    return double(ms);
   };
-  const float cell = cell_size_for(pm.radii, W, H);
-  uint64_t emitted = 0, kept = 0;
-  std::vector<uint64_t> base;          // first emission-order slot of each emitted photon
-  std::vector<PhotonRec> host_ph;
-  if (j.sd.n_light_tris > 0) {
+  double photon_ms = 0.0, cell_ms = 0.0;
+  float cell = 0.0f;
+  bool have_cell = false;
+  auto compute_cell = [&] {
+    const auto c0 = std::chrono::steady_clock::now();
+    cell = cell_size_for(pm.radii, W, H);
+    cell_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c0).count();
+    have_cell = true;
+  };
+  uint32_t emitted = 0, kept = 0, appended = 0;
+  const int count_threshold = int(0.5f * float(H) * float(W));
+  if (j.sd.n_light_tris > 0 && count_threshold > 0) {
     const int trace_threshold = int(10.f * float(H) * float(W));
-    const int count_threshold = int(0.5f * float(H) * float(W));
     const int depth_slots = std::max(1, j.sd.max_depth - 1);   // photons one emitted photon can store
     const float min_q = 1.0f - std::pow(0.1f, 1.0f / j.sd.max_depth);
-    uint64_t first = 0, cum = 0;
-    uint32_t appended = 0;
-    base.clear();
+    uint32_t first = 0;
     // first batch: what the previous iteration needed (+10%), else 2x the stored target
     size_t chunk = std::max<size_t>(size_t(1) << 16, pm.last_emitted ? size_t(pm.last_emitted * 1.1) + 1024
                                                                      : 2 * size_t(count_threshold));
     ck(cudaMemsetAsync(pm.append_count, 0, sizeof(uint32_t), j.stream), "photon count");
-    bool done = count_threshold <= 0;
-    std::vector<uint8_t> stored;
-    while (!done && first < uint64_t(trace_threshold)) {
+    ck(cudaMemsetAsync(pm.status, 0, sizeof(PmStatus), j.stream), "photon status");
+    for (;;) {
       const uint32_t n = uint32_t(std::min<uint64_t>(chunk, uint64_t(trace_threshold) - first));
       pm.append = grow(j, pm.append, pm.append_cap, size_t(appended) + size_t(n) * depth_slots, appended);
       pm.stored = grow(j, pm.stored, pm.stored_cap, n, 0);
+      pm.base = grow(j, pm.base, pm.base_cap, size_t(first) + n, first);
+      pm.scratch = grow(j, pm.scratch, pm.scratch_cap, size_t(n) / 2048 + 2, 0);
       PmEmitOut out{pm.append, pm.append_count, uint32_t(pm.append_cap), pm.stored, pm.stats};
-      time_device(photon_ms, [&] {
-        launch_pm_emit(j.sd, j.seed, t, uint32_t(first), n, min_q, out, j.stream);
-        ck(cudaGetLastError(), "photon launch");
-      });
-      stored.resize(n);
-      ck(cudaMemcpyAsync(stored.data(), pm.stored, n, cudaMemcpyDeviceToHost, j.stream), "photon counts");
-      ck(cudaMemcpyAsync(&appended, pm.append_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, j.stream), "photon count");
-      ck(cudaStreamSynchronize(j.stream), "photons");
+      ck(cudaEventRecord(ev[0], j.stream), "event");
+      launch_pm_emit(j.sd, j.seed, t, first, n, min_q, out, j.stream);
+      launch_pm_emit_scan(pm.stored, n, first, uint32_t(count_threshold), pm.base, pm.scratch, pm.status, j.stream);
+      ck(cudaGetLastError(), "photon launch");
+      ck(cudaEventRecord(ev[1], j.stream), "event");
+      ck(cudaMemcpyAsync(&pm.status->appended, pm.append_count, sizeof(uint32_t), cudaMemcpyDeviceToDevice, j.stream),
+         "photon count");
+      ck(cudaMemcpyAsync(pm.status_host, pm.status, sizeof(PmStatus), cudaMemcpyDeviceToHost, j.stream), "photon status");
+      ck(cudaEventRecord(ev[2], j.stream), "event");
+      if (!have_cell) compute_cell();           // overlaps the photon tracing
+      ck(cudaEventSynchronize(ev[2]), "photons");
+      photon_ms += elapsed(0, 1);
+      appended = pm.status_host->appended;
       if (appended > pm.append_cap) throw ApiError{HASTY_ERR_CUDA, "photon buffer overflow"};
       // the reference emits photon i while fewer than count_threshold are stored
-      for (uint32_t k = 0; k < n && !done; ++k) {
-        base.push_back(cum);
-        cum += stored[k];
-        if (cum >= uint64_t(count_threshold)) { emitted = first + k + 1; done = true; }
-      }
-      kept = cum;
-      if (!done) { first += n; emitted = first; }
+      if (pm.status_host->done) { emitted = pm.status_host->emitted; kept = pm.status_host->kept; break; }
+      first += n;
+      if (first >= uint32_t(trace_threshold)) { emitted = first; kept = pm.status_host->cum; break; }
       chunk *= 2;
     }
-    host_ph.resize(appended);
-    if (appended)
-      ck(cudaMemcpyAsync(host_ph.data(), pm.append, appended * sizeof(PhotonRec), cudaMemcpyDeviceToHost, j.stream), "photons");
-    ck(cudaStreamSynchronize(j.stream), "photons");
   }
-  // Photon map: the photons of the emitted range in emission order (slot =
-  // the emission's first slot + the photon's index within it), then a stable
-  // radix sort by hash cell, so each cell lists its photons in the order the
-  // reference stored them.
-  std::vector<PhotonRec> ordered(kept);
-  for (const PhotonRec& r : host_ph) {
-    uint32_t emit, k;
-    std::memcpy(&emit, &r.wi.w, 4);
-    std::memcpy(&k, &r.flux.w, 4);
-    if (emit < emitted) ordered[base[emit] + k] = r;
+  if (!have_cell) compute_cell();
+  // Photon map: the kept photons in emission order (slot = the emission's
+  // first slot + the photon's index within it), then a stable radix sort by
+  // hash cell, so each cell lists its photons in the order the reference
+  // stored them.
+  const uint32_t cap = std::max<uint32_t>(kept, 1u);
+  const uint32_t tiles = pm_sort_tiles(cap);
+  pm.src = grow(j, pm.src, pm.src_cap, cap, 0);
+  pm.perm[0] = grow(j, pm.perm[0], pm.perm_cap[0], cap, 0);
+  pm.perm[1] = grow(j, pm.perm[1], pm.perm_cap[1], cap, 0);
+  pm.flag = grow(j, pm.flag, pm.flag_cap, cap, 0);
+  pm.cell_of = grow(j, pm.cell_of, pm.cell_of_cap, cap, 0);
+  pm.hist = grow(j, pm.hist, pm.hist_cap, size_t(256) * tiles, 0);
+  pm.scratch = grow(j, pm.scratch, pm.scratch_cap, size_t(cap) / 2048 + size_t(tiles) / 8 + 2, 0);
+  pm.sorted = grow(j, pm.sorted, pm.sorted_cap, cap, 0);
+  pm.cells = grow(j, pm.cells, pm.cells_cap, cap, 0);
+  pm.cell_count = grow(j, pm.cell_count, pm.counts_cap, cap, 0);
+  // coordinates: three planes of `coords_cap / 3` slots
+  if (pm.coords_cap < 3 * size_t(cap)) {
+    j.release(pm.coords);
+    pm.coords = nullptr;
+    pm.coords_cap = 0;
+    pm.coords = grow(j, pm.coords, pm.coords_cap, 3 * size_t(cap), 0);
   }
-  const size_t np = ordered.size();
-  std::vector<int32_t> cxyz(3 * np);
-  int32_t lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-  for (size_t q = 0; q < np; ++q) {
-    const float* x = &ordered[q].xn.x;
-    for (int a = 0; a < 3; ++a) {
-      int32_t c = floor_i32(x[a] / cell);
-      cxyz[3 * q + a] = c;
-      if (q == 0 || c < lo[a]) lo[a] = c;
-      if (q == 0 || c > hi[a]) hi[a] = c;
+  const uint32_t plane = uint32_t(pm.coords_cap / 3);
+  ck(cudaEventRecord(ev[3], j.stream), "event");
+  launch_pm_place(pm.append, appended, pm.base, emitted, pm.status, cell, pm.src, pm.coords, plane, j.stream);
+  ck(cudaGetLastError(), "photon map launch");
+  const uint32_t* perm = nullptr;
+  if (kept > 1) {
+    ck(cudaMemcpyAsync(pm.status_host, pm.status, sizeof(PmStatus), cudaMemcpyDeviceToHost, j.stream), "cell bounds");
+    ck(cudaStreamSynchronize(j.stream), "cell bounds");
+    int which = 0;
+    for (int axis = 2; axis >= 0; --axis) {      // least significant key first: z, y, x
+      const uint32_t range = uint32_t(int64_t(pm.status_host->hi[axis]) - int64_t(pm.status_host->lo[axis]));
+      for (int shift = 0; shift < 32 && (range >> shift) != 0; shift += 8) {
+        launch_pm_sort_pass(pm.coords + size_t(axis) * plane, pm.status_host->lo[axis], shift, kept, perm,
+                            pm.perm[which], pm.hist, pm.scratch, j.stream);
+        perm = pm.perm[which];
+        which ^= 1;
+      }
     }
   }
-  const uint64_t nx = uint64_t(int64_t(hi[0]) - lo[0] + 1), ny = uint64_t(int64_t(hi[1]) - lo[1] + 1),
-                 nz = uint64_t(int64_t(hi[2]) - lo[2] + 1);
-  const bool fits = double(nx) * double(ny) * double(nz) < 9.0e18;      // linear cell key fits 64 bits
-  std::vector<uint64_t> key(np);
-  std::vector<uint32_t> perm(np), tmp(np);
-  for (size_t q = 0; q < np; ++q) perm[q] = uint32_t(q);
-  if (fits) {
-    for (size_t q = 0; q < np; ++q)
-      key[q] = (uint64_t(int64_t(cxyz[3 * q]) - lo[0]) * ny + uint64_t(int64_t(cxyz[3 * q + 1]) - lo[1])) * nz +
-               uint64_t(int64_t(cxyz[3 * q + 2]) - lo[2]);
-    uint64_t maxkey = 0;
-    for (uint64_t k : key) maxkey = std::max(maxkey, k);
-    for (int shift = 0; shift < 64 && (maxkey >> shift) != 0; shift += 16) {     // LSD radix, stable
-      std::vector<uint32_t> hist(65537, 0);
-      for (size_t q = 0; q < np; ++q) hist[((key[perm[q]] >> shift) & 0xFFFFu) + 1]++;
-      for (size_t b = 1; b < hist.size(); ++b) hist[b] += hist[b - 1];
-      for (size_t q = 0; q < np; ++q) tmp[hist[(key[perm[q]] >> shift) & 0xFFFFu]++] = perm[q];
-      perm.swap(tmp);
-    }
-  } else {                                                 // huge cell ranges: compare the coordinates
-    std::stable_sort(perm.begin(), perm.end(), [&](uint32_t a, uint32_t b) {
-      for (int c = 0; c < 3; ++c)
-        if (cxyz[3 * a + c] != cxyz[3 * b + c]) return cxyz[3 * a + c] < cxyz[3 * b + c];
-      return false;
-    });
-    for (size_t q = 0; q < np; ++q)   // equal coordinates <=> equal key (cell boundaries below)
-      key[perm[q]] = q > 0 && std::equal(&cxyz[3 * perm[q]], &cxyz[3 * perm[q]] + 3, &cxyz[3 * perm[q - 1]])
-                         ? key[perm[q - 1]] : uint64_t(q);
-  }
-  std::vector<PhotonRec> sorted(np);
-  std::vector<int4> cells;
-  std::vector<int32_t> counts;
-  for (size_t q = 0; q < np; ++q) {
-    const uint32_t src = perm[q];
-    sorted[q] = ordered[src];
-    if (q == 0 || key[src] != key[perm[q - 1]]) {
-      cells.push_back(make_int4(cxyz[3 * src], cxyz[3 * src + 1], cxyz[3 * src + 2], int(q)));
-      counts.push_back(0);
-    }
-    counts.back() += 1;
-  }
-  pm.sorted = grow(j, pm.sorted, pm.sorted_cap, std::max<size_t>(1, sorted.size()), 0);
-  pm.cells = grow(j, pm.cells, pm.cells_cap, std::max<size_t>(1, cells.size()), 0);
-  pm.cell_count = grow(j, pm.cell_count, pm.counts_cap, std::max<size_t>(1, cells.size()), 0);
-  if (!sorted.empty())
-    ck(cudaMemcpyAsync(pm.sorted, sorted.data(), sorted.size() * sizeof(PhotonRec), cudaMemcpyHostToDevice, j.stream), "photon map");
-  if (!cells.empty()) {
-    ck(cudaMemcpyAsync(pm.cells, cells.data(), cells.size() * sizeof(int4), cudaMemcpyHostToDevice, j.stream), "photon map");
-    ck(cudaMemcpyAsync(pm.cell_count, counts.data(), counts.size() * sizeof(int32_t), cudaMemcpyHostToDevice, j.stream), "photon map");
-  }
-  PmMapDev map{pm.sorted, pm.cells, pm.cell_count, int32_t(cells.size()), cell};
+  launch_pm_cells(pm.append, pm.src, pm.coords, plane, kept, perm, pm.sorted, pm.flag, pm.cell_of, pm.scratch,
+                  pm.cells, pm.cell_count, pm.n_cells, j.stream);
+  ck(cudaGetLastError(), "photon map launch");
+  ck(cudaEventRecord(ev[4], j.stream), "event");
+  PmMapDev map{pm.sorted, pm.cells, pm.cell_count, pm.n_cells, cell};
   const float ox = halton_value(2, t), oy = halton_value(3, t);
-  time_device(gather_ms, [&] {
-    launch_pm_gather(j.sd, map, pm.px, j.seed, t, ox, oy, int(emitted), pm.stats, j.stream);
-    ck(cudaGetLastError(), "gather launch");
-  });
+  launch_pm_gather(j.sd, map, pm.px, j.seed, t, ox, oy, int(emitted), pm.stats, j.stream);
+  ck(cudaGetLastError(), "gather launch");
+  ck(cudaEventRecord(ev[5], j.stream), "event");
   const size_t n = size_t(W) * H;
   ck(cudaMemcpyAsync(pm.radii.data(), pm.px.radii, n * sizeof(float), cudaMemcpyDeviceToHost, j.stream), "radii");
   ck(cudaStreamSynchronize(j.stream), "radii");
-  cudaEventDestroy(e0); cudaEventDestroy(e1);
+  const double map_ms = elapsed(3, 4), gather_ms = elapsed(4, 5);
+  for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  const double dev_ms = photon_ms + map_ms + gather_ms;
   pm.emitted = emitted;
-  pm.photons = np;
+  pm.photons = kept;
   pm.cell = cell;
   pm.iteration = t + 1;
   pm.device_ms += dev_ms;
   pm.photon_ms += photon_ms;
   pm.gather_ms += gather_ms;
+  pm.map_ms += map_ms;
+  pm.cell_ms += cell_ms;
   pm.last_emitted = emitted;
   pm.host_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count() - dev_ms;
 }
@@ -459,6 +457,47 @@ int hasty_pm_stats_get(hasty_job* job, hasty_pm_stats* out) {
     out->trial_cap = st[1];
     out->photon_ms = pm.photon_ms;
     out->gather_ms = pm.gather_ms;
+    out->cell_ms = pm.cell_ms;
+    out->map_ms = pm.map_ms;
+    return HASTY_OK;
+  });
+}
+
+int hasty_debug_pm_map(hasty_job* job, float* xyz, uint32_t* emission, uint32_t* index, int32_t* cells,
+                       int64_t* n_photons, int64_t* n_cells, float* cell) {
+  return guarded([&] {
+    pm_job(job);
+    if (!n_photons || !n_cells || !cell) throw ApiError{HASTY_ERR_ARG, "null count output"};
+    if (!job->pm || !job->pm->initialised || job->pm->iteration == 0)
+      throw ApiError{HASTY_ERR_ARG, "no photon-mapping iteration rendered"};
+    const PmDev& pm = *job->pm;
+    int32_t nc = 0;
+    ck(cudaMemcpyAsync(&nc, pm.n_cells, sizeof(int32_t), cudaMemcpyDeviceToHost, job->stream), "map");
+    ck(cudaStreamSynchronize(job->stream), "map");
+    *n_photons = int64_t(pm.photons);
+    *n_cells = nc;
+    *cell = pm.cell;
+    if (xyz && emission && index && pm.photons) {
+      std::vector<PhotonRec> ph(pm.photons);
+      ck(cudaMemcpyAsync(ph.data(), pm.sorted, ph.size() * sizeof(PhotonRec), cudaMemcpyDeviceToHost, job->stream), "map");
+      ck(cudaStreamSynchronize(job->stream), "map");
+      for (size_t q = 0; q < ph.size(); ++q) {
+        xyz[3 * q] = ph[q].xn.x; xyz[3 * q + 1] = ph[q].xn.y; xyz[3 * q + 2] = ph[q].xn.z;
+        std::memcpy(&emission[q], &ph[q].wi.w, 4);
+        std::memcpy(&index[q], &ph[q].flux.w, 4);
+      }
+    }
+    if (cells && nc > 0) {
+      std::vector<int4> c(static_cast<size_t>(nc));
+      std::vector<int32_t> cnt(static_cast<size_t>(nc));
+      ck(cudaMemcpyAsync(c.data(), pm.cells, c.size() * sizeof(int4), cudaMemcpyDeviceToHost, job->stream), "map");
+      ck(cudaMemcpyAsync(cnt.data(), pm.cell_count, cnt.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, job->stream), "map");
+      ck(cudaStreamSynchronize(job->stream), "map");
+      for (size_t k = 0; k < c.size(); ++k) {
+        cells[5 * k] = c[k].x; cells[5 * k + 1] = c[k].y; cells[5 * k + 2] = c[k].z;
+        cells[5 * k + 3] = c[k].w; cells[5 * k + 4] = cnt[k];
+      }
+    }
     return HASTY_OK;
   });
 }

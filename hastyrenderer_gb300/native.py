@@ -58,7 +58,7 @@ class PmStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("photons_emitted", ctypes.c_int64), ("photons_stored", ctypes.c_int64),
                 ("cell_size", ctypes.c_float), ("device_ms", ctypes.c_double), ("host_ms", ctypes.c_double),
                 ("media_overflow", ctypes.c_uint64), ("trial_cap", ctypes.c_uint64), ("photon_ms", ctypes.c_double),
-                ("gather_ms", ctypes.c_double)]
+                ("gather_ms", ctypes.c_double), ("cell_ms", ctypes.c_double), ("map_ms", ctypes.c_double)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -138,6 +138,7 @@ def lib() -> ctypes.CDLL:
         "hasty_pm_read": [P, I, P, SZ, SZ],
         "hasty_pm_read_radii": [P, P, SZ, SZ],
         "hasty_pm_stats_get": [P, P],
+        "hasty_debug_pm_map": [P, P, P, P, P, P, P, P],
         "hasty_job_render_pass_static": [P, I, P],
         "hasty_server_start": [P, P, P],
         "hasty_server_submit": [P, ctypes.c_char_p, ctypes.c_int32, P, P],

@@ -163,12 +163,14 @@ typedef struct hasty_pm_stats {
   int64_t photons_emitted;     /* last iteration */
   int64_t photons_stored;      /* last iteration */
   float cell_size;             /* hash-cell size of the last iteration */
-  double device_ms;            /* photon tracing + gather kernels, all iterations */
-  double host_ms;              /* host work (cell size, photon sort, copies), all iterations */
+  double device_ms;            /* photon tracing, map build and gather kernels, all iterations */
+  double host_ms;              /* wall time minus device_ms, all iterations */
   uint64_t media_overflow;     /* medium-stack pushes beyond 4 (dropped) */
   uint64_t trial_cap;          /* rejection loops that hit their bound */
   double photon_ms;            /* of device_ms: photon emission and tracing */
   double gather_ms;            /* of device_ms: per-pixel gather */
+  double cell_ms;              /* host time of the hash-cell size (computeCellSize), run while photons are traced */
+  double map_ms;               /* of device_ms: photon-map build (order, sort by cell, cell table) */
 } hasty_pm_stats;
 
 /* Renders `iterations` more progressive iterations (synchronous). */
@@ -181,6 +183,12 @@ int hasty_pm_read(hasty_job* job, int aov, float* host_rgb, size_t w, size_t h);
 /* Per-pixel gather radii after the last iteration (w*h floats). */
 int hasty_pm_read_radii(hasty_job* job, float* host, size_t w, size_t h);
 int hasty_pm_stats_get(hasty_job* job, hasty_pm_stats* stats);
+/* Photon map of the last iteration, for tests: photons in map order
+ * (position xyz[3n], emission index, index among the photons that emission
+ * stored) and the cell table cells[5 * n_cells] = (x, y, z, first photon,
+ * count). With null buffers only *n_photons, *n_cells and *cell are set. */
+int hasty_debug_pm_map(hasty_job* job, float* xyz, uint32_t* emission, uint32_t* index, int32_t* cells,
+                       int64_t* n_photons, int64_t* n_cells, float* cell);
 
 /* ---- Batching: many jobs in one persistent multi-job wavefront ------------
  * Path slots are shared by all jobs and refilled with new camera samples as

@@ -55,3 +55,75 @@ def test_photon_mapper_reset_repeats():
         assert np.array_equal(job.pm_read(0), a)
     finally:
         job.close()
+
+
+@pytest.fixture(scope="module")
+def room_160(tmp_path_factory):
+    from hastyrenderer_gb300 import scenes
+    d = tmp_path_factory.mktemp("pm_room160")
+    return scenes.textured_room(str(d), seed=5, width=160, height=120, spp=16, max_depth=8, tex_size=64)
+
+
+def test_photon_mapper_matches_checker_multi_tile(room_160):
+    """160x120: 9,600 stored photons per iteration, so the device map build
+    runs over several scan and sort tiles; every iteration against the CPU
+    checker's photon mapper (pinned bit-exact to the reference build). With
+    19,200 pixels a photon lying on a pixel's gather radius, its position one
+    ulp apart on the two sides, changes that pixel's photon count by one and
+    its radius by one shrink factor (measured: 2 pixels, 0.23%). Tolerances:
+    >= 99% of radii bit-equal, >= 99.9% within 1e-4 relative, all within 1e-2;
+    colour as the golden comparison."""
+    from hastyrenderer_gb300 import RenderJob
+    from oracle.oracle import PhotonMapper
+    pm = PhotonMapper(room_160)
+    job = RenderJob(room_160)
+    try:
+        for it in range(3):
+            ref = pm.iterate(1)
+            job.pm_render(1)
+            st = job.pm_stats()
+            assert st["photons_emitted"] == ref["emitted"] and st["photons_stored"] == ref["stored"], it
+            assert st["photons_stored"] > 4 * 2048
+            radii = job.pm_radii()
+            assert np.mean(radii == ref["radii"]) >= 0.99, it
+            rrel = np.abs(radii - ref["radii"]) / np.abs(ref["radii"])
+            assert np.mean(rrel <= 1e-4) >= 0.999 and rrel.max() <= 1e-2, (it, float(rrel.max()))
+            c, rc = job.pm_read(0), ref["color"] * np.float32(2.0) ** np.float32(job.info.exposure)
+            rel = np.abs(c - rc) / np.maximum(1e-3, np.abs(rc))
+            assert np.quantile(rel, 0.99) <= 1e-4 and rel.max() <= 1e-2, (it, float(np.quantile(rel, 0.99)), float(rel.max()))
+    finally:
+        job.close()
+        pm.close()
+
+
+def test_photon_map_order_and_cells(tmp_path):
+    """The device-built map at 320x240 (38,400 photons: 19 sort tiles, several
+    digit passes) against a host sort of the same photons: photons by hash cell
+    (floor(x / cell) per axis, cells in (x, y, z) order), then by emission index
+    and index within the emission; the cell table lists each run."""
+    from hastyrenderer_gb300 import RenderJob, scenes
+    path = scenes.textured_room(str(tmp_path), seed=9, width=320, height=240, spp=4, max_depth=8, tex_size=64)
+    job = RenderJob(path)
+    try:
+        for _ in range(2):
+            job.pm_render(1)
+            m = job.pm_map()
+            n = m["xyz"].shape[0]
+            assert n == job.pm_stats()["photons_stored"] and n > 16 * 2048
+            cell = np.float32(m["cell"])
+            c = np.floor((m["xyz"] / cell).astype(np.float64)).astype(np.int64)
+            order = np.lexsort((m["index"], m["emission"], c[:, 2], c[:, 1], c[:, 0]))
+            assert np.array_equal(order, np.arange(n))            # already in that order
+            # emission-order slots: (emission, index) pairs are unique
+            key = m["emission"].astype(np.uint64) << np.uint64(8) | m["index"].astype(np.uint64)
+            assert np.unique(key).size == n
+            new = np.ones(n, bool)
+            new[1:] = np.any(c[1:] != c[:-1], axis=1)
+            first = np.flatnonzero(new)
+            cells = m["cells"]
+            assert cells.shape[0] == first.size
+            assert np.array_equal(cells[:, 3], first)
+            assert np.array_equal(cells[:, 4], np.diff(np.append(first, n)))
+            assert np.array_equal(cells[:, :3], c[first])
+    finally:
+        job.close()
