@@ -138,7 +138,15 @@ __global__ void __launch_bounds__(256) k_raygen(SceneDev sc, PathsDev P, BatchDe
 //  * sample_path: the light strategy's sample and the BSDF sample of the
 //    vertex, queued as the slot's two rays.
 // The arithmetic is the single-kernel bounce's, in the same order.
-struct ResolveRes { bool sample; int shaded; V3 L; };
+struct ResolveRes { bool sample; int shaded; int cls; V3 L; };
+
+// Shading class of a material for grouping the sample queue: the lobes its
+// sampling and evaluation take (diffuse only; diffuse + GGX; dielectric).
+__device__ __forceinline__ int shade_class(const MaterialDev& m) {
+  if (m.transmission != 0.0f || m.vary_ior) return 2;
+  if (m.metallic == 0.0f && m.metallic_tex < 0 && m.specular == 0.0f) return 0;
+  return 1;
+}
 struct SampleRes { bool keep, emitB, emitL; int overflow, capped; V3 L; };
 
 __device__ __forceinline__ void store_vertex(const PathsDev& P, int s, const Inter& it, V3 tl) {
@@ -253,6 +261,7 @@ __device__ __forceinline__ ResolveRes resolve_path(const SceneDev& sc, const Pat
             store_vertex(P, s, it, tl);
             flags = (flags & (PF_WL_MASK | PF_NMED_MASK)) | uint32_t(depth);
             res.sample = true;
+            res.cls = shade_class(m);
           }
         }
       }
@@ -381,27 +390,50 @@ __device__ __forceinline__ uint64_t slot_key(const BatchDesc& b, int s, int npix
 
 // Paths of queue q: resolve; finished ones leave their radiance in
 // out_color, survivors are appended to the sample queue.
+// The block's survivors are appended to the sample queue grouped by shading
+// class (block order kept within a class), so that the sample kernel's warps
+// mostly run one class's code.
 __global__ void RESOLVE_BOUNDS k_resolve(SceneDev sc, PathsDev P, BatchDesc b, int q) {
+  constexpr int kWarps = 128 / 32;
+  __shared__ uint32_t s_cnt[kWarps][3];
+  __shared__ uint32_t s_base;
   const uint32_t n_in = P.counts[q];
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if ((i & ~31u) >= n_in) return;                 // whole warp past the queue
+  if (blockIdx.x * blockDim.x >= n_in) return;    // whole block past the queue
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < n_in;
   const int npix = sc.width * sc.height;
-  int s = valid ? P.pq[q][i] : 0;
+  const int s = valid ? P.pq[q][i] : 0;
   ResolveRes res;
   res.sample = false;
   res.shaded = 0;
+  res.cls = 0;
   if (valid) {
     res = resolve_path(sc, P, s, slot_key(b, s, npix));
     if (!res.sample) P.out_color[s] = f4(res.L, 0.f);
   }
-  unsigned kb = __ballot_sync(kFull, res.sample);
-  uint32_t lane = threadIdx.x & 31u;
-  uint32_t base = 0;
-  if (lane == 0 && kb) base = atomicAdd(&P.counts[kSampleCount], uint32_t(__popc(kb)));
-  base = __shfl_sync(kFull, base, 0);
-  if (res.sample) P.sq[base + __popc(kb & ((1u << lane) - 1u))] = s;
-  unsigned sb = __ballot_sync(kFull, res.shaded != 0);
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  unsigned mine = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const unsigned bc = __ballot_sync(kFull, res.sample && res.cls == c);
+    if (lane == 0) s_cnt[warp][c] = uint32_t(__popc(bc));
+    if (res.sample && res.cls == c) mine = bc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (int w = 0; w < kWarps; ++w) tot += s_cnt[w][0] + s_cnt[w][1] + s_cnt[w][2];
+    s_base = tot ? atomicAdd(&P.counts[kSampleCount], tot) : 0u;
+  }
+  __syncthreads();
+  if (res.sample) {
+    uint32_t off = s_base + uint32_t(__popc(mine & ((1u << lane) - 1u)));
+    for (int c = 0; c < res.cls; ++c)
+      for (int w = 0; w < kWarps; ++w) off += s_cnt[w][c];
+    for (uint32_t w = 0; w < warp; ++w) off += s_cnt[w][res.cls];
+    P.sq[off] = s;
+  }
+  const unsigned sb = __ballot_sync(kFull, res.shaded != 0);
   if (lane == 0 && sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
 }
 
