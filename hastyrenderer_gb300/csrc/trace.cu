@@ -95,12 +95,17 @@ __global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
     }
     return;
   }
+  // Light-sample rays (odd ids) of a scene whose only light is the
+  // environment are visible iff they hit nothing (Scene.cpp:575-585 with no
+  // emissive triangle), so they stop at their first hit.
+  const bool nee_any = sc.n_light_tris == 0;
   persistent_trace<KIND>(
       n, &P.counts[kFetchCounter],
       [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
         rid = rq[k];
         float4 o = P.ray_o[rid], d = P.ray_d[rid];
         tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
+        tr.any = nee_any && (rid & 1);
         nodes = sc.nodes;
         tris = sc.isect_tris;
       },
@@ -141,6 +146,7 @@ __global__ void TRACE_BOUNDS k_trace_multi(PathsDev P, MultiDev m) {
         const SceneDev& sc = m.jobs[m.slot_meta[rid >> 1].x].sc;
         float4 o = P.ray_o[rid], d = P.ray_d[rid];
         tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
+        tr.any = sc.n_light_tris == 0 && (rid & 1);   // as k_trace
         nodes = sc.nodes;
         tris = sc.isect_tris;
       },

@@ -160,9 +160,11 @@ struct TravBinary {
   bool neg_x, neg_y, neg_z;
   Hit best;
   int link, sp;
+  bool any;   // stop at the first triangle hit (visibility only); set after init
 
   HDI void init(float ox_, float oy_, float oz_, float dx_, float dy_, float dz_) {
     ox = ox_; oy = oy_; oz = oz_; dx = dx_; dy = dy_; dz = dz_;
+    any = false;
     best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
     iv = inverse_dir(dx, dy, dz);
     neg_x = iv.ix < 0.f; neg_y = iv.iy < 0.f; neg_z = iv.iz < 0.f;
@@ -210,7 +212,7 @@ struct TravBinary {
       int ti = first + k;
       tri_test(ox, oy, oz, dx, dy, dz, ld(&tris[3 * ti]), ld(&tris[3 * ti + 1]), ld(&tris[3 * ti + 2]), best);
     }
-    if (sp == 0) return true;
+    if (sp == 0 || (any && best.tri >= 0)) return true;
     link = stack[--sp];
     return false;
   }
@@ -293,9 +295,13 @@ struct TravWide {
   Hit best;
   uint2 ng, tg;
   int sp;
+  // Visibility only: stop at the first triangle hit (best is then a hit,
+  // not necessarily the closest). Set after init.
+  bool any;
 
   HDI void init(float ox_, float oy_, float oz_, float dx_, float dy_, float dz_) {
     ox = ox_; oy = oy_; oz = oz_; dx = dx_; dy = dy_; dz = dz_;
+    any = false;
     best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
     iv = inverse_dir(dx, dy, dz);
     neg_x = iv.ix < 0.f; neg_y = iv.iy < 0.f; neg_z = iv.iz < 0.f;
@@ -313,6 +319,7 @@ struct TravWide {
       int ti = int(tg.x + b);
       tri_test(ox, oy, oz, dx, dy, dz, ld(&tris[3 * ti]), ld(&tris[3 * ti + 1]), ld(&tris[3 * ti + 2]), best);
     }
+    if (any && best.tri >= 0) return true;
     if (ng.y <= 0x00FFFFFFu) {
       if (sp == 0) return true;
       ng = stack[--sp];
