@@ -41,7 +41,7 @@ B_SHADE = 2 * 96 + 92
 # capture of `bench.py --steps 1 --warmup 3 --spp-per-step 2`; the default run
 # renders the same batches (profiles/dram_per_launch_sphere_field_1920x1080.md).
 # The shading stage is one k_resolve and one k_sample launch per bounce.
-MEASURED_TRAFFIC = {"wide": {"k_trace": 115.9e6, "k_resolve+k_sample": 227.3e6 + 177.5e6}}
+MEASURED_TRAFFIC = {"wide": {"k_trace": 115.6e6, "k_resolve+k_sample": 228.6e6 + 177.7e6}}
 
 
 def peaks():
