@@ -5,6 +5,9 @@
 // (traverse.cuh), so each photon path and each gather path computes what the
 // CPU restatement computes for the same random stream.
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
 #include "device_common.cuh"
 #include "photon.h"
 #include "traverse.cuh"
@@ -13,6 +16,8 @@
 namespace hasty {
 namespace {
 using namespace dev;
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
 
 __device__ __forceinline__ Hit trace_ray(const SceneDev& sc, V3 o, V3 d) {
   return sc.bvh_kind == 1 ? trace_wide(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z)
@@ -124,67 +129,131 @@ __global__ void __launch_bounds__(128) k_pm_footprint(SceneDev sc, uint64_t seed
 }
 
 // ---- photon tracing: sampleLightRay + tracePhoton(causticsMap = true) -------
-// Scene.cpp:527-537 and PhotonMapping.cpp:191-270.
+// Scene.cpp:527-537 and PhotonMapping.cpp:191-270. Persistent: every lane
+// carries one photon and, when its photon ends, takes the next emission
+// index from `out.fetch`, so warps stay full although most photons end at
+// their first diffuse hit and a few bounce through glass and metal. Each
+// round of the loop traces one segment per lane and processes the vertex
+// it reaches; the random stream is drawn in tracePhoton's order.
 __global__ void __launch_bounds__(128) k_pm_emit(SceneDev sc, uint64_t seed, uint32_t iter, uint32_t first, uint32_t n,
                                                  float minQ, PmEmitOut out) {
-  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const uint32_t idx = first + k;
-  Rng r; r.seed(path_key(seed ^ kPhotonKeyMix, idx, iter));
-  int capped = 0, overflow = 0;
-  // emission ray
-  uint32_t kk = sample_cdf(sc.light_cdf, uint32_t(sc.n_light_tris), r, sc.light_guide, sc.light_guide_log2);
-  const int ltri = sc.light_tris[kk];
-  const float* lp = sc.tri_pos + 9 * int64_t(ltri);
-  V3 p0 = ld3(lp), p1 = ld3(lp + 3), p2 = ld3(lp + 6);
-  V3 nl = normalize(cross(p1 - p0, p2 - p0));
-  V3 bb = triangle_uniform(r);
-  Inter li = make_inter(sc, ltri, bb, nl);
-  float pdir;
-  V3 dir = hemisphere_cos(r, li.ng, pdir, capped);
-  V3 Le = ld3(sc.mats[li.mat].emission) * HINVPI_F;
-  V3 flux = Le * (fabsf(dot(li.ng, dir)) / (sc.light_pdf_area * pdir));
-  V3 o = ray_x(li, true), d = dir;
-  // trace
-  uint32_t stored = 0;
+  const uint32_t lane = threadIdx.x & 31u;
+  bool active = false, drained = false;
+  uint32_t k = 0, stored = 0;
+  Rng r;
+  V3 o, d, flux, tt;
   PmMedia lr;
-  Hit h = trace_ray(sc, o, d);
-  if (h.tri >= 0) {
-    Inter it = inter_from_hit(sc, h.tri, h.u, h.v);
-    flux = cwise(flux, beers(lr.transmittance(), norm(it.x - o)));
-    for (int depth = 0; depth < sc.max_depth; depth++) {
-      if (!(isfinite(flux.x) && isfinite(flux.y) && isfinite(flux.z))) break;
+  int depth = 0, prev_tri = -1, pend_ovf = 0;
+  bool first_seg = true;
+  int capped = 0, overflow = 0;                 // this lane's photon
+  uint32_t n_ovf = 0, n_cap = 0;                // photons of this lane with either
+  for (;;) {
+    if (!drained) {
+      const unsigned idle = __ballot_sync(kFull, !active);
+      const uint32_t n_idle = uint32_t(__popc(idle));
+      if (n_idle) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(out.fetch, n_idle);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= n || n - base <= n_idle) drained = true;
+        if (!active) {
+          const uint32_t kk = base + uint32_t(__popc(idle & ((1u << lane) - 1u)));
+          if (kk < n) {
+            // sampleLightRay: area-weighted light triangle, uniform point, cosine direction
+            k = kk;
+            r.seed(path_key(seed ^ kPhotonKeyMix, first + k, iter));
+            capped = overflow = 0;
+            const uint32_t li_k = sample_cdf(sc.light_cdf, uint32_t(sc.n_light_tris), r, sc.light_guide, sc.light_guide_log2);
+            const int ltri = sc.light_tris[li_k];
+            const float* lp = sc.tri_pos + 9 * int64_t(ltri);
+            const V3 p0 = ld3(lp), p1 = ld3(lp + 3), p2 = ld3(lp + 6);
+            const V3 nl = normalize(cross(p1 - p0, p2 - p0));
+            const V3 bb = triangle_uniform(r);
+            const Inter li = make_inter(sc, ltri, bb, nl);
+            float pdir;
+            const V3 dir = hemisphere_cos(r, li.ng, pdir, capped);
+            const V3 Le = ld3(sc.mats[li.mat].emission) * HINVPI_F;
+            flux = Le * (fabsf(dot(li.ng, dir)) / (sc.light_pdf_area * pdir));
+            o = ray_x(li, true);
+            d = dir;
+            lr = PmMedia();
+            depth = 0; stored = 0; prev_tri = -1; pend_ovf = 0;
+            first_seg = true;
+            active = true;
+          }
+        }
+      }
+    }
+    if (__ballot_sync(kFull, active) == 0) break;
+    if (!active) continue;
+    bool end = false;
+    const Hit h = trace_ray(sc, o, d);
+    Inter it;
+    if (first_seg) {
+      if (h.tri < 0) {
+        end = true;
+      } else {
+        it = inter_from_hit(sc, h.tri, h.u, h.v);
+        flux = cwise(flux, beers(lr.transmittance(), norm(it.x - o)));
+      }
+    } else if (h.tri < 0 || h.tri == prev_tri) {
+      end = true;
+    } else {
+      // the previous vertex's medium update (already applied) counts once the ray arrives
+      it = inter_from_hit(sc, h.tri, h.u, h.v);
+      overflow |= pend_ovf;
+      tt = cwise(tt, beers(lr.transmittance(), norm(it.x - o)));
+      const float q = fmaxf(minQ, 1.0f - norm(tt));
+      if (r.u01() <= q) {
+        end = true;
+      } else {
+        flux = cwise(flux, tt) / (1.0f - q);
+        depth += 1;
+      }
+    }
+    // the vertex at `depth`: one round of tracePhoton's loop
+    if (!end && (depth >= sc.max_depth || !(isfinite(flux.x) && isfinite(flux.y) && isfinite(flux.z)))) end = true;
+    if (!end) {
       const MaterialDev& m = sc.mats[it.mat];
-      V3 wo = -d;
+      const V3 wo = -d;
       if (has_diffuse_lobe(sc, m, it) && depth > 0) {
-        uint32_t slot = atomicAdd(out.count, 1u);
+        const uint32_t slot = atomicAdd(out.count, 1u);
         if (slot < out.cap) {
           PhotonRec rec;
           rec.xn = make_float4(it.x.x, it.x.y, it.x.z, dot(it.ng, wo));
-          rec.wi = make_float4(wo.x, wo.y, wo.z, __uint_as_float(idx));
+          rec.wi = make_float4(wo.x, wo.y, wo.z, __uint_as_float(first + k));
           rec.flux = make_float4(flux.x, flux.y, flux.z, __uint_as_float(stored));   // k-th photon of this emission
           out.photons[slot] = rec;
         }
         ++stored;
       }
-      BsdfSample s = sample_concentrated(sc, m, it, wo, lr, r, true, capped);
-      V3 tt = s.thrD + s.thrC;
-      if (is_zero(tt)) break;
-      V3 o2 = ray_x(it, s.outside);
-      Hit h2 = trace_ray(sc, o2, s.dir);
-      if (h2.tri < 0 || h2.tri == it.tri) break;
-      Inter it2 = inter_from_hit(sc, h2.tri, h2.u, h2.v);
-      overflow |= lr.update(sc, m, it, wo, s.dir);
-      tt = cwise(tt, beers(lr.transmittance(), norm(it2.x - o2)));
-      float q = fmaxf(minQ, 1.0f - norm(tt));
-      if (r.u01() <= q) break;
-      flux = cwise(flux, tt) / (1.0f - q);
-      it = it2; o = o2; d = s.dir;
+      const BsdfSample bs = sample_concentrated(sc, m, it, wo, lr, r, true, capped);
+      tt = bs.thrD + bs.thrC;
+      if (is_zero(tt)) {
+        end = true;
+      } else {
+        o = ray_x(it, bs.outside);
+        pend_ovf = lr.update(sc, m, it, wo, bs.dir);
+        d = bs.dir;
+        prev_tri = it.tri;
+        first_seg = false;
+      }
+    }
+    if (end) {
+      out.stored[k] = uint8_t(stored < 255u ? stored : 255u);
+      n_ovf += overflow ? 1u : 0u;
+      n_cap += capped ? 1u : 0u;
+      active = false;
     }
   }
-  out.stored[k] = uint8_t(stored < 255u ? stored : 255u);
-  if (overflow) atomicAdd(&out.stats[0], 1ull);
-  if (capped) atomicAdd(&out.stats[1], 1ull);
+  for (int off = 16; off > 0; off >>= 1) {
+    n_ovf += __shfl_down_sync(kFull, n_ovf, off);
+    n_cap += __shfl_down_sync(kFull, n_cap, off);
+  }
+  if (lane == 0) {
+    if (n_ovf) atomicAdd(&out.stats[0], (unsigned long long)n_ovf);
+    if (n_cap) atomicAdd(&out.stats[1], (unsigned long long)n_cap);
+  }
 }
 
 // ---- gather: pathTraceWithCausticsMap (PhotonMapping.cpp:404-503) -----------
@@ -455,7 +524,17 @@ void launch_pm_footprint(const SceneDev& sc, uint64_t seed, float* dist, cudaStr
 void launch_pm_emit(const SceneDev& sc, uint64_t seed, uint32_t iter, uint32_t first, uint32_t n, float min_q,
                     const PmEmitOut& out, cudaStream_t st) {
   if (n == 0) return;
-  k_pm_emit<<<(n + 127) / 128, 128, 0, st>>>(sc, seed, iter, first, n, min_q, out);
+  static int blocks = 0;                     // resident blocks of the persistent kernel
+  if (blocks == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pm_emit, 128, 0);
+    blocks = std::max(1, sms * std::max(1, per_sm));
+  }
+  cudaMemsetAsync(out.fetch, 0, sizeof(uint32_t), st);
+  const int grid = std::min<int64_t>(blocks, (int64_t(n) + 127) / 128);
+  k_pm_emit<<<grid, 128, 0, st>>>(sc, seed, iter, first, n, min_q, out);
 }
 
 void launch_pm_gather(const SceneDev& sc, const PmMapDev& map, const PmPixelsDev& px, uint64_t seed, uint32_t iter,

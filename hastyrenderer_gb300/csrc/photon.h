@@ -27,6 +27,7 @@ struct PmEmitOut {
   uint32_t cap;
   uint8_t* stored;         // per emitted photon of the launch: photons it stored
   unsigned long long* stats;   // [0] media overflow, [1] trial cap
+  uint32_t* fetch;         // emission counter of the persistent kernel (cleared per launch)
 };
 
 // Photon map of one iteration: photons sorted by (cell x, y, z, emission

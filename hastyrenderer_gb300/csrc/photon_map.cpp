@@ -29,6 +29,7 @@ struct PmDev {
   PhotonRec* append = nullptr;
   size_t append_cap = 0;
   uint32_t* append_count = nullptr;
+  uint32_t* fetch = nullptr;               // emission counter of the photon kernel
   uint8_t* stored = nullptr;
   size_t stored_cap = 0;
   PhotonRec* sorted = nullptr;
@@ -182,6 +183,7 @@ PmDev& pm_state(hasty_job& j) {
     pm->px.albedo = j.alloc<float>(3 * n);
     pm->stats = j.alloc<unsigned long long>(2);
     pm->append_count = j.alloc<uint32_t>(1);
+    pm->fetch = j.alloc<uint32_t>(1);
     pm->n_cells = j.alloc<int32_t>(1);
     pm->status = j.alloc<PmStatus>(1);
     ck(cudaHostAlloc(reinterpret_cast<void**>(&pm->status_host), sizeof(PmStatus), cudaHostAllocDefault), "cudaHostAlloc");
@@ -276,7 +278,7 @@ void pm_iteration(hasty_job& j, PmDev& pm) {
       pm.stored = grow(j, pm.stored, pm.stored_cap, n, 0);
       pm.base = grow(j, pm.base, pm.base_cap, size_t(first) + n, first);
       pm.scratch = grow(j, pm.scratch, pm.scratch_cap, size_t(n) / 2048 + 2, 0);
-      PmEmitOut out{pm.append, pm.append_count, uint32_t(pm.append_cap), pm.stored, pm.stats};
+      PmEmitOut out{pm.append, pm.append_count, uint32_t(pm.append_cap), pm.stored, pm.stats, pm.fetch};
       ck(cudaEventRecord(ev[0], j.stream), "event");
       launch_pm_emit(j.sd, j.seed, t, first, n, min_q, out, j.stream);
       launch_pm_emit_scan(pm.stored, n, first, uint32_t(count_threshold), pm.base, pm.scratch, pm.status, j.stream);
