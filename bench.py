@@ -227,6 +227,7 @@ def main():
     t0 = time.perf_counter()
     job = RenderJob(job_path, ctx)
     info = job.info
+    load_ms = (time.perf_counter() - t0) * 1e3
     W, H = info.width, info.height
     # each step's colour estimate is read back while the next step renders
     # (hasty_job_snapshot: estimate behind the step, copy on a copy stream)
@@ -340,7 +341,9 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": args.steps * args.spp_per_step * W * H * world / e2e_s, "unit": "samples/s",
                     "h2d_bytes_per_step": int(e2e_bytes_up // args.steps), "d2h_bytes_per_step": W * H * 3 * 4,
-                    "includes": "job load (parse, BVH build, upload) + steps + a colour read-back per step, each copied while the next step renders"},
+                    "includes": "job load (parse, BVH build, upload) + steps + a colour read-back per step, each copied while the next step renders",
+                    "load_ms": {"total": load_ms, "parse": info.parse_ms, "bvh_build": info.bvh_build_ms,
+                                "upload": info.upload_ms}},
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

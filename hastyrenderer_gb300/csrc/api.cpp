@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -158,6 +159,7 @@ int64_t upload_bytes(const hasty_job& j) {
 
 void upload_scene(hasty_job& j) {
   prepare_scene(j);
+  const auto u0 = std::chrono::steady_clock::now();
   HostScene& h = j.host;
   SceneDev& s = j.sd;
   hasty_job::Prepared& p = *j.prep;
@@ -199,6 +201,7 @@ void upload_scene(hasty_job& j) {
   s.env_is_sampled = h.env_texture ? 1 : 0;
   s.p_surface = !h.env_texture ? 1.0f : (!h.light_tris.empty() ? 0.5f : 0.0f);   // Scene.cpp:545
   ck(cudaStreamSynchronize(j.stream), "sync upload");   // the host arrays may be freed after this
+  j.upload_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - u0).count();
   j.prep.reset();
 }
 
@@ -285,7 +288,9 @@ hasty_job* as_job(hasty_job* j) {
 std::unique_ptr<hasty_job> hasty::load_job_host(hasty_ctx* ctx, const std::string& path) {
   std::unique_ptr<hasty_job> j(new hasty_job());
   j->ctx = ctx;
+  const auto t0 = std::chrono::steady_clock::now();
   load_render_job(path, j->host);
+  j->parse_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   j->seed = j->host.settings.seed;
   return j;
 }
@@ -380,6 +385,8 @@ int hasty_job_info_get(hasty_job* job, hasty_job_info* out) {
     out->samples_done = job->samples_done; out->bvh_depth = job->bvh_depth; out->bvh_build_ms = job->bvh_ms;
     out->device_bytes = job->bytes;
     out->bvh_tree_ms = job->bvh_tree_ms;
+    out->parse_ms = job->parse_ms;
+    out->upload_ms = job->upload_ms;
     return HASTY_OK;
   });
 }

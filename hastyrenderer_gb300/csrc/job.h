@@ -71,7 +71,7 @@ struct hasty_job {
   hasty_ctx* ctx = nullptr;
   HostScene host;
   int32_t bvh_depth = 0;
-  double bvh_ms = 0, bvh_tree_ms = 0;
+  double bvh_ms = 0, bvh_tree_ms = 0, parse_ms = 0, upload_ms = 0;
   SceneDev sd{};
   PathsDev pd{};                      // lane 0's path buffers (and the job's statistics)
   cudaStream_t stream = nullptr;      // uploads, accumulation (in batch order), read-back

@@ -14,6 +14,7 @@
 #include <map>
 #include <memory>
 #include <sstream>
+#include <exception>
 #include <thread>
 #include <unordered_map>
 
@@ -605,56 +606,83 @@ void load_render_job(const std::string& job_path, HostScene& sc) {
   check_job_settings(sc.settings, sc);
 }
 
+// Environment texture (Environment.h:98-130): texels, pixel weights
+// |rgb| sin(theta_center), the discrete distribution over them and their sum.
+void load_environment(const std::string& path, HostScene& sc) {
+  Img im = read_image(path);
+  if (im.ch != 3 && im.ch != 4) throw LoadError("environment texture: expected 3 or 4 channels");
+  sc.env_texture = true; sc.env_w = im.w; sc.env_h = im.h;
+  size_t n = size_t(im.w) * im.h;
+  sc.env_texels.resize(3 * n);
+  for (size_t i = 0; i < n; ++i) for (int c = 0; c < 3; ++c) sc.env_texels[3 * i + size_t(c)] = im.px[i * size_t(im.ch) + size_t(c)];
+  // pixel weights |rgb| sin(theta_center), Environment.h:107-112
+  sc.env_weights.resize(n);
+  const double kPi = 3.1415926535897932384;
+  float hf = float(im.h);
+  for (int y = 0; y < im.h; ++y) {
+    float theta = ((float(y) + 0.5f) / hf) * float(kPi);
+    float s = std::sin(theta);
+    for (int x = 0; x < im.w; ++x) {
+      const float* px = &sc.env_texels[3 * (size_t(y) * size_t(im.w) + size_t(x))];
+      float nn = std::sqrt(px[0] * px[0] + px[1] * px[1] + px[2] * px[2]);
+      sc.env_weights[size_t(y) * size_t(im.w) + size_t(x)] = nn * s;
+    }
+  }
+  sc.env_cdf = build_discrete_cdf(sc.env_weights.data(), n);
+  float vs = 0.f;
+  for (float v : sc.env_weights) vs += v;
+  sc.env_value_sum = vs;
+  if (!(vs > 0.f)) throw LoadError("environment texture is black; it cannot be importance sampled");
+}
+
 void load_scene_file(const std::string& scene_path, HostScene& sc) {
   std::string folder = folder_of(scene_path);
   JNode scene = read_json(scene_path);
   setup_camera(scene.req("camera"), sc.cam);
 
   const JNode& world = scene.req("world");
+  // The environment map is read and its sampling tables built on a thread of
+  // its own while the mesh is parsed (they share nothing).
+  std::exception_ptr env_error;
+  std::thread env_thread;
   if (const JNode* bg = world.get("background_color")) {
     sc.env_texture = false; vec3_of(*bg, sc.bg);
   } else {
-    Img im = read_image(resolve(folder, world.req("environment_texture").str()));
-    if (im.ch != 3 && im.ch != 4) throw LoadError("environment texture: expected 3 or 4 channels");
-    sc.env_texture = true; sc.env_w = im.w; sc.env_h = im.h;
-    size_t n = size_t(im.w) * im.h;
-    sc.env_texels.resize(3 * n);
-    for (size_t i = 0; i < n; ++i) for (int c = 0; c < 3; ++c) sc.env_texels[3 * i + size_t(c)] = im.px[i * size_t(im.ch) + size_t(c)];
-    // pixel weights |rgb| sin(theta_center), Environment.h:107-112
-    sc.env_weights.resize(n);
-    const double kPi = 3.1415926535897932384;
-    float hf = float(im.h);
-    for (int y = 0; y < im.h; ++y) {
-      float theta = ((float(y) + 0.5f) / hf) * float(kPi);
-      float s = std::sin(theta);
-      for (int x = 0; x < im.w; ++x) {
-        const float* px = &sc.env_texels[3 * (size_t(y) * size_t(im.w) + size_t(x))];
-        float nn = std::sqrt(px[0] * px[0] + px[1] * px[1] + px[2] * px[2]);
-        sc.env_weights[size_t(y) * size_t(im.w) + size_t(x)] = nn * s;
+    const std::string env_path = resolve(folder, world.req("environment_texture").str());
+    env_thread = std::thread([&sc, env_path, &env_error] {
+      try {
+        load_environment(env_path, sc);
+      } catch (...) {
+        env_error = std::current_exception();
+      }
+    });
+  }
+  // errors are reported in the reference's loading order: environment first
+  std::exception_ptr main_error;
+  ObjFile obj;
+  try {
+    if (const JNode* v = world.get("vary_glass_ior")) sc.vary_glass_ior = v->boolean();
+    if (const JNode* dj = world.get("dispersion")) {      // extension: Cauchy bands
+      const JNode& model = dj->req("model");
+      if (model.str() == "cauchy") sc.cauchy = true;
+      else if (model.str() != "ratio") throw LoadError("world.dispersion.model: expected \"cauchy\" or \"ratio\"");
+      if (const JNode* b = dj->get("b")) sc.cauchy_b = float(b->number());
+      if (const JNode* wv = dj->get("wavelengths")) {
+        if (wv->t != JNode::ARR || wv->items.size() != 3) throw LoadError("world.dispersion.wavelengths: expected 3 values (um)");
+        for (int k = 0; k < 3; ++k) {
+          sc.band_um[k] = float(wv->items[size_t(k)].number());
+          if (!(sc.band_um[k] > 0.0f)) throw LoadError("world.dispersion.wavelengths must be positive");
+        }
       }
     }
-    sc.env_cdf = build_discrete_cdf(sc.env_weights.data(), n);
-    float vs = 0.f;
-    for (float v : sc.env_weights) vs += v;
-    sc.env_value_sum = vs;
-    if (!(vs > 0.f)) throw LoadError("environment texture is black; it cannot be importance sampled");
-  }
-  if (const JNode* v = world.get("vary_glass_ior")) sc.vary_glass_ior = v->boolean();
-  if (const JNode* dj = world.get("dispersion")) {      // extension: Cauchy bands
-    const JNode& model = dj->req("model");
-    if (model.str() == "cauchy") sc.cauchy = true;
-    else if (model.str() != "ratio") throw LoadError("world.dispersion.model: expected \"cauchy\" or \"ratio\"");
-    if (const JNode* b = dj->get("b")) sc.cauchy_b = float(b->number());
-    if (const JNode* wv = dj->get("wavelengths")) {
-      if (wv->t != JNode::ARR || wv->items.size() != 3) throw LoadError("world.dispersion.wavelengths: expected 3 values (um)");
-      for (int k = 0; k < 3; ++k) {
-        sc.band_um[k] = float(wv->items[size_t(k)].number());
-        if (!(sc.band_um[k] > 0.0f)) throw LoadError("world.dispersion.wavelengths must be positive");
-      }
-    }
-  }
 
-  ObjFile obj = read_obj(resolve(folder, scene.req("mesh").str()), folder);
+    obj = read_obj(resolve(folder, scene.req("mesh").str()), folder);
+  } catch (...) {
+    main_error = std::current_exception();
+  }
+  if (env_thread.joinable()) env_thread.join();
+  if (env_error) std::rethrow_exception(env_error);
+  if (main_error) std::rethrow_exception(main_error);
   sc.vertices = std::move(obj.v); sc.normals = std::move(obj.vn); sc.texcoords = std::move(obj.vt);
 
   for (const MtlRec& m : obj.mtls) {                       // Scene.cpp:66-118
@@ -687,39 +715,63 @@ void load_scene_file(const std::string& scene_path, HostScene& sc) {
     sc.mats.push_back(d);
   }
 
-  std::vector<float> areas;
-  size_t n_tris = 0;
-  for (const ObjShapeRec& sh : obj.shapes) n_tris += sh.mat.size();
-  sc.tri_attr.reserve(n_tris);
-  sc.tri_pos.reserve(9 * n_tris);
-  for (size_t s = 0; s < obj.shapes.size(); ++s) {         // Scene.cpp:122-189
-    const ObjShapeRec& sh = obj.shapes[s];
-    size_t nf = sh.mat.size();
-    for (size_t f = 0; f < nf; ++f) {
+  // Triangles in shape order (Scene.cpp:122-189), filled on all host
+  // threads over contiguous ranges; the lights of each range are kept in
+  // order and joined, and a bad face is reported as the first one in order.
+  std::vector<size_t> shape_first(obj.shapes.size() + 1, 0);
+  for (size_t s = 0; s < obj.shapes.size(); ++s) shape_first[s + 1] = shape_first[s] + obj.shapes[s].mat.size();
+  const size_t n_tris = shape_first.back();
+  sc.tri_attr.resize(n_tris);
+  sc.tri_pos.resize(9 * n_tris);
+  struct Range { std::vector<int32_t> lights; std::vector<float> areas; size_t bad = SIZE_MAX; std::string msg; };
+  const unsigned hw = std::thread::hardware_concurrency();
+  const size_t n_ranges = std::max<size_t>(1, std::min<size_t>(hw ? hw : 4, n_tris / 65536 + 1));
+  std::vector<Range> ranges(n_ranges);
+  auto fill = [&](size_t r) {
+    Range& R = ranges[r];
+    const size_t g0 = n_tris * r / n_ranges, g1 = n_tris * (r + 1) / n_ranges;
+    size_t s = size_t(std::upper_bound(shape_first.begin(), shape_first.end(), g0) - shape_first.begin()) - 1;
+    for (size_t g = g0; g < g1; ++g) {
+      while (g >= shape_first[s + 1]) ++s;
+      const ObjShapeRec& sh = obj.shapes[s];
+      const size_t f = g - shape_first[s];
       TriAttr a{};
       for (int k = 0; k < 3; ++k) {
         const Corner& c = sh.corners[3 * f + size_t(k)];
-        if (c.v < 0 || size_t(c.v) * 3 + 2 >= sc.vertices.size()) throw LoadError("OBJ: vertex index out of range");
-        if (c.vn >= 0 && size_t(c.vn) * 3 + 2 >= sc.normals.size()) throw LoadError("OBJ: normal index out of range");
+        if (c.v < 0 || size_t(c.v) * 3 + 2 >= sc.vertices.size()) { R.bad = g; R.msg = "OBJ: vertex index out of range"; return; }
+        if (c.vn >= 0 && size_t(c.vn) * 3 + 2 >= sc.normals.size()) { R.bad = g; R.msg = "OBJ: normal index out of range"; return; }
         a.vi[k] = c.v; a.ni[k] = c.vn; a.ti[k] = c.vt;
       }
       a.mat = sh.mat[f];
-      if (a.mat < 0) throw LoadError(" error face has no material ");
+      if (a.mat < 0) { R.bad = g; R.msg = " error face has no material "; return; }
       a.geom = uint32_t(s); a.prim = uint32_t(f); a.smooth = sh.sg[f] != 0 ? 1u : 0u;
+      float* q = &sc.tri_pos[9 * g];
       for (int k = 0; k < 3; ++k)
-        for (int c = 0; c < 3; ++c) sc.tri_pos.push_back(sc.vertices[3 * size_t(a.vi[k]) + size_t(c)]);
+        for (int c = 0; c < 3; ++c) q[3 * k + c] = sc.vertices[3 * size_t(a.vi[k]) + size_t(c)];
       const MtlRec& m = obj.mtls[size_t(a.mat)];
       if (m.Ke[0] > 0.0f || m.Ke[1] > 0.0f || m.Ke[2] > 0.0f) {
-        if (m.Kd[0] > 0.0f || m.Kd[1] > 0.0f || m.Kd[2] > 0.0f || m.Ks[0] > 0.0f || m.Ks[1] > 0.0f || m.Ks[2] > 0.0f)
-          throw LoadError(" don't support non black diffuse materials with emission ");
-        sc.light_tris.push_back(int32_t(sc.tri_attr.size()));
-        const float* q = &sc.tri_pos[sc.tri_pos.size() - 9];
+        if (m.Kd[0] > 0.0f || m.Kd[1] > 0.0f || m.Kd[2] > 0.0f || m.Ks[0] > 0.0f || m.Ks[1] > 0.0f || m.Ks[2] > 0.0f) {
+          R.bad = g; R.msg = " don't support non black diffuse materials with emission "; return;
+        }
+        R.lights.push_back(int32_t(g));
         float e1[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]}, e2[3] = {q[6] - q[0], q[7] - q[1], q[8] - q[2]};
         float cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
-        areas.push_back(0.5f * std::sqrt(cx * cx + cy * cy + cz * cz));
+        R.areas.push_back(0.5f * std::sqrt(cx * cx + cy * cy + cz * cz));
       }
-      sc.tri_attr.push_back(a);
+      sc.tri_attr[g] = a;
     }
+  };
+  {
+    std::vector<std::thread> th;
+    for (size_t r = 1; r < n_ranges; ++r) th.emplace_back(fill, r);
+    fill(0);
+    for (std::thread& t : th) t.join();
+  }
+  std::vector<float> areas;
+  for (const Range& R : ranges) {
+    if (R.bad != SIZE_MAX) throw LoadError(R.msg);     // ranges are in order: the first bad face
+    sc.light_tris.insert(sc.light_tris.end(), R.lights.begin(), R.lights.end());
+    areas.insert(areas.end(), R.areas.begin(), R.areas.end());
   }
   sc.n_shapes = uint32_t(obj.shapes.size());
   if (sc.tri_attr.empty()) throw LoadError("scene has no triangles");

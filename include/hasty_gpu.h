@@ -73,6 +73,8 @@ typedef struct hasty_job_info {
   double bvh_build_ms;
   int64_t device_bytes;        /* device memory held by the job */
   double bvh_tree_ms;          /* part of bvh_build_ms spent building the binary tree */
+  double parse_ms;             /* job load: renderJob/scene JSON, OBJ/MTL and images read on the host */
+  double upload_ms;            /* job load: host-to-device copies of the scene (after the BVH build) */
 } hasty_job_info;
 
 typedef struct hasty_stats {
