@@ -337,6 +337,7 @@ __device__ __forceinline__ float warp_max(float v) {
 }
 
 constexpr int kSmallWarps = 4;
+static_assert(kBins == 32, "k_small sweeps one bin per lane");
 
 __global__ void __launch_bounds__(32 * kSmallWarps) k_small(const Task* tasks, int n_tasks, int max_leaf, int32_t* idx,
                                                             int32_t* scratch, const float4* tlo, const float4* thi,
@@ -395,33 +396,47 @@ __global__ void __launch_bounds__(32 * kSmallWarps) k_small(const Task* tasks, i
         }
       }
       __syncwarp();
-      if (lane == 0) {
-        for (int ax = 0; ax < 3; ++ax) {
-          if (!(ch[ax] - cl[ax] > 0.f)) continue;
-          float rarea[kBins];
-          int rcnt[kBins];
-          float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-          int cnt = 0;
-          for (int b = kBins - 1; b > 0; --b) {
-            if (bins.cnt[ax][b]) for (int j = 0; j < 3; ++j) { lo[j] = fminf(lo[j], o2f(bins.mn[ax][b][j])); hi[j] = fmaxf(hi[j], o2f(bins.mx[ax][b][j])); }
-            cnt += bins.cnt[ax][b];
-            rarea[b] = box_area(lo, hi);
-            rcnt[b] = cnt;
+      // SAH sweep with lane b on bin b of each axis: the boxes right of and
+      // left of each split come from suffix / prefix min-max over the lanes
+      // (exact in any order; empty bins contribute nothing), the cost is the
+      // host builder's expression, and the split kept is the first minimum
+      // in (axis, bin) order, as a sequential sweep with `cost < best` keeps.
+      float bestc = FLT_MAX;
+      int bkey = INT_MAX;
+      for (int ax = 0; ax < 3; ++ax) {
+        if (!(ch[ax] - cl[ax] > 0.f)) continue;          // warp-uniform
+        const int c = bins.cnt[ax][lane];
+        float rlo[3], rhi[3], llo[3], lhi[3];
+        for (int j = 0; j < 3; ++j) {
+          rlo[j] = llo[j] = c ? o2f(bins.mn[ax][lane][j]) : FLT_MAX;
+          rhi[j] = lhi[j] = c ? o2f(bins.mx[ax][lane][j]) : -FLT_MAX;
+        }
+        int rc = c, lc = c;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int rco = __shfl_down_sync(kAll, rc, o), lco = __shfl_up_sync(kAll, lc, o);
+          for (int j = 0; j < 3; ++j) {
+            const float a0 = __shfl_down_sync(kAll, rlo[j], o), a1 = __shfl_down_sync(kAll, rhi[j], o);
+            const float b0 = __shfl_up_sync(kAll, llo[j], o), b1 = __shfl_up_sync(kAll, lhi[j], o);
+            if (lane + o < 32) { rlo[j] = fminf(rlo[j], a0); rhi[j] = fmaxf(rhi[j], a1); }
+            if (lane >= o) { llo[j] = fminf(llo[j], b0); lhi[j] = fmaxf(lhi[j], b1); }
           }
-          float llo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, lhi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-          int lc = 0;
-          for (int b = 0; b < kBins - 1; ++b) {
-            if (bins.cnt[ax][b]) for (int j = 0; j < 3; ++j) { llo[j] = fminf(llo[j], o2f(bins.mn[ax][b][j])); lhi[j] = fmaxf(lhi[j], o2f(bins.mx[ax][b][j])); }
-            lc += bins.cnt[ax][b];
-            if (lc == 0 || rcnt[b + 1] == 0) continue;
-            float cost = box_area(llo, lhi) * float(lc) + rarea[b + 1] * float(rcnt[b + 1]);
-            if (cost < best) { best = cost; axis = ax; split = b; }
-          }
+          if (lane + o < 32) rc += rco;
+          if (lane >= o) lc += lco;
+        }
+        const float rarea = box_area(rlo, rhi);
+        const float rarea1 = __shfl_down_sync(kAll, rarea, 1);   // bins lane+1..31
+        const int rc1 = __shfl_down_sync(kAll, rc, 1);
+        if (lane < kBins - 1 && lc != 0 && rc1 != 0) {
+          const float cost = box_area(llo, lhi) * float(lc) + rarea1 * float(rc1);
+          if (cost < bestc) { bestc = cost; bkey = ax * kBins + lane; }
         }
       }
-      axis = __shfl_sync(kAll, axis, 0);
-      split = __shfl_sync(kAll, split, 0);
-      best = __shfl_sync(kAll, best, 0);
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oc = __shfl_xor_sync(kAll, bestc, o);
+        const int ok = __shfl_xor_sync(kAll, bkey, o);
+        if (oc < bestc || (oc == bestc && ok < bkey)) { bestc = oc; bkey = ok; }
+      }
+      if (bkey != INT_MAX) { axis = bkey / kBins; split = bkey % kBins; best = bestc; }
     }
     float leaf_cost = box_area(bl, bh) * float(tk.count);
     bool leaf = tk.count <= 1 || (tk.count <= max_leaf && (axis < 0 || leaf_cost <= best));
