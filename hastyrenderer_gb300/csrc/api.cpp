@@ -702,6 +702,14 @@ int hasty_job_outputs_wait(hasty_job* job) {
   });
 }
 
+int hasty_debug_obj_digest(const char* path, int chunks, uint64_t* digest, int64_t* n_tris, int64_t* n_shapes) {
+  return guarded([&] {
+    if (!path || !digest || chunks < 0 || chunks > 4096) throw ApiError{HASTY_ERR_ARG, "bad argument"};
+    *digest = obj_digest(path, size_t(chunks), n_tris, n_shapes);
+    return HASTY_OK;
+  });
+}
+
 int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* tri, float* t, float* u, float* v) {
   return guarded([&] {
     as_job(job);

@@ -17,6 +17,10 @@
 #include <exception>
 #include <thread>
 #include <unordered_map>
+#include <unistd.h>
+#include <sys/stat.h>
+#include <sys/mman.h>
+#include <fcntl.h>
 
 namespace hasty {
 namespace {
@@ -221,11 +225,17 @@ struct MtlRec {
   std::string map_Kd, map_Ns, map_Pm, map_bump;
 };
 struct Corner { int v, vt, vn; };
-struct ObjShapeRec { std::vector<Corner> corners; std::vector<int> mat; std::vector<uint32_t> sg; };
+// Triangles of all shapes in file order: corners (3 per triangle), material
+// and smoothing group per triangle; shape s holds triangles
+// [shape_first[s], shape_first[s + 1]).
 struct ObjFile {
   std::vector<float> v, vn, vt;
-  std::vector<ObjShapeRec> shapes;
+  std::vector<Corner> corners;
+  std::vector<int> mat;
+  std::vector<uint32_t> sg;
+  std::vector<size_t> shape_first{0};
   std::vector<MtlRec> mtls;
+  size_t n_shapes() const { return shape_first.size() - 1; }
 };
 
 const char* ws(const char* s) { while (*s == ' ' || *s == '\t') ++s; return s; }
@@ -371,34 +381,81 @@ void parse_obj_lines(const char* begin, const char* end, ObjChunk& c) {
 // at once and its lines are parsed on all host threads in chunks; a
 // sequential merge then resolves indices and assembles shapes in file order,
 // so the result is the one a single pass over the lines gives.
-ObjFile read_obj(const std::string& path, const std::string& mtl_dir, size_t force_chunks = 0) {
+// An OBJ file's bytes: mapped read-only when it is a regular file (the parse
+// threads then fault in their own parts of it), else read into memory.
+struct FileBytes {
+  const char* p = nullptr;
+  size_t n = 0;
+  void* map = nullptr;
   std::string buf;
-  try {
-    buf = slurp(path);
-  } catch (const LoadError&) {
-    throw LoadError("TinyObjReader error Cannot open file [" + path + "]");
+  explicit FileBytes(const std::string& path) {
+    const int fd = ::open(path.c_str(), O_RDONLY);
+    if (fd < 0) throw LoadError("TinyObjReader error Cannot open file [" + path + "]");
+    struct stat st;
+    if (::fstat(fd, &st) == 0 && S_ISREG(st.st_mode) && st.st_size > 0) {
+      void* m = ::mmap(nullptr, size_t(st.st_size), PROT_READ, MAP_PRIVATE, fd, 0);
+      if (m != MAP_FAILED) { map = m; p = static_cast<const char*>(m); n = size_t(st.st_size); }
+    }
+    ::close(fd);
+    if (!map) {
+      try {
+        buf = slurp(path);
+      } catch (const LoadError&) {
+        throw LoadError("TinyObjReader error Cannot open file [" + path + "]");
+      }
+      p = buf.data(); n = buf.size();
+    }
   }
-  const char* b0 = buf.data();
-  const char* b1 = b0 + buf.size();
+  ~FileBytes() { if (map) ::munmap(map, n); }
+  FileBytes(const FileBytes&) = delete;
+  FileBytes& operator=(const FileBytes&) = delete;
+};
+
+// Triangles a face of n corners gives (tinyobjloader fans polygons; a quad
+// is split in two): none below 3 corners.
+inline size_t face_tris(uint32_t n) { return n >= 3 ? size_t(n) - 2 : 0; }
+
+ObjFile read_obj(const std::string& path, const std::string& mtl_dir, size_t force_chunks = 0) {
+  FileBytes file(path);
+  const char* b0 = file.p;
+  const char* b1 = b0 + file.n;
   unsigned hw = std::thread::hardware_concurrency();
-  size_t n_chunks = std::max<size_t>(1, std::min<size_t>(hw ? hw : 4, buf.size() / (1u << 20) + 1));
+  size_t n_chunks = std::max<size_t>(1, std::min<size_t>(hw ? hw : 4, file.n / (1u << 20) + 1));
   n_chunks = std::min<size_t>(n_chunks, 64);
   if (force_chunks) n_chunks = force_chunks;
   std::vector<const char*> cut(n_chunks + 1, b1);
   cut[0] = b0;
   for (size_t k = 1; k < n_chunks; ++k) {
-    const char* t = b0 + buf.size() * k / n_chunks;
+    const char* t = b0 + file.n * k / n_chunks;
     if (t < cut[k - 1]) t = cut[k - 1];
-    const char* nl = static_cast<const char*>(std::memchr(t, '\n', size_t(b1 - t)));
+    const char* nl = t < b1 ? static_cast<const char*>(std::memchr(t, '\n', size_t(b1 - t))) : nullptr;
     cut[k] = nl ? nl + 1 : b1;
   }
   std::vector<ObjChunk> chunks(n_chunks);
-  {
+  auto on_chunks = [&](auto&& fn) {
     std::vector<std::thread> th;
-    for (size_t k = 1; k < n_chunks; ++k) th.emplace_back(parse_obj_lines, cut[k], cut[k + 1], std::ref(chunks[k]));
-    parse_obj_lines(cut[0], cut[1], chunks[0]);
+    for (size_t k = 1; k < n_chunks; ++k) th.emplace_back(fn, k);
+    fn(size_t(0));
     for (std::thread& t : th) t.join();
-  }
+  };
+  // Segments: the faces of a chunk between two directive positions, with
+  // the number of triangles they give.
+  struct Segment { size_t fa, fb, tris; size_t first_tri; int mat; uint32_t sg; };
+  std::vector<std::vector<Segment>> segs(n_chunks);
+  on_chunks([&](size_t k) {
+    parse_obj_lines(cut[k], cut[k + 1], chunks[k]);
+    const ObjChunk& c = chunks[k];
+    size_t fa = 0, di = 0;
+    while (fa <= c.faces.size()) {
+      while (di < c.directives.size() && c.directives[di].face_pos == fa) ++di;
+      const size_t fb = di < c.directives.size() ? c.directives[di].face_pos : c.faces.size();
+      Segment sg{fa, fb, 0, 0, -1, 0};
+      for (size_t f = fa; f < fb; ++f) sg.tris += face_tris(c.faces[f].n);
+      segs[k].push_back(sg);
+      if (fb == c.faces.size()) break;
+      fa = fb;
+    }
+  });
   ObjFile o;
   size_t nv = 0, nvn = 0, nvt = 0;
   for (const ObjChunk& c : chunks) { nv += c.v.size(); nvn += c.vn.size(); nvt += c.vt.size(); }
@@ -408,57 +465,82 @@ ObjFile read_obj(const std::string& path, const std::string& mtl_dir, size_t for
     o.vn.insert(o.vn.end(), c.vn.begin(), c.vn.end());
     o.vt.insert(o.vt.end(), c.vt.begin(), c.vt.end());
   }
+  // The reader's state machine over the directives in file order, one step
+  // per segment: materials by name from the libraries read so far, the
+  // smoothing group, and shapes cut at o/g when they hold triangles.
   std::map<std::string, int> mindex;
-  ObjShapeRec cur;
   int mat = -1; uint32_t sg = 0;
-  auto flush = [&]() { if (!cur.corners.empty()) o.shapes.push_back(std::move(cur)); cur = ObjShapeRec(); };
+  size_t tris = 0, shape_tris = 0;
   auto apply = [&](const ObjChunk::Directive& d) {
     switch (d.kind) {
-      case ObjChunk::kFlush: flush(); break;
+      case ObjChunk::kFlush:
+        if (shape_tris) { o.shape_first.push_back(tris); shape_tris = 0; }
+        break;
       case ObjChunk::kUseMtl: { auto it = mindex.find(d.arg); mat = it == mindex.end() ? -1 : it->second; break; }
       case ObjChunk::kMtlLib: read_mtl(resolve(mtl_dir, d.arg), o.mtls, mindex); break;
       case ObjChunk::kSmooth: sg = d.sg; break;
     }
   };
-  std::vector<Corner> poly;
-  size_t base_v = 0, base_vt = 0, base_vn = 0;
-  for (const ObjChunk& c : chunks) {
+  for (size_t k = 0; k < n_chunks; ++k) {
+    const ObjChunk& c = chunks[k];
     size_t di = 0;
-    for (size_t fi = 0; fi < c.faces.size(); ++fi) {
-      while (di < c.directives.size() && c.directives[di].face_pos == fi) apply(c.directives[di++]);
-      const ObjChunk::Face& f = c.faces[fi];
-      poly.clear();
-      for (uint32_t k = 0; k < f.n; ++k) {
-        const ObjChunk::RawCorner& r = c.corners[size_t(f.first) + k];
-        Corner cr;
-        cr.v = rel_index(r.v, base_v + f.lv);
-        cr.vt = rel_index(r.vt, base_vt + f.lvt);
-        cr.vn = rel_index(r.vn, base_vn + f.lvn);
-        poly.push_back(cr);
-      }
-      if (poly.size() < 3) continue;
-      auto tri = [&](size_t a, size_t b, size_t cc) {
-        cur.corners.push_back(poly[a]); cur.corners.push_back(poly[b]); cur.corners.push_back(poly[cc]);
-        cur.mat.push_back(mat); cur.sg.push_back(sg);
-      };
-      if (poly.size() == 3) tri(0, 1, 2);
-      else if (poly.size() == 4) {
-        // tinyobjloader splits a quad along its shorter diagonal
-        auto P = [&](size_t k, int a) {
-          const size_t i = 3 * size_t(poly[k].v) + size_t(a);
-          return poly[k].v >= 0 && i < o.v.size() ? o.v[i] : 0.0f;
-        };
-        float d02 = 0, d13 = 0;
-        for (int a = 0; a < 3; ++a) { float x = P(2, a) - P(0, a), y = P(3, a) - P(1, a); d02 += x * x; d13 += y * y; }
-        if (d02 < d13) { tri(0, 1, 2); tri(0, 2, 3); } else { tri(0, 1, 3); tri(1, 2, 3); }
-      } else {
-        for (size_t k = 1; k + 1 < poly.size(); ++k) tri(0, k, k + 1);
-      }
+    for (Segment& g : segs[k]) {
+      while (di < c.directives.size() && c.directives[di].face_pos == g.fa) apply(c.directives[di++]);
+      g.first_tri = tris; g.mat = mat; g.sg = sg;
+      tris += g.tris; shape_tris += g.tris;
     }
     while (di < c.directives.size()) apply(c.directives[di++]);
-    base_v += c.v.size() / 3; base_vt += c.vt.size() / 2; base_vn += c.vn.size() / 3;
   }
-  flush();
+  if (shape_tris) o.shape_first.push_back(tris);
+  o.corners.resize(3 * tris);
+  o.mat.resize(tris);
+  o.sg.resize(tris);
+  // Faces to triangles on all threads, each segment at its place.
+  std::vector<size_t> base_v(n_chunks + 1, 0), base_vt(n_chunks + 1, 0), base_vn(n_chunks + 1, 0);
+  for (size_t k = 0; k < n_chunks; ++k) {
+    base_v[k + 1] = base_v[k] + chunks[k].v.size() / 3;
+    base_vt[k + 1] = base_vt[k] + chunks[k].vt.size() / 2;
+    base_vn[k + 1] = base_vn[k] + chunks[k].vn.size() / 3;
+  }
+  on_chunks([&](size_t k) {
+    const ObjChunk& c = chunks[k];
+    std::vector<Corner> poly;
+    for (const Segment& g : segs[k]) {
+      size_t t = g.first_tri;
+      auto tri = [&](size_t a, size_t b, size_t cc) {
+        o.corners[3 * t] = poly[a]; o.corners[3 * t + 1] = poly[b]; o.corners[3 * t + 2] = poly[cc];
+        o.mat[t] = g.mat; o.sg[t] = g.sg;
+        ++t;
+      };
+      for (size_t fi = g.fa; fi < g.fb; ++fi) {
+        const ObjChunk::Face& f = c.faces[fi];
+        if (f.n < 3) continue;
+        poly.clear();
+        for (uint32_t q = 0; q < f.n; ++q) {
+          const ObjChunk::RawCorner& r = c.corners[size_t(f.first) + q];
+          Corner cr;
+          cr.v = rel_index(r.v, base_v[k] + f.lv);
+          cr.vt = rel_index(r.vt, base_vt[k] + f.lvt);
+          cr.vn = rel_index(r.vn, base_vn[k] + f.lvn);
+          poly.push_back(cr);
+        }
+        if (poly.size() == 3) {
+          tri(0, 1, 2);
+        } else if (poly.size() == 4) {
+          // tinyobjloader splits a quad along its shorter diagonal
+          auto P = [&](size_t q, int a) {
+            const size_t i = 3 * size_t(poly[q].v) + size_t(a);
+            return poly[q].v >= 0 && i < o.v.size() ? o.v[i] : 0.0f;
+          };
+          float d02 = 0, d13 = 0;
+          for (int a = 0; a < 3; ++a) { float x = P(2, a) - P(0, a), y = P(3, a) - P(1, a); d02 += x * x; d13 += y * y; }
+          if (d02 < d13) { tri(0, 1, 2); tri(0, 2, 3); } else { tri(0, 1, 3); tri(1, 2, 3); }
+        } else {
+          for (size_t q = 1; q + 1 < poly.size(); ++q) tri(0, q, q + 1);
+        }
+      }
+    }
+  });
   return o;
 }
 
@@ -539,6 +621,19 @@ void setup_camera(const JNode& cj, CameraDev& c) {      // Camera.cpp:9-38
 }
 
 }  // namespace
+
+uint64_t obj_digest(const std::string& path, size_t chunks, int64_t* n_tris, int64_t* n_shapes) {
+  const ObjFile o = read_obj(path, folder_of(path), chunks);
+  uint64_t h = 1469598103934665603ull;                       // FNV-1a over the words
+  auto mix = [&](uint64_t w) { for (int b = 0; b < 8; ++b) { h ^= (w >> (8 * b)) & 0xFFu; h *= 1099511628211ull; } };
+  for (const Corner& c : o.corners) { mix(uint32_t(c.v)); mix(uint32_t(c.vt)); mix(uint32_t(c.vn)); }
+  for (size_t t = 0; t < o.mat.size(); ++t) { mix(uint32_t(o.mat[t])); mix(o.sg[t]); }
+  for (size_t f : o.shape_first) mix(f);
+  mix(o.v.size()); mix(o.vn.size()); mix(o.vt.size()); mix(o.mtls.size());
+  if (n_tris) *n_tris = int64_t(o.mat.size());
+  if (n_shapes) *n_shapes = int64_t(o.n_shapes());
+  return h;
+}
 
 std::vector<double> build_discrete_cdf(const float* w, size_t n) {
   std::vector<double> cdf;
@@ -718,8 +813,7 @@ void load_scene_file(const std::string& scene_path, HostScene& sc) {
   // Triangles in shape order (Scene.cpp:122-189), filled on all host
   // threads over contiguous ranges; the lights of each range are kept in
   // order and joined, and a bad face is reported as the first one in order.
-  std::vector<size_t> shape_first(obj.shapes.size() + 1, 0);
-  for (size_t s = 0; s < obj.shapes.size(); ++s) shape_first[s + 1] = shape_first[s] + obj.shapes[s].mat.size();
+  const std::vector<size_t>& shape_first = obj.shape_first;
   const size_t n_tris = shape_first.back();
   sc.tri_attr.resize(n_tris);
   sc.tri_pos.resize(9 * n_tris);
@@ -733,18 +827,17 @@ void load_scene_file(const std::string& scene_path, HostScene& sc) {
     size_t s = size_t(std::upper_bound(shape_first.begin(), shape_first.end(), g0) - shape_first.begin()) - 1;
     for (size_t g = g0; g < g1; ++g) {
       while (g >= shape_first[s + 1]) ++s;
-      const ObjShapeRec& sh = obj.shapes[s];
       const size_t f = g - shape_first[s];
       TriAttr a{};
       for (int k = 0; k < 3; ++k) {
-        const Corner& c = sh.corners[3 * f + size_t(k)];
+        const Corner& c = obj.corners[3 * g + size_t(k)];
         if (c.v < 0 || size_t(c.v) * 3 + 2 >= sc.vertices.size()) { R.bad = g; R.msg = "OBJ: vertex index out of range"; return; }
         if (c.vn >= 0 && size_t(c.vn) * 3 + 2 >= sc.normals.size()) { R.bad = g; R.msg = "OBJ: normal index out of range"; return; }
         a.vi[k] = c.v; a.ni[k] = c.vn; a.ti[k] = c.vt;
       }
-      a.mat = sh.mat[f];
+      a.mat = obj.mat[g];
       if (a.mat < 0) { R.bad = g; R.msg = " error face has no material "; return; }
-      a.geom = uint32_t(s); a.prim = uint32_t(f); a.smooth = sh.sg[f] != 0 ? 1u : 0u;
+      a.geom = uint32_t(s); a.prim = uint32_t(f); a.smooth = obj.sg[g] != 0 ? 1u : 0u;
       float* q = &sc.tri_pos[9 * g];
       for (int k = 0; k < 3; ++k)
         for (int c = 0; c < 3; ++c) q[3 * k + c] = sc.vertices[3 * size_t(a.vi[k]) + size_t(c)];
@@ -773,7 +866,7 @@ void load_scene_file(const std::string& scene_path, HostScene& sc) {
     sc.light_tris.insert(sc.light_tris.end(), R.lights.begin(), R.lights.end());
     areas.insert(areas.end(), R.areas.begin(), R.areas.end());
   }
-  sc.n_shapes = uint32_t(obj.shapes.size());
+  sc.n_shapes = uint32_t(obj.n_shapes());
   if (sc.tri_attr.empty()) throw LoadError("scene has no triangles");
   if (sc.tri_attr.size() >= (size_t(1) << 31) - 2) throw LoadError("scene has too many triangles");
   sc.light_cdf = build_discrete_cdf(areas.data(), areas.size());

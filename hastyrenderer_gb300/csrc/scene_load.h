@@ -88,5 +88,10 @@ std::vector<uint32_t> build_cdf_guide(const std::vector<double>& cdf, uint32_t& 
 
 // Halton offsets of pass k (core/include/Hasty/Random.h:14-63).
 float halton_value(uint32_t base, uint32_t k);
+// Parses an OBJ file (and its MTL libraries) with `chunks` parse chunks (0:
+// as many as the loader would use): a digest of the triangles' corner
+// indices, materials, smoothing groups and shape boundaries, for checking
+// that the result does not depend on the chunking.
+uint64_t obj_digest(const std::string& path, size_t chunks, int64_t* n_tris, int64_t* n_shapes);
 
 }  // namespace hasty

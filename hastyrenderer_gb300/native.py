@@ -128,6 +128,7 @@ def lib() -> ctypes.CDLL:
         "hasty_job_write_outputs_async": [P, ctypes.c_char_p, I],
         "hasty_job_outputs_wait": [P],
         "hasty_debug_intersect": [P, P, SZ, P, P, P, P],
+        "hasty_debug_obj_digest": [ctypes.c_char_p, I, P, P, P],
         "hasty_debug_tri_ids": [P, P, P, SZ],
         "hasty_debug_host_trace": [ctypes.c_char_p, I, P, SZ, P, P, P, P, P],
         "hasty_debug_bsdf": [I, P, SZ, P, SZ, P],

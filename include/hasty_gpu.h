@@ -316,6 +316,10 @@ int hasty_job_render_pass_static(hasty_job* job, int pass, double* d_color);
 
 /* Closest hits of n rays given as n x 6 host floats (origin, direction):
  * global triangle index (-1 miss), t, u, v. */
+/* Parses an OBJ file with `chunks` parse chunks (0: automatic), no device
+ * needed, for tests: a digest of the triangles (corner indices, materials,
+ * smoothing groups, shape boundaries) and their counts. */
+int hasty_debug_obj_digest(const char* path, int chunks, uint64_t* digest, int64_t* n_tris, int64_t* n_shapes);
 int hasty_debug_intersect(hasty_job* job, const float* rays, size_t n, int32_t* tri, float* t, float* u, float* v);
 /* The same closest-hit traversal run on the CPU (no device needed): loads the
  * job on the host, builds the BVH (kind 0 binary, 1 compressed 8-wide) and

@@ -47,3 +47,60 @@ def test_cli_argument_errors(tmp_path):
     assert r.returncode == 1 and "usage" in r.stdout
     r = subprocess.run([exe, "job.json", str(tmp_path / "missing")], capture_output=True, text=True)
     assert r.returncode == 1 and "not a directory" in r.stdout
+
+
+def _obj_digest(path, chunks):
+    lib = native.lib()
+    d, nt, ns = ctypes.c_uint64(), ctypes.c_int64(), ctypes.c_int64()
+    assert lib.hasty_debug_obj_digest(str(path).encode(), chunks, ctypes.byref(d), ctypes.byref(nt), ctypes.byref(ns)) == 0
+    return d.value, nt.value, ns.value
+
+
+def _edge_obj(tmp_path):
+    """An OBJ with the reader's edge cases: polygons of 2 to 6 corners (fans,
+    quads split along the shorter diagonal, degenerate faces skipped),
+    negative and partial indices, o/g cuts including empty shapes, usemtl of
+    unknown names, a second mtllib mid-file, smoothing groups and 'off'."""
+    import random
+    rnd = random.Random(7)
+    lines = ["mtllib a.mtl", "o first", "usemtl red"]
+    nv = 0
+    faces = 0
+    for i in range(6000):
+        r = rnd.random()
+        if r < 0.05:
+            lines.append(rnd.choice(["o obj%d" % i, "g g%d" % i, "usemtl red", "usemtl blue", "usemtl nope",
+                                     "s %d" % rnd.randint(0, 3), "s off", "mtllib b.mtl", "# comment", "o", "g a b"]))
+        elif r < 0.4 or nv < 3:
+            for _ in range(rnd.randint(1, 3)):
+                lines.append("v %g %g %g" % tuple(rnd.uniform(-5, 5) for _ in range(3)))
+                nv += 1
+        else:
+            n = rnd.choice([3, 3, 3, 4, 4, 5, 6, 2])
+            idx = [rnd.randint(1, nv) if rnd.random() < 0.8 else -rnd.randint(1, nv) for _ in range(n)]
+            form = rnd.choice(["%d", "%d/1", "%d//2", "%d/2/1"])
+            lines.append("f " + " ".join(form % x for x in idx))
+            faces += max(0, n - 2)
+    lines = lines[:3] + ["vt 0.5 0.5", "vt 0.1 0.9", "vn 0 1 0", "vn 1 0 0"] + lines[3:]
+    (tmp_path / "a.mtl").write_text("newmtl red\nKd 1 0 0\nnewmtl blue\nKd 0 0 1\n")
+    (tmp_path / "b.mtl").write_text("newmtl green\nKd 0 1 0\n")
+    p = tmp_path / "edge.obj"
+    p.write_text("\n".join(lines) + "\n")
+    return p, faces
+
+
+def test_obj_reader_independent_of_chunking(tmp_path):
+    """The mesh reader parses a file's lines in chunks on all host threads and
+    assembles triangles per chunk at offsets from a pass over the directives;
+    the triangles (corners, materials, smoothing groups, shapes) must be the
+    ones a single pass gives, for any number of chunks."""
+    p, tris = _edge_obj(tmp_path)
+    ref = _obj_digest(p, 1)
+    assert ref[1] == tris and ref[2] > 10
+    for chunks in (2, 3, 5, 8, 13, 16, 31, 64, 0):
+        assert _obj_digest(p, chunks) == ref, chunks
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "scenes")
+    for name in ("cornell", "field", "room"):
+        q = os.path.join(golden, name, "scene.obj")
+        one = _obj_digest(q, 1)
+        assert all(_obj_digest(q, c) == one for c in (2, 7, 16))
