@@ -37,11 +37,13 @@ WORKLOAD = "sphere_field_800x_icosphere3_1024002tri_1920x1080_dof6_sky2048x1024_
 # the triangle's attributes (92 B); texel reads are not counted.
 B_SHADE = 2 * 96 + 92
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, averaged
-# over the 12 bounces of one 4,147,200-path batch, wide BVH) from one ncu
-# capture of `bench.py --steps 1 --warmup 3 --spp-per-step 2`; the default run
-# renders the same batches (profiles/dram_per_launch_sphere_field_1920x1080.md).
-# The shading stage is one k_resolve and one k_sample launch per bounce.
-MEASURED_TRAFFIC = {"wide": {"k_trace": 115.6e6, "k_resolve+k_sample": 228.6e6 + 177.7e6}}
+# over the 12 bounces of one 8-pass batch of 16,588,800 paths, wide BVH) from
+# one ncu capture of `bench.py --steps 1 --warmup 3 --spp-per-step 8`, the
+# batches of the default run (profiles/dram_per_launch_sphere_field_1920x1080.md;
+# captures of 2- and 4-pass batches gave 1/4 and 1/2 of these bytes). The
+# shading stage is one k_resolve and one k_sample launch per bounce.
+MEASURED_TRAFFIC = {"wide": {"k_trace": 461.0e6, "k_resolve+k_sample": 938.7e6 + 748.4e6}}
+MEASURED_TRAFFIC_PASSES = 8
 
 
 def peaks():
@@ -305,7 +307,10 @@ def main():
         roof, kernels = None, []
         if bvh_costs is not None:
             b_ray = 32 + 16 + 64 * bvh_costs["nodes_per_ray"] + 48 * bvh_costs["tris_per_ray"]
-            traffic = MEASURED_TRAFFIC.get(args.bvh, {}) if args.spp_per_step % 2 == 0 else {}
+            # the measured bytes scale with the passes in a batch
+            batch_passes = min(args.spp_per_step, max(1, info.paths_in_flight // (W * H)))
+            traffic = {k: v * batch_passes / MEASURED_TRAFFIC_PASSES
+                       for k, v in MEASURED_TRAFFIC.get(args.bvh, {}).items()}
             n_launch = max(trace_launches, 1)
             rays_st, shaded_st = st1["rays"] - st0["rays"], st1["shaded"] - st0["shaded"]
             for name, work, unit_bytes, ms in (("k_trace", rays_st, b_ray, trace_ms),

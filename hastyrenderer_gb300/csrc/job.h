@@ -202,8 +202,9 @@ namespace hasty {
 // given (api.cpp).
 void alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st,
                       unsigned long long* stats = nullptr);
-// Single-job path state sized to j.capacity, allocated on first use.
-void ensure_paths(hasty_job& j);
+// Single-job path state for at least `need` paths (at most j.capacity),
+// allocated on first use and grown when a call needs more.
+void ensure_paths(hasty_job& j, int64_t need);
 // Loads renderJob.json, builds the BVH and uploads the scene. `plain`: also
 // the FP64 accumulators, estimate buffer and statistics of the single-job
 // path; without it the job holds only the scene (multi-job engine use).

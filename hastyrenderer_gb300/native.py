@@ -32,7 +32,8 @@ class JobInfo(ctypes.Structure):
                 ("n_light_triangles", ctypes.c_int64), ("n_shapes", ctypes.c_int32), ("n_materials", ctypes.c_int32),
                 ("env_is_texture", ctypes.c_int32), ("exposure", ctypes.c_float), ("samples_done", ctypes.c_int32),
                 ("bvh_depth", ctypes.c_int32), ("bvh_build_ms", ctypes.c_double), ("device_bytes", ctypes.c_int64),
-                ("bvh_tree_ms", ctypes.c_double), ("parse_ms", ctypes.c_double), ("upload_ms", ctypes.c_double)]
+                ("bvh_tree_ms", ctypes.c_double), ("parse_ms", ctypes.c_double), ("upload_ms", ctypes.c_double),
+                ("paths_in_flight", ctypes.c_int64)]
 
 
 class Stats(ctypes.Structure):

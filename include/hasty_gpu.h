@@ -75,6 +75,7 @@ typedef struct hasty_job_info {
   double bvh_tree_ms;          /* part of bvh_build_ms spent building the binary tree */
   double parse_ms;             /* job load: renderJob/scene JSON, OBJ/MTL and images read on the host */
   double upload_ms;            /* job load: host-to-device copies of the scene (after the BVH build) */
+  int64_t paths_in_flight;     /* camera samples per batch at most (whole passes) */
 } hasty_job_info;
 
 typedef struct hasty_stats {
