@@ -230,9 +230,18 @@ int64_t default_capacity(int64_t npix) {
 
 // Resident blocks per SM of the persistent closest-hit kernel while two
 // render lanes run: fewer than fit (9 on GB300) leaves room for the other
-// lane's shading blocks. Measured on the 1080p sphere field (M samples/s):
-// all 822, 7: 829, 6: 834, 5: 836-840, 4: 822, 3: 788.
+// lane's shading blocks. Measured on the 1080p sphere field (M samples/s),
+// 2-pass batches: all 822, 7: 829, 6: 834, 5: 836-840, 4: 822, 3: 788;
+// 8-pass batches: all 883, 7: 897, 6: 897, 5: 900, 4: 903, 3: 865.
 constexpr int kLaneTraceBlocksPerSM = 5;
+// HASTY_LANE_TRACE_BLOCKS overrides it (0: no cap).
+int lane_trace_blocks() {
+  static const int v = [] {
+    const char* e = std::getenv("HASTY_LANE_TRACE_BLOCKS");
+    return e ? std::max(0, std::atoi(e)) : kLaneTraceBlocksPerSM;
+  }();
+  return v;
+}
 
 // One batch of passes on render lane `lane` (the two lanes alternate; see
 // hasty_job): ray generation and the bounces on the lane's stream, then the
@@ -254,7 +263,7 @@ void render_batch(hasty_job& j, int n_passes, int lane, bool more_batches) {
       (void)cudaGetLastError();        // "not ready" is an answer, not an error to report later
     }
   }
-  const int trace_cap = (j.stage_timing || !other_busy) ? 0 : kLaneTraceBlocksPerSM;
+  const int trace_cap = (j.stage_timing || !other_busy) ? 0 : lane_trace_blocks();
   if (j.lane_free_valid[lane]) ck(cudaStreamWaitEvent(ls, j.lane_free[lane], 0), "lane wait");
   launch_raygen(j.sd, pd, b, ls);
   int max_paths = b.n_paths;
