@@ -290,7 +290,8 @@ void render_batch(hasty_job& j, int n_passes, int lane, bool more_batches) {
   ck(cudaEventRecord(j.lane_free[lane], j.stream), "lane event");
   j.lane_free_valid[lane] = true;
   j.trace_launches += uint64_t(j.sd.max_depth);
-  j.kernel_launches += uint64_t(2 + 2 * j.sd.max_depth);
+  // raygen and accumulate, and per bounce: trace, resolve, sample
+  j.kernel_launches += uint64_t(2 + 3 * j.sd.max_depth);
   j.samples_done += n_passes;
 }
 
