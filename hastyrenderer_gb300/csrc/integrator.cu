@@ -762,7 +762,7 @@ __global__ void RESOLVE_BOUNDS k_resolve_multi(PathsDev P, MultiDev m, const Job
   if (lane == 0 && sb) atomicAdd(&P.stats[ST_SHADED], (unsigned long long)__popc(sb));
 }
 
-__global__ void SAMPLE_BOUNDS k_sample_multi(PathsDev P, MultiDev m, const JobDev* __restrict__ jobs) {
+__global__ void __launch_bounds__(kSampleThreads, 2) k_sample_multi(PathsDev P, MultiDev m, const JobDev* __restrict__ jobs) {
   const uint32_t n_in = P.counts[kSampleCount];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if ((i & ~31u) >= n_in) return;
@@ -967,7 +967,7 @@ void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int cap, int b
   k_multi_regen<<<(cap + 255) / 256, 256, 0, st>>>(p, m, m.jobs);
   launch_trace_multi(p, m, bvh_kind, 2 * cap, st, trace_blocks_per_sm);
   k_resolve_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m, m.jobs);
-  k_sample_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m, m.jobs);
+  k_sample_multi<<<(cap + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(p, m, m.jobs);
   k_compact_count<<<nb, kCompactThreads, 0, st>>>(m, cap);
   k_compact_scan<<<1, 1024, 0, st>>>(p, m, nb);
   k_compact_scatter<<<nb, kCompactThreads, 0, st>>>(p, m, cap);
