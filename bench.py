@@ -42,7 +42,7 @@ B_SHADE = 2 * 96 + 92
 # batches of the default run (profiles/dram_per_launch_sphere_field_1920x1080.md;
 # captures of 2- and 4-pass batches gave 1/4 and 1/2 of these bytes). The
 # shading stage is one k_resolve and one k_sample launch per bounce.
-MEASURED_TRAFFIC = {"wide": {"k_trace": 461.0e6, "k_resolve+k_sample": 938.7e6 + 748.4e6}}
+MEASURED_TRAFFIC = {"wide": {"k_trace": 461.4e6, "k_resolve+k_sample": 939.9e6 + 738.9e6}}
 MEASURED_TRAFFIC_PASSES = 8
 
 
