@@ -359,30 +359,11 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
   return res;
 }
 
-// Minimum resident blocks per SM asked of the compiler for the resolve and
-// sample kernels (0: no bound beyond the block size). Both are latency-bound
-// (dependent loads of hit, triangle, material, texture), so occupancy pays
-// more than the registers it costs: 8 blocks of 128 threads (64 registers)
-// measured fastest for both on GB300, ahead of 4, 6 and 12.
-#ifndef HASTY_SHADE_MIN_BLOCKS
-#define HASTY_SHADE_MIN_BLOCKS 8
-#endif
-#ifndef HASTY_RESOLVE_MIN_BLOCKS
-#define HASTY_RESOLVE_MIN_BLOCKS HASTY_SHADE_MIN_BLOCKS
-#endif
-#ifndef HASTY_SAMPLE_MIN_BLOCKS
-#define HASTY_SAMPLE_MIN_BLOCKS HASTY_SHADE_MIN_BLOCKS
-#endif
-#if HASTY_RESOLVE_MIN_BLOCKS > 0
-#define RESOLVE_BOUNDS __launch_bounds__(128, HASTY_RESOLVE_MIN_BLOCKS)
-#else
-#define RESOLVE_BOUNDS __launch_bounds__(128)
-#endif
-#if HASTY_SAMPLE_MIN_BLOCKS > 0
-#define SAMPLE_BOUNDS __launch_bounds__(128, HASTY_SAMPLE_MIN_BLOCKS)
-#else
-#define SAMPLE_BOUNDS __launch_bounds__(128)
-#endif
+// Block shapes of the resolve and sample kernels (single-job and engine):
+// both are latency-bound (dependent loads of hit, triangle, material,
+// texture), so occupancy pays more than registers: 64 registers, 1024
+// threads per SM (8 blocks of 128 measured ahead of 4, 6 and 12 at 128
+// threads); the block sizes are set at kResolveThreads and kSampleThreads.
 
 __device__ __forceinline__ uint64_t slot_key(const BatchDesc& b, int s, int npix) {
   return path_key(b.seed, uint32_t(s % npix), b.pass_base + uint32_t(s / npix));
@@ -738,7 +719,7 @@ __device__ __forceinline__ void finish_multi(const PathsDev& P, const MultiDev& 
 // The job table is passed as a restrict pointer of its own: no store of the
 // kernel writes it, so its scene fields are loaded once rather than again after
 // every path-state store.
-__global__ void RESOLVE_BOUNDS k_resolve_multi(PathsDev P, MultiDev m, const JobDev* __restrict__ jobs) {
+__global__ void __launch_bounds__(kResolveThreads, 4) k_resolve_multi(PathsDev P, MultiDev m, const JobDev* __restrict__ jobs) {
   const uint32_t q = m.ctl[0];
   const uint32_t n_in = P.counts[q];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -966,7 +947,7 @@ void launch_multi_iteration(const PathsDev& p, const MultiDev& m, int cap, int b
   k_multi_plan<<<1, 1, 0, st>>>(p, m);
   k_multi_regen<<<(cap + 255) / 256, 256, 0, st>>>(p, m, m.jobs);
   launch_trace_multi(p, m, bvh_kind, 2 * cap, st, trace_blocks_per_sm);
-  k_resolve_multi<<<(cap + 127) / 128, 128, 0, st>>>(p, m, m.jobs);
+  k_resolve_multi<<<(cap + kResolveThreads - 1) / kResolveThreads, kResolveThreads, 0, st>>>(p, m, m.jobs);
   k_sample_multi<<<(cap + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(p, m, m.jobs);
   k_compact_count<<<nb, kCompactThreads, 0, st>>>(m, cap);
   k_compact_scan<<<1, 1024, 0, st>>>(p, m, nb);
