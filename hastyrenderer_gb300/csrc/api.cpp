@@ -232,7 +232,9 @@ int64_t default_capacity(int64_t npix) {
 // render lanes run: fewer than fit (9 on GB300) leaves room for the other
 // lane's shading blocks. Measured on the 1080p sphere field (M samples/s),
 // 2-pass batches: all 822, 7: 829, 6: 834, 5: 836-840, 4: 822, 3: 788;
-// 8-pass batches: all 883, 7: 897, 6: 897, 5: 900, 4: 903, 3: 865.
+// 8-pass batches: all 883, 7: 897, 6: 897, 5: 900, 4: 903, 3: 865;
+// with the 256/512-thread shading blocks: all 942, 7: 938, 6: 943, 5: 948,
+// 4: 940.
 constexpr int kLaneTraceBlocksPerSM = 5;
 // HASTY_LANE_TRACE_BLOCKS overrides it (0: no cap).
 int lane_trace_blocks() {
