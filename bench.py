@@ -142,6 +142,23 @@ def cpu_baseline(job_path: str, budget_s: float = 12.0, threads: int = 0):
                                                "shaded_per_sample": shaded / max(samples, 1), "rays_per_sample": rays / max(samples, 1)}
 
 
+def replica_seed(rank: int) -> int:
+    """Random streams of rank `rank`'s replica: every rank renders its own
+    passes of the same job (weak scaling, no data-path exchange)."""
+    return 1000 + rank
+
+
+def max_over_ranks(value: float, dist, device: str) -> float:
+    """The largest of the ranks' values (the job's time is its slowest
+    rank's); `dist` None means one rank."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference_arm(args, job_path: str, rank: int):
     if rank != 0:
         return
@@ -201,7 +218,9 @@ def main():
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local_rank)
+        if args.impl == "ours":
+            torch.cuda.set_device(local_rank)
+        # the reference arm runs on the host cores only (gloo, no device)
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
 
     base = os.environ.get("HASTY_BENCH_DIR", os.path.join(tempfile.gettempdir(), "hasty_bench_c1"))
@@ -248,7 +267,7 @@ def main():
 
     # ---- device-resident timing (both render lanes, as a user's render runs)
     job.reset()
-    job.set_seed(1000 + rank)
+    job.set_seed(replica_seed(rank))
     for _ in range(args.warmup):
         job.render_passes(args.spp_per_step)
     job.sync()
@@ -285,10 +304,7 @@ def main():
     job.set_stage_timing(False)
     dev_s = (s1["kernel_ms"] - s0["kernel_ms"]) * 1e-3
     t = max(dev_s, 1e-9)
-    if dist is not None:
-        tt = torch.tensor([t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
+    t = max_over_ranks(t, dist, "cuda")
     samples = args.steps * args.spp_per_step * W * H
     rays = s1["rays"] - s0["rays"]
     shaded = s1["shaded"] - s0["shaded"]
