@@ -150,3 +150,19 @@ def test_cli_end_to_end(cornell, tmp_path, every):
     ref.render_passes(ref.info.num_samples)
     for aov, name in zip(AOVS, NAMES):
         np.testing.assert_array_equal(read_exr(str(tmp_path / (name + ".exr"))), ref.compute_estimate(aov))
+
+
+def test_job_info_load_times_and_paths(cornell):
+    """hasty_job_info reports the load's parts and the paths-in-flight
+    setting (whole passes, up to 16M paths); path buffers follow a change."""
+    job = _job(cornell)
+    i = job.info
+    npix = i.width * i.height
+    assert i.parse_ms > 0 and i.upload_ms >= 0 and i.bvh_build_ms > 0
+    assert i.paths_in_flight % npix == 0 and npix <= i.paths_in_flight <= max(npix, 1 << 24)
+    job.set_paths_in_flight(3 * npix + 5)
+    assert job.info.paths_in_flight == 3 * npix
+    job.render_passes(7)
+    ref = _job(cornell)
+    ref.render_passes(7)
+    np.testing.assert_array_equal(job.compute_estimate(0), ref.compute_estimate(0))
