@@ -15,7 +15,7 @@ ranks (each rank renders its own pass range of the same job: weak scaling);
 `e2e` is the same metric through the C ABI including the job load (host
 parse, BVH build, host->device upload) and a device->host read of the colour
 estimate of every step (hasty_job_snapshot: copied while the next step
-renders, as a progressive viewer reads it). `cpu_baseline` times the CPU checker (oracle/)
+renders, as a progressive viewer reads it). `cpu_baseline` times the CPU oracle (oracle/)
 on this host's cores on a bounded crop of the same job.
 """
 from __future__ import annotations
@@ -114,9 +114,9 @@ def make_job(base: str, seed: int = 0) -> str:
 
 
 def cpu_baseline(job_path: str, budget_s: float = 12.0, threads: int = 0):
-    """CPU checker on this host's cores: rows of a centred 128-pixel-wide crop,
+    """CPU oracle on this host's cores: rows of a centred 128-pixel-wide crop,
     one pass each, until the time budget is spent. Also returns the BVH node
-    visits and triangle tests per ray of the checker's binary BVH."""
+    visits and triangle tests per ray of the oracle's binary BVH."""
     from oracle.oracle import Oracle
     ora = Oracle(job_path)
     info = ora.info()
@@ -383,7 +383,7 @@ def run_photon(args):
     640x480, depth 8: one stochastic progressive iteration per step (photon
     tracing until 0.5*W*H caustic photons are stored, photon-map build, gather
     of every pixel). value = pixels gathered per second by the wall clock (the
-    host part of an iteration is real work); the CPU baseline is the checker's
+    host part of an iteration is real work); the CPU baseline is the oracle's
     photon mapper (one thread, as one reference render thread) on the same
     scene at 160x120."""
     import numpy as np

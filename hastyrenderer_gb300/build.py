@@ -1,7 +1,7 @@
 """Builds the native library and CLI in-tree (no CMake, no torch extension).
 
     python -m hastyrenderer_gb300.build            # library + CLI
-    python -m hastyrenderer_gb300.build --oracle   # also the CPU checker under oracle/
+    python -m hastyrenderer_gb300.build --oracle   # also the CPU oracle under oracle/
 
 CUDA sources are compiled for sm_103a only; `integrator.cu` without FMA
 contraction (products and sums round like the reference's scalar C++), and
@@ -110,7 +110,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
 
 
 def build_oracle(with_reference: bool | None = None, verbose: bool = False) -> None:
-    """CPU checker: oracle/_build/liboracle.so, and the reference build under
+    """CPU oracle: oracle/_build/liboracle.so, and the reference build under
     oracle/_ref when the reference sources are present on this machine."""
     odir = os.path.join(ROOT, "oracle")
     targets = ["port"]

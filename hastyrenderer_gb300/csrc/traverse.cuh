@@ -7,7 +7,7 @@
 //
 // The ray/triangle test is Moeller-Trumbore in Embree's sign conventions and
 // rounds every product and sum separately (no FMA contraction), so t, u, v
-// and the chosen triangle are the ones the CPU checker computes. The far
+// and the chosen triangle are the ones the CPU oracle computes. The far
 // limit is applied to the divided distance and ties at equal t go to the
 // smaller triangle id, so the answer does not depend on traversal order.
 // Binary-BVH box tests round each step once and are padded by

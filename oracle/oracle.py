@@ -1,4 +1,4 @@
-"""Oracle (test infrastructure only): ctypes access to the CPU checker.
+"""Oracle (test infrastructure only): ctypes access to the CPU oracle.
 
 ``Oracle`` drives the CPU restatement (oracle/port, built to
 oracle/_build/liboracle.so); ``ReferenceBuild`` drives the reference's own
@@ -121,7 +121,7 @@ class ReferenceBuild(_Base):
 
 
 class PhotonMapper:
-    """Photon mapper of the CPU checker (oracle/port/oracle_pm.cpp) or of the
+    """Photon mapper of the CPU oracle (oracle/port/oracle_pm.cpp) or of the
     reference build (oracle/ref_pm_harness.cpp): `iterate(n)` runs n more
     progressive iterations and returns the current images (H, W, 3), the
     radii (H, W) and {emitted, stored, iteration} of the last iteration."""
@@ -202,7 +202,7 @@ def halton(base: int, k: int) -> float:
 
 def property_test(which: int, n: int, seed: int = 0) -> np.ndarray:
     """The reference's unit tests (apps/Tests.cpp) run as loops in the CPU
-    checker; returns the quantities each test asserts on."""
+    oracle; returns the quantities each test asserts on."""
     L = _load(PORT_LIB, "hor")
     L.hor_property.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, ctypes.c_void_p]
     out = np.zeros(8, np.float64)

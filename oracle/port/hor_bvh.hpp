@@ -1,5 +1,5 @@
 // Oracle (test infrastructure only): closest-hit ray queries for the CPU
-// checker, standing in for Embree's rtcIntersect1 as the reference calls it
+// oracle, standing in for Embree's rtcIntersect1 as the reference calls it
 // (core/src/Scene.cpp:281-303: tnear 1e-6, tfar +inf, u/v = weights of the
 // triangle's 2nd/3rd vertex, Ng = (v1-v0)x(v2-v0) unnormalised).
 //
@@ -9,7 +9,7 @@
 // (binned SAH, 32 bins, leaves of at most 4 triangles). Ties at equal t go to
 // the smaller primitive index so that the answer does not depend on the
 // traversal order. A double-precision brute-force query serves as a
-// second, independent checker.
+// second, independent check.
 #pragma once
 #include <algorithm>
 #include <cfloat>

@@ -1,5 +1,5 @@
 // Oracle (test infrastructure only): readers for the render-job surface used by
-// the CPU checker and by the stand-in headers under oracle/shims/.
+// the CPU oracle and by the stand-in headers under oracle/shims/.
 //  * JSON: a small DOM for renderJob.json and the scene JSON
 //    (core/src/RenderJob.cpp:10-28, core/src/Scene.cpp:12-31, core/src/Camera.cpp:9-25).
 //  * OBJ/MTL: the subset of tinyobjloader semantics the reference relies on

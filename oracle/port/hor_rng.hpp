@@ -1,5 +1,5 @@
 // Oracle (test infrastructure only): the project's PCG-family random stream and
-// the libstdc++ discrete-distribution draw, restated for the CPU checker.
+// the libstdc++ discrete-distribution draw, restated for the CPU oracle.
 //
 // The reference's RNG is shishua (core/src/Random.cpp:5-47, pinned commit
 // ed0d60a8b35fb6aba711dcbc24aaeda78c623b45 in cmake/AddShishua.cmake:3), read

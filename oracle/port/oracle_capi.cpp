@@ -1,4 +1,4 @@
-// Oracle (test infrastructure only): C entry points of the CPU checker,
+// Oracle (test infrastructure only): C entry points of the CPU oracle,
 // loaded with ctypes by tests/, __graft_entry__.smoke() and bench.py's
 // CPU-baseline leg. Nothing in the product links against this library.
 #include "oracle_core.hpp"

@@ -1,5 +1,5 @@
 """CUDA path against the reference's own outputs (golden fixtures written by
-the reference build, tests/golden/) and against the CPU checker (oracle/) on
+the reference build, tests/golden/) and against the CPU oracle (oracle/) on
 the same seeded scenes and per-path random streams. All calls go through the
 C ABI (hastyrenderer_gb300.native)."""
 import os
@@ -43,9 +43,9 @@ def _check_hits(g, c):
 
 
 @pytest.mark.parametrize("name,lo,hi", [("cornell", -1.0, 2.0), ("field", -3.0, 4.0), ("room", -2.0, 3.0)])
-def test_intersect_matches_checker(name, lo, hi):
+def test_intersect_matches_oracle(name, lo, hi):
     """Closest hits: triangle ids agree on >= 99.99% of rays (exactly, in
-    practice), t within 1e-5 relative; the checker's BVH answer is the same
+    practice), t within 1e-5 relative; the oracle's BVH answer is the same
     as a brute-force scan with the same FP32 triangle test."""
     job = _job(golden_job(name))
     ora = Oracle(golden_job(name))
@@ -110,9 +110,9 @@ def test_sixteen_passes_match_reference(name):
 
 @pytest.mark.parametrize("name", ["cornell", "field", "room"])
 def test_image_ztest(name):
-    """Per-pixel means at S = 64 spp against the checker at 16*S spp from the
+    """Per-pixel means at S = 64 spp against the oracle at 16*S spp from the
     same streams: |mean_gpu - mean_cpu| <= 4 sigma per pixel, sigma from the
-    per-sample variance of the checker's 16*S samples for both estimates (its
+    per-sample variance of the oracle's 16*S samples for both estimates (its
     own Monte Carlo noise included). Sun and caustic paths make the radiance
     heavy-tailed, so the sample variance can underestimate sigma on a few
     pixels: at most 0.5% of pixels may exceed 4 sigma, and the signed

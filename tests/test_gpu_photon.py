@@ -64,10 +64,10 @@ def room_160(tmp_path_factory):
     return scenes.textured_room(str(d), seed=5, width=160, height=120, spp=16, max_depth=8, tex_size=64)
 
 
-def test_photon_mapper_matches_checker_multi_tile(room_160):
+def test_photon_mapper_matches_oracle_multi_tile(room_160):
     """160x120: 9,600 stored photons per iteration, so the device map build
     runs over several scan and sort tiles; every iteration against the CPU
-    checker's photon mapper (pinned bit-exact to the reference build). With
+    oracle's photon mapper (pinned bit-exact to the reference build). With
     19,200 pixels a photon lying on a pixel's gather radius, its position one
     ulp apart on the two sides, changes that pixel's photon count by one and
     its radius by one shrink factor (measured: 2 pixels, 0.23%). Tolerances:

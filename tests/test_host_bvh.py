@@ -1,5 +1,5 @@
 """Host-side loader, BVH builders and the traversal code (the same source the
-GPU runs, compiled for the host) against the CPU checker: no GPU needed."""
+GPU runs, compiled for the host) against the CPU oracle: no GPU needed."""
 import os
 
 import numpy as np
@@ -37,7 +37,7 @@ def test_traversal_exact(kind, name, lo, hi):
 
 def test_full_size_scene(tmp_path):
     """The 1,024,002-triangle benchmark scene: both trees agree with the
-    checker's BVH; the wide tree is shallower and has fewer nodes."""
+    oracle's BVH; the wide tree is shallower and has fewer nodes."""
     from hastyrenderer_gb300 import scenes
     job = scenes.sphere_field(str(tmp_path / "c1"), seed=0)
     rays = _rays(8000, 11, -10.0, 10.0)

@@ -1,6 +1,6 @@
-"""The CPU checker (oracle/port) against fixtures written by the reference's
+"""The CPU oracle (oracle/port) against fixtures written by the reference's
 own code (tests/golden/make_golden.py, from the build under oracle/_ref), and
-the reference's unit tests (apps/Tests.cpp) run on the checker."""
+the reference's unit tests (apps/Tests.cpp) run on the oracle."""
 import os
 
 import numpy as np
@@ -66,7 +66,7 @@ def test_rng_stream_spec():
         assert np.array_equal(rng_stream(seed, pixel, p, 16), g[key])
 
 
-# ---- the reference's unit tests (apps/Tests.cpp), run on the checker -------
+# ---- the reference's unit tests (apps/Tests.cpp), run on the oracle -------
 def test_rodrigues_rotation():                      # Tests.cpp:40-52
     assert property_test(0, 200)[0] <= 1e-4 * np.sqrt(3)
 
