@@ -41,7 +41,7 @@ extern "C" {
 #define HASTY_ERR_MEMORY (-4)     /* device allocation failed */
 #define HASTY_ERR_IO (-5)         /* output could not be written (CLI exit code 5) */
 #define HASTY_ERR_STOPPED (-6)    /* job was stopped before the requested passes ran */
-#define HASTY_ERR_MISSING (-7)    /* entry point unavailable in this build */
+#define HASTY_ERR_MISSING (-7)    /* entry point not compiled into the library */
 
 /* hasty_ctx_create flags */
 #define HASTY_CTX_BINARY_BVH 1u   /* binary BVH instead of the compressed 8-wide one */
