@@ -40,8 +40,8 @@ B_SHADE = 2 * 96 + 92
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, averaged
 # over the 12 bounces of one 8-pass batch of 16,588,800 paths, wide BVH) from
 # one ncu capture of `bench.py --steps 1 --warmup 3 --spp-per-step 8`, the
-# batches of the default run (profiles/dram_per_launch_sphere_field_1920x1080.md;
-# captures of 2- and 4-pass batches gave 1/4 and 1/2 of these bytes). The
+# batches of the default run (captures of 2- and 4-pass batches gave 1/4 and
+# 1/2 of these bytes). The
 # shading stage is one k_resolve and one k_sample launch per bounce.
 MEASURED_TRAFFIC = {"wide": {"k_trace": 461.4e6, "k_resolve+k_sample": 939.9e6 + 738.9e6}}
 MEASURED_TRAFFIC_PASSES = 8

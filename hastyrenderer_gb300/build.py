@@ -111,15 +111,18 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
 
 def build_oracle(with_reference: bool | None = None, verbose: bool = False) -> None:
     """CPU oracle: oracle/_build/liboracle.so, and the reference build under
-    oracle/_ref when the reference sources are present on this machine."""
+    oracle/_ref when HASTY_REFERENCE_DIR names a checkout of the reference
+    (its core/src and core/include directories are compiled from there)."""
     odir = os.path.join(ROOT, "oracle")
     targets = ["port"]
-    ref = os.environ.get("HASTY_REFERENCE_DIR", "/root/reference")
+    ref = os.environ.get("HASTY_REFERENCE_DIR", "")
     if with_reference is None:
-        with_reference = os.path.isdir(os.path.join(ref, "core", "src"))
+        with_reference = bool(ref) and os.path.isdir(os.path.join(ref, "core", "src"))
     if with_reference:
+        if not ref:
+            raise RuntimeError("the reference build needs HASTY_REFERENCE_DIR (a checkout of the reference)")
         targets.append("ref")
-    cmd = ["make", "-C", odir, f"-j{min(8, os.cpu_count() or 4)}", f"REF={ref}"] + targets
+    cmd = ["make", "-C", odir, f"-j{min(8, os.cpu_count() or 4)}"] + ([f"REF={ref}"] if ref else []) + targets
     r = subprocess.run(cmd, capture_output=not verbose, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed\n{r.stdout}\n{r.stderr}")

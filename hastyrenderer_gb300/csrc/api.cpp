@@ -41,8 +41,8 @@ namespace {
 
 }  // namespace
 
-void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st,
-                             unsigned long long* stats) {
+void hasty::carve_paths(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc,
+                        unsigned long long* stats) {
   auto A = [&](size_t bytes) { return alloc(bytes); };
   p.capacity = int32_t(cap);
   size_t c = size_t(cap);
@@ -67,13 +67,26 @@ void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::f
   p.out_color = static_cast<float4*>(A(c * sizeof(float4)));
   p.out_normal = static_cast<float4*>(A(c * sizeof(float4)));
   p.out_albedo = static_cast<float4*>(A(c * sizeof(float4)));
-  if (stats) {
-    p.stats = stats;
-  } else {
-    p.stats = static_cast<unsigned long long*>(A(size_t(n_stats) * sizeof(unsigned long long)));
-    ck(cudaMemsetAsync(p.stats, 0, sizeof(unsigned long long) * size_t(n_stats), st), "memset stats");
-  }
+  p.stats = stats ? stats : static_cast<unsigned long long*>(A(size_t(n_stats) * sizeof(unsigned long long)));
+}
+
+void hasty::alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st,
+                             unsigned long long* stats) {
+  carve_paths(p, cap, n_stats, alloc, stats);
+  if (!stats) ck(cudaMemsetAsync(p.stats, 0, sizeof(unsigned long long) * size_t(n_stats), st), "memset stats");
   ck(cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * kCountSlots, st), "memset counts");
+}
+
+int64_t hasty::carved_bytes(int64_t cap, int n_stats, size_t align, size_t extra_blocks, size_t extra_bytes) {
+  size_t used = 0;
+  auto count = [&](size_t bytes) -> void* {
+    used = ((used + align - 1) / align) * align + bytes;
+    return reinterpret_cast<void*>(uintptr_t(align));   // never dereferenced
+  };
+  PathsDev p{};
+  carve_paths(p, cap, n_stats, count, nullptr);
+  for (size_t k = 0; k < extra_blocks; ++k) count(extra_bytes);
+  return int64_t(used);
 }
 
 // Path-state buffers of the single-job path are allocated at the first

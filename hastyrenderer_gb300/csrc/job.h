@@ -197,11 +197,18 @@ struct hasty_job {
 
 
 namespace hasty {
-// Carves path-state buffers for `cap` slots out of `alloc` and clears the
-// queue counters; statistics are carved and cleared too unless `stats` is
-// given (api.cpp).
+// Carves path-state buffers for `cap` slots out of `alloc` (no device
+// work); statistics are carved too unless `stats` is given.
+void carve_paths(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc,
+                 unsigned long long* stats = nullptr);
+// carve_paths, then clears the queue counters, and the statistics when they
+// were carved (api.cpp).
 void alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st,
                       unsigned long long* stats = nullptr);
+// Bytes that carve_paths for `cap` slots followed by `extra_blocks` blocks of
+// `extra_bytes` takes from a carving allocator whose blocks start on
+// `align`-byte boundaries.
+int64_t carved_bytes(int64_t cap, int n_stats, size_t align, size_t extra_blocks, size_t extra_bytes);
 // Single-job path state for at least `need` paths (at most j.capacity),
 // allocated on first use and grown when a call needs more.
 void ensure_paths(hasty_job& j, int64_t need);

@@ -18,14 +18,20 @@
 //
 // Set-up. The first call on each device looks up the array's device address
 // (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture begins.
+// before any stream capture begins. The address is kept for the life of the
+// process: after cudaDeviceReset (or anything else that destroys and
+// recreates the device's primary context) this entry point must not be
+// called again in that process.
 //
 // Sharing. Every call uses the same array and the array keeps whatever the
 // last call left in it. Each call clears what must start at zero (queue
 // counters, statistics, the normal and albedo sums and the caller's output)
 // before its kernels run. Calls whose GPU work overlaps (jobs rendering
 // through this entry point on different streams, or from several host
-// threads, at the same time) race on the array and produce garbage.
+// threads, at the same time) race on the array and produce garbage. Note
+// that each job has its own stream and the call returns before its GPU work
+// ends, so two calls on two different jobs from one host thread already
+// overlap: call hasty_job_sync on the first job before calling on another.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -38,8 +44,16 @@ namespace hasty {
 namespace {
 
 constexpr size_t kStaticBytes = size_t(8) << 20;
-constexpr int kStaticMaxPixels = 16384;   // 436 B of path state + 48 B of sums per pixel
+constexpr int kStaticMaxPixels = 16384;   // path state + 48 B of sums per pixel
 constexpr int kMaxDevices = 64;
+constexpr size_t kCarveAlign = 256;
+
+// Bytes one call carves from g_scratch for a frame of npix pixels: the path
+// state of npix slots (the same carving as every other path pool) and the
+// normal and albedo sums, each block on a kCarveAlign boundary.
+int64_t static_bytes_needed(int64_t npix) {
+  return carved_bytes(npix, ST_COUNT, kCarveAlign, 2, sizeof(double) * 3 * size_t(npix));
+}
 
 static __device__ __align__(256) unsigned char g_scratch[kStaticBytes];
 
@@ -69,16 +83,17 @@ extern "C" int hasty_job_render_pass_static(hasty_job* job, int pass, double* d_
     if (!job) throw ApiError{HASTY_ERR_ARG, "null job handle"};
     if (!d_color) throw ApiError{HASTY_ERR_ARG, "null output buffer"};
     if (pass < 0) throw ApiError{HASTY_ERR_ARG, "negative pass index"};
-    const int npix = job->sd.width * job->sd.height;
-    if (npix > kStaticMaxPixels)
-      throw ApiError{HASTY_ERR_ARG, "frame of " + std::to_string(npix) +
-                                        " pixels exceeds the static scratch limit of " +
+    const int64_t npix64 = int64_t(job->sd.width) * int64_t(job->sd.height);
+    if (npix64 <= 0 || npix64 > kStaticMaxPixels)
+      throw ApiError{HASTY_ERR_ARG, "frame of " + std::to_string(npix64) +
+                                        " pixels is outside the static scratch limit of 1.." +
                                         std::to_string(kStaticMaxPixels) + " pixels"};
+    const int npix = int(npix64);
     ck(cudaSetDevice(job->ctx->device), "cudaSetDevice");
     unsigned char* base = scratch_address(job->ctx->device);
     size_t used = 0;
     auto carve = [&](size_t bytes) -> void* {
-      size_t off = (used + 255) & ~size_t(255);
+      size_t off = (used + kCarveAlign - 1) & ~(kCarveAlign - 1);
       if (off + bytes > kStaticBytes) throw ApiError{HASTY_ERR_ARG, "frame does not fit the static scratch"};
       used = off + bytes;
       return base + off;
@@ -106,6 +121,16 @@ extern "C" int hasty_job_render_pass_static(hasty_job* job, int pass, double* d_
     }
     launch_accumulate(job->sd, p, b, d_color, sum_normal, sum_albedo, job->stream);
     ck(cudaGetLastError(), "static render launch");
+    return HASTY_OK;
+  });
+}
+
+extern "C" int hasty_debug_static_scratch(int64_t* max_pixels, int64_t* bytes_needed, int64_t* capacity) {
+  return guarded([&] {
+    if (!max_pixels || !bytes_needed || !capacity) throw ApiError{HASTY_ERR_ARG, "null argument"};
+    *max_pixels = kStaticMaxPixels;
+    *bytes_needed = static_bytes_needed(kStaticMaxPixels);
+    *capacity = int64_t(kStaticBytes);
     return HASTY_OK;
   });
 }

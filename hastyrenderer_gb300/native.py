@@ -142,6 +142,7 @@ def lib() -> ctypes.CDLL:
         "hasty_pm_stats_get": [P, P],
         "hasty_debug_pm_map": [P, P, P, P, P, P, P, P],
         "hasty_job_render_pass_static": [P, I, P],
+        "hasty_debug_static_scratch": [P, P, P],
         "hasty_server_start": [P, P, P],
         "hasty_server_submit": [P, ctypes.c_char_p, ctypes.c_int32, P, P],
         "hasty_server_poll": [P, P, SZ, P, ctypes.c_int32],

@@ -310,10 +310,17 @@ int hasty_server_stop(hasty_server* srv);
  * makes no cudaMalloc/cudaFree and uses one fixed 8 MiB static device array
  * as scratch, so frames above 16384 pixels (e.g. 128 x 128) are rejected
  * with HASTY_ERR_ARG. The first call on each device looks up that array's
- * address; make it before any stream capture begins. All calls share the
- * array: calls whose GPU work overlaps (other streams, other threads) race.
+ * address; make it before any stream capture begins; that address stays
+ * cached for the process, so do not call this again after cudaDeviceReset.
+ * All calls share the array: calls whose GPU work overlaps (other streams,
+ * other threads) race. Each job renders on its own stream and the call is
+ * asynchronous, so calls on two different jobs overlap unless the first
+ * job is synced (hasty_job_sync) before the second call.
  * No counterpart in the reference (it renders through its own buffers). */
 int hasty_job_render_pass_static(hasty_job* job, int pass, double* d_color);
+/* Test hook (no device needed): the static scratch's pixel limit, the bytes a
+ * frame of that many pixels carves from it, and its size. */
+int hasty_debug_static_scratch(int64_t* max_pixels, int64_t* bytes_needed, int64_t* capacity);
 
 /* Closest hits of n rays given as n x 6 host floats (origin, direction):
  * global triangle index (-1 miss), t, u, v. */

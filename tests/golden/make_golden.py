@@ -3,6 +3,7 @@ integrator code, built under oracle/_ref by `make -C oracle ref` (needs the
 reference sources, so this runs on the development machine only; the
 fixtures are committed and travel with the tests).
 
+  HASTY_REFERENCE_DIR=<reference checkout> python -m hastyrenderer_gb300.build --oracle
   python tests/golden/make_golden.py
 
 Fixtures:

@@ -3,6 +3,7 @@ own photon mapper (core/src/PhotonMapping.cpp, driven by
 oracle/ref_pm_harness.cpp in the build under oracle/_ref; needs the reference
 sources, so this runs on the development machine only).
 
+  HASTY_REFERENCE_DIR=<reference checkout> python -m hastyrenderer_gb300.build --oracle
   python tests/golden/make_golden_pm.py
 
 Fixtures: pm_<name>.npz for the golden scenes cornell (area light, glossy

@@ -41,6 +41,18 @@ def test_errors_are_status_codes():
     assert lib.hasty_job_outputs_wait(None) == -1
 
 
+def test_static_scratch_holds_its_largest_frame():
+    """The no-allocation entry point's static array holds the path state and
+    sums of the largest frame it accepts, carved exactly as a call carves it
+    (the same sizes and 256-byte alignment as every path pool)."""
+    lib = native.lib()
+    mx, need, cap = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    assert lib.hasty_debug_static_scratch(ctypes.byref(mx), ctypes.byref(need), ctypes.byref(cap)) == 0
+    assert mx.value >= 128 * 128
+    assert 0 < need.value <= cap.value, (need.value, cap.value)
+    assert lib.hasty_debug_static_scratch(None, None, None) == -1
+
+
 def test_cli_argument_errors(tmp_path):
     exe = os.path.join(os.path.dirname(native.LIB_PATH), "hasty_gpu_render")
     r = subprocess.run([exe], capture_output=True, text=True)
