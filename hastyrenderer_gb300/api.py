@@ -258,16 +258,23 @@ def host_trace(job_path: str, rays: np.ndarray, kind: int = 1):
     return tri, t, u, v, {"triangles": int(info[0]), "nodes": int(info[1]), "depth": int(info[2])}
 
 
+BATCH_PACKED = 0   # HASTY_BATCH_PACKED
+BATCH_REGEN = 1    # HASTY_BATCH_REGEN
+
+
 def batch_render(jobs, passes, paths_in_flight: int = 0, regen_fraction: float = 0.0, max_iterations: int = 0,
-                 ctx: Context | None = None) -> dict:
-    """Renders passes[i] further passes of jobs[i] in one multi-job run (path
-    regeneration over a shared pool; one CUDA-graph launch); the results are
-    added to each job's accumulators. Returns the batch statistics."""
+                 mode: int = BATCH_PACKED, lanes: int = 0, ctx: Context | None = None) -> dict:
+    """Renders passes[i] further passes of jobs[i] in one multi-job run and
+    adds the results to each job's accumulators. mode BATCH_PACKED (default):
+    the jobs' passes packed into batches of paths_in_flight camera samples on
+    `lanes` alternating render lanes (results bit-identical to render_passes);
+    BATCH_REGEN: path regeneration over a shared pool in one CUDA-graph
+    launch. Returns the batch statistics."""
     ctx = ctx or jobs[0].ctx
     n = len(jobs)
     handles = (ctypes.c_void_p * n)(*[j._h.value for j in jobs])
     ps = (ctypes.c_int32 * n)(*[int(p) for p in passes])
-    cfg = native.BatchConfig(int(paths_in_flight), float(regen_fraction), int(max_iterations))
+    cfg = native.BatchConfig(int(paths_in_flight), float(regen_fraction), int(max_iterations), int(mode), int(lanes))
     st = native.BatchStats()
     check(native.lib().hasty_batch_render(ctx._h, handles, ps, n, ctypes.byref(cfg), ctypes.byref(st)))
     return {k: getattr(st, k) for k, _ in native.BatchStats._fields_}

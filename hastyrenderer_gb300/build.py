@@ -33,7 +33,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-s
 CU_SOURCES = ["integrator.cu", "trace.cu", "static_scratch.cu", "bvh_gpu.cu", "photon.cu", "photon_build.cu"]
 # Extra nvcc flags for experiments (e.g. HASTY_NVCC_FLAGS="-DHASTY_OUTLINE_MASK=3").
 EXTRA_NVCC = os.environ.get("HASTY_NVCC_FLAGS", "").split()
-CPP_SOURCES = ["api.cpp", "engine.cpp", "server.cpp", "scene_load.cpp", "bvh_build.cpp", "image_out.cpp", "photon_map.cpp"]
+CPP_SOURCES = ["api.cpp", "engine.cpp", "packed.cpp", "server.cpp", "scene_load.cpp", "bvh_build.cpp", "image_out.cpp", "photon_map.cpp"]
 
 
 def cuda_home() -> str:

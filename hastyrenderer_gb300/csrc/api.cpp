@@ -249,14 +249,18 @@ int64_t default_capacity(int64_t npix) {
 // with the 256/512-thread shading blocks: all 942, 7: 938, 6: 943, 5: 948,
 // 4: 940.
 constexpr int kLaneTraceBlocksPerSM = 5;
+}  // namespace
+
 // HASTY_LANE_TRACE_BLOCKS overrides it (0: no cap).
-int lane_trace_blocks() {
+int hasty::lane_trace_blocks() {
   static const int v = [] {
     const char* e = std::getenv("HASTY_LANE_TRACE_BLOCKS");
     return e ? std::max(0, std::atoi(e)) : kLaneTraceBlocksPerSM;
   }();
   return v;
 }
+
+namespace {
 
 // One batch of passes on render lane `lane` (the two lanes alternate; see
 // hasty_job): ray generation and the bounces on the lane's stream, then the

@@ -223,23 +223,13 @@ uint32_t engine_regen_threshold(float fraction, int64_t cap) {
 
 }  // namespace hasty
 
-using namespace hasty;
-
-extern "C" {
-
-int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, size_t n_jobs, const hasty_batch_config* cfg,
-                       hasty_batch_stats* out) {
+// Regeneration mode of hasty_batch_render (the arguments are checked and the
+// jobs' streams synchronised by the caller).
+int hasty::batch_render_regen(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, size_t n_jobs,
+                              const hasty_batch_config* cfg, hasty_batch_stats* out) {
   return guarded([&] {
-    if (!ctx || (n_jobs && (!jobs || !passes))) throw ApiError{HASTY_ERR_ARG, "null argument"};
     uint64_t n_segments = 0;
-    for (size_t i = 0; i < n_jobs; ++i) {
-      if (!jobs[i] || passes[i] < 0) throw ApiError{HASTY_ERR_ARG, "bad job or pass count"};
-      if (jobs[i]->ctx != ctx) throw ApiError{HASTY_ERR_ARG, "job belongs to another context"};
-      if (jobs[i]->sd.max_depth <= 0) throw ApiError{HASTY_ERR_ARG, "max_depth must be positive for batching"};
-      if (!jobs[i]->acc[0]) throw ApiError{HASTY_ERR_ARG, "job has no accumulators"};
-      n_segments += uint64_t(passes[i]);
-      ck(cudaStreamSynchronize(jobs[i]->stream), "job sync");
-    }
+    for (size_t i = 0; i < n_jobs; ++i) n_segments += uint64_t(passes[i]);
     if (n_segments >= (uint64_t(1) << 30)) throw ApiError{HASTY_ERR_ARG, "too many passes in one batch"};
     auto t0 = std::chrono::steady_clock::now();
     // Two engines on two streams, each with half the pool, take alternate
@@ -340,5 +330,3 @@ int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, 
     return HASTY_OK;
   });
 }
-
-}  // extern "C"

@@ -92,5 +92,8 @@ int64_t engine_pool_size(int64_t requested);
 // and sums that fall out of L2 cost more than contended atomics.
 uint32_t engine_lanes(int64_t cap, uint32_t npix);
 uint32_t engine_regen_threshold(float fraction, int64_t cap);
+// hasty_batch_render in HASTY_BATCH_REGEN mode (engine.cpp).
+int batch_render_regen(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, size_t n_jobs,
+                       const hasty_batch_config* cfg, hasty_batch_stats* out);
 
 }  // namespace hasty

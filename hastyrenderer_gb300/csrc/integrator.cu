@@ -98,31 +98,81 @@ struct Media {
   }
 };
 
-__global__ void __launch_bounds__(256) k_raygen(SceneDev sc, PathsDev P, BatchDesc b) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s == 0) {
-    uint32_t n = sc.max_depth > 0 ? uint32_t(b.n_paths) : 0u;
-    P.counts[0] = n; P.counts[1] = 0; P.counts[2] = n; P.counts[3] = 0;
-    atomicAdd(&P.stats[ST_PATHS], (unsigned long long)b.n_paths);
+// Where a kernel finds a path's job. OneJob: a batch of passes of one job
+// (scene and batch as kernel parameters). ChunkTable (packed batches): the
+// chunk named by the path's flags.
+struct OneJob {
+  SceneDev sc;
+  BatchDesc b;
+};
+__device__ __forceinline__ int n_paths_of(const OneJob& j) { return j.b.n_paths; }
+__device__ __forceinline__ int n_paths_of(const ChunkTable& t) { return t.n_paths; }
+__device__ __forceinline__ uint32_t flags_of(const OneJob&, const PathsDev&, int) { return 0u; }
+__device__ __forceinline__ uint32_t flags_of(const ChunkTable&, const PathsDev& P, int s) {
+  return __float_as_uint(P.rad[s].w);
+}
+__device__ __forceinline__ const SceneDev& scene_of(const OneJob& j, uint32_t) { return j.sc; }
+__device__ __forceinline__ const SceneDev& scene_of(const ChunkTable& t, uint32_t flags) {
+  return t.c[flags >> PF_CHUNK_SHIFT].sc;
+}
+// Pass and pixel of slot s in its batch.
+struct SlotPos { uint64_t seed; uint32_t px, pass; int chunk; };
+__device__ __forceinline__ SlotPos slot_pos(const OneJob& j, int s, uint32_t) {
+  const int npix = j.sc.width * j.sc.height;
+  const int k = s / npix;
+  return {j.b.seed, uint32_t(s - k * npix), j.b.pass_base + uint32_t(k), 0};
+}
+__device__ __forceinline__ SlotPos chunk_pos(const ChunkTable& t, int s, int c) {
+  const ChunkDev& ch = t.c[c];
+  const int local = s - ch.first_slot;
+  const int k = local / ch.npix;
+  return {ch.seed, uint32_t(local - k * ch.npix), ch.pass_base + uint32_t(k), c};
+}
+__device__ __forceinline__ SlotPos slot_pos(const ChunkTable& t, int s, uint32_t flags) {
+  return chunk_pos(t, s, int(flags >> PF_CHUNK_SHIFT));
+}
+// Chunk of slot s at ray generation (chunks are in slot order).
+__device__ __forceinline__ int chunk_of_slot(const ChunkTable& t, int s) {
+  int lo = 0, hi = t.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (t.c[mid].first_slot <= s) lo = mid; else hi = mid - 1;
   }
-  if (s >= b.n_paths) return;
-  int npix = sc.width * sc.height;
-  int k = s / npix, px = s - k * npix;
-  uint32_t pass = b.pass_base + uint32_t(k);
-  int x = px % sc.width, y = px / sc.width;
-  Rng r; r.seed(path_key(b.seed, uint32_t(px), pass));
+  return lo;
+}
+__device__ __forceinline__ SlotPos raygen_pos(const OneJob& j, int s) { return slot_pos(j, s, 0u); }
+__device__ __forceinline__ SlotPos raygen_pos(const ChunkTable& t, int s) { return chunk_pos(t, s, chunk_of_slot(t, s)); }
+__device__ __forceinline__ int max_depth_of(const OneJob& j) { return j.sc.max_depth; }
+__device__ __forceinline__ int max_depth_of(const ChunkTable&) { return 1; }   // batches of positive depths only
+
+template <class Src>
+__global__ void __launch_bounds__(256) k_raygen(const __grid_constant__ Src src, PathsDev P) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n_paths = n_paths_of(src);
+  if (s == 0) {
+    uint32_t n = max_depth_of(src) > 0 ? uint32_t(n_paths) : 0u;
+    P.counts[0] = n; P.counts[1] = 0; P.counts[2] = n; P.counts[3] = 0;
+    atomicAdd(&P.stats[ST_PATHS], (unsigned long long)n_paths);
+  }
+  if (s >= n_paths) return;
+  const SlotPos sp = raygen_pos(src, s);
+  const uint32_t chunk_bits = uint32_t(sp.chunk) << PF_CHUNK_SHIFT;
+  const SceneDev& sc = scene_of(src, chunk_bits);
+  const uint32_t px = sp.px, pass = sp.pass;
+  int x = int(px % uint32_t(sc.width)), y = int(px / uint32_t(sc.width));
+  Rng r; r.seed(path_key(sp.seed, px, pass));
   float ox = halton(2, pass), oy = halton(3, pass);
   V3 o, d; int capped = 0;
   camera_ray(sc.cam, r, float(x) + ox, float(y) + oy, float(sc.width), float(sc.height), o, d, capped);
   if (capped) atomicAdd(&P.stats[ST_TRIAL_CAP], 1ull);
   P.rng[s] = r.state;
   P.thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
-  P.rad[s] = make_float4(0.f, 0.f, 0.f, __uint_as_float(PF_CAMERA | PF_PEND_B));
+  P.rad[s] = make_float4(0.f, 0.f, 0.f, __uint_as_float(PF_CAMERA | PF_PEND_B | chunk_bits));
   P.out_color[s] = make_float4(0.f, 0.f, 0.f, 0.f);
   P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f);
   P.out_albedo[s] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (sc.max_depth <= 0) return;
-  P.ray_o[2 * s] = f4(o, 0.f);
+  P.ray_o[2 * s] = f4(o, __uint_as_float(uint32_t(sp.chunk)));
   P.ray_d[2 * s] = f4(d, 0.f);
   P.pq[0][s] = s;
   P.rq[0][s] = 2 * s;
@@ -259,7 +309,7 @@ __device__ __forceinline__ ResolveRes resolve_path(const SceneDev& sc, const Pat
             P.rng[s] = r.state;
             P.thr[s] = f4(thr, thr4.w);
             store_vertex(P, s, it, tl);
-            flags = (flags & (PF_WL_MASK | PF_NMED_MASK)) | uint32_t(depth);
+            flags = (flags & (PF_WL_MASK | PF_NMED_MASK | PF_CHUNK_MASK)) | uint32_t(depth);
             res.sample = true;
             res.cls = shade_class(m);
           }
@@ -290,6 +340,7 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
   const MaterialDev& m = sc.mats[it.mat];
   const V3 thr = xyz(P.thr[s]);
   const V3 d = xyz(P.ray_d[2 * s]);
+  const float ray_w = __uint_as_float(flags >> PF_CHUNK_SHIFT);   // chunk of a packed batch (0 otherwise)
   Media M(P, s, int((flags & PF_NMED_MASK) >> PF_NMED_SHIFT));
   Rng r; r.inc = Rng::inc_of(key); r.state = P.rng[s];
   V3 wo = -d;
@@ -324,7 +375,7 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
         overflow |= ovL;
         P.nee_c[s] = f4(cwise(thr, c3), pBL);
         P.nee_t[s] = f4(TL, __int_as_float(ltri));
-        P.ray_o[2 * s + 1] = f4(oL, 0.f);
+        P.ray_o[2 * s + 1] = f4(oL, ray_w);
         P.ray_d[2 * s + 1] = f4(dL, 0.f);
         emitL = true;
       }
@@ -345,14 +396,14 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
       overflow |= M.update(sc, m, it, wo, bs.dir, wl);
       P.thr[s] = f4(thr, bs.pdf);
       P.pend_b[s] = f4(t2, __int_as_float(it.tri));
-      P.ray_o[2 * s] = f4(ray_x(it, bs.outside), 0.f);
+      P.ray_o[2 * s] = f4(ray_x(it, bs.outside), ray_w);
       P.ray_d[2 * s] = f4(bs.dir, 0.f);
       emitB = true;
     }
   }
   P.rng[s] = r.state;
   uint32_t nf = uint32_t(depth) | (uint32_t(wl + 1) << PF_WL_SHIFT) | (uint32_t(M.n) << PF_NMED_SHIFT) |
-                (emitB ? PF_PEND_B : 0u) | (emitL ? PF_PEND_L : 0u);
+                (emitB ? PF_PEND_B : 0u) | (emitL ? PF_PEND_L : 0u) | (flags & PF_CHUNK_MASK);
   res.keep = emitB || emitL;
   if (res.keep) P.rad[s] = f4(L, __uint_as_float(nf));
   res.L = L;
@@ -365,9 +416,6 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
 // threads per SM (8 blocks of 128 measured ahead of 4, 6 and 12 at 128
 // threads); the block sizes are set at kResolveThreads and kSampleThreads.
 
-__device__ __forceinline__ uint64_t slot_key(const BatchDesc& b, int s, int npix) {
-  return path_key(b.seed, uint32_t(s % npix), b.pass_base + uint32_t(s / npix));
-}
 
 // Paths of queue q: resolve; finished ones leave their radiance in
 // out_color, survivors are appended to the sample queue.
@@ -379,7 +427,8 @@ __device__ __forceinline__ uint64_t slot_key(const BatchDesc& b, int s, int npix
 // 256: 903 (shading 8.32 -> 8.00 ms per step), 512: 888 (the larger blocks
 // interleave worse with the other render lane's tracing).
 constexpr int kResolveThreads = 256;
-__global__ void __launch_bounds__(kResolveThreads, 4) k_resolve(SceneDev sc, PathsDev P, BatchDesc b, int q) {
+template <class Src>
+__global__ void __launch_bounds__(kResolveThreads, 4) k_resolve(const __grid_constant__ Src src, PathsDev P, int q) {
   constexpr int kWarps = kResolveThreads / 32;
   __shared__ uint32_t s_cnt[kWarps][3];
   __shared__ uint32_t s_base;
@@ -387,14 +436,15 @@ __global__ void __launch_bounds__(kResolveThreads, 4) k_resolve(SceneDev sc, Pat
   if (blockIdx.x * blockDim.x >= n_in) return;    // whole block past the queue
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < n_in;
-  const int npix = sc.width * sc.height;
   const int s = valid ? P.pq[q][i] : 0;
   ResolveRes res;
   res.sample = false;
   res.shaded = 0;
   res.cls = 0;
   if (valid) {
-    res = resolve_path(sc, P, s, slot_key(b, s, npix));
+    const uint32_t fl = flags_of(src, P, s);
+    const SlotPos sp = slot_pos(src, s, fl);
+    res = resolve_path(scene_of(src, fl), P, s, path_key(sp.seed, sp.px, sp.pass));
     if (!res.sample) P.out_color[s] = f4(res.L, 0.f);
   }
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -429,7 +479,8 @@ __global__ void __launch_bounds__(kResolveThreads, 4) k_resolve(SceneDev sc, Pat
 // samples/s (shading ms per step): 128: 903 (8.00), 256: 942 (7.41),
 // 512: 946 (7.17), 1024: 904-929 (7.25).
 constexpr int kSampleThreads = 512;
-__global__ void __launch_bounds__(kSampleThreads, 2) k_sample(SceneDev sc, PathsDev P, BatchDesc b, int q) {
+template <class Src>
+__global__ void __launch_bounds__(kSampleThreads, 2) k_sample(const __grid_constant__ Src src, PathsDev P, int q) {
   const uint32_t n_in = P.counts[kSampleCount];
   uint32_t* pq_cnt = &P.counts[q ^ 1];
   uint32_t* rq_cnt = &P.counts[2 + (q ^ 1)];
@@ -438,13 +489,14 @@ __global__ void __launch_bounds__(kSampleThreads, 2) k_sample(SceneDev sc, Paths
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if ((i & ~31u) >= n_in) return;
   const bool valid = i < n_in;
-  const int npix = sc.width * sc.height;
   int s = valid ? P.sq[i] : 0;
   SampleRes res;
   res.keep = res.emitB = res.emitL = false;
   res.overflow = res.capped = 0;
   if (valid) {
-    res = sample_path(sc, P, s, slot_key(b, s, npix));
+    const uint32_t fl = flags_of(src, P, s);
+    const SlotPos sp = slot_pos(src, s, fl);
+    res = sample_path(scene_of(src, fl), P, s, path_key(sp.seed, sp.px, sp.pass));
     if (!res.keep) P.out_color[s] = f4(res.L, 0.f);
   }
   // warp-ballot compaction of the surviving paths and their rays
@@ -466,16 +518,21 @@ __global__ void __launch_bounds__(kSampleThreads, 2) k_sample(SceneDev sc, Paths
   }
 }
 
-// Adds one batch of per-sample values into the FP64 accumulators, passes in
-// order; a sample whose radiance has a NaN is dropped with its AOVs
+// Adds passes [0, n_passes) of the slots from `first` (pass k of pixel px in
+// slot first + k * npix + px) into the FP64 accumulators, one pass after the
+// other: acc = ((acc + v_0) + v_1) + ..., so the sums do not depend on how
+// the passes were grouped into batches (single job, packed batches, serving).
+// A sample whose radiance has a NaN is dropped with its AOVs
 // (core/src/PathTracing.cpp:132-142).
-__global__ void k_accumulate(PathsDev P, BatchDesc b, int npix, double* acc_c, double* acc_n, double* acc_a) {
+__global__ void k_accumulate(PathsDev P, int first, int n_passes, int npix, double* acc_c, double* acc_n,
+                             double* acc_a) {
   int px = blockIdx.x * blockDim.x + threadIdx.x;
   if (px >= npix) return;
-  double c[3] = {0, 0, 0}, n[3] = {0, 0, 0}, a[3] = {0, 0, 0};
+  double c[3], n[3], a[3];
+  for (int q = 0; q < 3; ++q) { c[q] = acc_c[3 * px + q]; n[q] = acc_n[3 * px + q]; a[q] = acc_a[3 * px + q]; }
   unsigned nan = 0;
-  for (int k = 0; k < b.n_passes; ++k) {
-    int s = k * npix + px;
+  for (int k = 0; k < n_passes; ++k) {
+    int64_t s = first + int64_t(k) * npix + px;
     float4 cc = P.out_color[s];
     if (cc.x != cc.x || cc.y != cc.y || cc.z != cc.z) { ++nan; continue; }
     float4 nn = P.out_normal[s], aa = P.out_albedo[s];
@@ -483,7 +540,7 @@ __global__ void k_accumulate(PathsDev P, BatchDesc b, int npix, double* acc_c, d
     n[0] += nn.x; n[1] += nn.y; n[2] += nn.z;
     a[0] += aa.x; a[1] += aa.y; a[2] += aa.z;
   }
-  for (int q = 0; q < 3; ++q) { acc_c[3 * px + q] += c[q]; acc_n[3 * px + q] += n[q]; acc_a[3 * px + q] += a[q]; }
+  for (int q = 0; q < 3; ++q) { acc_c[3 * px + q] = c[q]; acc_n[3 * px + q] = n[q]; acc_a[3 * px + q] = a[q]; }
   if (nan) atomicAdd(&P.stats[ST_NAN], (unsigned long long)nan);
 }
 
@@ -499,20 +556,34 @@ __global__ void k_estimate(const double* acc, int n, float den, float scale, flo
 
 void launch_raygen(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, cudaStream_t st) {
   int blocks = (b.n_paths + 255) / 256;
-  k_raygen<<<blocks > 0 ? blocks : 1, 256, 0, st>>>(sc, p, b);
+  k_raygen<OneJob><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(OneJob{sc, b}, p);
+}
+
+void launch_raygen_packed(const ChunkTable& t, const PathsDev& p, cudaStream_t st) {
+  int blocks = (t.n_paths + 255) / 256;
+  k_raygen<ChunkTable><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(t, p);
 }
 
 void launch_shade(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, int q, int max_paths, cudaStream_t st) {
-  int blocks = (max_paths + 127) / 128;
-  if (blocks < 1) blocks = 1;
   cudaMemsetAsync(&p.counts[kSampleCount], 0, sizeof(uint32_t), st);
-  k_resolve<<<(max_paths + kResolveThreads - 1) / kResolveThreads, kResolveThreads, 0, st>>>(sc, p, b, q);
-  k_sample<<<(max_paths + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(sc, p, b, q);
+  const OneJob src{sc, b};
+  k_resolve<OneJob><<<(max_paths + kResolveThreads - 1) / kResolveThreads, kResolveThreads, 0, st>>>(src, p, q);
+  k_sample<OneJob><<<(max_paths + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(src, p, q);
+}
+
+void launch_shade_packed(const ChunkTable& t, const PathsDev& p, int q, int max_paths, cudaStream_t st) {
+  cudaMemsetAsync(&p.counts[kSampleCount], 0, sizeof(uint32_t), st);
+  k_resolve<ChunkTable><<<(max_paths + kResolveThreads - 1) / kResolveThreads, kResolveThreads, 0, st>>>(t, p, q);
+  k_sample<ChunkTable><<<(max_paths + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(t, p, q);
 }
 
 void launch_accumulate(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, double* ac, double* an, double* aa, cudaStream_t st) {
-  int npix = sc.width * sc.height;
-  k_accumulate<<<(npix + 255) / 256, 256, 0, st>>>(p, b, npix, ac, an, aa);
+  launch_accumulate_range(p, 0, sc.width * sc.height, b.n_passes, ac, an, aa, st);
+}
+
+void launch_accumulate_range(const PathsDev& p, int first, int npix, int n_passes, double* ac, double* an, double* aa,
+                             cudaStream_t st) {
+  k_accumulate<<<(npix + 255) / 256, 256, 0, st>>>(p, first, n_passes, npix, ac, an, aa);
 }
 
 void launch_estimate(const double* acc, int n, float den, float scale, float* out, cudaStream_t st) {

@@ -222,4 +222,7 @@ std::unique_ptr<hasty_job> load_job(hasty_ctx* ctx, const std::string& path, boo
 std::unique_ptr<hasty_job> load_job_host(hasty_ctx* ctx, const std::string& path);
 int64_t prepare_job_upload(hasty_job& j);
 void finish_job_load(hasty_job& j, bool plain);
+// Resident blocks per SM of the persistent closest-hit kernel while another
+// render lane's batch runs beside it (api.cpp).
+int lane_trace_blocks();
 }  // namespace hasty

@@ -1,0 +1,89 @@
+// Packed multi-job batches (batching and serving). A batch is filled with
+// chunks of consecutive passes of several resident jobs, laid out one after
+// another in the slots of one render lane; the lane runs the same wavefront
+// kernels as the single-job path (ray generation, then per bounce closest
+// hit, resolve, sample), the kernels finding each path's job through the
+// chunk table passed as a kernel parameter. Lanes alternate on their own
+// streams, so one batch's tracing overlaps another's shading; every batch's
+// accumulation runs on one accumulation stream in batch order, and adds each
+// pass into the job's FP64 sums one pass after the other. A job's image is
+// therefore bit-identical to the single-job path's, whatever it is batched
+// with.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "job.h"
+
+namespace hasty {
+
+constexpr int kMaxLanes = 4;
+
+// A job as packed batches see it.
+struct PackedJob {
+  SceneDev sc;
+  uint64_t seed = 0;
+  double* acc[3] = {nullptr, nullptr, nullptr};   // FP64 sums: colour, normal, albedo (npix x 3 each)
+  int32_t npix = 0;
+};
+
+// n_passes consecutive passes of job `job` from pass_base.
+struct PackedChunk {
+  int job;
+  uint32_t pass_base;
+  int32_t n_passes;
+};
+
+struct PackedLanes {
+  hasty_ctx* ctx = nullptr;
+  int n_lanes = 0;
+  int64_t lane_paths = 0;                 // path slots of each lane
+  int bvh_kind = 1;
+  PathsDev pd[kMaxLanes] = {};
+  cudaStream_t lane_stream[kMaxLanes] = {};
+  cudaEvent_t lane_done[kMaxLanes] = {}, lane_free[kMaxLanes] = {};
+  bool lane_free_valid[kMaxLanes] = {};
+  cudaStream_t acc_stream = nullptr;      // accumulation, in batch order
+  cudaEvent_t acc_ready = nullptr;
+  unsigned long long* stats = nullptr;    // StatIndex counters of every lane
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+  int next_lane = 0;
+  uint64_t batches = 0, launches = 0;
+
+  PackedLanes() = default;
+  PackedLanes(const PackedLanes&) = delete;
+  PackedLanes& operator=(const PackedLanes&) = delete;
+  ~PackedLanes();
+
+  // lanes: 1..kMaxLanes; lane_paths: slots per lane (whole frames of every
+  // job must fit: the caller checks).
+  void init(hasty_ctx* c, int lanes, int64_t lane_paths);
+  // Makes every lane wait for work already enqueued on `s` (accumulators
+  // cleared there, for instance).
+  void wait_for(cudaStream_t s);
+  // Enqueues one batch on the next lane (asynchronous). `overlap`: other
+  // batches run at the same time (the closest-hit grid then leaves room for
+  // their shading). Chunks must fit one lane and number at most kMaxChunks.
+  void launch(const std::vector<PackedJob>& jobs, const std::vector<PackedChunk>& chunks, bool overlap);
+  void read_stats(unsigned long long* out);
+
+ private:
+  void* alloc(size_t b);
+};
+
+// Fills one batch: passes of the jobs in `order` (job indices), each job's
+// next passes in order (pass_base[j], left[j] updated), up to `slots` path
+// slots and kMaxChunks chunks. A job whose next pass does not fit the space
+// left is skipped for this batch. Returns the chunks (empty when nothing is
+// left).
+std::vector<PackedChunk> pack_batch(const std::vector<PackedJob>& jobs, const std::vector<int>& order,
+                                    std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots);
+
+// Path slots of a lane: 16M camera samples (whole frames of the largest
+// job at least), or `requested` when positive.
+int64_t packed_lane_paths(int64_t requested, int64_t largest_frame);
+
+}  // namespace hasty

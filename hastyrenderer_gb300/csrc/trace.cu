@@ -122,6 +122,37 @@ __global__ void k_trace_rays(SceneDev sc, const float* rays, int n, float4* hits
   hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
 }
 
+// Packed multi-job batches: each ray names its chunk in ray_o.w (bits), and
+// the chunk's BVH comes from the kernel-parameter table.
+template <int KIND>
+__global__ void TRACE_BOUNDS k_trace_packed(const __grid_constant__ TraceTable T, PathsDev P, int q) {
+  const uint32_t n = P.counts[2 + q];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
+  const int32_t* rq = P.rq[q];
+  if (!kPersistent<KIND>) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+      int rid = rq[i];
+      float4 o = P.ray_o[rid], d = P.ray_d[rid];
+      const TraceChunk& c = T.c[__float_as_uint(o.w)];
+      Hit h = trace_any<KIND>(c.nodes, c.tris, o.x, o.y, o.z, d.x, d.y, d.z);
+      P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+    }
+    return;
+  }
+  persistent_trace<KIND>(
+      n, &P.counts[kFetchCounter],
+      [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
+        rid = rq[k];
+        float4 o = P.ray_o[rid], d = P.ray_d[rid];
+        const TraceChunk& c = T.c[__float_as_uint(o.w)];
+        tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
+        tr.any = c.nee_first_hit != 0 && (rid & 1);   // as k_trace
+        nodes = c.nodes;
+        tris = c.tris;
+      },
+      [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
+}
+
 // Multi-job engine: each ray belongs to the job of its path slot (ray id / 2).
 // All jobs of one engine share the BVH layout of their context (KIND).
 template <int KIND>
@@ -195,6 +226,17 @@ void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int 
   cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
   if (k) k_trace_multi<1><<<blocks, 128, 0, st>>>(p, m);
   else k_trace_multi<0><<<blocks, 128, 0, st>>>(p, m);
+}
+
+void launch_trace_packed(const TraceTable& t, const PathsDev& p, int q, int max_rays, cudaStream_t st, int blocks_per_sm) {
+  static PersistentShape shape[2] = {{0, 0}, {0, 0}};
+  const int k = t.bvh_kind == 1 ? 1 : 0;
+  if (!shape[k].sms) shape[k] = k ? persistent_shape(k_trace_packed<1>) : persistent_shape(k_trace_packed<0>);
+  int blocks = k ? std::min(persistent_blocks(shape[k], blocks_per_sm), std::max(1, (max_rays + 127) / 128))
+                 : std::max(1, (max_rays + 127) / 128);
+  cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
+  if (k) k_trace_packed<1><<<blocks, 128, 0, st>>>(t, p, q);
+  else k_trace_packed<0><<<blocks, 128, 0, st>>>(t, p, q);
 }
 
 void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cudaStream_t st, int blocks_per_sm) {

@@ -22,6 +22,8 @@ enum : uint32_t {
   PF_PEND_B = 1u << 14,           // BSDF-sampled ray queued in ray slot 2s
   PF_PEND_L = 1u << 15,           // light-sampled ray queued in ray slot 2s+1
   PF_CAMERA = 1u << 16,           // pending ray is the camera ray
+  PF_CHUNK_SHIFT = 24,            // packed batches: chunk of the path's job (0 otherwise); also
+  PF_CHUNK_MASK = 0xFFu << 24,    // the bits of ray_o.w of the path's rays
 };
 constexpr int kMaxMedia = 4;
 
@@ -70,6 +72,50 @@ void launch_shade(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, int
 void launch_accumulate(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, double* acc_color, double* acc_normal,
                        double* acc_albedo, cudaStream_t stream);
 void launch_estimate(const double* acc, int n, float den, float scale, float* out, cudaStream_t stream);
+
+// Packed multi-job batches (batching and serving). A batch lays out chunks
+// of consecutive passes of several jobs one after another in slot space:
+// chunk c covers slots [first_slot, first_slot + n_passes * npix), slot
+// first_slot + k * npix + px being pass pass_base + k of pixel px of its
+// job. Every path carries its chunk index in its flags (PF_CHUNK_*) and its
+// rays in ray_o.w, so the kernels find the job's scene, seed and accumulators
+// without a per-slot table. The tables travel as kernel parameters.
+constexpr int kMaxChunks = 64;
+struct ChunkDev {
+  SceneDev sc;
+  uint64_t seed;
+  int32_t first_slot;
+  uint32_t pass_base;
+  int32_t npix;
+  int32_t n_passes;
+};
+struct ChunkTable {
+  int32_t n;            // chunks
+  int32_t n_paths;      // slots of all chunks
+  ChunkDev c[kMaxChunks];
+};
+// The closest-hit kernel's part of a chunk.
+struct TraceChunk {
+  const float4* nodes;
+  const float4* tris;
+  int32_t nee_first_hit;   // light rays stop at their first hit (environment-only lighting)
+  int32_t pad;
+};
+struct TraceTable {
+  int32_t n;
+  int32_t bvh_kind;     // of every chunk (a context's jobs share one BVH layout)
+  TraceChunk c[kMaxChunks];
+};
+static_assert(sizeof(ChunkTable) < 32000, "kernel parameters are limited to 32764 bytes");
+
+void launch_raygen_packed(const ChunkTable& t, const PathsDev& p, cudaStream_t stream);
+void launch_trace_packed(const TraceTable& t, const PathsDev& p, int q, int max_rays, cudaStream_t stream,
+                         int blocks_per_sm = 0);
+void launch_shade_packed(const ChunkTable& t, const PathsDev& p, int q, int max_paths, cudaStream_t stream);
+// Adds slots [first_slot, first_slot + n_passes * npix) (passes in order) into
+// FP64 accumulators of npix pixels.
+void launch_accumulate_range(const PathsDev& p, int first_slot, int npix, int n_passes, double* acc_color,
+                             double* acc_normal, double* acc_albedo, cudaStream_t stream);
 
 // Closest-hit queries of arbitrary rays (n x 6 floats, device memory).
 void launch_trace_rays(const SceneDev& sc, const float* rays, int n, float4* hits, cudaStream_t stream);

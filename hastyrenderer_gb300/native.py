@@ -45,14 +45,14 @@ class Stats(ctypes.Structure):
 
 class BatchConfig(ctypes.Structure):
     _fields_ = [("paths_in_flight", ctypes.c_int64), ("regen_fraction", ctypes.c_float),
-                ("max_iterations", ctypes.c_int32)]
+                ("max_iterations", ctypes.c_int32), ("mode", ctypes.c_int32), ("lanes", ctypes.c_int32)]
 
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("device_ms", ctypes.c_double), ("wall_ms", ctypes.c_double), ("samples", ctypes.c_uint64),
                 ("rays", ctypes.c_uint64), ("shaded", ctypes.c_uint64), ("nan_samples", ctypes.c_uint64),
                 ("saturated", ctypes.c_uint64), ("iterations", ctypes.c_uint64), ("paths_in_flight", ctypes.c_int64),
-                ("engine_bytes", ctypes.c_int64)]
+                ("engine_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_uint64)]
 
 
 class PmStats(ctypes.Structure):

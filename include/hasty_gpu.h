@@ -193,20 +193,35 @@ int hasty_pm_stats_get(hasty_job* job, hasty_pm_stats* stats);
 int hasty_debug_pm_map(hasty_job* job, float* xyz, uint32_t* emission, uint32_t* index, int32_t* cells,
                        int64_t* n_photons, int64_t* n_cells, float* cell);
 
-/* ---- Batching: many jobs in one persistent multi-job wavefront ------------
- * Path slots are shared by all jobs and refilled with new camera samples as
- * paths finish (regeneration); one CUDA graph launch whose conditional
- * while-node repeats regenerate/trace/shade on the device runs the whole batch.
- * Two such engines, each with half the pool and its own stream, take
- * alternate passes of every job so that one's tracing overlaps the other's
- * shading. Each job's samples are accumulated in int64 fixed point (2^-32),
- * which is order-independent: a job's result is bit-identical alone or in
- * any mix, on one engine or two.
+/* ---- Batching: many jobs in one multi-job wavefront ----------------------
+ * Two modes.
+ * HASTY_BATCH_PACKED (default): the jobs' passes are packed, in job order,
+ * into batches of up to paths_in_flight camera samples (chunks of
+ * consecutive passes of several jobs side by side); each batch runs the
+ * single-job path's wavefront kernels with the chunk table as a kernel
+ * parameter, on one of `lanes` render lanes (streams) that alternate, so one
+ * batch's tracing overlaps another's shading. Accumulation adds each pass to
+ * the job's FP64 sums in pass order, so a job's result is bit-identical to
+ * hasty_job_render_passes of the same passes, alone or in any mix.
+ * HASTY_BATCH_REGEN: path slots are shared by all jobs and refilled with new
+ * camera samples as paths finish (regeneration); one CUDA graph launch whose
+ * conditional while-node repeats regenerate/trace/shade on the device runs
+ * the whole batch. Two such engines, each with half the pool and its own
+ * stream, take alternate passes of every job so that one's tracing overlaps
+ * the other's shading. Each job's samples are accumulated in int64 fixed
+ * point (2^-32), which is order-independent: a job's result is bit-identical
+ * alone or in any mix, on one engine or two, and equal to the FP64 sums to
+ * 2^-32 per sample.
  * No counterpart in the reference (its jobs run one at a time). */
+#define HASTY_BATCH_PACKED 0
+#define HASTY_BATCH_REGEN 1
+
 typedef struct hasty_batch_config {
-  int64_t paths_in_flight;     /* path-slot pool (both engines together); 0 = 4M */
-  float regen_fraction;        /* refill when live paths < fraction * pool; 0 = 0.9, >= 1 every iteration */
-  int32_t max_iterations;      /* device-side loop bound; 0 = 50M */
+  int64_t paths_in_flight;     /* packed: path slots per lane, 0 = 16M; regen: the shared pool, 0 = 4M */
+  float regen_fraction;        /* regen: refill when live paths < fraction * pool; 0 = 0.9, >= 1 every iteration */
+  int32_t max_iterations;      /* regen: device-side loop bound; 0 = 50M */
+  int32_t mode;                /* HASTY_BATCH_PACKED or HASTY_BATCH_REGEN */
+  int32_t lanes;               /* packed: render lanes (batches in flight), 1..4; 0 = 2 */
 } hasty_batch_config;
 
 typedef struct hasty_batch_stats {
@@ -216,10 +231,11 @@ typedef struct hasty_batch_stats {
   uint64_t rays;
   uint64_t shaded;
   uint64_t nan_samples;
-  uint64_t saturated;          /* samples clamped to +/-2^30 in fixed point */
-  uint64_t iterations;         /* engine iterations (one bounce of every live path each; the longer engine) */
-  int64_t paths_in_flight;     /* both engines together */
-  int64_t engine_bytes;        /* device memory of the engine (path pool, fixed-point sums) */
+  uint64_t saturated;          /* regen: samples clamped to +/-2^30 in fixed point */
+  uint64_t iterations;         /* regen: engine iterations (the longer engine); packed: batches */
+  int64_t paths_in_flight;     /* path slots of all lanes / both engines together */
+  int64_t engine_bytes;        /* device memory of the lanes or engines (path state, fixed-point sums) */
+  uint64_t kernel_launches;    /* packed: kernels launched */
 } hasty_batch_stats;
 
 /* Renders passes[i] further passes of jobs[i] (all from ctx) in one run and

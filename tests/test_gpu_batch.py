@@ -1,5 +1,11 @@
-"""Multi-job engine (batching): results independent of the mix, equal to the
-single-job path, robust to heavy slot regeneration."""
+"""Batching (hasty_batch_render), both modes.
+
+Packed batches run the single-job path's kernels over chunks of several jobs
+and add each pass to the job's FP64 sums in pass order, so a job's sums are
+bit-identical to hasty_job_render_passes of the same passes, alone or in any
+mix, for any batch size and lane count. The regeneration engine sums in
+int64 fixed point: bit-identical alone or mixed, equal to the FP64 path to
+fixed-point resolution."""
 import os
 
 import numpy as np
@@ -20,32 +26,54 @@ def _sums(job):
     return [job.read_sums(a)[0] for a in (0, 1, 2)]
 
 
-def test_alone_equals_mixed():
+@pytest.mark.parametrize("mode", [0, 1], ids=["packed", "regen"])
+def test_alone_equals_mixed(mode):
     """Each job's image is bit-identical rendered alone or batched with others."""
     from hastyrenderer_gb300.api import batch_render
     passes = [3, 5, 2, 4]
     mixed = [_job(n) for n in NAMES]
-    st = batch_render(mixed, passes)
+    st = batch_render(mixed, passes, mode=mode)
     assert st["samples"] == sum(p * j.width * j.height for p, j in zip(passes, mixed))
     for name, p, jm in zip(NAMES, passes, mixed):
         alone = _job(name)
-        batch_render([alone], [p])
+        batch_render([alone], [p], mode=mode)
         for a, b in zip(_sums(jm), _sums(alone)):
             assert np.array_equal(a, b), name
         assert jm.read_sums()[1] == p
 
 
-def test_batch_matches_single_job_path():
-    """Same streams as hasty_job_render_passes: sums agree to fixed-point
-    resolution (2^-32 per sample), AOVs too."""
+@pytest.mark.parametrize("lanes,paths", [(2, 0), (1, 3000), (2, 2500), (3, 4000), (4, 1100)])
+def test_packed_equals_single_job_path(lanes, paths):
+    """Packed batches (small lanes force many batches, chunks split across
+    batches and several jobs per batch) give exactly the single-job path's
+    sums, a second call continuing the pass sequence."""
+    from hastyrenderer_gb300.api import batch_render
+    passes = [5, 7, 3, 6]
+    packed = [_job(n) for n in NAMES]
+    st = batch_render(packed, passes, paths_in_flight=paths, lanes=lanes)
+    st2 = batch_render(packed, [2, 1, 3, 2], paths_in_flight=paths, lanes=lanes)
+    assert st["samples"] == sum(p * j.width * j.height for p, j in zip(passes, packed))
+    if paths:
+        assert st["iterations"] >= st["samples"] // paths     # batches
+    for name, p, p2, jb in zip(NAMES, passes, [2, 1, 3, 2], packed):
+        plain = _job(name)
+        plain.render_passes(p, sync=True)
+        plain.render_passes(p2, sync=True)
+        assert jb.read_sums()[1] == p + p2
+        for a, b in zip(_sums(jb), _sums(plain)):
+            assert np.array_equal(a, b), (name, lanes, paths)
+
+
+def test_regen_matches_single_job_path():
+    """Regeneration engine against hasty_job_render_passes: the same streams;
+    sums agree to fixed-point resolution (2^-32 per sample), AOVs too."""
     from hastyrenderer_gb300.api import batch_render
     for name in NAMES:
         jb, jp = _job(name), _job(name)
-        batch_render([jb], [4])
+        batch_render([jb], [4], mode=1)
         jp.render_passes(4, sync=True)
         for a, b in zip(_sums(jb), _sums(jp)):
-            close = np.isclose(a, b, rtol=1e-6, atol=1e-8)
-            assert close.mean() >= 0.999, (name, close.mean())
+            np.testing.assert_allclose(a, b, rtol=1e-6, atol=4 * 2.0 ** -32 * 4)
 
 
 def test_small_pool_regeneration():
@@ -53,14 +81,33 @@ def test_small_pool_regeneration():
     result is still bit-identical to the default pool."""
     from hastyrenderer_gb300.api import batch_render
     a, b = _job("field"), _job("field")
-    st_a = batch_render([a], [8])
-    st = batch_render([b], [8], paths_in_flight=700, regen_fraction=1.0)
+    st_a = batch_render([a], [8], mode=1)
+    st = batch_render([b], [8], paths_in_flight=700, regen_fraction=1.0, mode=1)
     # 4608 samples through 700 slots: several refills, so more iterations
     # than one wave of max_depth bounces needs
     assert st["samples"] == st_a["samples"] == 8 * 24 * 24
     assert st["iterations"] > st_a["iterations"]
     assert st["iterations"] > 12
     for x, y in zip(_sums(a), _sums(b)):
+        assert np.array_equal(x, y)
+
+
+def test_regen_iteration_bound_then_recovers():
+    """The engine's device-side loop guard: a batch that needs more
+    iterations than max_iterations stops with HASTY_ERR_CUDA ("iteration
+    bound") instead of running on, and the context stays usable: the next
+    batch on it renders normally."""
+    from hastyrenderer_gb300 import HastyError
+    from hastyrenderer_gb300.api import batch_render
+    j = _job("cornell")
+    with pytest.raises(HastyError) as e:
+        batch_render([j], [4], max_iterations=3, mode=1)
+    assert e.value.code == -3 and "iteration bound" in str(e.value)
+    ok, ref = _job("cornell"), _job("cornell")
+    st = batch_render([ok], [4], mode=1)
+    assert st["samples"] == 4 * 32 * 32
+    batch_render([ref], [4], mode=1)
+    for x, y in zip(_sums(ok), _sums(ref)):
         assert np.array_equal(x, y)
 
 

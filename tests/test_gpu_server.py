@@ -24,7 +24,7 @@ def _batch_sums(name, passes, seed):
     from hastyrenderer_gb300 import RenderJob, batch_render
     j = RenderJob(_path(name))
     j.set_seed(seed)
-    batch_render([j], [passes])
+    batch_render([j], [passes], mode=1)
     return [j.read_sums(a)[0] for a in (0, 1, 2)], j
 
 
