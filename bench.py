@@ -1,22 +1,36 @@
-"""Benchmark of the plain single-job path tracer on the large seeded workload.
+"""Benchmarks of the GB300 path tracer. One JSON line per run (rank 0).
 
-Workload: 800 subdivision-3 icospheres + ground (1,024,002 triangles), FP32
-2048x1024 procedural sky (importance sampled), 1920x1080, thin lens with 6
-aperture blades, max depth 12; one step = SPP_PER_STEP passes (camera samples
-per pixel) over the full frame, rendered as one batch of 16.6M paths. Inputs
-stay resident on the device; the working set (path state ~7 GB per render
-lane, BVH + triangles ~0.3 GB) is far larger than L2, so no explicit flush is
-done between steps.
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Workloads (seeded synthetic scenes; no external dataset is involved):
 
-Prints one JSON line (rank 0). `value` is camera samples per second over all
-ranks (each rank renders its own pass range of the same job: weak scaling);
-`e2e` is the same metric through the C ABI including the job load (host
-parse, BVH build, host->device upload) and a device->host read of the colour
-estimate of every step (hasty_job_snapshot: copied while the next step
-renders, as a progressive viewer reads it). `cpu_baseline` times the CPU oracle (oracle/)
-on this host's cores on a bounded crop of the same job.
+* batch (default): 64 render jobs of the mixed distribution (procedural
+  Cornell box or sphere field of 50/200/800 subdivision-3 icospheres with the
+  2048x1024 FP32 sky; 128x128 .. 1024x768; 16..1024 spp log-uniform; depth
+  8..16). One step renders every job's full pass count in one
+  hasty_batch_render call (packed batches, parameters from the autotuner).
+  `value` is camera samples per second of the batched steps (device time);
+  `plain` is the same jobs one after another through
+  hasty_job_render_passes (device and wall time), `batched_over_plain` the
+  ratios. Every job's image is checked bit-identical between the two.
+* plain: one large job, 800 icospheres + ground (1,024,002 triangles),
+  1920x1080, thin lens with 6 aperture blades, sky, depth 12; one step = 8
+  passes.
+* cornell: the procedural Cornell box (34 triangles), 256x256, pinhole, 64
+  spp, depth 8, roulette from depth 3; one step = the full 64-pass render.
+* serve: Poisson arrivals (20 jobs/s for 120 s) of the mixed distribution
+  through hasty_server_*; p50/p95/p99 latency beside throughput.
+* stress: 10.36M triangles, 3840x2160, depth 32, one pass per step.
+* photon: the photon mapper on a 640x480 textured room.
+
+Inputs stay resident on the device in the timed region; the working sets
+(path state of ~7 GB per render lane) are far larger than L2, so no flush is
+needed (photon: flushed, its scene fits in L2). `e2e` is the same metric
+through the C ABI with host data: scene files loaded (parse, BVH build,
+host->device upload) and every image read back to the host inside the timed
+region. `cpu_baseline` times the CPU oracle (oracle/, the reference
+integrator restated) on this host's cores on a bounded sample of the same
+workload; `--impl reference` times the same sample as its own line.
 """
 from __future__ import annotations
 
@@ -33,18 +47,29 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SPP_PER_STEP = 8
-WORKLOAD = "sphere_field_800x_icosphere3_1024002tri_1920x1080_dof6_sky2048x1024_depth12"
+WORKLOAD_PLAIN = "sphere_field_800x_icosphere3_1024002tri_1920x1080_dof6_sky2048x1024_depth12"
+WORKLOAD_CORNELL = "cornell_box_34tri_256x256_64spp_depth8_rr3"
+WORKLOAD_BATCH = "mixed_64_jobs_cornell_or_field50_200_800_128x128_to_1024x768_spp16_1024_depth8_16"
 # Algorithmic bytes per shaded vertex: path state read + write (2 x 96 B) and
 # the triangle's attributes (92 B); texel reads are not counted.
 B_SHADE = 2 * 96 + 92
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum, averaged
-# over the 12 bounces of one 8-pass batch of 16,588,800 paths, wide BVH) from
-# one ncu capture of `bench.py --steps 1 --warmup 3 --spp-per-step 8`, the
-# batches of the default run (captures of 2- and 4-pass batches gave 1/4 and
-# 1/2 of these bytes). The
-# shading stage is one k_resolve and one k_sample launch per bounce.
-MEASURED_TRAFFIC = {"wide": {"k_trace": 461.4e6, "k_resolve+k_sample": 939.9e6 + 738.9e6}}
-MEASURED_TRAFFIC_PASSES = 8
+# Per-unit hardware counters of the wavefront kernels from ncu captures of
+# the 800-icosphere field (1080p, 8-pass batches of 16.6M paths, averaged over
+# the 12 bounces): DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum)
+# per traced ray (461.4 MB per closest-hit launch over 3.57M rays) and per
+# shaded vertex (1678.8 MB per resolve + sample launch pair over 1.407M
+# vertices), and for the closest-hit kernel warp instructions and thread
+# instructions per ray (smsp__inst_executed.sum,
+# smsp__thread_inst_executed.sum; None until captured). They give each
+# kernel's traffic, and the closest-hit kernel's issue rate, for the units a
+# launch processed.
+COUNTERS = {
+    "k_trace": {"dram_bytes_per_ray": 461.4e6 / 3.57e6, "warp_inst_per_ray": None, "thread_inst_per_ray": None},
+    "k_resolve+k_sample": {"dram_bytes_per_vertex": 1678.8e6 / 1.407e6},
+}
+REF_PASSES_PER_STEP = 8      # reference arm: passes of the CPU sample per step
+ISSUE_PER_SM_PER_CLOCK = 4   # warp instructions per SM and clock (one per scheduler)
+SMS = 152
 
 
 def peaks():
@@ -105,7 +130,7 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def make_job(base: str, seed: int = 0) -> str:
+def make_plain_job(base: str, seed: int = 0) -> str:
     from hastyrenderer_gb300 import scenes
     path = os.path.join(base, "renderJob.json")
     if not os.path.exists(path):
@@ -113,34 +138,18 @@ def make_job(base: str, seed: int = 0) -> str:
     return path
 
 
-def cpu_baseline(job_path: str, budget_s: float = 12.0, threads: int = 0):
-    """CPU oracle on this host's cores: rows of a centred 128-pixel-wide crop,
-    one pass each, until the time budget is spent. Also returns the BVH node
-    visits and triangle tests per ray of the oracle's binary BVH."""
-    from oracle.oracle import Oracle
-    ora = Oracle(job_path)
-    info = ora.info()
-    threads = threads or (os.cpu_count() or 1)
-    W, H = info["width"], info["height"]
-    cw = 128
-    x0 = (W - cw) // 2
-    y = H // 2 - 32
-    samples = 0
-    rays = nodes = tris = shaded = 0
-    t0 = time.perf_counter()
-    k = 0
-    while time.perf_counter() - t0 < budget_s:
-        r = ora.render(k // 8, 1, x0, y + 8 * (k % 8), cw, 8, threads)
-        st = r["stats"]
-        samples += cw * 8
-        rays += int(st[0]); nodes += int(st[2]); tris += int(st[3]); shaded += int(st[4])
-        k += 1
-    dt = time.perf_counter() - t0
-    ora.close()
-    return {"value": samples / dt, "unit": "samples/s", "cores": threads, "kind": "port",
-            "sample": f"{samples} camera samples of a centred {cw}x64 crop (passes 0..{k // 8}), {dt:.1f} s",
-            "mrays_per_s": rays / dt * 1e-6}, {"nodes_per_ray": nodes / max(rays, 1), "tris_per_ray": tris / max(rays, 1),
-                                               "shaded_per_sample": shaded / max(samples, 1), "rays_per_sample": rays / max(samples, 1)}
+def make_cornell_job(base: str, seed: int = 0) -> str:
+    from hastyrenderer_gb300 import scenes
+    path = os.path.join(base, "renderJob.json")
+    if not os.path.exists(path):
+        scenes.cornell_box(base, seed=seed, width=256, height=256, spp=64, max_depth=8, roulette_start_depth=3)
+    return path
+
+
+def mix_jobs():
+    from hastyrenderer_gb300 import workloads
+    base = os.environ.get("HASTY_BENCH_MIX", os.path.join(tempfile.gettempdir(), "hasty_bench_mix"))
+    return workloads.mixed_jobs(base, n_jobs=64, seed=0)
 
 
 def replica_seed(rank: int) -> int:
@@ -160,90 +169,316 @@ def max_over_ranks(value: float, dist, device: str) -> float:
     return float(t.item())
 
 
-def run_reference_arm(args, job_path: str, rank: int):
+# ---------------------------------------------------------------------------
+# CPU oracle on the host cores: bounded, representative samples of each
+# workload (shared by cpu_baseline and the reference arm, so both time the
+# same pixels).
+
+def strided_rows(h: int, stride: int, phase: int = 0) -> list[int]:
+    return list(range(phase % stride, h, stride))
+
+
+class CpuSampler:
+    """Times the CPU oracle on strided full-width rows (every `stride`-th row,
+    denser where a frame has fewer than 4 rows per host thread) of one or more jobs,
+    pass after pass, and estimates the workload's CPU samples/s.
+
+    jobs: list of (job_path, weight) where weight is the job's share of the
+    workload in camera samples; rows of every job are rendered for passes
+    0, 1, 2, ... (one round = one pass of every job's row set) until the time
+    budget is spent. The estimate is sum(weights) / sum(weight_j * t_j) with
+    t_j the measured seconds per camera sample of job j."""
+
+    def __init__(self, jobs, stride: int = 16, threads: int = 0):
+        from oracle.oracle import Oracle
+        self.threads = threads or (os.cpu_count() or 1)
+        self.stride = stride
+        self.items = []
+        for path, weight in jobs:
+            o = Oracle(path)
+            info = o.info()
+            # at least 4 rows per host thread, so every call keeps all threads busy
+            st = max(1, min(stride, info["height"] // (4 * self.threads)))
+            self.items.append({"oracle": o, "weight": weight, "w": info["width"], "h": info["height"],
+                               "stride": st, "rows": strided_rows(info["height"], st), "time": 0.0, "samples": 0,
+                               "rays": 0, "nodes": 0, "tris": 0, "shaded": 0})
+        self.rounds = 0
+
+    def run_round(self):
+        for it in self.items:
+            o = it["oracle"]
+            t0 = time.perf_counter()
+            r = o.render_rows(self.rounds, 1, it["rows"][0], it["stride"], len(it["rows"]), self.threads)
+            st = r["stats"]
+            it["rays"] += int(st[0]); it["nodes"] += int(st[2]); it["tris"] += int(st[3]); it["shaded"] += int(st[4])
+            it["time"] += time.perf_counter() - t0
+            it["samples"] += it["w"] * len(it["rows"])
+        self.rounds += 1
+
+    def run(self, budget_s: float, min_rounds: int = 1):
+        t0 = time.perf_counter()
+        while self.rounds < min_rounds or time.perf_counter() - t0 < budget_s:
+            self.run_round()
+        return time.perf_counter() - t0
+
+    def estimate(self) -> float:
+        wsum = sum(it["weight"] for it in self.items)
+        tsum = sum(it["weight"] * it["time"] / max(it["samples"], 1) for it in self.items)
+        return wsum / tsum
+
+    def totals(self):
+        s = sum(it["samples"] for it in self.items)
+        t = sum(it["time"] for it in self.items)
+        keys = ("rays", "nodes", "tris", "shaded")
+        agg = {k: sum(it[k] for it in self.items) for k in keys}
+        return s, t, agg
+
+    def close(self):
+        for it in self.items:
+            it["oracle"].close()
+
+
+def cpu_jobs(workload: str):
+    """(job_path, weight) pairs of the CPU sample of a workload, with the
+    sample's description. For the mixed batch: two jobs of each scene class
+    (Cornell box; fields of 50, 200 and 800 icospheres), the first two of the
+    mix in job order, each class weighted by its share of the mix's camera
+    samples (split evenly over its two jobs)."""
+    if workload == "plain":
+        return [(make_plain_job(_bench_dir("hasty_bench_c1")), 1.0)], "whole 1920x1080 frame, every 16th row", 16
+    if workload == "cornell":
+        return [(make_cornell_job(_bench_dir("hasty_bench_c0")), 1.0)], "every row of the 256x256 frame", 1
+    jobs = mix_jobs()
+    from hastyrenderer_gb300 import workloads
+    classes = {}
+    for j in jobs:
+        classes.setdefault((j["kind"], j["spheres"]), []).append(j)
+    out = []
+    desc = []
+    for key, members in sorted(classes.items()):
+        share = sum(workloads.job_samples(j) for j in members)
+        picked = members[:2]
+        for j in picked:
+            out.append((j["path"], share / len(picked)))
+        desc.append(f"{key[0]}{key[1] or ''}: jobs {[jobs.index(j) for j in picked]}")
+    return out, "every 8th row of " + "; ".join(desc) + ", weighted by class share of the mix's samples", 8
+
+
+def _bench_dir(name: str) -> str:
+    d = os.environ.get("HASTY_BENCH_DIR_" + name.upper(), os.path.join(tempfile.gettempdir(), name))
+    os.makedirs(d, exist_ok=True)
+    return d
+
+
+def cpu_baseline(workload: str, budget_s: float):
+    jobs, desc, stride = cpu_jobs(workload)
+    smp = CpuSampler(jobs, stride=stride)
+    dt = smp.run(budget_s)
+    v = smp.estimate()
+    s, t, agg = smp.totals()
+    smp.close()
+    line = {"value": v, "unit": "samples/s", "cores": smp.threads, "kind": "port",
+            "sample": f"{desc}; {smp.rounds} passes, {s} camera samples, {dt:.1f} s"}
+    costs = {"nodes_per_ray": agg["nodes"] / max(agg["rays"], 1), "tris_per_ray": agg["tris"] / max(agg["rays"], 1),
+             "rays_per_sample": agg["rays"] / max(s, 1), "shaded_per_sample": agg["shaded"] / max(s, 1)}
+    return line, costs
+
+
+def run_reference_arm(args, rank: int):
+    """The reference integrator's CPU path (the oracle, its restatement) on
+    this host's cores: the same strided sample as cpu_baseline, one pass of
+    every sampled row per step, all host threads. Rank 0 only."""
     if rank != 0:
         return
-    from oracle.oracle import Oracle
-    threads = os.cpu_count() or 1
-    ora = Oracle(job_path)
-    info = ora.info()
-    cw, ch = 96, 16
-    x0, y0 = (info["width"] - cw) // 2, info["height"] // 2 - ch
+    workload = args.workload if args.workload in ("plain", "cornell") else "batch"
+    jobs, desc, stride = cpu_jobs(workload)
+    smp = CpuSampler(jobs, stride=stride)
     for _ in range(args.warmup):
-        ora.render(0, 1, x0, y0, cw, ch, threads)
+        smp.run_round()
+    for it in smp.items:
+        it.update(time=0.0, samples=0)
     t0 = time.perf_counter()
-    for k in range(args.steps):
-        ora.render(k, 1, x0, y0, cw, ch, threads)
+    for _ in range(args.steps * REF_PASSES_PER_STEP):
+        smp.run_round()
     dt = time.perf_counter() - t0
-    v = args.steps * cw * ch / dt
+    v = smp.estimate()
+    s, _, _ = smp.totals()
+    smp.close()
+    wl = {"plain": WORKLOAD_PLAIN, "cornell": WORKLOAD_CORNELL}.get(workload, WORKLOAD_BATCH)
     line = {"impl": "reference", "metric": "samples/s", "value": v, "unit": "samples/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "step": f"{cw}x{ch} crop x 1 pass on {threads} host threads"},
-            "cpu_baseline": {"value": v, "unit": "samples/s", "cores": threads, "kind": "port",
-                             "sample": f"{cw}x{ch} centred crop, 1 pass per step, {args.steps} steps"},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / max(args.steps, 1) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural scenes)",
+            "config": {"workload": wl, "step": f"{REF_PASSES_PER_STEP} passes of the sampled rows ({desc}) on "
+                                               f"{smp.threads} host threads"},
+            "cpu_baseline": {"value": v, "unit": "samples/s", "cores": smp.threads, "kind": "port",
+                             "sample": f"{desc}; {args.steps * REF_PASSES_PER_STEP} timed passes, {s} camera samples, "
+                                       f"{dt:.1f} s"},
             "e2e": {"value": v, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# Rooflines of the wavefront kernels from a stage-timed run (one render lane,
+# so each kernel's time is its own).
+
+def kernel_rooflines(workload: str, stage: dict, hbm: float, peak_kind: str, sm_mhz, costs):
+    """stage: trace_ms, shade_ms, trace_launches, rays, shaded of a
+    stage-timed run. Returns (kernels, dominant)."""
+    n = max(stage["trace_launches"], 1)
+    cnt = COUNTERS.get(workload, {})
+    rays_l = stage["rays"] / n
+    trace_ms = stage["trace_ms"] / n
+    k_trace = {"kernel": "k_trace", "unit_of_work": "traced ray", "units_per_launch": rays_l, "ms_per_launch": trace_ms}
+    c = cnt.get("k_trace", {})
+    k_trace["traffic"] = c["dram_bytes_per_ray"] * rays_l if c.get("dram_bytes_per_ray") else None
+    mhz = sm_mhz or 2070.0
+    if c.get("warp_inst_per_ray"):
+        achieved = c["warp_inst_per_ray"] * rays_l / (trace_ms * 1e-3) * 1e-9
+        peak = SMS * ISSUE_PER_SM_PER_CLOCK * mhz * 1e-3
+        k_trace.update(bound="issue", achieved=achieved, peak=peak, unit="G warp-inst/s", frac=achieved / peak,
+                       peak_kind=f"{SMS} SMs x {ISSUE_PER_SM_PER_CLOCK} schedulers x {mhz:.0f} MHz (median under load)",
+                       active_lanes_per_inst=c["thread_inst_per_ray"] / c["warp_inst_per_ray"],
+                       warp_inst_per_ray=c["warp_inst_per_ray"])
+    else:
+        k_trace.update(bound="issue", achieved=None, peak=None, unit="G warp-inst/s", frac=None,
+                       note="instruction counts not captured for this workload")
+    if costs:
+        model = 32 + 16 + 64 * costs["nodes_per_ray"] + 48 * costs["tris_per_ray"]
+        k_trace["hbm_model"] = {"bytes_per_ray": model, "note": "ray + hit + 64 B per binary-BVH node visit and 48 B per "
+                                "triangle test counted by the CPU oracle: an upper bound on traffic, not a bound "
+                                "on this kernel (its upper tree levels stay in L1/L2)",
+                                "gbs": model * rays_l / (trace_ms * 1e-3) * 1e-9}
+    verts_l = stage["shaded"] / n
+    shade_ms = stage["shade_ms"] / n
+    alg = B_SHADE * verts_l
+    ach = alg / (shade_ms * 1e-3) * 1e-9
+    c = cnt.get("k_resolve+k_sample", {})
+    k_shade = {"kernel": "k_resolve+k_sample", "unit_of_work": "shaded vertex", "units_per_launch": verts_l,
+               "ms_per_launch": shade_ms, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+               "frac": ach / hbm, "peak_kind": peak_kind, "bytes_per_unit": B_SHADE,
+               "algorithmic_bytes_per_launch": alg,
+               "traffic": c["dram_bytes_per_vertex"] * verts_l if c.get("dram_bytes_per_vertex") else None}
+    kernels = [k_trace, k_shade]
+    dominant = dict(max(kernels, key=lambda k: k["ms_per_launch"]))
+    dominant["note"] = "dominant kernel by device time, timed alone (stage timing keeps one render lane)"
+    return kernels, dominant
+
+
+def stage_split(job_list, passes_list):
+    """Renders the jobs one after another with stage timing and returns the
+    summed stage times and work (for the rooflines)."""
+    out = {"trace_ms": 0.0, "shade_ms": 0.0, "trace_launches": 0, "rays": 0, "shaded": 0, "kernel_ms": 0.0}
+    for job, p in zip(job_list, passes_list):
+        job.set_stage_timing(True)
+        s0 = job.stats()
+        job.render_passes(p, sync=True)
+        s1 = job.stats()
+        job.set_stage_timing(False)
+        for k in out:
+            out[k] += s1[k] - s0[k]
+    return out
+
+
+def tuned_batch_args(args, jobs, ctx):
+    """Batching parameters from the autotuner (cached per GPU name), tuned on
+    16 jobs spread over the mix, 8 passes each."""
+    import torch
+    from hastyrenderer_gb300 import RenderJob, autotune
+    if args.no_tune:
+        return {"mode": 0, "lanes": 2, "paths_in_flight": 1 << 24}, {"source": "defaults"}
+    path = autotune.default_path(torch.cuda.get_device_name())
+    res = autotune.load(path)
+    if res:
+        res["source"] = path
+    else:
+        calib = [RenderJob(j["path"], ctx) for j in jobs[::4]]
+        res = autotune.tune_batch(calib, passes=8, out_path=path)
+        for c in calib:
+            c.close()
+        res["source"] = "tuned now"
+    info = {k: res[k] for k in ("mode", "lanes", "paths_in_flight", "regen_fraction", "samples_per_s", "source")
+            if k in res}
+    info["candidates"] = len(res.get("trials", []))
+    return autotune.batch_args(res), info
+
+
+# ---------------------------------------------------------------------------
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=32)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default: 3 batch, 16 plain/cornell)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--spp-per-step", type=int, default=SPP_PER_STEP)
+    ap.add_argument("--workload", default="batch", choices=["batch", "plain", "cornell", "serve", "stress", "photon"])
+    ap.add_argument("--spp-per-step", type=int, default=SPP_PER_STEP, help="plain: passes per step")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--bvh", default="wide", choices=["wide", "binary"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "stress", "photon"],
-                    help="plain: the large single job (default); batch: the 64-job mix batched vs one by one; "
-                         "serve: Poisson arrivals over the server; stress: 10.36M-triangle 4K scene, one pass per step; "
-                         "photon: the photon mapper on the textured room, one progressive iteration per step")
-    ap.add_argument("--jobs", type=int, default=64, help="batch/serve: jobs in the mix (serve: scene pool = half)")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: arrivals per second")
     ap.add_argument("--duration", type=float, default=120.0, help="serve: seconds of arrivals")
-    ap.add_argument("--no-tune", action="store_true", help="batch/serve: skip the autotuner (engine defaults)")
+    ap.add_argument("--policy", type=int, default=0, help="serve: 0 round robin, 1 shortest remaining first")
+    ap.add_argument("--no-tune", action="store_true", help="batch/serve: skip the autotuner (defaults)")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 3 if args.workload == "batch" else 16
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        dist = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")     # the reference arm runs on the host cores only
+        run_reference_arm(args, rank)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
     if args.workload == "stress":
         return run_stress(args)
     if args.workload == "photon":
         return run_photon(args)
-    if args.workload != "plain":
-        return run_mixed(args)
+    if args.workload == "serve":
+        return run_serve(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    return run_single(args)
 
-    rank = int(os.environ.get("RANK", "0"))
+
+def _dist_setup(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        if args.impl == "ours":
-            torch.cuda.set_device(local_rank)
-        # the reference arm runs on the host cores only (gloo, no device)
-        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if world <= 1:
+        return None, 0, 1, local_rank
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local_rank)
+    dist.init_process_group("nccl")
+    return dist, dist.get_rank(), world, local_rank
 
-    base = os.environ.get("HASTY_BENCH_DIR", os.path.join(tempfile.gettempdir(), "hasty_bench_c1"))
-    if rank == 0:
-        os.makedirs(base, exist_ok=True)
-        job_path = make_job(base)
-    if dist is not None:
-        dist.barrier()
-    job_path = os.path.join(base, "renderJob.json")
 
-    if args.impl == "reference":
-        run_reference_arm(args, job_path, rank)
-        if dist is not None:
-            dist.destroy_process_group()
-        return
-
+def run_single(args):
+    """plain (the 1080p sphere field, SPP_PER_STEP passes per step) or
+    cornell (the 256x256 box, the whole 64-pass render per step): replicas on
+    every rank (weak scaling)."""
     import torch
     from hastyrenderer_gb300 import Context, RenderJob
+    dist, rank, world, local_rank = _dist_setup(args)
+    if args.workload == "plain":
+        job_path = make_plain_job(_bench_dir("hasty_bench_c1")) if rank == 0 else None
+        wl, passes = WORKLOAD_PLAIN, args.spp_per_step
+    else:
+        job_path = make_cornell_job(_bench_dir("hasty_bench_c0")) if rank == 0 else None
+        wl, passes = WORKLOAD_CORNELL, 64
+    if dist is not None:
+        dist.barrier()
+    job_path = os.path.join(_bench_dir("hasty_bench_c1" if args.workload == "plain" else "hasty_bench_c0"),
+                            "renderJob.json")
     torch.cuda.init()
     ctx = Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0)
 
-    # ---- end to end through the C ABI: load (parse, BVH, upload) + steps with read-back
+    # end to end through the C ABI: load (parse, BVH, upload) + steps, each
+    # step's colour estimate read back to the host while the next renders
     if dist is not None:
         dist.barrier()
     t0 = time.perf_counter()
@@ -251,119 +486,64 @@ def main():
     info = job.info
     load_ms = (time.perf_counter() - t0) * 1e3
     W, H = info.width, info.height
-    # each step's colour estimate is read back while the next step renders
-    # (hasty_job_snapshot: estimate behind the step, copy on a copy stream)
-    est_sum = 0.0
     for k in range(args.steps):
-        job.render_passes(args.spp_per_step)
+        job.render_passes(passes)
         if k:
-            est, _ = job.snapshot_get()
-            est_sum += float(est[0, 0, 0])
+            job.snapshot_get()
         job.snapshot()
     est, n_est = job.snapshot_get()
     e2e_s = time.perf_counter() - t0
-    assert n_est == args.steps * args.spp_per_step
-    e2e_bytes_up = info.device_bytes
+    assert n_est == args.steps * passes
     del est
 
-    # ---- device-resident timing (both render lanes, as a user's render runs)
+    # device-resident timing (both render lanes, as a user's render runs)
     job.reset()
     job.set_seed(replica_seed(rank))
     for _ in range(args.warmup):
-        job.render_passes(args.spp_per_step)
+        job.render_passes(passes)
     job.sync()
     s0 = job.stats()
     sampler = ClockSampler(local_rank)
-    start = torch.cuda.Event(enable_timing=True)
-    end = torch.cuda.Event(enable_timing=True)
     with sampler:
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
-        start.record()
         w0 = time.perf_counter()
         for _ in range(args.steps):
-            job.render_passes(args.spp_per_step)
+            job.render_passes(passes)
         job.sync()
         torch.cuda.synchronize()
-        end.record()
-        end.synchronize()
         wall = time.perf_counter() - w0
         if dist is not None:
             dist.barrier()
     s1 = job.stats()
-    # Per-stage split for the roofline: the same steps with stage timing,
-    # which keeps one render lane so that kernel times are not shared.
-    job.set_stage_timing(True)
-    job.render_passes(args.spp_per_step)
-    job.sync()
-    st0 = job.stats()
-    for _ in range(args.steps):
-        job.render_passes(args.spp_per_step)
-    job.sync()
-    st1 = job.stats()
-    job.set_stage_timing(False)
-    dev_s = (s1["kernel_ms"] - s0["kernel_ms"]) * 1e-3
-    t = max(dev_s, 1e-9)
-    t = max_over_ranks(t, dist, "cuda")
-    samples = args.steps * args.spp_per_step * W * H
-    rays = s1["rays"] - s0["rays"]
-    shaded = s1["shaded"] - s0["shaded"]
-    trace_ms = st1["trace_ms"] - st0["trace_ms"]
-    shade_ms = st1["shade_ms"] - st0["shade_ms"]
-    one_lane_ms = st1["kernel_ms"] - st0["kernel_ms"]
-    launches = s1["kernel_launches"] - s0["kernel_launches"]
-    trace_launches = st1["trace_launches"] - st0["trace_launches"]
+    stage = stage_split([job] * args.steps, [passes] * args.steps)
+    t = max_over_ranks(max((s1["kernel_ms"] - s0["kernel_ms"]) * 1e-3, 1e-9), dist, "cuda")
+    samples = args.steps * passes * W * H
     clocks = sampler.summary()
-
     if rank == 0:
         hbm, peak_kind = peaks()
-        cpu, bvh_costs = (None, None)
+        cpu, costs = (None, None)
         if not args.no_cpu_baseline:
-            cpu, bvh_costs = cpu_baseline(job_path, args.cpu_budget)
-        roof, kernels = None, []
-        if bvh_costs is not None:
-            b_ray = 32 + 16 + 64 * bvh_costs["nodes_per_ray"] + 48 * bvh_costs["tris_per_ray"]
-            # the measured bytes scale with the passes in a batch
-            batch_passes = min(args.spp_per_step, max(1, info.paths_in_flight // (W * H)))
-            traffic = {k: v * batch_passes / MEASURED_TRAFFIC_PASSES
-                       for k, v in MEASURED_TRAFFIC.get(args.bvh, {}).items()}
-            n_launch = max(trace_launches, 1)
-            rays_st, shaded_st = st1["rays"] - st0["rays"], st1["shaded"] - st0["shaded"]
-            for name, work, unit_bytes, ms in (("k_trace", rays_st, b_ray, trace_ms),
-                                                ("k_resolve+k_sample", shaded_st, B_SHADE, shade_ms)):
-                per_launch_bytes = work * unit_bytes / n_launch
-                achieved = per_launch_bytes / (ms * 1e-3 / n_launch) / 1e9
-                kernels.append({"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                                "frac": achieved / hbm, "peak_kind": peak_kind,
-                                "traffic": traffic.get(name), "algorithmic_bytes_per_launch": per_launch_bytes,
-                                "ms_per_launch": ms / n_launch,
-                                "bytes_per_unit": unit_bytes, "unit_of_work": "ray" if name == "k_trace" else "shaded vertex"})
-            kernels[0].update({"bvh_nodes_per_ray": bvh_costs["nodes_per_ray"], "tris_per_ray": bvh_costs["tris_per_ray"]})
-            roof = dict(max(kernels, key=lambda k: k["ms_per_launch"]))
-            roof["note"] = ("dominant kernel by device time, timed alone (one render lane); traffic = measured DRAM "
-                            "bytes per launch (ncu), well below the algorithmic bytes because L1/L2 hold the upper "
-                            "BVH levels")
+            cpu, costs = cpu_baseline(args.workload, args.cpu_budget)
+        kernels, roof = kernel_rooflines(args.workload, stage, hbm, peak_kind, clocks.get("sm_mhz"), costs)
         line = {
             "metric": "samples/s", "value": samples * world / t, "unit": "samples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "spp_per_step": args.spp_per_step, "width": W, "height": H, "bvh": args.bvh,
+            "config": {"workload": wl, "passes_per_step": passes, "width": W, "height": H, "bvh": args.bvh,
                        "max_depth": info.max_depth, "triangles": info.n_triangles,
-                       "l2": "working set > L2 (path state + BVH), no flush", "parallelism": f"replicas x{world}"},
-            "mrays_per_s": rays * world / t * 1e-6,
-            "stage_ms_per_step": {"trace": trace_ms / args.steps, "shade": shade_ms / args.steps,
-                                  "one_lane_total": one_lane_ms / args.steps,
-                                  "note": "same steps with stage timing, which keeps one render lane; the timed "
-                                          "run uses two lanes, one batch's trace overlapping the other's shading"},
+                       "l2": "working set > L2 (path state + scene), no flush", "parallelism": f"replicas x{world}"},
+            "mrays_per_s": (s1["rays"] - s0["rays"]) * world / t * 1e-6,
+            "stage_ms_per_step": {"trace": stage["trace_ms"] / args.steps, "shade": stage["shade_ms"] / args.steps,
+                                  "one_lane_total": stage["kernel_ms"] / args.steps,
+                                  "note": "same steps with stage timing (one render lane); the timed run uses two"},
             "wall_ms_per_step": wall / args.steps * 1e3,
-            "gpu_launches": launches,
-            "roofline": roof,
-            "kernels": kernels,
-            "cpu_baseline": cpu,
-            "e2e": {"value": args.steps * args.spp_per_step * W * H * world / e2e_s, "unit": "samples/s",
-                    "h2d_bytes_per_step": int(e2e_bytes_up // args.steps), "d2h_bytes_per_step": W * H * 3 * 4,
-                    "includes": "job load (parse, BVH build, upload) + steps + a colour read-back per step, each copied while the next step renders",
+            "gpu_launches": s1["kernel_launches"] - s0["kernel_launches"],
+            "roofline": roof, "kernels": kernels, "cpu_baseline": cpu,
+            "e2e": {"value": samples * world / e2e_s, "unit": "samples/s",
+                    "h2d_bytes_per_step": int(info.device_bytes // args.steps), "d2h_bytes_per_step": W * H * 3 * 4,
+                    "includes": "job load (parse, BVH build, upload) + steps + a colour read-back per step",
                     "load_ms": {"total": load_ms, "parse": info.parse_ms, "bvh_build": info.bvh_build_ms,
                                 "upload": info.upload_ms}},
             "clocks": clocks,
@@ -372,6 +552,205 @@ def main():
     job.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_batch(args):
+    """The 64-job mix: batched (packed batches) against the same jobs one by
+    one through the single-job path, with bit-identical images."""
+    import numpy as np
+    import torch
+    from hastyrenderer_gb300 import Context, RenderJob, batch_render, workloads
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if rank != 0:
+        return
+    torch.cuda.init()
+    t_gen = time.perf_counter()
+    jobs = mix_jobs()
+    gen_s = time.perf_counter() - t_gen
+    ctx = Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0)
+    spp = [j["spp"] for j in jobs]
+    total = sum(workloads.job_samples(j) for j in jobs)
+    hbm, peak_kind = peaks()
+
+    # end to end through the C ABI: load every job (parse, BVH build, upload),
+    # one batched render, every job's colour estimate read to the host
+    t0 = time.perf_counter()
+    resident = [RenderJob(j["path"], ctx) for j in jobs]
+    load_s = time.perf_counter() - t0
+    eargs, tune = tuned_batch_args(args, jobs, ctx)   # (tuning is not part of the end-to-end time)
+    for r in resident:
+        r.reset()
+    t1 = time.perf_counter()
+    batch_render(resident, spp, **eargs)
+    images = [r.compute_estimate() for r in resident]
+    e2e_s = load_s + (time.perf_counter() - t1)
+    h2d = sum(r.info.device_bytes for r in resident)
+    d2h = sum(im.nbytes for im in images)
+    del images
+
+    # plain: one job after another (device time from each job's own events)
+    plain_sums, per_class = [], {}
+    plain_ms, plain_rays = 0.0, 0
+    for r in resident:
+        r.reset()
+    sampler = ClockSampler(local_rank)
+    with sampler:
+        w0 = time.perf_counter()
+        for j, r, p in zip(jobs, resident, spp):
+            s0 = r.stats()
+            r.render_passes(p, sync=True)
+            s1 = r.stats()
+            ms = s1["kernel_ms"] - s0["kernel_ms"]
+            plain_ms += ms
+            plain_rays += s1["rays"] - s0["rays"]
+            key = f"{j['kind']}{j['spheres'] or ''}"
+            c = per_class.setdefault(key, {"samples": 0, "plain_ms": 0.0})
+            c["samples"] += workloads.job_samples(j)
+            c["plain_ms"] += ms
+            plain_sums.append(r.read_sums()[0])
+            r.release_paths()
+        plain_wall = time.perf_counter() - w0
+        # batched: warm-up steps, then the timed steps
+        for _ in range(args.warmup):
+            for r in resident:
+                r.reset()
+            batch_render(resident, spp, **eargs)
+        torch.cuda.synchronize()
+        dev_ms, wall_ms, rays, launches, batches = 0.0, 0.0, 0, 0, 0
+        identical = True
+        for _ in range(args.steps):
+            for r in resident:
+                r.reset()
+            torch.cuda.synchronize()
+            w1 = time.perf_counter()
+            st = batch_render(resident, spp, **eargs)
+            torch.cuda.synchronize()
+            wall_ms += (time.perf_counter() - w1) * 1e3
+            dev_ms += st["device_ms"]
+            rays += st["rays"]
+            launches += st["kernel_launches"]
+            batches += st["iterations"]
+            identical = identical and all(np.array_equal(r.read_sums()[0], ps) for r, ps in zip(resident, plain_sums))
+    clocks = sampler.summary()
+    # stage split on 1/8 of every job's passes (one render lane, for the rooflines)
+    for r in resident:
+        r.reset()
+    stage = stage_split(resident, [max(1, p // 8) for p in spp])
+    for r in resident:
+        r.release_paths()
+        r.close()
+    cpu, costs = (None, None)
+    if not args.no_cpu_baseline:
+        cpu, costs = cpu_baseline("batch", args.cpu_budget)
+    kernels, roof = kernel_rooflines("batch", stage, hbm, peak_kind, clocks.get("sm_mhz"), costs)
+    batch_sps = total * args.steps / (dev_ms * 1e-3)
+    plain_sps = total / (plain_ms * 1e-3)
+    for c in per_class.values():
+        c["plain_samples_per_s"] = c["samples"] / (c["plain_ms"] * 1e-3)
+    line = {
+        "metric": "samples/s", "value": batch_sps, "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
+        "config": {"workload": WORKLOAD_BATCH, "jobs": len(jobs), "samples_per_step": total,
+                   "step": "every job's full pass count in one hasty_batch_render call",
+                   "batching": eargs, "l2": "working set > L2 (path state + scenes), no flush",
+                   "parallelism": "one GPU"},
+        "mrays_per_s": rays / (dev_ms * 1e-3) * 1e-6,
+        "wall_ms_per_step": wall_ms / args.steps,
+        "plain": {"value": plain_sps, "unit": "samples/s", "device_ms": plain_ms, "wall_ms": plain_wall * 1e3,
+                  "mrays_per_s": plain_rays / (plain_ms * 1e-3) * 1e-6, "per_class": per_class,
+                  "note": "the same jobs one after another through hasty_job_render_passes"},
+        "batched_over_plain": {"device": plain_ms / (dev_ms / args.steps),
+                               "wall": plain_wall * 1e3 / (wall_ms / args.steps)},
+        "images_bit_identical_to_plain": identical,
+        "batches_per_step": batches / args.steps,
+        "gpu_launches": launches,
+        "roofline": roof, "kernels": kernels,
+        "stage_ms_per_step": {"trace": stage["trace_ms"] * 8, "shade": stage["shade_ms"] * 8,
+                              "note": "1/8 of every job's passes with stage timing (one render lane), scaled by 8"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": total / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "includes": "loading all 64 jobs (parse, BVH build, upload) + one batched render + every colour "
+                            "estimate read to the host", "load_s": load_s, "scene_generation_s": gen_s},
+        "autotune": tune, "clocks": clocks, "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Serving: Poisson arrivals of the mixed distribution over a warm pool of
+    32 scenes, through hasty_server_* (packed batches on the tuned lanes)."""
+    import numpy as np
+    import torch
+    from hastyrenderer_gb300 import Context, Server, workloads
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if rank != 0:
+        return
+    torch.cuda.init()
+    jobs = mix_jobs()
+    ctx = Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0)
+    eargs, tune = tuned_batch_args(args, jobs, ctx)
+    lanes = eargs.get("lanes", 2)
+    paths = eargs.get("paths_in_flight", 1 << 24)
+    pool = jobs[: max(1, len(jobs) // 2)]
+    base = os.path.dirname(os.path.dirname(pool[0]["path"]))
+    reqs = workloads.poisson_requests(pool, os.path.join(base, f"requests_{args.rate:g}_{args.duration:g}"),
+                                      rate=args.rate, duration=args.duration, seed=1)
+    cfg = dict(memory_budget=120 << 30, max_resident_jobs=32, max_resident_scenes=32, lanes=lanes,
+               paths_in_flight=paths, policy=args.policy)
+    srv = Server(ctx, **cfg)
+    t0 = time.perf_counter()
+    for j in pool:                       # warm the scene cache: one cheap request per scene
+        srv.submit(j["path"], passes=1)
+    srv.wait_idle(-1)
+    for r in srv.poll(max_results=len(pool) + 8, wait_ms=0):
+        srv.release(r["id"])
+    warm_s = time.perf_counter() - t0
+    st0 = srv.stats()
+    results = []
+    sampler = ClockSampler(local_rank)
+    with sampler:
+        t0 = time.perf_counter()
+        k = 0
+        while k < len(reqs) or len(results) < len(reqs):
+            now = time.perf_counter() - t0
+            while k < len(reqs) and reqs[k]["t"] <= now:
+                srv.submit(reqs[k]["path"], passes=reqs[k]["spp"], seed=reqs[k]["seed"])
+                k += 1
+            wait = 0 if k >= len(reqs) else max(0, int((reqs[k]["t"] - (time.perf_counter() - t0)) * 1e3))
+            for r in srv.poll(wait_ms=max(1, min(wait, 50)) if k < len(reqs) else 200):
+                if r["status"] == 0:
+                    img = srv.read(r["id"])   # host result as a caller reads it
+                    del img
+                srv.release(r["id"])
+                results.append(r)
+        span = time.perf_counter() - t0
+    st1 = srv.stats()
+    srv.stop()
+    ok = [r for r in results if r["status"] == 0]
+    lat = np.array([r["latency_ms"] for r in ok]) if ok else np.zeros(1)
+    samples = sum(r["samples"] for r in ok)
+    dev_ms = st1["device_ms"] - st0["device_ms"]
+    offered = sum(r["width"] * r["height"] * r["spp"] for r in reqs) / args.duration
+    line = {
+        "metric": "samples/s", "value": samples / span, "unit": "samples/s", "n_gpus": 1, "steps": len(reqs),
+        "warmup": len(pool), "ms_per_step": span * 1e3 / max(len(reqs), 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
+        "config": {"workload": f"serving_poisson_{args.rate:g}_per_s_{args.duration:g}_s", "requests": len(reqs),
+                   "scene_pool": len(pool), "server": cfg},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                       "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+        "completed": len(ok), "failed": len(results) - len(ok),
+        "device_samples_per_s": samples / max(dev_ms * 1e-3, 1e-9),
+        "mrays_per_s": (st1["rays"] - st0["rays"]) / max(dev_ms * 1e-3, 1e-9) * 1e-6,
+        "offered_samples_per_s": offered, "offered_over_served": offered / max(samples / span, 1e-9),
+        "batches": st1["batches"] - st0["batches"], "gpu_launches": st1["kernel_launches"] - st0["kernel_launches"],
+        "peak_resident_bytes": st1["peak_resident_bytes"], "warm_s": warm_s, "span_s": span,
+        "autotune": tune, "clocks": sampler.summary(),
+    }
+    print(json.dumps(line), flush=True)
 
 
 PHOTON_WORKLOAD = "photon_mapping_textured_room_640x480_tex256_depth8_caustics_map"
@@ -523,159 +902,6 @@ def run_stress(args):
     print(json.dumps(line), flush=True)
     job.close()
 
-
-def _rel_diff(a, b):
-    import numpy as np
-    den = float(np.linalg.norm(b.astype(np.float64)))
-    return float(np.linalg.norm(a.astype(np.float64) - b.astype(np.float64))) / max(den, 1e-30)
-
-
-def _tuned(args, jobs, ctx):
-    """Engine parameters from the autotuner (cached per GPU name)."""
-    import torch
-    from hastyrenderer_gb300 import RenderJob, autotune
-    path = autotune.default_path(torch.cuda.get_device_name())
-    if args.no_tune:
-        return {"paths_in_flight": 1 << 22, "regen_fraction": 0.9, "source": "defaults"}
-    cached = autotune.load(path)
-    if cached:
-        cached["source"] = path
-        return cached
-    calib = [RenderJob(j["path"], ctx) for j in jobs[:16]]
-    res = autotune.tune_batch(calib, passes=2, out_path=path)
-    for c in calib:
-        c.close()
-    res["source"] = "tuned now"
-    return res
-
-
-def run_mixed(args):
-    """Mixed-job workloads: batching (the same jobs one by one through
-    hasty_job_render_passes, then all at once through hasty_batch_render) or
-    serving (Poisson arrivals through hasty_server_*)."""
-    import numpy as np
-    import torch
-    from hastyrenderer_gb300 import Context, RenderJob, Server, autotune, batch_render, workloads
-    rank = int(os.environ.get("RANK", "0"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if rank != 0:
-        return
-    torch.cuda.init()
-    base = os.environ.get("HASTY_BENCH_MIX", os.path.join(tempfile.gettempdir(), "hasty_bench_mix"))
-    t_gen = time.perf_counter()
-    jobs = workloads.mixed_jobs(base, n_jobs=args.jobs, seed=0)
-    gen_s = time.perf_counter() - t_gen
-    ctx = Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0)
-    tune = _tuned(args, jobs, ctx)
-    engine_args = autotune.batch_args(tune)
-    hbm, peak_kind = peaks()
-    sampler = ClockSampler(local_rank)
-
-    if args.workload == "batch":
-        total = sum(workloads.job_samples(j) for j in jobs)
-        t0 = time.perf_counter()
-        resident = [RenderJob(j["path"], ctx) for j in jobs]
-        load_s = time.perf_counter() - t0
-        spp = [j["spp"] for j in jobs]
-        plain_est = []
-        with sampler:
-            # plain drop-in, one job after another (device time from the job's own CUDA events)
-            plain_ms = 0.0
-            plain_rays = 0
-            w0 = time.perf_counter()
-            for job, p in zip(resident, spp):
-                s0 = job.stats()
-                job.render_passes(p, sync=True)
-                s1 = job.stats()
-                plain_ms += s1["kernel_ms"] - s0["kernel_ms"]
-                plain_rays += s1["rays"] - s0["rays"]
-                plain_est.append(job.compute_estimate())
-                job.release_paths()
-                job.reset()
-            plain_wall = time.perf_counter() - w0
-            for _ in range(max(args.warmup - 2, 0)):   # the autotuner's trials already warmed the engine
-                batch_render(resident[:8], [2] * 8, **engine_args)
-                for job in resident[:8]:
-                    job.reset()
-            w0 = time.perf_counter()
-            st = batch_render(resident, spp, **engine_args)
-            batch_wall = time.perf_counter() - w0
-        diffs = [_rel_diff(job.compute_estimate(), ref) for job, ref in zip(resident, plain_est)]
-        batch_sps = total / (st["device_ms"] * 1e-3)
-        plain_sps = total / (plain_ms * 1e-3)
-        line = {
-            "metric": "samples/s", "value": batch_sps, "unit": "samples/s", "n_gpus": 1, "steps": 1,
-            "warmup": args.warmup, "ms_per_step": st["device_ms"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
-            "config": {"workload": f"mixed_{len(jobs)}_jobs_batched", "jobs": len(jobs), "samples": total,
-                       "engine": engine_args, "l2": "working set > L2 (path pool + scenes), no flush"},
-            "mrays_per_s": st["rays"] / (st["device_ms"] * 1e-3) * 1e-6,
-            "plain": {"value": plain_sps, "unit": "samples/s", "device_ms": plain_ms, "wall_ms": plain_wall * 1e3,
-                      "mrays_per_s": plain_rays / (plain_ms * 1e-3) * 1e-6},
-            "batched_over_plain": batch_sps / plain_sps,
-            "wall": {"batched_ms": batch_wall * 1e3, "plain_ms": plain_wall * 1e3, "load_s": load_s,
-                     "scene_generation_s": gen_s},
-            "equal_estimate": {"max_rel_l2_diff_vs_plain": max(diffs), "note": "same samples; fixed-point vs FP64 sums"},
-            "engine_iterations": st["iterations"], "engine_bytes": st["engine_bytes"],
-            "autotune": {k: tune[k] for k in ("paths_in_flight", "regen_fraction", "samples_per_s", "source") if k in tune},
-            "clocks": sampler.summary(), "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
-        }
-        print(json.dumps(line), flush=True)
-        return
-
-    # serving: Poisson arrivals over a warm scene pool
-    pool = jobs[: max(1, len(jobs) // 2)]
-    reqs = workloads.poisson_requests(pool, os.path.join(base, f"requests_{args.rate:g}_{args.duration:g}"),
-                                      rate=args.rate, duration=args.duration, seed=1)
-    srv = Server(ctx, memory_budget=120 << 30, max_resident_jobs=32, max_resident_scenes=32, **engine_args)
-    t0 = time.perf_counter()
-    for j in pool:                       # warm the scene cache: one cheap request per scene
-        srv.submit(j["path"], passes=1)
-    srv.wait_idle(-1)
-    for r in srv.poll(max_results=len(pool) + 8, wait_ms=0):
-        srv.release(r["id"])
-    warm_s = time.perf_counter() - t0
-    st0 = srv.stats()
-    results = []
-    with sampler:
-        t0 = time.perf_counter()
-        k = 0
-        while k < len(reqs) or len(results) < len(reqs):
-            now = time.perf_counter() - t0
-            while k < len(reqs) and reqs[k]["t"] <= now:
-                srv.submit(reqs[k]["path"], passes=reqs[k]["spp"], seed=reqs[k]["seed"])
-                k += 1
-            wait = 0 if k >= len(reqs) else max(0, int((reqs[k]["t"] - (time.perf_counter() - t0)) * 1e3))
-            for r in srv.poll(wait_ms=max(1, min(wait, 50)) if k < len(reqs) else 200):
-                if r["status"] == 0:
-                    img = srv.read(r["id"])   # host result as a caller reads it
-                    del img
-                srv.release(r["id"])
-                results.append(r)
-        span = time.perf_counter() - t0
-    st1 = srv.stats()
-    srv.stop()
-    ok = [r for r in results if r["status"] == 0]
-    lat = np.array([r["latency_ms"] for r in ok]) if ok else np.zeros(1)
-    samples = sum(r["samples"] for r in ok)
-    dev_ms = st1["device_ms"] - st0["device_ms"]
-    line = {
-        "metric": "samples/s", "value": samples / span, "unit": "samples/s", "n_gpus": 1, "steps": len(reqs),
-        "warmup": len(pool), "ms_per_step": span * 1e3 / max(len(reqs), 1), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
-        "config": {"workload": f"serving_poisson_{args.rate:g}_per_s_{args.duration:g}_s", "requests": len(reqs),
-                   "scene_pool": len(pool), "engine": engine_args, "max_resident_jobs": 32, "memory_budget": 120 << 30},
-        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
-                       "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
-        "completed": len(ok), "failed": len(results) - len(ok),
-        "device_samples_per_s": samples / max(dev_ms * 1e-3, 1e-9),
-        "mrays_per_s": (st1["rays"] - st0["rays"]) / max(dev_ms * 1e-3, 1e-9) * 1e-6,
-        "offered_samples_per_s": sum(r["width"] * r["height"] * r["spp"] for r in reqs) / args.duration,
-        "peak_resident_bytes": st1["peak_resident_bytes"], "warm_s": warm_s, "span_s": span,
-        "autotune": {k: tune[k] for k in ("paths_in_flight", "regen_fraction", "samples_per_s", "source") if k in tune},
-        "clocks": sampler.summary(),
-    }
-    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

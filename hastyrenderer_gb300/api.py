@@ -280,11 +280,16 @@ def batch_render(jobs, passes, paths_in_flight: int = 0, regen_fraction: float =
     return {k: getattr(st, k) for k, _ in native.BatchStats._fields_}
 
 
+SERVE_ROUND_ROBIN = 0     # HASTY_SERVE_ROUND_ROBIN
+SERVE_SHORTEST_FIRST = 1  # HASTY_SERVE_SHORTEST_FIRST
+
+
 class Server:
-    """Request loop over the multi-job engine (hasty_server_* in the C ABI):
-    requests are admitted by device-memory footprint, scenes stay resident
-    and are shared, and the passes of resident requests are interleaved in
-    one continuously running engine.
+    """Request loop over packed multi-job batches (hasty_server_* in the C
+    ABI): requests are admitted by device-memory footprint, scenes stay
+    resident and are shared, and the passes of resident requests are packed
+    into batches that keep the render lanes busy; a request arriving while
+    others render joins the next batch.
 
         srv = Server(max_resident_jobs=32, memory_budget=120 << 30)
         rid = srv.submit("job/renderJob.json", passes=64, seed=7)

@@ -45,7 +45,8 @@ void PackedLanes::wait_for(cudaStream_t s) {
   if (s != acc_stream) ck(cudaStreamWaitEvent(acc_stream, acc_ready, 0), "wait");
 }
 
-void PackedLanes::launch(const std::vector<PackedJob>& jobs, const std::vector<PackedChunk>& chunks, bool overlap) {
+void PackedLanes::launch(const std::vector<PackedJob>& jobs, const std::vector<PackedChunk>& chunks, bool overlap,
+                         cudaEvent_t start) {
   if (chunks.empty()) return;
   if (chunks.size() > size_t(kMaxChunks)) throw ApiError{HASTY_ERR_ARG, "too many chunks in one batch"};
   // Tables as kernel parameters (the launch copies them).
@@ -81,6 +82,7 @@ void PackedLanes::launch(const std::vector<PackedJob>& jobs, const std::vector<P
   PathsDev& p = pd[lane];
   cudaStream_t ls = lane_stream[lane];
   if (lane_free_valid[lane]) ck(cudaStreamWaitEvent(ls, lane_free[lane], 0), "lane wait");
+  if (start) ck(cudaEventRecord(start, ls), "event");
   const int trace_cap = overlap && n_lanes > 1 ? lane_trace_blocks() : 0;
   const int n_paths = ct.n_paths;
   launch_raygen_packed(ct, p, ls);
@@ -123,7 +125,8 @@ PackedLanes::~PackedLanes() {
 }
 
 std::vector<PackedChunk> pack_batch(const std::vector<PackedJob>& jobs, const std::vector<int>& order,
-                                    std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots) {
+                                    std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots,
+                                    int64_t job_samples) {
   std::vector<PackedChunk> out;
   int64_t used = 0;
   for (int j : order) {
@@ -132,11 +135,12 @@ std::vector<PackedChunk> pack_batch(const std::vector<PackedJob>& jobs, const st
     const int64_t npix = jobs[size_t(j)].npix;
     const int64_t fit = (slots - used) / npix;
     if (fit <= 0) continue;
-    const int32_t k = int32_t(std::min<int64_t>(fit, left[size_t(j)]));
-    out.push_back({j, pass_base[size_t(j)], k});
+    int64_t k = std::min<int64_t>(fit, left[size_t(j)]);
+    if (job_samples > 0) k = std::min<int64_t>(k, std::max<int64_t>(1, job_samples / npix));
+    out.push_back({j, pass_base[size_t(j)], int32_t(k)});
     pass_base[size_t(j)] += uint32_t(k);
-    left[size_t(j)] -= k;
-    used += int64_t(k) * npix;
+    left[size_t(j)] -= int32_t(k);
+    used += k * npix;
   }
   return out;
 }

@@ -67,7 +67,10 @@ struct PackedLanes {
   // Enqueues one batch on the next lane (asynchronous). `overlap`: other
   // batches run at the same time (the closest-hit grid then leaves room for
   // their shading). Chunks must fit one lane and number at most kMaxChunks.
-  void launch(const std::vector<PackedJob>& jobs, const std::vector<PackedChunk>& chunks, bool overlap);
+  // `start` (optional, a timing event) is recorded on the lane's stream when
+  // the batch can start.
+  void launch(const std::vector<PackedJob>& jobs, const std::vector<PackedChunk>& chunks, bool overlap,
+              cudaEvent_t start = nullptr);
   void read_stats(unsigned long long* out);
 
  private:
@@ -76,11 +79,13 @@ struct PackedLanes {
 
 // Fills one batch: passes of the jobs in `order` (job indices), each job's
 // next passes in order (pass_base[j], left[j] updated), up to `slots` path
-// slots and kMaxChunks chunks. A job whose next pass does not fit the space
-// left is skipped for this batch. Returns the chunks (empty when nothing is
-// left).
+// slots and kMaxChunks chunks, and (when job_samples > 0) at most
+// job_samples camera samples of one job (one pass at least). A job whose
+// next pass does not fit the space left is skipped for this batch. Returns
+// the chunks (empty when nothing is left).
 std::vector<PackedChunk> pack_batch(const std::vector<PackedJob>& jobs, const std::vector<int>& order,
-                                    std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots);
+                                    std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots,
+                                    int64_t job_samples = 0);
 
 // Path slots of a lane: 16M camera samples (whole frames of the largest
 // job at least), or `requested` when positive.

@@ -1,13 +1,13 @@
-// Serving: a request loop over the multi-job engine (hasty_server_* in
+// Serving: a request loop over packed multi-job batches (hasty_server_* in
 // hasty_gpu.h). Three kinds of threads share one mutex:
 //   * callers submit requests, poll finished ones and read their images;
 //   * loader threads parse scenes and build BVHs on the host, then upload
 //     them once the device-memory budget has room (scene cache keyed by the
 //     scene file; scenes without users are evicted least recently used);
-//   * the engine thread admits requests (job slot + accumulator bytes within
-//     the budget), queues their passes round-robin into the engine's segment
-//     ring, runs engine waves, and retires requests whose samples have all
-//     finished (their fixed-point sums are copied to the host).
+//   * the batch thread admits requests (a job slot and FP64 sums within the
+//     budget), packs the passes of the resident requests into a batch
+//     whenever a render lane frees up, and retires requests whose last batch
+//     has been accumulated (their sums are copied to the host).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -25,7 +25,7 @@
 #include <thread>
 #include <vector>
 
-#include "engine.h"
+#include "packed.h"
 
 namespace hasty {
 namespace {
@@ -58,14 +58,20 @@ struct Request {
   double t_submit = 0, t_admit = 0, t_done = 0;
   int slot = -1;
   SceneEntry* scene = nullptr;
-  unsigned long long* d_acc = nullptr;
+  double* d_acc = nullptr;            // FP64 sums on the device: colour, normal, albedo (npix x 3 each)
   int64_t acc_bytes = 0;
   uint32_t npix = 0;
-  uint32_t lanes = 1;                 // accumulator lanes (engine_lanes)
-  int32_t passes_issued = 0;
+  int32_t passes_issued = 0;          // passes packed into launched batches
   float exposure = 0.f;
-  std::vector<long long> acc;         // 9 fixed-point sums per pixel, after completion
+  std::vector<double> acc;            // the sums after completion (3 x npix x 3)
   bool reported = false;
+};
+
+// A launched batch: its timing events and the requests whose last passes it
+// holds.
+struct InFlight {
+  cudaEvent_t start = nullptr, end = nullptr;
+  std::vector<Request*> finishing;
 };
 
 constexpr int64_t kDefaultBudget = int64_t(120) << 30;
@@ -84,10 +90,10 @@ using namespace hasty;
 struct hasty_server {
   hasty_ctx* ctx = nullptr;
   hasty_server_config cfg{};
-  Engine engine;
+  PackedLanes lanes;
   std::mutex mu;
   std::condition_variable cv_work, cv_load, cv_done;
-  std::thread engine_thread;
+  std::thread batch_thread;
   std::vector<std::thread> loaders;
   bool stopping = false;
   int fatal_code = HASTY_OK;
@@ -96,18 +102,18 @@ struct hasty_server {
   int64_t next_id = 1;
   std::map<int64_t, std::unique_ptr<Request>> requests;
   std::deque<Request*> pending;       // submitted, not yet resident (FIFO)
-  std::vector<Request*> slots;        // resident requests by engine job slot
+  std::vector<Request*> slots;        // resident requests by job slot
   std::deque<int64_t> finished;       // finished, not yet returned by poll
   std::map<std::string, std::unique_ptr<SceneEntry>> scenes;
   int64_t scene_bytes = 0, acc_bytes = 0, peak_bytes = 0;
   uint64_t use_clock = 0;
   size_t rr = 0;
-  uint64_t submitted = 0, admitted = 0, completed = 0, failed = 0, samples = 0, waves = 0;
+  uint64_t submitted = 0, admitted = 0, completed = 0, failed = 0, samples = 0, batches = 0, launches = 0;
   double device_ms = 0;
-  unsigned long long engine_stats[MS_COUNT] = {};
+  unsigned long long lane_stats[ST_COUNT] = {};
 
   double now_ms() const { return std::chrono::duration<double, std::milli>(Clock::now() - t0).count(); }
-  int64_t resident_bytes() const { return engine.bytes + scene_bytes + acc_bytes; }
+  int64_t resident_bytes() const { return lanes.bytes + scene_bytes + acc_bytes; }
   void note_peak() { peak_bytes = std::max(peak_bytes, resident_bytes()); }
 
   // --- all *_locked functions run with `mu` held ---
@@ -178,9 +184,13 @@ struct hasty_server {
       int slot = -1;
       for (size_t k = 0; k < slots.size(); ++k) if (!slots[k]) { slot = int(k); break; }
       if (slot < 0) return;
-      const uint32_t lanes = engine_lanes(cfg.paths_in_flight, r->npix);
-      int64_t need = int64_t(r->npix) * 9 * 8 * lanes;
-      if (engine.bytes + e->bytes + need > cfg.memory_budget) {
+      const int64_t need = int64_t(r->npix) * 9 * int64_t(sizeof(double));
+      if (int64_t(r->npix) > lanes.lane_paths) {
+        it = pending.erase(it);
+        finish_locked(r, Request::kFailed, HASTY_ERR_ARG, "frame is larger than a render lane (paths_in_flight)");
+        continue;
+      }
+      if (lanes.bytes + e->bytes + need > cfg.memory_budget) {
         it = pending.erase(it);
         finish_locked(r, Request::kFailed, HASTY_ERR_MEMORY, "request does not fit the server's memory budget");
         continue;
@@ -204,7 +214,6 @@ struct hasty_server {
       r->slot = slot;
       r->t_admit = now_ms();
       r->acc_bytes = need;
-      r->lanes = lanes;
       r->exposure = e->job->host.cam.exposure;
       acc_bytes += need;
       note_peak();
@@ -214,7 +223,7 @@ struct hasty_server {
     }
   }
 
-  bool has_unqueued_passes() const {
+  bool has_unissued_passes() const {
     for (Request* r : slots) if (r && r->state == Request::kActive && r->passes_issued < r->passes) return true;
     return false;
   }
@@ -234,112 +243,138 @@ struct hasty_server {
     }
   }
 
-  void engine_loop();
+  void batch_loop();
   void loader_loop();
 };
 
-void hasty_server::engine_loop() {
-  std::vector<unsigned long long> done;
-  cudaEvent_t ea = nullptr, eb = nullptr;
+void hasty_server::batch_loop() {
+  std::vector<PackedJob> jobs(slots.size());
+  std::vector<uint32_t> pass_base(slots.size(), 0);
+  std::vector<int32_t> left(slots.size(), 0);
+  std::deque<InFlight> inflight;
+  std::vector<cudaEvent_t> spare;     // timing events for reuse
+  cudaEvent_t origin = nullptr;       // reference point of the batches' device times
+  cudaStream_t copy_stream = nullptr;
+  double covered_ms = 0.0;            // device time counted so far ends here (ms after origin)
+  auto take_event = [&]() {
+    if (!spare.empty()) { cudaEvent_t e = spare.back(); spare.pop_back(); return e; }
+    cudaEvent_t e = nullptr;
+    ck(cudaEventCreate(&e), "event");
+    return e;
+  };
   try {
     ck(cudaSetDevice(ctx->device), "cudaSetDevice");
-    ck(cudaEventCreate(&ea), "event");
-    ck(cudaEventCreate(&eb), "event");
+    ck(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "stream");
+    ck(cudaEventCreate(&origin), "event");
+    ck(cudaEventRecord(origin, lanes.acc_stream), "event");
     for (;;) {
       std::vector<Request*> newly;
+      std::vector<int> order;
       {
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
           if (stopping) break;
           admit_locked(newly);
-          if (!newly.empty() || engine.busy() || has_unqueued_passes()) break;
+          if (!newly.empty() || !inflight.empty() || has_unissued_passes()) break;
           cv_work.wait_for(lk, std::chrono::milliseconds(50));
         }
         if (stopping) break;
+        // visiting order of the resident requests with passes left
+        const size_t n = slots.size();
+        for (size_t k = 0; k < n; ++k) {
+          const size_t i = (rr + k) % n;
+          Request* r = slots[i];
+          if (r && r->state == Request::kActive && r->passes_issued < r->passes) order.push_back(int(i));
+        }
+        if (cfg.policy == HASTY_SERVE_SHORTEST_FIRST) {
+          std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            const Request* a = slots[size_t(x)];
+            const Request* b = slots[size_t(y)];
+            return uint64_t(a->passes - a->passes_issued) * a->npix < uint64_t(b->passes - b->passes_issued) * b->npix;
+          });
+        }
       }
       for (Request* r : newly) {
-        ck(cudaMallocAsync(reinterpret_cast<void**>(&r->d_acc), size_t(r->acc_bytes), engine.stream), "cudaMallocAsync (sums)");
-        ck(cudaMemsetAsync(r->d_acc, 0, size_t(r->acc_bytes), engine.stream), "memset sums");
-        JobDev d;
-        std::memset(&d, 0, sizeof(d));
-        d.sc = r->scene->job->sd;
-        d.sc.width = int32_t(r->st.width);
-        d.sc.height = int32_t(r->st.height);
-        d.sc.max_depth = r->st.max_depth;
-        d.sc.rr_start = r->st.roulette_start;
-        d.sc.rr_q = r->st.roulette_q;
-        d.sc.two_strategies = (r->scene->job->host.has_light() && r->st.use_mis) ? 1 : 0;
-        d.acc = r->d_acc;
-        d.seed = r->seed;
-        d.npix = r->npix;
-        d.lanes = r->lanes;
-        engine.set_job(r->slot, d);
+        ck(cudaMallocAsync(reinterpret_cast<void**>(&r->d_acc), size_t(r->acc_bytes), lanes.acc_stream),
+           "cudaMallocAsync (sums)");
+        ck(cudaMemsetAsync(r->d_acc, 0, size_t(r->acc_bytes), lanes.acc_stream), "memset sums");
+        PackedJob& j = jobs[size_t(r->slot)];
+        j.sc = r->scene->job->sd;
+        j.sc.width = int32_t(r->st.width);
+        j.sc.height = int32_t(r->st.height);
+        j.sc.max_depth = r->st.max_depth;
+        j.sc.rr_start = r->st.roulette_start;
+        j.sc.rr_q = r->st.roulette_q;
+        j.sc.two_strategies = (r->scene->job->host.has_light() && r->st.use_mis) ? 1 : 0;
+        j.seed = r->seed;
+        j.npix = int32_t(r->npix);
+        for (int a = 0; a < 3; ++a) j.acc[a] = r->d_acc + size_t(a) * 3 * r->npix;
+        pass_base[size_t(r->slot)] = 0;
+        left[size_t(r->slot)] = r->passes;
       }
-      // queue passes round-robin over the resident requests; a turn issues
-      // consecutive passes of one request up to quantum_samples camera samples
-      // (one pass at least), so small frames do not alternate pass by pass
-      const size_t n = slots.size();
-      while (engine.unissued() < uint64_t(cfg.lookahead_samples) && engine.free_segments() > 0) {
-        bool any = false;
-        for (size_t k = 0; k < n && engine.free_segments() > 0; ++k) {
-          Request* r = slots[(rr + k) % n];
-          if (!r || r->state != Request::kActive || r->passes_issued >= r->passes) continue;
-          int64_t turn = 0;
-          do {
-            engine.append(r->slot, uint32_t(r->passes_issued), r->npix);
-            r->passes_issued++;
-            turn += int64_t(r->npix);
-          } while (r->passes_issued < r->passes && turn < cfg.quantum_samples && engine.free_segments() > 0);
-          any = true;
-          if (engine.unissued() >= uint64_t(cfg.lookahead_samples)) { rr = (rr + k + 1) % n; break; }
+      if (!newly.empty()) lanes.wait_for(lanes.acc_stream);   // sums cleared before any lane adds to them
+      // one batch per free lane
+      while (int(inflight.size()) < lanes.n_lanes && !order.empty()) {
+        std::vector<PackedChunk> chunks =
+            pack_batch(jobs, order, pass_base, left, lanes.lane_paths, cfg.quantum_samples);
+        if (chunks.empty()) break;
+        InFlight f;
+        f.start = take_event();
+        f.end = take_event();
+        lanes.launch(jobs, chunks, true, f.start);
+        ck(cudaEventRecord(f.end, lanes.acc_stream), "event");
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          for (const PackedChunk& c : chunks) {
+            Request* r = slots[size_t(c.job)];
+            r->passes_issued += c.n_passes;
+            if (r->passes_issued == r->passes) f.finishing.push_back(r);
+          }
+          if (!order.empty()) rr = size_t(chunks.back().job + 1) % slots.size();
+          ++batches;
+          launches = lanes.launches;
         }
-        if (!any) break;
+        inflight.push_back(std::move(f));
+        order.erase(std::remove_if(order.begin(), order.end(), [&](int i) { return left[size_t(i)] <= 0; }),
+                    order.end());
       }
-      // the wait above ends only with work queued or in flight
-      {
-        ck(cudaEventRecord(ea, engine.stream), "event");
-        bool bound = false;
-        engine.run_wave(uint32_t(cfg.wave_iterations), &bound);
-        ck(cudaEventRecord(eb, engine.stream), "event");
-        ck(cudaEventSynchronize(eb), "event");
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ea, eb);
-        if (bound) throw ApiError{HASTY_ERR_CUDA, "engine iteration bound reached"};
-        engine.read_done(done);
-        unsigned long long st[MS_COUNT];
-        engine.stats(st);
-        std::vector<Request*> retire;
-        for (Request* r : slots) {
-          if (r && r->state == Request::kActive && r->passes_issued == r->passes &&
-              done[size_t(r->slot)] == uint64_t(r->npix) * uint64_t(r->passes))
-            retire.push_back(r);
-        }
-        for (Request* r : retire) {
-          r->acc.resize(size_t(r->npix) * 9);
-          launch_fold_lanes(r->d_acc, int(r->npix), int(r->lanes), engine.stream);
-          ck(cudaMemcpyAsync(r->acc.data(), r->d_acc, r->acc.size() * sizeof(r->acc[0]), cudaMemcpyDeviceToHost,
-                             engine.stream), "copy sums");
-          ck(cudaFreeAsync(r->d_acc, engine.stream), "cudaFreeAsync (sums)");
-          r->d_acc = nullptr;
-        }
-        if (!retire.empty()) ck(cudaStreamSynchronize(engine.stream), "copy sums");
-        std::lock_guard<std::mutex> lk(mu);
-        device_ms += ms;
-        ++waves;
-        std::memcpy(engine_stats, st, sizeof(st));
-        for (Request* r : retire) {
-          slots[size_t(r->slot)] = nullptr;
-          acc_bytes -= r->acc_bytes;
-          samples += uint64_t(r->npix) * uint64_t(r->passes);
-          finish_locked(r, Request::kDone, HASTY_OK, "");
-        }
+      if (inflight.empty()) continue;
+      // the oldest batch: wait for its accumulation, then retire its requests
+      InFlight f = std::move(inflight.front());
+      inflight.pop_front();
+      ck(cudaEventSynchronize(f.end), "batch");
+      float t_start = 0.f, t_end = 0.f;
+      ck(cudaEventElapsedTime(&t_start, origin, f.start), "event time");
+      ck(cudaEventElapsedTime(&t_end, origin, f.end), "event time");
+      const double busy = std::max(0.0, double(t_end) - std::max(covered_ms, double(t_start)));
+      covered_ms = std::max(covered_ms, double(t_end));
+      spare.push_back(f.start);
+      spare.push_back(f.end);
+      for (Request* r : f.finishing) {
+        r->acc.resize(size_t(r->npix) * 9);
+        ck(cudaMemcpyAsync(r->acc.data(), r->d_acc, size_t(r->acc_bytes), cudaMemcpyDeviceToHost, copy_stream),
+           "copy sums");
+        ck(cudaFreeAsync(r->d_acc, copy_stream), "cudaFreeAsync (sums)");
+        r->d_acc = nullptr;
+      }
+      if (!f.finishing.empty()) ck(cudaStreamSynchronize(copy_stream), "copy sums");
+      unsigned long long st[ST_COUNT];
+      lanes.read_stats(st);
+      std::lock_guard<std::mutex> lk(mu);
+      device_ms += busy;
+      std::memcpy(lane_stats, st, sizeof(st));
+      for (Request* r : f.finishing) {
+        slots[size_t(r->slot)] = nullptr;
+        acc_bytes -= r->acc_bytes;
+        samples += uint64_t(r->npix) * uint64_t(r->passes);
+        finish_locked(r, Request::kDone, HASTY_OK, "");
       }
     }
   } catch (const ApiError& e) {
     std::lock_guard<std::mutex> lk(mu);
     fatal_code = e.code;
     fatal = e.msg;
-    fail_all_locked(e.code, "server engine failed: " + e.msg);
+    fail_all_locked(e.code, "server batch loop failed: " + e.msg);
     stopping = true;
     cv_load.notify_all();
     cv_done.notify_all();
@@ -347,13 +382,18 @@ void hasty_server::engine_loop() {
     std::lock_guard<std::mutex> lk(mu);
     fatal_code = HASTY_ERR_CUDA;
     fatal = e.what();
-    fail_all_locked(HASTY_ERR_CUDA, std::string("server engine failed: ") + e.what());
+    fail_all_locked(HASTY_ERR_CUDA, std::string("server batch loop failed: ") + e.what());
     stopping = true;
     cv_load.notify_all();
     cv_done.notify_all();
   }
-  if (ea) cudaEventDestroy(ea);
-  if (eb) cudaEventDestroy(eb);
+  // batches still in flight finish before their events and sums go away
+  for (int k = 0; k < lanes.n_lanes; ++k) if (lanes.lane_stream[k]) cudaStreamSynchronize(lanes.lane_stream[k]);
+  if (lanes.acc_stream) cudaStreamSynchronize(lanes.acc_stream);
+  for (InFlight& f : inflight) { spare.push_back(f.start); spare.push_back(f.end); }
+  for (cudaEvent_t e : spare) cudaEventDestroy(e);
+  if (origin) cudaEventDestroy(origin);
+  if (copy_stream) { cudaStreamSynchronize(copy_stream); cudaStreamDestroy(copy_stream); }
 }
 
 void hasty_server::loader_loop() {
@@ -382,7 +422,7 @@ void hasty_server::loader_loop() {
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
           if (stopping) { code = HASTY_ERR_STOPPED; msg = "server stopped"; break; }
-          if (engine.bytes + est > cfg.memory_budget) {
+          if (lanes.bytes + est > cfg.memory_budget) {
             code = HASTY_ERR_MEMORY;
             msg = "scene needs " + std::to_string(est) + " device bytes; the server's memory budget cannot hold it";
             break;
@@ -453,14 +493,16 @@ Request* finished_request(hasty_server* s, int64_t id, int aov, size_t w, size_t
 }
 
 void clamp_config(hasty_server_config& c) {
-  c.paths_in_flight = engine_pool_size(c.paths_in_flight);
+  if (c.lanes <= 0) c.lanes = 2;
+  if (c.lanes > kMaxLanes) throw ApiError{HASTY_ERR_ARG, "render lanes must be 1.." + std::to_string(kMaxLanes)};
+  c.paths_in_flight = packed_lane_paths(c.paths_in_flight, 1);
   if (c.max_resident_jobs <= 0) c.max_resident_jobs = 32;
   if (c.max_resident_scenes <= 0) c.max_resident_scenes = 32;
-  if (c.wave_iterations <= 0) c.wave_iterations = 16;
   if (c.memory_budget <= 0) c.memory_budget = kDefaultBudget;
-  if (c.lookahead_samples <= 0) c.lookahead_samples = 4 * c.paths_in_flight;
   if (c.loader_threads <= 0) c.loader_threads = 2;
-  if (c.quantum_samples <= 0) c.quantum_samples = c.paths_in_flight / 2;
+  if (c.quantum_samples <= 0) c.quantum_samples = std::max<int64_t>(1, c.paths_in_flight / 4);
+  if (c.policy != HASTY_SERVE_ROUND_ROBIN && c.policy != HASTY_SERVE_SHORTEST_FIRST)
+    throw ApiError{HASTY_ERR_ARG, "unknown serving policy"};
 }
 
 }  // namespace
@@ -474,13 +516,12 @@ int hasty_server_start(hasty_ctx* ctx, const hasty_server_config* cfg, hasty_ser
     s->ctx = ctx;
     if (cfg) s->cfg = *cfg;
     clamp_config(s->cfg);
-    s->engine.init(ctx, s->cfg.paths_in_flight, s->cfg.max_resident_jobs, 4096,
-                   engine_regen_threshold(s->cfg.regen_fraction, s->cfg.paths_in_flight), 0xFFFFFFF0u);
+    s->lanes.init(ctx, s->cfg.lanes, s->cfg.paths_in_flight);
     s->slots.assign(size_t(s->cfg.max_resident_jobs), nullptr);
     s->t0 = Clock::now();
     s->note_peak();
     hasty_server* raw = s.get();
-    s->engine_thread = std::thread([raw] { raw->engine_loop(); });
+    s->batch_thread = std::thread([raw] { raw->batch_loop(); });
     for (int k = 0; k < s->cfg.loader_threads; ++k) s->loaders.emplace_back([raw] { raw->loader_loop(); });
     *out = s.release();
     return HASTY_OK;
@@ -558,9 +599,7 @@ int hasty_server_read_sums(hasty_server* s, int64_t id, int aov, double* host, s
     if (!s || !host) throw ApiError{HASTY_ERR_ARG, "null argument"};
     std::lock_guard<std::mutex> lk(s->mu);
     Request* r = finished_request(s, id, aov, w, h);
-    const double inv = 1.0 / kFixedScale;
-    for (size_t px = 0; px < size_t(r->npix); ++px)
-      for (int c = 0; c < 3; ++c) host[3 * px + size_t(c)] = 0.0 + double(r->acc[size_t(3 * aov + c) * r->npix + px]) * inv;
+    std::memcpy(host, r->acc.data() + size_t(aov) * 3 * r->npix, sizeof(double) * 3 * r->npix);
     return HASTY_OK;
   });
 }
@@ -570,14 +609,10 @@ int hasty_server_read(hasty_server* s, int64_t id, int aov, float* host, size_t 
     if (!s || !host) throw ApiError{HASTY_ERR_ARG, "null argument"};
     std::lock_guard<std::mutex> lk(s->mu);
     Request* r = finished_request(s, id, aov, w, h);
-    const double inv = 1.0 / kFixedScale;
     const float den = 1e-7f + float(r->passes);
     const float scale = aov == HASTY_AOV_COLOR ? std::pow(2.0f, r->exposure) : 1.0f;
-    for (size_t px = 0; px < size_t(r->npix); ++px)
-      for (int c = 0; c < 3; ++c) {
-        double sum = 0.0 + double(r->acc[size_t(3 * aov + c) * r->npix + px]) * inv;
-        host[3 * px + size_t(c)] = (float(sum) / den) * scale;
-      }
+    const double* sums = r->acc.data() + size_t(aov) * 3 * r->npix;
+    for (size_t i = 0; i < size_t(r->npix) * 3; ++i) host[i] = (float(sums[i]) / den) * scale;
     return HASTY_OK;
   });
 }
@@ -601,13 +636,13 @@ int hasty_server_stats_get(hasty_server* s, hasty_server_stats* out) {
     std::memset(out, 0, sizeof(*out));
     out->submitted = s->submitted; out->admitted = s->admitted; out->completed = s->completed; out->failed = s->failed;
     out->samples = s->samples;
-    out->rays = s->engine_stats[MS_RAYS]; out->shaded = s->engine_stats[MS_SHADED];
-    out->waves = s->waves; out->iterations = s->engine.iterations;
+    out->rays = s->lane_stats[ST_RAYS]; out->shaded = s->lane_stats[ST_SHADED];
+    out->batches = s->batches; out->kernel_launches = s->launches;
     out->device_ms = s->device_ms;
     out->uptime_ms = s->now_ms();
     out->resident_bytes = s->resident_bytes();
     out->peak_resident_bytes = s->peak_bytes;
-    out->engine_bytes = s->engine.bytes;
+    out->engine_bytes = s->lanes.bytes;
     int rj = 0;
     for (Request* r : s->slots) if (r) ++rj;
     out->resident_jobs = rj;
@@ -627,7 +662,7 @@ int hasty_server_wait_idle(hasty_server* s, int32_t timeout_ms) {
     bool ok = timeout_ms < 0 ? (s->cv_done.wait(lk, idle), true)
                              : s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), idle);
     if (!ok) throw ApiError{HASTY_ERR_STOPPED, "requests still running at the timeout"};
-    if (s->fatal_code != HASTY_OK) throw ApiError{s->fatal_code, "server engine failed: " + s->fatal};
+    if (s->fatal_code != HASTY_OK) throw ApiError{s->fatal_code, "server batch loop failed: " + s->fatal};
     return HASTY_OK;
   });
 }
@@ -641,17 +676,17 @@ int hasty_server_stop(hasty_server* s) {
     s->cv_load.notify_all();
     s->cv_done.notify_all();
   }
-  if (s->engine_thread.joinable()) s->engine_thread.join();
+  if (s->batch_thread.joinable()) s->batch_thread.join();
   for (std::thread& t : s->loaders) if (t.joinable()) t.join();
   {
     std::lock_guard<std::mutex> lk(s->mu);
     s->fail_all_locked(HASTY_ERR_STOPPED, "server stopped");
   }
-  // request sums still on the device belong to the engine stream's pool
+  // request sums still on the device were allocated on the accumulation stream
   for (auto& kv : s->requests) {
-    if (kv.second->d_acc) cudaFreeAsync(kv.second->d_acc, s->engine.stream);
+    if (kv.second->d_acc) cudaFreeAsync(kv.second->d_acc, s->lanes.acc_stream);
   }
-  if (s->engine.stream) cudaStreamSynchronize(s->engine.stream);
+  if (s->lanes.acc_stream) cudaStreamSynchronize(s->lanes.acc_stream);
   delete s;
   return HASTY_OK;
 }

@@ -63,11 +63,10 @@ class PmStats(ctypes.Structure):
 
 
 class ServerConfig(ctypes.Structure):
-    _fields_ = [("paths_in_flight", ctypes.c_int64), ("regen_fraction", ctypes.c_float),
-                ("max_resident_jobs", ctypes.c_int32), ("max_resident_scenes", ctypes.c_int32),
-                ("wave_iterations", ctypes.c_int32), ("memory_budget", ctypes.c_int64),
-                ("lookahead_samples", ctypes.c_int64), ("loader_threads", ctypes.c_int32),
-                ("quantum_samples", ctypes.c_int64)]
+    _fields_ = [("paths_in_flight", ctypes.c_int64), ("lanes", ctypes.c_int32), ("max_resident_jobs", ctypes.c_int32),
+                ("max_resident_scenes", ctypes.c_int32), ("loader_threads", ctypes.c_int32),
+                ("memory_budget", ctypes.c_int64), ("quantum_samples", ctypes.c_int64), ("policy", ctypes.c_int32),
+                ("pad", ctypes.c_int32)]
 
 
 class ServerResult(ctypes.Structure):
@@ -80,7 +79,7 @@ class ServerResult(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("admitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
                 ("failed", ctypes.c_uint64), ("samples", ctypes.c_uint64), ("rays", ctypes.c_uint64),
-                ("shaded", ctypes.c_uint64), ("waves", ctypes.c_uint64), ("iterations", ctypes.c_uint64),
+                ("shaded", ctypes.c_uint64), ("batches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64),
                 ("device_ms", ctypes.c_double), ("uptime_ms", ctypes.c_double), ("resident_bytes", ctypes.c_int64),
                 ("peak_resident_bytes", ctypes.c_int64), ("engine_bytes", ctypes.c_int64),
                 ("resident_jobs", ctypes.c_int32), ("resident_scenes", ctypes.c_int32), ("pending", ctypes.c_int32)]

@@ -244,34 +244,39 @@ typedef struct hasty_batch_stats {
 int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, size_t n_jobs,
                        const hasty_batch_config* cfg, hasty_batch_stats* stats);
 
-/* ---- Serving: a request loop over the multi-job engine ---------------------
+/* ---- Serving: a request loop over packed multi-job batches ----------------
  * Requests (a renderJob.json, a pass count, a seed) are admitted while job
  * slots and the device-memory budget allow: scene + BVH + textures of each
- * resident scene, 72 B per pixel and accumulator lane of fixed-point sums per
- * resident request (one lane per 256 samples of a pixel that can be in
- * flight, 1..16: only tiny frames get several, so their pixels' atomics do not
- * serialise), plus the engine's path pool. Scenes are cached by scene file and shared by
+ * resident scene, 72 B per pixel of FP64 sums per resident request, plus the
+ * render lanes' path state. Scenes are cached by scene file and shared by
  * the requests that use them; a scene no request uses is evicted when room is
  * needed. Loader threads parse scenes and build BVHs on the host while the
- * engine renders. Resident requests' passes are interleaved round-robin (a
- * turn issues consecutive passes of one request up to quantum_samples camera
- * samples) in one continuously running engine, so requests that arrive while others render
- * start as soon as path slots free up. A request's result is bit-identical to
- * hasty_batch_render of the same job, seed and pass count, alone or in any mix.
- * The server's functions are internally synchronised (any host thread).
+ * GPU renders. The passes of the resident requests are packed into batches
+ * (as hasty_batch_render's packed mode) that run on `lanes` render lanes, a
+ * new batch being formed whenever a lane frees up, so requests that arrive
+ * while others render join the next batch. Each batch takes at most
+ * quantum_samples camera samples of one request; requests are visited
+ * round-robin (HASTY_SERVE_ROUND_ROBIN) or by fewest samples left
+ * (HASTY_SERVE_SHORTEST_FIRST). A request's sums are added pass by pass in
+ * FP64, so its result is bit-identical to hasty_job_render_passes (and to
+ * hasty_batch_render) of the same job, seed and pass count, alone or in any
+ * mix. The server's functions are internally synchronised (any host thread).
  * No counterpart in the reference (its viewer renders one job per process). */
 typedef struct hasty_server hasty_server;
 
+#define HASTY_SERVE_ROUND_ROBIN 0
+#define HASTY_SERVE_SHORTEST_FIRST 1
+
 typedef struct hasty_server_config {
-  int64_t paths_in_flight;     /* engine path pool; 0 = 4M */
-  float regen_fraction;        /* as hasty_batch_config; 0 = 0.9 */
+  int64_t paths_in_flight;     /* path slots per render lane; 0 = 16M (raised to the largest frame) */
+  int32_t lanes;               /* render lanes (batches in flight), 1..4; 0 = 2 */
   int32_t max_resident_jobs;   /* requests rendering at once; 0 = 32 */
   int32_t max_resident_scenes; /* scenes kept on the device; 0 = 32 */
-  int32_t wave_iterations;     /* engine iterations between host checks; 0 = 16 */
-  int64_t memory_budget;       /* device bytes; 0 = 120 GB */
-  int64_t lookahead_samples;   /* samples queued ahead of the engine; 0 = 4 x paths_in_flight */
   int32_t loader_threads;      /* 0 = 2 */
-  int64_t quantum_samples;     /* camera samples of one request's round-robin turn; 0 = paths_in_flight / 2 */
+  int64_t memory_budget;       /* device bytes; 0 = 120 GB */
+  int64_t quantum_samples;     /* camera samples of one request per batch at most; 0 = paths_in_flight / 4 */
+  int32_t policy;              /* HASTY_SERVE_ROUND_ROBIN (0) or HASTY_SERVE_SHORTEST_FIRST */
+  int32_t pad;
 } hasty_server_config;
 
 typedef struct hasty_server_result {
@@ -289,12 +294,13 @@ typedef struct hasty_server_stats {
   uint64_t submitted, admitted, completed, failed;
   uint64_t samples;            /* camera samples of completed requests */
   uint64_t rays, shaded;
-  uint64_t waves, iterations;
-  double device_ms;            /* device time of the engine's waves (CUDA events) */
+  uint64_t batches;            /* packed batches launched */
+  uint64_t kernel_launches;
+  double device_ms;            /* time the GPU had a batch in flight (CUDA events; overlapping batches once) */
   double uptime_ms;
-  int64_t resident_bytes;      /* engine + scenes + resident requests */
+  int64_t resident_bytes;      /* render lanes + scenes + resident requests */
   int64_t peak_resident_bytes;
-  int64_t engine_bytes;
+  int64_t engine_bytes;        /* render lanes (path state) */
   int32_t resident_jobs, resident_scenes, pending;
 } hasty_server_stats;
 

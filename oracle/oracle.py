@@ -40,6 +40,7 @@ def _load(path: str, prefix: str) -> ctypes.CDLL:
         L.hor_rng_stream.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, I, P]
         L.hor_halton.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
         L.hor_halton.restype = ctypes.c_float
+        L.hor_render_rows.argtypes = [P] + [I] * 8 + [P] * 5
     _libs[path] = L
     return L
 
@@ -93,6 +94,18 @@ class Oracle(_Base):
 
     def set_seed(self, seed: int) -> None:
         self.L.hor_set_seed(self.h, ctypes.c_uint64(seed))
+
+    def render_rows(self, pass0: int, npasses: int, y0: int, row_stride: int, n_rows: int, nthreads: int = 0) -> dict:
+        """Full-width rows y0, y0 + row_stride, ... (n_rows of them) over
+        passes [pass0, pass0 + npasses); arrays hold the rendered rows."""
+        w = self.info()["width"]
+        c = np.zeros((n_rows, w, 3)); c2 = np.zeros_like(c); n = np.zeros_like(c); a = np.zeros_like(c)
+        st = np.zeros(6, np.uint64)
+        rc = self.L.hor_render_rows(self.h, pass0, npasses, 0, y0, w, n_rows, row_stride, nthreads, c.ctypes.data,
+                                    c2.ctypes.data, n.ctypes.data, a.ctypes.data, st.ctypes.data)
+        if rc != 0:
+            raise RuntimeError("bad row stride")
+        return {"color": c, "color_sq": c2, "normal": n, "albedo": a, "stats": st}
 
     def intersect(self, rays: np.ndarray, fp64: bool = False, brute: bool = False):
         r = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)

@@ -68,9 +68,20 @@ void hor_set_seed(void* p, uint64_t seed) { static_cast<Handle*>(p)->sc.settings
 // color (NaN samples dropped, as PathTracing.cpp:132-142), its square,
 // normal and albedo AOVs. Buffers are w*h*3 doubles, row-major.
 // stats[6]: rays, nan samples, bvh nodes visited, triangle tests, shaded vertices, paths.
+// Rows y0, y0 + row_stride, ..., (h rows) of the same window; the buffers
+// hold the h rendered rows.
+int hor_render_rows(void* p, int pass0, int npasses, int x0, int y0, int w, int h, int row_stride, int nthreads,
+                    double* color, double* color_sq, double* normal, double* albedo, uint64_t* stats);
+
 int hor_render(void* p, int pass0, int npasses, int x0, int y0, int w, int h, int nthreads,
                double* color, double* color_sq, double* normal, double* albedo, uint64_t* stats) {
+  return hor_render_rows(p, pass0, npasses, x0, y0, w, h, 1, nthreads, color, color_sq, normal, albedo, stats);
+}
+
+int hor_render_rows(void* p, int pass0, int npasses, int x0, int y0, int w, int h, int row_stride, int nthreads,
+                    double* color, double* color_sq, double* normal, double* albedo, uint64_t* stats) {
   const Scene& sc = static_cast<Handle*>(p)->sc;
+  if (row_stride < 1) return -1;
   if (nthreads < 1) nthreads = int(std::max(1u, std::thread::hardware_concurrency()));
   std::atomic<int> next_row{0};
   std::vector<RenderStats> per(static_cast<size_t>(nthreads));
@@ -84,7 +95,7 @@ int hor_render(void* p, int pass0, int npasses, int x0, int y0, int w, int h, in
         double c[3] = {0, 0, 0}, c2[3] = {0, 0, 0}, nn[3] = {0, 0, 0}, aa[3] = {0, 0, 0};
         for (int ps = pass0; ps < pass0 + npasses; ++ps) {
           V3 n, a;
-          V3 L = render_sample(sc, uint32_t(x0 + xx), uint32_t(y0 + row), uint32_t(ps), n, a, st);
+          V3 L = render_sample(sc, uint32_t(x0 + xx), uint32_t(y0 + row * row_stride), uint32_t(ps), n, a, st);
           if (L != L) { st.nan++; continue; }
           for (int q = 0; q < 3; ++q) { c[q] += L[q]; c2[q] += double(L[q]) * L[q]; nn[q] += n[q]; aa[q] += a[q]; }
         }

@@ -49,14 +49,21 @@ def test_device_tree_equals_host_tree(name, binary):
     assert (g[0] >= 0).mean() > 0.05
 
 
+def _sphere_field_800():
+    """The 1,024,002-triangle sphere field (800 icospheres), generated once."""
+    from hastyrenderer_gb300 import scenes
+    base = os.path.join(tempfile.gettempdir(), "hasty_test_sphere_field_800")
+    path = os.path.join(base, "renderJob.json")
+    if not os.path.exists(path):
+        scenes.sphere_field(base, seed=0, n_spheres=800, subdiv=3, width=1920, height=1080, spp=256, max_depth=12)
+    return path
+
+
 def test_device_tree_full_size():
     """1,024,002 triangles: identical hits on random rays; the device build
     is the default and reports its time."""
-    import bench
     from hastyrenderer_gb300 import Context
-    base = os.path.join(tempfile.gettempdir(), "hasty_bench_c1")
-    os.makedirs(base, exist_ok=True)
-    path = bench.make_job(base)
+    path = _sphere_field_800()
     rng = np.random.default_rng(11)
     o = rng.uniform([-10, 0, -10], [10, 20, 10], (200000, 3))
     d = rng.normal(size=(200000, 3))
@@ -79,10 +86,7 @@ def test_device_layout_equals_host_layout(name):
     import ctypes
     from hastyrenderer_gb300 import native
     if name == "full":
-        import bench
-        base = os.path.join(tempfile.gettempdir(), "hasty_bench_c1")
-        os.makedirs(base, exist_ok=True)
-        path = bench.make_job(base)
+        path = _sphere_field_800()
     else:
         path = os.path.join(GOLDEN, "scenes", name, "renderJob.json")
     info = (ctypes.c_int64 * 8)()

@@ -1,8 +1,9 @@
-"""Serving (hasty_server_*): continuous batching of requests over the
-multi-job engine. A request's sums are bit-identical to hasty_batch_render of
-the same job, seed and pass count (fixed-point accumulation is independent of
-the mix and of the pass interleaving); admission respects the memory budget;
-scenes are shared; failures are reported per request."""
+"""Serving (hasty_server_*): continuous batching of requests over packed
+multi-job batches. A request's sums are bit-identical to hasty_batch_render
+and to hasty_job_render_passes of the same job, seed and pass count (passes
+are added in order in FP64 whatever they are batched with), under either
+batch-formation policy; admission respects the memory budget; scenes are
+shared; failures are reported per request."""
 import os
 import shutil
 import tempfile
@@ -24,7 +25,7 @@ def _batch_sums(name, passes, seed):
     from hastyrenderer_gb300 import RenderJob, batch_render
     j = RenderJob(_path(name))
     j.set_seed(seed)
-    batch_render([j], [passes], mode=1)
+    batch_render([j], [passes])
     return [j.read_sums(a)[0] for a in (0, 1, 2)], j
 
 
@@ -43,7 +44,7 @@ def test_server_results_equal_batch():
     from hastyrenderer_gb300 import Server
     reqs = [("cornell", 3, 11), ("field", 5, 12), ("room", 2, 13), ("room_nomis", 4, 14), ("cornell", 6, 15),
             ("field", 1, 16)]
-    with Server(paths_in_flight=1 << 15, max_resident_jobs=4, wave_iterations=4) as srv:
+    with Server(paths_in_flight=1 << 15, max_resident_jobs=4, quantum_samples=3000) as srv:
         ids = [srv.submit(_path(n), passes=p, seed=s) for n, p, s in reqs]
         got = _collect(srv, len(ids))
         st = srv.stats()
@@ -61,10 +62,12 @@ def test_server_results_equal_batch():
             srv.release(rid)
 
 
-def test_server_alone_equals_mixed():
-    """The same request alone on an idle server and among many others."""
-    from hastyrenderer_gb300 import Server
-    with Server(paths_in_flight=1 << 14, wave_iterations=2) as srv:
+@pytest.mark.parametrize("policy", [0, 1], ids=["round_robin", "shortest_first"])
+def test_server_alone_equals_mixed(policy):
+    """The same request alone on an idle server and among many others, and
+    equal to the single-job path."""
+    from hastyrenderer_gb300 import RenderJob, Server
+    with Server(paths_in_flight=1 << 14, quantum_samples=2048, policy=policy, lanes=3) as srv:
         rid = srv.submit(_path("room"), passes=3, seed=99)
         _collect(srv, 1)
         alone = srv.read_sums(rid)
@@ -73,10 +76,14 @@ def test_server_alone_equals_mixed():
         others += [srv.submit(_path(n), passes=2, seed=8) for n in NAMES]
         _collect(srv, len(others) + 1)
         assert np.array_equal(srv.read_sums(rid2), alone)
+        plain = RenderJob(_path("room"))
+        plain.set_seed(99)
+        plain.render_passes(3, sync=True)
+        assert np.array_equal(plain.read_sums()[0], alone)
 
 
 def test_server_memory_budget_admission():
-    """A budget that holds the engine, one scene and one request at a time:
+    """A budget that holds the render lanes, one scene and one request at a time:
     requests still all finish, one after another, within the budget."""
     from hastyrenderer_gb300 import Server
     cfg = dict(paths_in_flight=1 << 14, max_resident_jobs=4)
@@ -118,7 +125,7 @@ def test_server_failures_reported_per_request():
 
 def test_server_stop_with_work_in_flight():
     from hastyrenderer_gb300 import Server
-    srv = Server(paths_in_flight=1 << 14, wave_iterations=1)
+    srv = Server(paths_in_flight=1 << 14, quantum_samples=1024)
     for n in NAMES * 3:
         srv.submit(_path(n), passes=64)
     srv.stop()   # returns; unfinished requests are dropped
