@@ -323,8 +323,31 @@ def run_reference_arm(args, rank: int):
 # so each kernel's time is its own).
 
 def kernel_rooflines(workload: str, stage: dict, hbm: float, peak_kind: str, sm_mhz, costs):
-    """stage: trace_ms, shade_ms, trace_launches, rays, shaded of a
-    stage-timed run. Returns (kernels, dominant)."""
+    """stage: trace_ms, shade_ms, trace_launches, path_ms, path_launches,
+    rays, shaded, paths of a stage-timed run (wavefront jobs, path-kernel
+    jobs or both). Returns (kernels, dominant)."""
+    kernels = []
+    mhz = sm_mhz or 2070.0
+    if stage["path_launches"]:
+        n = stage["path_launches"]
+        ms = stage["path_ms"] / n
+        c = COUNTERS.get(workload, {}).get("k_paths", {})
+        k = {"kernel": "k_paths", "unit_of_work": "camera sample", "units_per_launch": stage["paths"] / n,
+             "ms_per_launch": ms, "bound": "issue", "unit": "G warp-inst/s",
+             "traffic": c["dram_bytes_per_sample"] * stage["paths"] / n if c.get("dram_bytes_per_sample") else None}
+        if c.get("warp_inst_per_sample"):
+            ach = c["warp_inst_per_sample"] * stage["paths"] / n / (ms * 1e-3) * 1e-9
+            peak = SMS * ISSUE_PER_SM_PER_CLOCK * mhz * 1e-3
+            k.update(achieved=ach, peak=peak, frac=ach / peak,
+                     peak_kind=f"{SMS} SMs x {ISSUE_PER_SM_PER_CLOCK} schedulers x {mhz:.0f} MHz (median under load)",
+                     active_lanes_per_inst=c["thread_inst_per_sample"] / c["warp_inst_per_sample"])
+        else:
+            k.update(achieved=None, peak=None, frac=None, note="instruction counts not captured for this workload")
+        kernels.append(k)
+    if not stage["trace_launches"]:
+        dominant = dict(max(kernels, key=lambda k: k["ms_per_launch"] * 1.0))
+        dominant["note"] = "dominant kernel by device time, timed alone (stage timing keeps one render lane)"
+        return kernels, dominant
     n = max(stage["trace_launches"], 1)
     cnt = COUNTERS.get(workload, {})
     rays_l = stage["rays"] / n
@@ -332,7 +355,6 @@ def kernel_rooflines(workload: str, stage: dict, hbm: float, peak_kind: str, sm_
     k_trace = {"kernel": "k_trace", "unit_of_work": "traced ray", "units_per_launch": rays_l, "ms_per_launch": trace_ms}
     c = cnt.get("k_trace", {})
     k_trace["traffic"] = c["dram_bytes_per_ray"] * rays_l if c.get("dram_bytes_per_ray") else None
-    mhz = sm_mhz or 2070.0
     if c.get("warp_inst_per_ray"):
         achieved = c["warp_inst_per_ray"] * rays_l / (trace_ms * 1e-3) * 1e-9
         peak = SMS * ISSUE_PER_SM_PER_CLOCK * mhz * 1e-3
@@ -359,24 +381,34 @@ def kernel_rooflines(workload: str, stage: dict, hbm: float, peak_kind: str, sm_
                "frac": ach / hbm, "peak_kind": peak_kind, "bytes_per_unit": B_SHADE,
                "algorithmic_bytes_per_launch": alg,
                "traffic": c["dram_bytes_per_vertex"] * verts_l if c.get("dram_bytes_per_vertex") else None}
-    kernels = [k_trace, k_shade]
-    dominant = dict(max(kernels, key=lambda k: k["ms_per_launch"]))
+    kernels += [k_trace, k_shade]
+    # dominant by total device time of the run
+    totals = {"k_paths": stage["path_ms"], "k_trace": stage["trace_ms"], "k_resolve+k_sample": stage["shade_ms"]}
+    dominant = dict(max(kernels, key=lambda k: totals[k["kernel"]]))
     dominant["note"] = "dominant kernel by device time, timed alone (stage timing keeps one render lane)"
     return kernels, dominant
 
 
 def stage_split(job_list, passes_list):
     """Renders the jobs one after another with stage timing and returns the
-    summed stage times and work (for the rooflines)."""
-    out = {"trace_ms": 0.0, "shade_ms": 0.0, "trace_launches": 0, "rays": 0, "shaded": 0, "kernel_ms": 0.0}
+    summed stage times and work for the rooflines: rays and shaded vertices
+    of the wavefront jobs, camera samples of the path-kernel jobs."""
+    out = {"trace_ms": 0.0, "shade_ms": 0.0, "trace_launches": 0, "rays": 0, "shaded": 0, "kernel_ms": 0.0,
+           "path_ms": 0.0, "path_launches": 0, "paths": 0}
     for job, p in zip(job_list, passes_list):
+        path_kernel = job.info.path_kernel
         job.set_stage_timing(True)
         s0 = job.stats()
         job.render_passes(p, sync=True)
         s1 = job.stats()
         job.set_stage_timing(False)
-        for k in out:
+        for k in ("trace_ms", "shade_ms", "trace_launches", "kernel_ms", "path_ms", "path_launches"):
             out[k] += s1[k] - s0[k]
+        if path_kernel:
+            out["paths"] += s1["paths"] - s0["paths"]
+        else:
+            out["rays"] += s1["rays"] - s0["rays"]
+            out["shaded"] += s1["shaded"] - s0["shaded"]
     return out
 
 
@@ -536,6 +568,7 @@ def run_single(args):
                        "l2": "working set > L2 (path state + scene), no flush", "parallelism": f"replicas x{world}"},
             "mrays_per_s": (s1["rays"] - s0["rays"]) * world / t * 1e-6,
             "stage_ms_per_step": {"trace": stage["trace_ms"] / args.steps, "shade": stage["shade_ms"] / args.steps,
+                                  "path_kernel": stage["path_ms"] / args.steps,
                                   "one_lane_total": stage["kernel_ms"] / args.steps,
                                   "note": "same steps with stage timing (one render lane); the timed run uses two"},
             "wall_ms_per_step": wall / args.steps * 1e3,
@@ -668,6 +701,7 @@ def run_batch(args):
         "gpu_launches": launches,
         "roofline": roof, "kernels": kernels,
         "stage_ms_per_step": {"trace": stage["trace_ms"] * 8, "shade": stage["shade_ms"] * 8,
+                              "path_kernel": stage["path_ms"] * 8,
                               "note": "1/8 of every job's passes with stage timing (one render lane), scaled by 8"},
         "cpu_baseline": cpu,
         "e2e": {"value": total / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),

@@ -24,6 +24,8 @@ class Context:
 
     BINARY_BVH = 1   # HASTY_CTX_BINARY_BVH
     HOST_BVH = 2     # HASTY_CTX_HOST_BVH: build the BVH on the host instead of the GPU
+    WAVEFRONT = 4    # HASTY_CTX_WAVEFRONT: never the path kernel
+    PATH_KERNEL = 8  # HASTY_CTX_PATH_KERNEL: the path kernel for every scene
 
     def __init__(self, device: int = 0, flags: int = 0):
         self._h = ctypes.c_void_p()

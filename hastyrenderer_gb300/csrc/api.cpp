@@ -62,7 +62,6 @@ void hasty::carve_paths(PathsDev& p, int64_t cap, int n_stats, const std::functi
   p.rq[0] = static_cast<int32_t*>(A(2 * c * sizeof(int32_t)));
   p.rq[1] = static_cast<int32_t*>(A(2 * c * sizeof(int32_t)));
   p.counts = static_cast<uint32_t*>(A(kCountSlots * sizeof(uint32_t)));
-  p.vtx = static_cast<float4*>(A(6 * c * sizeof(float4)));
   p.sq = static_cast<int32_t*>(A(c * sizeof(int32_t)));
   p.out_color = static_cast<float4*>(A(c * sizeof(float4)));
   p.out_normal = static_cast<float4*>(A(c * sizeof(float4)));
@@ -96,7 +95,7 @@ namespace {
 // Frees the path buffers of p (not the statistics it points to).
 void release_path_buffers(hasty_job& j, PathsDev& p) {
   void* bufs[] = {p.rng, p.thr, p.rad, p.pend_b, p.nee_c, p.nee_t, p.med, p.med_geom, p.ray_o, p.ray_d, p.hit,
-                  p.pq[0], p.pq[1], p.rq[0], p.rq[1], p.counts, p.vtx, p.sq, p.out_color, p.out_normal, p.out_albedo};
+                  p.pq[0], p.pq[1], p.rq[0], p.rq[1], p.counts, p.sq, p.out_color, p.out_normal, p.out_albedo};
   for (void* b : bufs) j.release(b);
   unsigned long long* stats = p.stats;
   p = PathsDev{};
@@ -227,8 +226,8 @@ void clear_accumulators(hasty_job& j) {
   ck(cudaMemsetAsync(j.pd.stats, 0, sizeof(unsigned long long) * ST_COUNT, j.stream), "memset stats");
   j.lanes_wait_main = true;
   j.samples_done = 0;
-  j.kernel_ms = j.trace_ms = j.shade_ms = 0.0;
-  j.trace_launches = j.kernel_launches = 0;
+  j.kernel_ms = j.trace_ms = j.shade_ms = j.path_ms = 0.0;
+  j.trace_launches = j.kernel_launches = j.path_launches = 0;
 }
 
 // Up to 16M camera samples in flight per render lane (about 7 GB of path
@@ -250,6 +249,34 @@ int64_t default_capacity(int64_t npix) {
 // 4: 940.
 constexpr int kLaneTraceBlocksPerSM = 5;
 }  // namespace
+
+// Largest scene the path kernel takes by default: none. Measured on GB300
+// (M samples/s, path kernel vs wavefront): Cornell box 1024x768 475 vs 607,
+// 128x128 389 vs 496; 64k-triangle field 1024x768 924 vs 2365; 1.02M
+// triangles 256x192 318 vs 822, at 64, 96 or 128 registers per thread. Its
+// path state stays in L2, but the wavefront's shading kernels are bound by
+// load latency at 35-52% of HBM bandwidth, not by their traffic, and the
+// path kernel loses more to idle lanes, block barriers and undivided
+// traversal than it saves. HASTY_PATH_KERNEL_TRIS (or HASTY_CTX_PATH_KERNEL)
+// selects it.
+constexpr int64_t kPathKernelMaxTris = 0;
+
+int64_t hasty::path_kernel_max_triangles() {
+  static const int64_t v = [] {
+    const char* e = std::getenv("HASTY_PATH_KERNEL_TRIS");
+    return e ? std::max<int64_t>(0, std::atoll(e)) : kPathKernelMaxTris;
+  }();
+  return v;
+}
+
+bool hasty::use_path_kernel(const hasty_ctx* ctx, const SceneDev& sc) {
+  if (sc.max_depth <= 0 || (ctx->flags & HASTY_CTX_WAVEFRONT)) return false;
+  return (ctx->flags & HASTY_CTX_PATH_KERNEL) || int64_t(sc.n_tris) <= path_kernel_max_triangles();
+}
+
+void hasty::alloc_path_slots(PathsDev& p, const std::function<void*(size_t)>& alloc, unsigned long long* stats) {
+  carve_paths(p, path_slots(), ST_COUNT, alloc, stats);
+}
 
 // HASTY_LANE_TRACE_BLOCKS overrides it (0: no cap).
 int hasty::lane_trace_blocks() {
@@ -284,8 +311,6 @@ void render_batch(hasty_job& j, int n_passes, int lane, bool more_batches) {
   }
   const int trace_cap = (j.stage_timing || !other_busy) ? 0 : lane_trace_blocks();
   if (j.lane_free_valid[lane]) ck(cudaStreamWaitEvent(ls, j.lane_free[lane], 0), "lane wait");
-  launch_raygen(j.sd, pd, b, ls);
-  int max_paths = b.n_paths;
   auto timed = [&](int stage, auto&& fn) {
     if (!j.stage_timing) { fn(); return; }
     cudaEvent_t a, c;
@@ -295,12 +320,25 @@ void render_batch(hasty_job& j, int n_passes, int lane, bool more_batches) {
     ck(cudaEventRecord(c, ls), "event record");
     j.pending_events.push_back({a, c, stage});
   };
-  for (int bounce = 0; bounce < j.sd.max_depth; ++bounce) {
-    int q = bounce & 1;
-    timed(1, [&] { launch_trace(j.sd, pd, q, 2 * max_paths, ls, trace_cap); });
-    ck(cudaMemsetAsync(&pd.counts[q ^ 1], 0, sizeof(uint32_t), ls), "memset count");
-    ck(cudaMemsetAsync(&pd.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), ls), "memset count");
-    timed(2, [&] { launch_shade(j.sd, pd, b, q, max_paths, ls); });
+  if (j.path_kernel) {
+    PathsDev& slots = j.slots[lane];
+    if (!slots.rng) {
+      alloc_path_slots(slots, [&](size_t bytes) { return static_cast<void*>(j.alloc<uint8_t>(bytes)); }, j.pd.stats);
+      ck(cudaMemsetAsync(slots.counts, 0, sizeof(uint32_t) * kCountSlots, ls), "memset counts");
+    }
+    timed(3, [&] { launch_paths(j.sd, b, slots, pd, ls); });
+    j.path_launches += 1;
+  } else {
+    launch_raygen(j.sd, pd, b, ls);
+    const int max_paths = b.n_paths;
+    for (int bounce = 0; bounce < j.sd.max_depth; ++bounce) {
+      int q = bounce & 1;
+      timed(1, [&] { launch_trace(j.sd, pd, q, 2 * max_paths, ls, trace_cap); });
+      ck(cudaMemsetAsync(&pd.counts[q ^ 1], 0, sizeof(uint32_t), ls), "memset count");
+      ck(cudaMemsetAsync(&pd.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), ls), "memset count");
+      timed(2, [&] { launch_shade(j.sd, pd, b, q, max_paths, ls); });
+    }
+    j.trace_launches += uint64_t(j.sd.max_depth);
   }
   ck(cudaEventRecord(j.lane_done[lane], ls), "lane event");
   ck(cudaStreamWaitEvent(j.stream, j.lane_done[lane], 0), "lane wait");
@@ -308,9 +346,9 @@ void render_batch(hasty_job& j, int n_passes, int lane, bool more_batches) {
   ck(cudaGetLastError(), "kernel launch");
   ck(cudaEventRecord(j.lane_free[lane], j.stream), "lane event");
   j.lane_free_valid[lane] = true;
-  j.trace_launches += uint64_t(j.sd.max_depth);
-  // raygen and accumulate, and per bounce: trace, resolve, sample
-  j.kernel_launches += uint64_t(2 + 3 * j.sd.max_depth);
+  // wavefront: raygen and accumulate, and per bounce trace, resolve, sample;
+  // path kernel: it and accumulate
+  j.kernel_launches += j.path_kernel ? 2u : uint64_t(2 + 3 * j.sd.max_depth);
   j.samples_done += n_passes;
 }
 
@@ -336,6 +374,7 @@ void hasty::finish_job_load(hasty_job& job, bool plain) {
   ck(cudaSetDevice(j->ctx->device), "cudaSetDevice");
   ck(cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking), "stream");
   upload_scene(*j);
+  j->path_kernel = use_path_kernel(j->ctx, j->sd);
   int64_t npix = int64_t(j->sd.width) * j->sd.height;
   j->capacity = default_capacity(npix);
   if (plain) {
@@ -424,6 +463,7 @@ int hasty_job_info_get(hasty_job* job, hasty_job_info* out) {
     out->parse_ms = job->parse_ms;
     out->upload_ms = job->upload_ms;
     out->paths_in_flight = job->capacity;
+    out->path_kernel = job->path_kernel ? 1 : 0;
     return HASTY_OK;
   });
 }
@@ -548,6 +588,7 @@ int hasty_job_stats_get(hasty_job* job, hasty_stats* out) {
     out->kernel_ms = job->kernel_ms;
     out->trace_ms = job->trace_ms; out->shade_ms = job->shade_ms;
     out->trace_launches = job->trace_launches; out->kernel_launches = job->kernel_launches;
+    out->path_ms = job->path_ms; out->path_launches = job->path_launches;
     return HASTY_OK;
   });
 }

@@ -9,7 +9,9 @@
 // Random numbers are drawn in the reference's order, one PCG32 stream per
 // (job seed, pixel, pass).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include "device_common.cuh"
+#include "traverse.cuh"
 #include "wavefront.h"
 
 namespace hasty {
@@ -145,6 +147,30 @@ __device__ __forceinline__ SlotPos raygen_pos(const ChunkTable& t, int s) { retu
 __device__ __forceinline__ int max_depth_of(const OneJob& j) { return j.sc.max_depth; }
 __device__ __forceinline__ int max_depth_of(const ChunkTable&) { return 1; }   // batches of positive depths only
 
+// Camera sample sp of job scene sc into path slot s: the camera ray (queued
+// as the slot's BSDF ray), throughput 1, AOVs cleared. Returns whether the
+// path traces at all (max_depth > 0).
+__device__ __forceinline__ bool start_path(const SceneDev& sc, const PathsDev& P, int s, const SlotPos& sp,
+                                           int& capped) {
+  const uint32_t chunk_bits = uint32_t(sp.chunk) << PF_CHUNK_SHIFT;
+  const uint32_t px = sp.px, pass = sp.pass;
+  int x = int(px % uint32_t(sc.width)), y = int(px / uint32_t(sc.width));
+  Rng r; r.seed(path_key(sp.seed, px, pass));
+  float ox = halton(2, pass), oy = halton(3, pass);
+  V3 o, d;
+  camera_ray(sc.cam, r, float(x) + ox, float(y) + oy, float(sc.width), float(sc.height), o, d, capped);
+  P.rng[s] = r.state;
+  P.thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
+  P.rad[s] = make_float4(0.f, 0.f, 0.f, __uint_as_float(PF_CAMERA | PF_PEND_B | chunk_bits));
+  P.out_color[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  P.out_albedo[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (sc.max_depth <= 0) return false;
+  P.ray_o[2 * s] = f4(o, __uint_as_float(uint32_t(sp.chunk)));
+  P.ray_d[2 * s] = f4(d, 0.f);
+  return true;
+}
+
 template <class Src>
 __global__ void __launch_bounds__(256) k_raygen(const __grid_constant__ Src src, PathsDev P) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -156,24 +182,10 @@ __global__ void __launch_bounds__(256) k_raygen(const __grid_constant__ Src src,
   }
   if (s >= n_paths) return;
   const SlotPos sp = raygen_pos(src, s);
-  const uint32_t chunk_bits = uint32_t(sp.chunk) << PF_CHUNK_SHIFT;
-  const SceneDev& sc = scene_of(src, chunk_bits);
-  const uint32_t px = sp.px, pass = sp.pass;
-  int x = int(px % uint32_t(sc.width)), y = int(px / uint32_t(sc.width));
-  Rng r; r.seed(path_key(sp.seed, px, pass));
-  float ox = halton(2, pass), oy = halton(3, pass);
-  V3 o, d; int capped = 0;
-  camera_ray(sc.cam, r, float(x) + ox, float(y) + oy, float(sc.width), float(sc.height), o, d, capped);
+  int capped = 0;
+  const bool traced = start_path(scene_of(src, uint32_t(sp.chunk) << PF_CHUNK_SHIFT), P, s, sp, capped);
   if (capped) atomicAdd(&P.stats[ST_TRIAL_CAP], 1ull);
-  P.rng[s] = r.state;
-  P.thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
-  P.rad[s] = make_float4(0.f, 0.f, 0.f, __uint_as_float(PF_CAMERA | PF_PEND_B | chunk_bits));
-  P.out_color[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-  P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-  P.out_albedo[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (sc.max_depth <= 0) return;
-  P.ray_o[2 * s] = f4(o, __uint_as_float(uint32_t(sp.chunk)));
-  P.ray_d[2 * s] = f4(d, 0.f);
+  if (!traced) return;
   P.pq[0][s] = s;
   P.rq[0][s] = 2 * s;
 }
@@ -183,8 +195,8 @@ __global__ void __launch_bounds__(256) k_raygen(const __grid_constant__ Src src,
 // continue:
 //  * resolve_path: resolve the previous vertex's light sample and the BSDF
 //    sample's hit (self-intersection, MIS weight, depth limit, miss, emitter,
-//    Russian roulette); a path that survives leaves its vertex record (the
-//    interaction and the transmittance-and-roulette factor) for
+//    Russian roulette); a path that survives leaves its transmittance-and-
+//    roulette factor (its hit stays in place) for
 //  * sample_path: the light strategy's sample and the BSDF sample of the
 //    vertex, queued as the slot's two rays.
 // The arithmetic is the single-kernel bounce's, in the same order.
@@ -198,29 +210,6 @@ __device__ __forceinline__ int shade_class(const MaterialDev& m) {
   return 1;
 }
 struct SampleRes { bool keep, emitB, emitL; int overflow, capped; V3 L; };
-
-__device__ __forceinline__ void store_vertex(const PathsDev& P, int s, const Inter& it, V3 tl) {
-  float4* v = P.vtx + 6 * int64_t(s);
-  v[0] = make_float4(it.x.x, it.x.y, it.x.z, it.h);
-  v[1] = make_float4(it.ng.x, it.ng.y, it.ng.z, it.u);
-  v[2] = make_float4(it.ns.x, it.ns.y, it.ns.z, it.v);
-  v[3] = make_float4(it.tan.x, it.tan.y, it.tan.z, __int_as_float(it.tri));
-  v[4] = make_float4(it.bit.x, it.bit.y, it.bit.z, __int_as_float(it.mat));
-  v[5] = make_float4(__uint_as_float(it.geom | (it.has_uv ? 0x80000000u : 0u)), tl.x, tl.y, tl.z);
-}
-
-__device__ __forceinline__ void load_vertex(const PathsDev& P, int s, Inter& it, V3& tl) {
-  const float4* v = P.vtx + 6 * int64_t(s);
-  float4 a = v[0], b = v[1], c = v[2], d = v[3], e = v[4], f = v[5];
-  it.x = xyz(a); it.h = a.w;
-  it.ng = xyz(b); it.u = b.w;
-  it.ns = xyz(c); it.v = c.w;
-  it.tan = xyz(d); it.tri = __float_as_int(d.w);
-  it.bit = xyz(e); it.mat = __float_as_int(e.w);
-  uint32_t g = __float_as_uint(f.x);
-  it.geom = g & 0x7FFFFFFFu; it.has_uv = (g & 0x80000000u) != 0;
-  tl = V3(f.y, f.z, f.w);
-}
 
 __device__ __forceinline__ ResolveRes resolve_path(const SceneDev& sc, const PathsDev& P, int s, uint64_t key) {
   ResolveRes res;
@@ -308,7 +297,11 @@ __device__ __forceinline__ ResolveRes resolve_path(const SceneDev& sc, const Pat
             tl = tl / (1.0f - qrr);
             P.rng[s] = r.state;
             P.thr[s] = f4(thr, thr4.w);
-            store_vertex(P, s, it, tl);
+            // the sample kernel rebuilds the interaction from the hit (as
+            // here: inter_from_hit of the same triangle and u, v) and takes
+            // the transmittance-and-roulette factor from pend_b, which this
+            // bounce has consumed
+            P.pend_b[s] = f4(tl, 0.f);
             flags = (flags & (PF_WL_MASK | PF_NMED_MASK | PF_CHUNK_MASK)) | uint32_t(depth);
             res.sample = true;
             res.cls = shade_class(m);
@@ -334,9 +327,9 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
   uint32_t flags = __float_as_uint(rad.w);
   V3 L = xyz(rad);
   const int depth = int(flags & PF_DEPTH_MASK);
-  Inter it;
-  V3 tl;
-  load_vertex(P, s, it, tl);
+  const float4 hb = P.hit[2 * s];
+  const Inter it = inter_from_hit(sc, __float_as_int(hb.w), hb.y, hb.z);
+  const V3 tl = xyz(P.pend_b[s]);
   const MaterialDev& m = sc.mats[it.mat];
   const V3 thr = xyz(P.thr[s]);
   const V3 d = xyz(P.ray_d[2 * s]);
@@ -518,6 +511,140 @@ __global__ void __launch_bounds__(kSampleThreads, 2) k_sample(const __grid_const
   }
 }
 
+// ---- Path kernel for cache-resident scenes ---------------------------------
+// One persistent thread carries one camera sample through all of its bounces
+// (closest hits, resolve, sample) and takes the next sample of the batch when
+// its path ends (one atomic per warp hands out samples in order). Its path
+// state lives in a pool of one slot per resident thread (a few tens of MB,
+// which stays in L2) instead of a batch-sized pool that every bounce streams
+// through HBM; each finished sample goes to the batch's output arrays at its
+// sample index, as the wavefront leaves it. The bounce is resolve_path and
+// sample_path, the wavefront's own code, and random numbers are keyed by the
+// sample, so every sample's value is the wavefront's bit for bit. For scenes
+// whose BVH and triangles stay in L1/L2, where the wavefront's per-bounce
+// path-state traffic, not the closest-hit search, bounds the rate.
+
+template <int KIND> struct PathTrav { using T = TravBinary; };
+template <> struct PathTrav<1> { using T = TravWide; };
+
+template <int KIND>
+__device__ __forceinline__ float4 closest_hit(const SceneDev& sc, float4 o, float4 d, bool first_hit) {
+  typename PathTrav<KIND>::T tr;
+  typename PathTrav<KIND>::T::Entry stack[PathTrav<KIND>::T::kDepth];
+  tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
+  tr.any = first_hit;
+  while (!tr.step(sc.nodes, sc.isect_tris, stack)) {}
+  return make_float4(tr.best.t, tr.best.u, tr.best.v, __int_as_float(tr.best.tri));
+}
+
+// The threads of a block run the loop together until all of them are done,
+// in three stages separated by block barriers: closest hits of the pending
+// rays, resolve, sample. All warps of a block are then in the same stage's
+// code at once, as in the wavefront's separate kernels, rather than spread
+// over the whole kernel (whose code does not fit the instruction cache).
+// Lanes without a path take new samples (one atomic per warp) at the top of
+// an iteration.
+constexpr int kPathBlockThreads = 256;
+#ifndef HASTY_PATH_MIN_BLOCKS
+#define HASTY_PATH_MIN_BLOCKS 2
+#endif
+template <class Src, int KIND>
+__global__ void __launch_bounds__(kPathBlockThreads, HASTY_PATH_MIN_BLOCKS) k_paths(const __grid_constant__ Src src, PathsDev P,
+                                                                PathsDev O) {
+  __shared__ int s_more;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;   // this thread's path slot
+  const uint32_t n = uint32_t(n_paths_of(src));
+  const uint32_t lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  if (s == 0) atomicAdd(&P.stats[ST_PATHS], (unsigned long long)n);
+  unsigned long long n_rays = 0, n_shaded = 0, n_over = 0, n_cap = 0;
+  int g = -1;              // sample index of the path in the slot (-1: none)
+  bool drained = false;    // warp-uniform: every sample of the batch has been handed out
+  uint64_t key = 0;
+  for (;;) {
+    // ---- new samples for lanes without a path
+    const unsigned need = __ballot_sync(kFull, g < 0);
+    if (need && !drained) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(&P.counts[kFetchCounter], uint32_t(__popc(need)));
+      base = __shfl_sync(kFull, base, 0);
+      if (base + uint32_t(__popc(need)) >= n) drained = true;
+      if (g < 0) {
+        const uint32_t gi = base + uint32_t(__popc(need & below));
+        if (gi < n) {
+          g = int(gi);
+          const SlotPos sp = raygen_pos(src, g);
+          key = path_key(sp.seed, sp.px, sp.pass);
+          int capped = 0;
+          const bool traced = start_path(scene_of(src, uint32_t(sp.chunk) << PF_CHUNK_SHIFT), P, s, sp, capped);
+          n_cap += unsigned(capped);
+          if (!traced) {
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            O.out_color[g] = z; O.out_normal[g] = z; O.out_albedo[g] = z;
+            g = -1;
+          }
+        }
+      }
+    }
+    if (threadIdx.x == 0) s_more = 0;
+    __syncthreads();
+    if (g >= 0 || !drained) s_more = 1;
+    __syncthreads();
+    if (!s_more) break;
+    // ---- closest hits
+    if (g >= 0) {
+      const uint32_t fl = __float_as_uint(P.rad[s].w);
+      const SceneDev& sc = scene_of(src, fl);
+      for (int r = 0; r < 2; ++r) {
+        if (!(fl & (r ? PF_PEND_L : PF_PEND_B))) continue;
+        // light rays of environment-only lighting: visible iff nothing is hit
+        P.hit[2 * s + r] = closest_hit<KIND>(sc, P.ray_o[2 * s + r], P.ray_d[2 * s + r], r == 1 && sc.n_light_tris == 0);
+        ++n_rays;
+      }
+    }
+    __syncthreads();
+    // ---- resolve
+    bool live = false;
+    V3 L(0.f, 0.f, 0.f);
+    if (g >= 0) {
+      const uint32_t fl = __float_as_uint(P.rad[s].w);
+      const ResolveRes rr = resolve_path(scene_of(src, fl), P, s, key);
+      n_shaded += unsigned(rr.shaded);
+      live = rr.sample;
+      L = rr.L;
+    }
+    __syncthreads();
+    // ---- sample
+    if (live) {
+      const uint32_t fl = __float_as_uint(P.rad[s].w);
+      const SampleRes sr = sample_path(scene_of(src, fl), P, s, key);
+      n_over += unsigned(sr.overflow);
+      n_cap += unsigned(sr.capped);
+      live = sr.keep;
+      L = sr.L;
+    }
+    if (g >= 0 && !live) {
+      O.out_color[g] = f4(L, 0.f);
+      O.out_normal[g] = P.out_normal[s];
+      O.out_albedo[g] = P.out_albedo[s];
+      g = -1;
+    }
+    __syncthreads();
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    n_rays += __shfl_down_sync(kFull, n_rays, o);
+    n_shaded += __shfl_down_sync(kFull, n_shaded, o);
+    n_over += __shfl_down_sync(kFull, n_over, o);
+    n_cap += __shfl_down_sync(kFull, n_cap, o);
+  }
+  if (lane == 0) {
+    if (n_rays) atomicAdd(&P.stats[ST_RAYS], n_rays);
+    if (n_shaded) atomicAdd(&P.stats[ST_SHADED], n_shaded);
+    if (n_over) atomicAdd(&P.stats[ST_MEDIA_OVERFLOW], n_over);
+    if (n_cap) atomicAdd(&P.stats[ST_TRIAL_CAP], n_cap);
+  }
+}
+
 // Adds passes [0, n_passes) of the slots from `first` (pass k of pixel px in
 // slot first + k * npix + px) into the FP64 accumulators, one pass after the
 // other: acc = ((acc + v_0) + v_1) + ..., so the sums do not depend on how
@@ -575,6 +702,40 @@ void launch_shade_packed(const ChunkTable& t, const PathsDev& p, int q, int max_
   cudaMemsetAsync(&p.counts[kSampleCount], 0, sizeof(uint32_t), st);
   k_resolve<ChunkTable><<<(max_paths + kResolveThreads - 1) / kResolveThreads, kResolveThreads, 0, st>>>(t, p, q);
   k_sample<ChunkTable><<<(max_paths + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(t, p, q);
+}
+
+namespace {
+template <class K>
+int path_grid_of(K kernel) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPathBlockThreads, 0);
+  return std::max(1, sms) * std::max(1, per_sm);
+}
+int path_grid() {
+  static int g = 0;
+  if (!g) g = std::max(path_grid_of(k_paths<OneJob, 1>), path_grid_of(k_paths<ChunkTable, 1>));
+  return g;
+}
+template <class Src>
+void launch_paths_src(const Src& src, int n_paths, int bvh_kind, const PathsDev& slots, const PathsDev& out,
+                      cudaStream_t st) {
+  const int grid = std::min(path_grid(), std::max(1, (n_paths + kPathBlockThreads - 1) / kPathBlockThreads));
+  cudaMemsetAsync(&slots.counts[kFetchCounter], 0, sizeof(uint32_t), st);
+  if (bvh_kind == 1) k_paths<Src, 1><<<grid, kPathBlockThreads, 0, st>>>(src, slots, out);
+  else k_paths<Src, 0><<<grid, kPathBlockThreads, 0, st>>>(src, slots, out);
+}
+}  // namespace
+
+int64_t path_slots() { return int64_t(path_grid()) * kPathBlockThreads; }
+
+void launch_paths(const SceneDev& sc, const BatchDesc& b, const PathsDev& slots, const PathsDev& out, cudaStream_t st) {
+  launch_paths_src(OneJob{sc, b}, b.n_paths, sc.bvh_kind, slots, out, st);
+}
+
+void launch_paths_packed(const ChunkTable& t, int bvh_kind, const PathsDev& slots, const PathsDev& out, cudaStream_t st) {
+  launch_paths_src(t, t.n_paths, bvh_kind, slots, out, st);
 }
 
 void launch_accumulate(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, double* ac, double* an, double* aa, cudaStream_t st) {

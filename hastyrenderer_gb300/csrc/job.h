@@ -126,10 +126,14 @@ struct hasty_job {
   int32_t samples_done = 0;
   uint64_t seed = 0;
   std::atomic<bool> stop{false};
-  double kernel_ms = 0.0, trace_ms = 0.0, shade_ms = 0.0;
-  uint64_t trace_launches = 0, kernel_launches = 0;
+  double kernel_ms = 0.0, trace_ms = 0.0, shade_ms = 0.0, path_ms = 0.0;
+  uint64_t trace_launches = 0, kernel_launches = 0, path_launches = 0;
+  // Path kernel (cache-resident scenes): slot pools of the two render lanes,
+  // allocated on first use.
+  PathsDev slots[2] = {};
+  bool path_kernel = false;
   bool stage_timing = false;
-  // (start, end, stage) with stage 0: whole batch, 1: trace, 2: shade
+  // (start, end, stage) with stage 0: whole batch, 1: trace, 2: shade, 3: path kernel
   struct Ev { cudaEvent_t a, b; int stage; };
   std::vector<Ev> pending_events;
 
@@ -165,7 +169,8 @@ struct hasty_job {
     for (auto& e : pending_events) {
       float ms = 0.f;
       if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) {
-        if (e.stage == 0) kernel_ms += ms; else if (e.stage == 1) trace_ms += ms; else shade_ms += ms;
+        if (e.stage == 0) kernel_ms += ms; else if (e.stage == 1) trace_ms += ms;
+        else if (e.stage == 2) shade_ms += ms; else path_ms += ms;
       }
       cudaEventDestroy(e.a); cudaEventDestroy(e.b);
     }
@@ -225,4 +230,12 @@ void finish_job_load(hasty_job& j, bool plain);
 // Resident blocks per SM of the persistent closest-hit kernel while another
 // render lane's batch runs beside it (api.cpp).
 int lane_trace_blocks();
+// Whether a scene is rendered by the path kernel: scenes of at most
+// path_kernel_max_triangles() triangles (their BVH and triangles stay in
+// L1/L2; HASTY_PATH_KERNEL_TRIS sets the bound, 0: never), unless the
+// context says otherwise (HASTY_CTX_WAVEFRONT, HASTY_CTX_PATH_KERNEL).
+int64_t path_kernel_max_triangles();
+bool use_path_kernel(const hasty_ctx* ctx, const SceneDev& sc);
+// Slot pool of the path kernel (path_slots() slots; its statistics are `stats`).
+void alloc_path_slots(PathsDev& p, const std::function<void*(size_t)>& alloc, unsigned long long* stats);
 }  // namespace hasty

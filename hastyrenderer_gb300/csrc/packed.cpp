@@ -35,6 +35,9 @@ void PackedLanes::init(hasty_ctx* c, int lanes, int64_t paths) {
     ck(cudaEventCreateWithFlags(&lane_done[k], cudaEventDisableTiming), "event");
     ck(cudaEventCreateWithFlags(&lane_free[k], cudaEventDisableTiming), "event");
     alloc_paths_into(pd[k], lane_paths, ST_COUNT, [&](size_t b) { return alloc(b); }, acc_stream, stats);
+    // the path kernel's slot pool, so the lanes' footprint is fixed from the start
+    alloc_path_slots(slots[k], [&](size_t b) { return alloc(b); }, stats);
+    ck(cudaMemsetAsync(slots[k].counts, 0, sizeof(uint32_t) * kCountSlots, acc_stream), "memset counts");
   }
   wait_for(acc_stream);
 }
@@ -85,13 +88,18 @@ void PackedLanes::launch(const std::vector<PackedJob>& jobs, const std::vector<P
   if (start) ck(cudaEventRecord(start, ls), "event");
   const int trace_cap = overlap && n_lanes > 1 ? lane_trace_blocks() : 0;
   const int n_paths = ct.n_paths;
-  launch_raygen_packed(ct, p, ls);
-  for (int bounce = 0; bounce < max_depth; ++bounce) {
-    const int q = bounce & 1;
-    launch_trace_packed(tt, p, q, 2 * n_paths, ls, trace_cap);
-    ck(cudaMemsetAsync(&p.counts[q ^ 1], 0, sizeof(uint32_t), ls), "memset count");
-    ck(cudaMemsetAsync(&p.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), ls), "memset count");
-    launch_shade_packed(ct, p, q, n_paths, ls);
+  const bool path_kernel = jobs[size_t(chunks[0].job)].path_kernel;
+  if (path_kernel) {
+    launch_paths_packed(ct, bvh_kind, slots[lane], p, ls);
+  } else {
+    launch_raygen_packed(ct, p, ls);
+    for (int bounce = 0; bounce < max_depth; ++bounce) {
+      const int q = bounce & 1;
+      launch_trace_packed(tt, p, q, 2 * n_paths, ls, trace_cap);
+      ck(cudaMemsetAsync(&p.counts[q ^ 1], 0, sizeof(uint32_t), ls), "memset count");
+      ck(cudaMemsetAsync(&p.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), ls), "memset count");
+      launch_shade_packed(ct, p, q, n_paths, ls);
+    }
   }
   ck(cudaEventRecord(lane_done[lane], ls), "lane event");
   ck(cudaStreamWaitEvent(acc_stream, lane_done[lane], 0), "lane wait");
@@ -103,7 +111,7 @@ void PackedLanes::launch(const std::vector<PackedJob>& jobs, const std::vector<P
   ck(cudaEventRecord(lane_free[lane], acc_stream), "lane event");
   lane_free_valid[lane] = true;
   ++batches;
-  launches += uint64_t(1 + 3 * max_depth) + chunks.size();
+  launches += (path_kernel ? 1u : uint64_t(1 + 3 * max_depth)) + chunks.size();
 }
 
 void PackedLanes::read_stats(unsigned long long* out) {
@@ -145,6 +153,24 @@ std::vector<PackedChunk> pack_batch(const std::vector<PackedJob>& jobs, const st
   return out;
 }
 
+std::vector<int> class_order(const std::vector<PackedJob>& jobs, const std::vector<int>& order, bool path_kernel) {
+  std::vector<int> out;
+  for (int j : order) if (jobs[size_t(j)].path_kernel == path_kernel) out.push_back(j);
+  return out;
+}
+
+std::vector<PackedChunk> pack_next(const std::vector<PackedJob>& jobs, const std::vector<int>& order,
+                                   std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots,
+                                   int64_t job_samples, bool& path_turn) {
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const bool cls = path_turn;
+    path_turn = !path_turn;
+    std::vector<PackedChunk> c = pack_batch(jobs, class_order(jobs, order, cls), pass_base, left, slots, job_samples);
+    if (!c.empty()) return c;
+  }
+  return {};
+}
+
 int64_t packed_lane_paths(int64_t requested, int64_t largest_frame) {
   int64_t p = requested > 0 ? requested : (int64_t(1) << 24);
   return std::max(p, largest_frame);
@@ -173,6 +199,7 @@ void batch_render_packed(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes
     pj[i].seed = j->seed;
     for (int a = 0; a < 3; ++a) pj[i].acc[a] = j->acc[a];
     pj[i].npix = j->sd.width * j->sd.height;
+    pj[i].path_kernel = j->path_kernel;
     base[i] = uint32_t(j->samples_done);
     left[i] = passes[i];
     largest = std::max<int64_t>(largest, pj[i].npix);
@@ -188,8 +215,9 @@ void batch_render_packed(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes
   ck(cudaEventCreate(&b), "event");
   ck(cudaEventRecord(a, L.acc_stream), "event");
   L.wait_for(L.acc_stream);
+  bool path_turn = true;
   for (;;) {
-    std::vector<PackedChunk> chunks = pack_batch(pj, order, base, left, lane_paths);
+    std::vector<PackedChunk> chunks = pack_next(pj, order, base, left, lane_paths, 0, path_turn);
     if (chunks.empty()) break;
     bool more = false;
     for (int i : order) more = more || left[size_t(i)] > 0;

@@ -27,6 +27,7 @@ struct PackedJob {
   uint64_t seed = 0;
   double* acc[3] = {nullptr, nullptr, nullptr};   // FP64 sums: colour, normal, albedo (npix x 3 each)
   int32_t npix = 0;
+  bool path_kernel = false;                      // rendered by the path kernel (use_path_kernel)
 };
 
 // n_passes consecutive passes of job `job` from pass_base.
@@ -42,6 +43,7 @@ struct PackedLanes {
   int64_t lane_paths = 0;                 // path slots of each lane
   int bvh_kind = 1;
   PathsDev pd[kMaxLanes] = {};
+  PathsDev slots[kMaxLanes] = {};         // path-kernel slot pools
   cudaStream_t lane_stream[kMaxLanes] = {};
   cudaEvent_t lane_done[kMaxLanes] = {}, lane_free[kMaxLanes] = {};
   bool lane_free_valid[kMaxLanes] = {};
@@ -67,6 +69,8 @@ struct PackedLanes {
   // Enqueues one batch on the next lane (asynchronous). `overlap`: other
   // batches run at the same time (the closest-hit grid then leaves room for
   // their shading). Chunks must fit one lane and number at most kMaxChunks.
+  // A batch whose jobs all use the path kernel (use_path_kernel) runs the
+  // path kernel, any other the wavefront; pack_batch keeps the two apart.
   // `start` (optional, a timing event) is recorded on the lane's stream when
   // the batch can start.
   void launch(const std::vector<PackedJob>& jobs, const std::vector<PackedChunk>& chunks, bool overlap,
@@ -86,6 +90,13 @@ struct PackedLanes {
 std::vector<PackedChunk> pack_batch(const std::vector<PackedJob>& jobs, const std::vector<int>& order,
                                     std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots,
                                     int64_t job_samples = 0);
+// Jobs of `order` in one kernel class (path kernel or wavefront), order kept.
+std::vector<int> class_order(const std::vector<PackedJob>& jobs, const std::vector<int>& order, bool path_kernel);
+// Alternates the two kernel classes between consecutive batches while both
+// have passes left, so batches of either class run side by side on the lanes.
+std::vector<PackedChunk> pack_next(const std::vector<PackedJob>& jobs, const std::vector<int>& order,
+                                   std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots,
+                                   int64_t job_samples, bool& path_turn);
 
 // Path slots of a lane: 16M camera samples (whole frames of the largest
 // job at least), or `requested` when positive.

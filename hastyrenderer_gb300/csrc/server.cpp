@@ -256,6 +256,7 @@ void hasty_server::batch_loop() {
   cudaEvent_t origin = nullptr;       // reference point of the batches' device times
   cudaStream_t copy_stream = nullptr;
   double covered_ms = 0.0;            // device time counted so far ends here (ms after origin)
+  bool path_turn = true;              // kernel class of the next batch (pack_next)
   auto take_event = [&]() {
     if (!spare.empty()) { cudaEvent_t e = spare.back(); spare.pop_back(); return e; }
     cudaEvent_t e = nullptr;
@@ -308,6 +309,7 @@ void hasty_server::batch_loop() {
         j.sc.two_strategies = (r->scene->job->host.has_light() && r->st.use_mis) ? 1 : 0;
         j.seed = r->seed;
         j.npix = int32_t(r->npix);
+        j.path_kernel = use_path_kernel(ctx, j.sc);
         for (int a = 0; a < 3; ++a) j.acc[a] = r->d_acc + size_t(a) * 3 * r->npix;
         pass_base[size_t(r->slot)] = 0;
         left[size_t(r->slot)] = r->passes;
@@ -316,7 +318,7 @@ void hasty_server::batch_loop() {
       // one batch per free lane
       while (int(inflight.size()) < lanes.n_lanes && !order.empty()) {
         std::vector<PackedChunk> chunks =
-            pack_batch(jobs, order, pass_base, left, lanes.lane_paths, cfg.quantum_samples);
+            pack_next(jobs, order, pass_base, left, lanes.lane_paths, cfg.quantum_samples, path_turn);
         if (chunks.empty()) break;
         InFlight f;
         f.start = take_event();

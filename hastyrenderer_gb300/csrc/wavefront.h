@@ -31,7 +31,8 @@ struct PathsDev {
   uint64_t* rng;        // PCG32 state
   float4* thr;          // xyz: path throughput up to the pending BSDF sample, w: its pdf
   float4* rad;          // xyz: radiance gathered so far, w: flags
-  float4* pend_b;       // xyz: BSDF-sample weight (f|cos|/pdf * RR/Beer of its vertex), w: vertex triangle
+  float4* pend_b;       // xyz: BSDF-sample weight (f|cos|/pdf * RR/Beer of its vertex), w: vertex triangle;
+                        // between the resolve and the sample kernel: the vertex's Beer/roulette factor
   float4* nee_c;        // xyz: throughput * f * |cos| of the light sample, w: BSDF pdf of its direction
   float4* nee_t;        // xyz: medium transmittance along the light ray, w: sampled light triangle (-1: env)
   float4* med;          // 4 per path: medium transmittance xyz, IOR
@@ -42,7 +43,6 @@ struct PathsDev {
   int32_t* pq[2];       // path queues
   int32_t* rq[2];       // ray queues (ray ids 2s, 2s+1)
   uint32_t* counts;     // [pq0, pq1, rq0, rq1, trace fetch counter, sample-queue length, 2 spare]
-  float4* vtx;          // 6 per path: vertex record from the resolve to the sample kernel
   int32_t* sq;          // sample queue (paths that continue past resolve)
   float4* out_color;    // per slot: final radiance of the sample
   float4* out_normal;
@@ -116,6 +116,16 @@ void launch_shade_packed(const ChunkTable& t, const PathsDev& p, int q, int max_
 // FP64 accumulators of npix pixels.
 void launch_accumulate_range(const PathsDev& p, int first_slot, int npix, int n_passes, double* acc_color,
                              double* acc_normal, double* acc_albedo, cudaStream_t stream);
+
+// Path kernel (scenes that stay in L1/L2): persistent threads, each carrying
+// one camera sample through all its bounces in a slot of `slots` (path_slots()
+// slots at least), finished samples written to `out`'s per-sample arrays
+// (out_color/out_normal/out_albedo, indexed like a wavefront batch). Same
+// samples as the wavefront kernels, bit for bit.
+int64_t path_slots();
+void launch_paths(const SceneDev& sc, const BatchDesc& b, const PathsDev& slots, const PathsDev& out, cudaStream_t stream);
+void launch_paths_packed(const ChunkTable& t, int bvh_kind, const PathsDev& slots, const PathsDev& out,
+                         cudaStream_t stream);
 
 // Closest-hit queries of arbitrary rays (n x 6 floats, device memory).
 void launch_trace_rays(const SceneDev& sc, const float* rays, int n, float4* hits, cudaStream_t stream);

@@ -33,14 +33,15 @@ class JobInfo(ctypes.Structure):
                 ("env_is_texture", ctypes.c_int32), ("exposure", ctypes.c_float), ("samples_done", ctypes.c_int32),
                 ("bvh_depth", ctypes.c_int32), ("bvh_build_ms", ctypes.c_double), ("device_bytes", ctypes.c_int64),
                 ("bvh_tree_ms", ctypes.c_double), ("parse_ms", ctypes.c_double), ("upload_ms", ctypes.c_double),
-                ("paths_in_flight", ctypes.c_int64)]
+                ("paths_in_flight", ctypes.c_int64), ("path_kernel", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
     _fields_ = [("rays", ctypes.c_uint64), ("shaded", ctypes.c_uint64), ("paths", ctypes.c_uint64),
                 ("nan_samples", ctypes.c_uint64), ("media_overflow", ctypes.c_uint64), ("trial_cap", ctypes.c_uint64),
                 ("kernel_ms", ctypes.c_double), ("trace_ms", ctypes.c_double), ("shade_ms", ctypes.c_double),
-                ("trace_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64)]
+                ("trace_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("path_ms", ctypes.c_double),
+                ("path_launches", ctypes.c_uint64)]
 
 
 class BatchConfig(ctypes.Structure):

@@ -46,6 +46,9 @@ extern "C" {
 /* hasty_ctx_create flags */
 #define HASTY_CTX_BINARY_BVH 1u   /* binary BVH instead of the compressed 8-wide one */
 #define HASTY_CTX_HOST_BVH 2u     /* build the BVH on the host instead of the GPU */
+#define HASTY_CTX_WAVEFRONT 4u    /* never the path kernel (every scene on the wavefront kernels) */
+#define HASTY_CTX_PATH_KERNEL 8u  /* the path kernel for every scene (default: the wavefront, or the
+                                   * path kernel for scenes of at most HASTY_PATH_KERNEL_TRIS triangles) */
 
 #define HASTY_AOV_COLOR 0
 #define HASTY_AOV_NORMAL 1
@@ -76,6 +79,8 @@ typedef struct hasty_job_info {
   double parse_ms;             /* job load: renderJob/scene JSON, OBJ/MTL and images read on the host */
   double upload_ms;            /* job load: host-to-device copies of the scene (after the BVH build) */
   int64_t paths_in_flight;     /* camera samples per batch at most (whole passes) */
+  int32_t path_kernel;         /* 1: rendered by the path kernel (cache-resident scene), 0: the wavefront */
+  int32_t pad;
 } hasty_job_info;
 
 typedef struct hasty_stats {
@@ -90,6 +95,8 @@ typedef struct hasty_stats {
   double shade_ms;             /* device time in shading kernels (stage timing on) */
   uint64_t trace_launches;     /* closest-hit kernel launches */
   uint64_t kernel_launches;    /* all kernel launches of the passes rendered so far */
+  double path_ms;              /* device time in the path kernel (stage timing on) */
+  uint64_t path_launches;      /* path-kernel launches */
 } hasty_stats;
 
 int hasty_last_error(char* buf, size_t len);
