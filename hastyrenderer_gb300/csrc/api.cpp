@@ -42,7 +42,7 @@ namespace {
 }  // namespace
 
 void hasty::carve_paths(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc,
-                        unsigned long long* stats) {
+                        unsigned long long* stats, int64_t media_blocks) {
   auto A = [&](size_t bytes) { return alloc(bytes); };
   p.capacity = int32_t(cap);
   size_t c = size_t(cap);
@@ -54,6 +54,10 @@ void hasty::carve_paths(PathsDev& p, int64_t cap, int n_stats, const std::functi
   p.nee_t = static_cast<float4*>(A(c * sizeof(float4)));
   p.med = static_cast<float4*>(A(c * kMaxMedia * sizeof(float4)));
   p.med_geom = static_cast<int32_t*>(A(c * kMaxMedia * sizeof(int32_t)));
+  p.med_block = static_cast<int32_t*>(A(c * sizeof(int32_t)));
+  p.med_pool_blocks = int32_t(media_blocks > 0 ? media_blocks : std::max<int64_t>(64, cap / 4));
+  p.med_pool = static_cast<float4*>(A(size_t(p.med_pool_blocks) * kMediaBlock * sizeof(float4)));
+  p.med_pool_geom = static_cast<int32_t*>(A(size_t(p.med_pool_blocks) * kMediaBlock * sizeof(int32_t)));
   p.ray_o = static_cast<float4*>(A(2 * c * sizeof(float4)));
   p.ray_d = static_cast<float4*>(A(2 * c * sizeof(float4)));
   p.hit = static_cast<float4*>(A(2 * c * sizeof(float4)));
@@ -94,7 +98,8 @@ int64_t hasty::carved_bytes(int64_t cap, int n_stats, size_t align, size_t extra
 namespace {
 // Frees the path buffers of p (not the statistics it points to).
 void release_path_buffers(hasty_job& j, PathsDev& p) {
-  void* bufs[] = {p.rng, p.thr, p.rad, p.pend_b, p.nee_c, p.nee_t, p.med, p.med_geom, p.ray_o, p.ray_d, p.hit,
+  void* bufs[] = {p.rng, p.thr, p.rad, p.pend_b, p.nee_c, p.nee_t, p.med, p.med_geom, p.med_block, p.med_pool,
+                  p.med_pool_geom, p.ray_o, p.ray_d, p.hit,
                   p.pq[0], p.pq[1], p.rq[0], p.rq[1], p.counts, p.sq, p.out_color, p.out_normal, p.out_albedo};
   for (void* b : bufs) j.release(b);
   unsigned long long* stats = p.stats;
@@ -275,7 +280,9 @@ bool hasty::use_path_kernel(const hasty_ctx* ctx, const SceneDev& sc) {
 }
 
 void hasty::alloc_path_slots(PathsDev& p, const std::function<void*(size_t)>& alloc, unsigned long long* stats) {
-  carve_paths(p, path_slots(), ST_COUNT, alloc, stats);
+  // a slot keeps its overflow block for all the paths it carries in a launch
+  const int64_t n = path_slots();
+  carve_paths(p, n, ST_COUNT, alloc, stats, std::max<int64_t>(64, n / 2));
 }
 
 // HASTY_LANE_TRACE_BLOCKS overrides it (0: no cap).
@@ -585,6 +592,7 @@ int hasty_job_stats_get(hasty_job* job, hasty_stats* out) {
     ck(cudaMemcpy(s, job->pd.stats, sizeof(s), cudaMemcpyDeviceToHost), "copy stats");
     out->rays = s[ST_RAYS]; out->shaded = s[ST_SHADED]; out->paths = s[ST_PATHS]; out->nan_samples = s[ST_NAN];
     out->media_overflow = s[ST_MEDIA_OVERFLOW]; out->trial_cap = s[ST_TRIAL_CAP];
+    out->stack_overflow = s[ST_STACK_OVERFLOW];
     out->kernel_ms = job->kernel_ms;
     out->trace_ms = job->trace_ms; out->shade_ms = job->shade_ms;
     out->trace_launches = job->trace_launches; out->kernel_launches = job->kernel_launches;

@@ -33,6 +33,9 @@ void Engine::init(hasty_ctx* c, int64_t capacity, int slots, uint32_t segments, 
     seg_cap <<= 1;
   }
   alloc_paths_into(pd, cap, MS_COUNT, [&](size_t b) { return alloc(b); }, stream);
+  // Slots are refilled without a batch boundary to return overflow blocks
+  // at, so the engine keeps the medium stack to its first kMaxMedia entries.
+  pd.med_pool_blocks = 0;
   d_jobs = static_cast<JobDev*>(alloc(sizeof(JobDev) * size_t(job_slots)));
   d_segs = static_cast<SegDev*>(alloc(sizeof(SegDev) * size_t(seg_cap)));
   d_window = static_cast<uint32_t*>(alloc(sizeof(uint32_t) * 2));
@@ -326,6 +329,7 @@ int hasty::batch_render_regen(hasty_ctx* ctx, hasty_job** jobs, const int32_t* p
       }
       out->rays = st[MS_RAYS]; out->shaded = st[MS_SHADED]; out->nan_samples = st[MS_NAN];
       out->saturated = st[MS_SATURATED];
+      out->media_overflow = st[MS_MEDIA_OVERFLOW];
     }
     return HASTY_OK;
   });

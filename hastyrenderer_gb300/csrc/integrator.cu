@@ -38,22 +38,37 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* counter, uint32_t cnt
 }
 
 // Medium stack of one path (LightRayInfo, core/src/LightRayInfo.cpp:8-126),
-// bounded to kMaxMedia entries; a push beyond that is dropped and counted.
-// Medium stack of a path, read and updated in place in the path state
-// (P.med / P.med_geom, kMaxMedia entries per slot): only the depth n is held
-// in a register, so paths outside any medium never touch the stack.
+// read and updated in place in the path state: only the depth n is held in
+// a register, so paths outside any medium never touch it. Entries 0..3 are
+// the path's own (P.med / P.med_geom); deeper entries live in the path's
+// overflow block, taken from the batch's pool on the first push past 4
+// (rare: nested glass). kMediaMax entries in all; a push beyond that, or
+// with the pool exhausted, is dropped and counted.
 struct Media {
   int n;
+  const PathsDev& P;
+  int s;
   float4* med;
   int32_t* geom;
-  __device__ Media(const PathsDev& P, int s, int count)
-      : n(count), med(P.med + kMaxMedia * int64_t(s)), geom(P.med_geom + kMaxMedia * int64_t(s)) {}
+  __device__ Media(const PathsDev& P_, int s_, int count)
+      : n(count), P(P_), s(s_), med(P_.med + kMaxMedia * int64_t(s_)), geom(P_.med_geom + kMaxMedia * int64_t(s_)) {}
+  __device__ int64_t pool_index(int k) const {
+    return int64_t(P.med_block[s]) * kMediaBlock + (k - kMaxMedia);
+  }
+  __device__ float4 entry(int k) const { return k < kMaxMedia ? med[k] : P.med_pool[pool_index(k)]; }
+  __device__ int32_t geom_at(int k) const { return k < kMaxMedia ? geom[k] : P.med_pool_geom[pool_index(k)]; }
+  __device__ void set(int k, float4 e, int32_t g) {
+    if (k < kMaxMedia) { med[k] = e; geom[k] = g; return; }
+    const int64_t i = pool_index(k);
+    P.med_pool[i] = e;
+    P.med_pool_geom[i] = g;
+  }
   // first entry of medium g, -1 when absent
   __device__ int find(int g) const {
-    for (int i = 0; i < n; ++i) if (geom[i] == g) return i;
+    for (int i = 0; i < n; ++i) if (geom_at(i) == g) return i;
     return -1;
   }
-  __device__ V3 T(int k) const { return xyz(med[k]); }
+  __device__ V3 T(int k) const { return xyz(entry(k)); }
   __device__ V3 transmittance() const { return n > 0 ? T(0) : V3(1.f, 1.f, 1.f); }
   __device__ float outside_ior(const Inter& it, V3 wfrom) const {
     if (dot(wfrom, it.ng) < 0.0f) {
@@ -63,6 +78,19 @@ struct Media {
     }
     return n == 0 ? 1.0f : med[0].w;
   }
+  // Whether a push can be stored: below kMaxMedia always; deeper with an
+  // overflow block (the batch's pool must have some), taken now if the path
+  // has none.
+  __device__ bool room_for_push() {
+    if (n < kMaxMedia) return true;
+    if (n >= kMediaMax || P.med_pool_blocks <= 0) return false;
+    if (n == kMaxMedia && P.med_block[s] < 0) {
+      const uint32_t b = atomicAdd(&P.counts[kMediaPoolCounter], 1u);
+      if (b >= uint32_t(P.med_pool_blocks)) return false;
+      P.med_block[s] = int32_t(b);
+    }
+    return true;
+  }
   // Transmittance() of the stack that update(sc, m, it, wfrom, wto, wl)
   // would leave, without changing it (the light sample's stack is only
   // needed for that); overflow as update's return value.
@@ -70,7 +98,7 @@ struct Media {
                                     int& overflow) const {
     float nf = dot(it.ng, wfrom), nt = dot(it.ng, wto);
     if (nf >= 0.0f && nt < 0.0f) {
-      if (n >= kMaxMedia) { overflow = 1; return T(0); }
+      if (n >= kMediaMax || (n >= kMaxMedia && P.med_pool_blocks <= 0)) { overflow = 1; return T(0); }
       return n == 0 ? mat_albedo(sc, m, it) : T(0);
     }
     if (nf < 0.0f && nt >= 0.0f) {
@@ -81,18 +109,17 @@ struct Media {
     return transmittance();
   }
   // Push or pop for a direction change at `it` (in place); returns 1 when a
-  // push overflowed.
+  // push was dropped.
   __device__ int update(const SceneDev& sc, const MaterialDev& m, const Inter& it, V3 wfrom, V3 wto, int wl) {
     float nf = dot(it.ng, wfrom), nt = dot(it.ng, wto);
     if (nf >= 0.0f && nt < 0.0f) {
-      if (n >= kMaxMedia) return 1;
-      med[n] = f4(mat_albedo(sc, m, it), mat_ior(m, wl));
-      geom[n] = int(it.geom);
+      if (!room_for_push()) return 1;
+      set(n, f4(mat_albedo(sc, m, it), mat_ior(m, wl)), int(it.geom));
       ++n;
     } else if (nf < 0.0f && nt >= 0.0f) {
       int idx = find(int(it.geom));
       if (idx >= 0) {
-        for (int j = idx; j < n - 1; ++j) { med[j] = med[j + 1]; geom[j] = geom[j + 1]; }
+        for (int j = idx; j < n - 1; ++j) set(j, entry(j + 1), geom_at(j + 1));
         --n;
       }
     }
@@ -151,7 +178,7 @@ __device__ __forceinline__ int max_depth_of(const ChunkTable&) { return 1; }   /
 // as the slot's BSDF ray), throughput 1, AOVs cleared. Returns whether the
 // path traces at all (max_depth > 0).
 __device__ __forceinline__ bool start_path(const SceneDev& sc, const PathsDev& P, int s, const SlotPos& sp,
-                                           int& capped) {
+                                           int& capped, bool keep_media_block = false) {
   const uint32_t chunk_bits = uint32_t(sp.chunk) << PF_CHUNK_SHIFT;
   const uint32_t px = sp.px, pass = sp.pass;
   int x = int(px % uint32_t(sc.width)), y = int(px / uint32_t(sc.width));
@@ -165,6 +192,7 @@ __device__ __forceinline__ bool start_path(const SceneDev& sc, const PathsDev& P
   P.out_color[s] = make_float4(0.f, 0.f, 0.f, 0.f);
   P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f);
   P.out_albedo[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!keep_media_block) P.med_block[s] = -1;
   if (sc.max_depth <= 0) return false;
   P.ray_o[2 * s] = f4(o, __uint_as_float(uint32_t(sp.chunk)));
   P.ray_d[2 * s] = f4(d, 0.f);
@@ -178,6 +206,7 @@ __global__ void __launch_bounds__(256) k_raygen(const __grid_constant__ Src src,
   if (s == 0) {
     uint32_t n = max_depth_of(src) > 0 ? uint32_t(n_paths) : 0u;
     P.counts[0] = n; P.counts[1] = 0; P.counts[2] = n; P.counts[3] = 0;
+    P.counts[kMediaPoolCounter] = 0;
     atomicAdd(&P.stats[ST_PATHS], (unsigned long long)n_paths);
   }
   if (s >= n_paths) return;
@@ -528,12 +557,14 @@ template <int KIND> struct PathTrav { using T = TravBinary; };
 template <> struct PathTrav<1> { using T = TravWide; };
 
 template <int KIND>
-__device__ __forceinline__ float4 closest_hit(const SceneDev& sc, float4 o, float4 d, bool first_hit) {
+__device__ __forceinline__ float4 closest_hit(const SceneDev& sc, float4 o, float4 d, bool first_hit,
+                                              unsigned long long& overflows) {
   typename PathTrav<KIND>::T tr;
   typename PathTrav<KIND>::T::Entry stack[PathTrav<KIND>::T::kDepth];
   tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
   tr.any = first_hit;
   while (!tr.step(sc.nodes, sc.isect_tris, stack)) {}
+  overflows += tr.overflow ? 1u : 0u;
   return make_float4(tr.best.t, tr.best.u, tr.best.v, __int_as_float(tr.best.tri));
 }
 
@@ -557,7 +588,8 @@ __global__ void __launch_bounds__(kPathBlockThreads, HASTY_PATH_MIN_BLOCKS) k_pa
   const uint32_t lane = threadIdx.x & 31u;
   const unsigned below = (1u << lane) - 1u;
   if (s == 0) atomicAdd(&P.stats[ST_PATHS], (unsigned long long)n);
-  unsigned long long n_rays = 0, n_shaded = 0, n_over = 0, n_cap = 0;
+  P.med_block[s] = -1;     // the slot's medium overflow block, kept for all its paths of this launch
+  unsigned long long n_rays = 0, n_shaded = 0, n_over = 0, n_cap = 0, n_stack = 0;
   int g = -1;              // sample index of the path in the slot (-1: none)
   bool drained = false;    // warp-uniform: every sample of the batch has been handed out
   uint64_t key = 0;
@@ -576,7 +608,8 @@ __global__ void __launch_bounds__(kPathBlockThreads, HASTY_PATH_MIN_BLOCKS) k_pa
           const SlotPos sp = raygen_pos(src, g);
           key = path_key(sp.seed, sp.px, sp.pass);
           int capped = 0;
-          const bool traced = start_path(scene_of(src, uint32_t(sp.chunk) << PF_CHUNK_SHIFT), P, s, sp, capped);
+          const bool traced =
+              start_path(scene_of(src, uint32_t(sp.chunk) << PF_CHUNK_SHIFT), P, s, sp, capped, true);
           n_cap += unsigned(capped);
           if (!traced) {
             const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -598,7 +631,8 @@ __global__ void __launch_bounds__(kPathBlockThreads, HASTY_PATH_MIN_BLOCKS) k_pa
       for (int r = 0; r < 2; ++r) {
         if (!(fl & (r ? PF_PEND_L : PF_PEND_B))) continue;
         // light rays of environment-only lighting: visible iff nothing is hit
-        P.hit[2 * s + r] = closest_hit<KIND>(sc, P.ray_o[2 * s + r], P.ray_d[2 * s + r], r == 1 && sc.n_light_tris == 0);
+        P.hit[2 * s + r] =
+            closest_hit<KIND>(sc, P.ray_o[2 * s + r], P.ray_d[2 * s + r], r == 1 && sc.n_light_tris == 0, n_stack);
         ++n_rays;
       }
     }
@@ -636,8 +670,10 @@ __global__ void __launch_bounds__(kPathBlockThreads, HASTY_PATH_MIN_BLOCKS) k_pa
     n_shaded += __shfl_down_sync(kFull, n_shaded, o);
     n_over += __shfl_down_sync(kFull, n_over, o);
     n_cap += __shfl_down_sync(kFull, n_cap, o);
+    n_stack += __shfl_down_sync(kFull, n_stack, o);
   }
   if (lane == 0) {
+    if (n_stack) atomicAdd(&P.stats[ST_STACK_OVERFLOW], n_stack);
     if (n_rays) atomicAdd(&P.stats[ST_RAYS], n_rays);
     if (n_shaded) atomicAdd(&P.stats[ST_SHADED], n_shaded);
     if (n_over) atomicAdd(&P.stats[ST_MEDIA_OVERFLOW], n_over);
@@ -722,7 +758,9 @@ template <class Src>
 void launch_paths_src(const Src& src, int n_paths, int bvh_kind, const PathsDev& slots, const PathsDev& out,
                       cudaStream_t st) {
   const int grid = std::min(path_grid(), std::max(1, (n_paths + kPathBlockThreads - 1) / kPathBlockThreads));
-  cudaMemsetAsync(&slots.counts[kFetchCounter], 0, sizeof(uint32_t), st);
+  // fetch counter, sample-queue length (unused here) and medium-pool counter
+  static_assert(kMediaPoolCounter == kFetchCounter + 2, "counters cleared together");
+  cudaMemsetAsync(&slots.counts[kFetchCounter], 0, 3 * sizeof(uint32_t), st);
   if (bvh_kind == 1) k_paths<Src, 1><<<grid, kPathBlockThreads, 0, st>>>(src, slots, out);
   else k_paths<Src, 0><<<grid, kPathBlockThreads, 0, st>>>(src, slots, out);
 }
@@ -906,6 +944,7 @@ __global__ void __launch_bounds__(256) k_multi_regen(PathsDev P, MultiDev m, con
   P.rad[s] = make_float4(0.f, 0.f, 0.f, __uint_as_float(PF_CAMERA | PF_PEND_B));
   P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f);
   P.out_albedo[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  P.med_block[s] = -1;
   P.ray_o[2 * s] = f4(o, 0.f);
   P.ray_d[2 * s] = f4(d, 0.f);
   P.pq[q][m.ctl[3] + i] = s;

@@ -204,8 +204,11 @@ struct hasty_job {
 namespace hasty {
 // Carves path-state buffers for `cap` slots out of `alloc` (no device
 // work); statistics are carved too unless `stats` is given.
+// The medium-stack overflow pool gets media_blocks blocks (0: one per 4
+// slots, 64 at least: 80 B per slot; a scene of six nested glass shells took
+// more than one per 64).
 void carve_paths(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc,
-                 unsigned long long* stats = nullptr);
+                 unsigned long long* stats = nullptr, int64_t media_blocks = 0);
 // carve_paths, then clears the queue counters, and the statistics when they
 // were carved (api.cpp).
 void alloc_paths_into(PathsDev& p, int64_t cap, int n_stats, const std::function<void*(size_t)>& alloc, cudaStream_t st,

@@ -244,6 +244,7 @@ void batch_render_packed(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes
     out->paths_in_flight = lane_paths * n_lanes;
     out->engine_bytes = L.bytes;
     out->kernel_launches = L.launches;
+    out->media_overflow = st[ST_MEDIA_OVERFLOW];
   }
 }
 

@@ -46,13 +46,24 @@ template <int KIND> constexpr bool kPersistent = KIND == 1;
 template <int KIND> struct TravOf { using T = TravBinary; };
 template <> struct TravOf<1> { using T = TravWide; };
 
+// Adds this warp's count of rays whose traversal stack overflowed to `stat`
+// (one atomic per warp, only when there are any).
+__device__ __forceinline__ void add_overflows(unsigned long long* stat, uint32_t mine) {
+  const unsigned b = __ballot_sync(kFullMask, mine != 0);
+  if (!b) return;
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_down_sync(kFullMask, mine, o);
+  if ((threadIdx.x & 31u) == 0) atomicAdd(stat, (unsigned long long)mine);
+}
+
+// Returns the number of this thread's rays whose traversal stack overflowed.
 template <int KIND, class Fetch, class Done>
-__device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* next, Fetch fetch, Done done) {
+__device__ __forceinline__ uint32_t persistent_trace(uint32_t n, uint32_t* next, Fetch fetch, Done done) {
   typename TravOf<KIND>::T tr;
   typename TravOf<KIND>::T::Entry stack[TravOf<KIND>::T::kDepth];
   const float4* nodes = nullptr;
   const float4* tris = nullptr;
   int rid = 0;
+  uint32_t overflows = 0;
   bool active = false;
   bool drained = false;                 // warp-uniform: the queue has been handed out
   const uint32_t lane = threadIdx.x & 31u;
@@ -77,9 +88,11 @@ __device__ __forceinline__ void persistent_trace(uint32_t n, uint32_t* next, Fet
     if (__ballot_sync(kFullMask, active) == 0) break;   // drained: an all-idle warp always refills otherwise
     if (active && tr.step(nodes, tris, stack)) {
       done(rid, tr.best);
+      overflows += tr.overflow ? 1u : 0u;
       active = false;
     }
   }
+  return overflows;
 }
 
 template <int KIND>
@@ -100,7 +113,7 @@ __global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
   // environment are visible iff they hit nothing (Scene.cpp:575-585 with no
   // emissive triangle), so they stop at their first hit.
   const bool nee_any = sc.n_light_tris == 0;
-  persistent_trace<KIND>(
+  const uint32_t overflows = persistent_trace<KIND>(
       n, &P.counts[kFetchCounter],
       [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
         rid = rq[k];
@@ -111,6 +124,7 @@ __global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
         tris = sc.isect_tris;
       },
       [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
+  add_overflows(&P.stats[ST_STACK_OVERFLOW], overflows);
 }
 
 template <int KIND>
@@ -139,7 +153,7 @@ __global__ void TRACE_BOUNDS k_trace_packed(const __grid_constant__ TraceTable T
     }
     return;
   }
-  persistent_trace<KIND>(
+  const uint32_t overflows = persistent_trace<KIND>(
       n, &P.counts[kFetchCounter],
       [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
         rid = rq[k];
@@ -151,6 +165,7 @@ __global__ void TRACE_BOUNDS k_trace_packed(const __grid_constant__ TraceTable T
         tris = c.tris;
       },
       [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
+  add_overflows(&P.stats[ST_STACK_OVERFLOW], overflows);
 }
 
 // Multi-job engine: each ray belongs to the job of its path slot (ray id / 2).
@@ -171,7 +186,7 @@ __global__ void TRACE_BOUNDS k_trace_multi(PathsDev P, MultiDev m) {
     }
     return;
   }
-  persistent_trace<KIND>(
+  const uint32_t overflows = persistent_trace<KIND>(
       n, &P.counts[kFetchCounter],
       [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
         rid = rq[k];
@@ -183,6 +198,7 @@ __global__ void TRACE_BOUNDS k_trace_multi(PathsDev P, MultiDev m) {
         tris = sc.isect_tris;
       },
       [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
+  add_overflows(&P.stats[ST_STACK_OVERFLOW], overflows);
 }
 
 // Resident blocks of a persistent trace kernel on the current device.

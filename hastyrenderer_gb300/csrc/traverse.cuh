@@ -161,10 +161,12 @@ struct TravBinary {
   Hit best;
   int link, sp;
   bool any;   // stop at the first triangle hit (visibility only); set after init
+  bool overflow;   // a subtree was skipped because the stack was full
 
   HDI void init(float ox_, float oy_, float oz_, float dx_, float dy_, float dz_) {
     ox = ox_; oy = oy_; oz = oz_; dx = dx_; dy = dy_; dz = dz_;
     any = false;
+    overflow = false;
     best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
     iv = inverse_dir(dx, dy, dz);
     neg_x = iv.ix < 0.f; neg_y = iv.iy < 0.f; neg_z = iv.iz < 0.f;
@@ -195,7 +197,7 @@ struct TravBinary {
         int far_l = l1;
         link = l0;
         if (t1min < t0min) { link = l1; far_l = l0; }
-        if (sp < kStack) stack[sp++] = far_l;
+        if (sp < kStack) stack[sp++] = far_l; else overflow = true;
       } else if (h0) {
         link = l0;
       } else if (h1) {
@@ -298,10 +300,12 @@ struct TravWide {
   // Visibility only: stop at the first triangle hit (best is then a hit,
   // not necessarily the closest). Set after init.
   bool any;
+  bool overflow;   // a node group was skipped because the stack was full
 
   HDI void init(float ox_, float oy_, float oz_, float dx_, float dy_, float dz_) {
     ox = ox_; oy = oy_; oz = oz_; dx = dx_; dy = dy_; dz = dz_;
     any = false;
+    overflow = false;
     best.t = kInf; best.u = best.v = 0.f; best.tri = -1;
     iv = inverse_dir(dx, dy, dz);
     neg_x = iv.ix < 0.f; neg_y = iv.iy < 0.f; neg_z = iv.iz < 0.f;
@@ -329,7 +333,9 @@ struct TravWide {
     uint32_t imask = ng.y & 0xFFu;
     uint32_t node = ng.x + popc(imask & ~(0xFFFFFFFFu << slot));
     ng.y &= ~(1u << bit);
-    if (ng.y > 0x00FFFFFFu && sp < kWideStack) stack[sp++] = ng;
+    if (ng.y > 0x00FFFFFFu) {
+      if (sp < kWideStack) stack[sp++] = ng; else overflow = true;
+    }
 
     float4 f0 = ld(&nodes[5 * node + 0]);
     float4 f1 = ld(&nodes[5 * node + 1]);

@@ -17,15 +17,24 @@ enum : uint32_t {
   PF_DEPTH_MASK = 0xFFu,          // depth of the vertex the pending BRDF ray leaves from
   PF_WL_SHIFT = 8,                // wavelength + 1 (0: not chosen yet)
   PF_WL_MASK = 0x3u << 8,
-  PF_NMED_SHIFT = 10,             // media on the stack (0..4)
-  PF_NMED_MASK = 0x7u << 10,
   PF_PEND_B = 1u << 14,           // BSDF-sampled ray queued in ray slot 2s
   PF_PEND_L = 1u << 15,           // light-sampled ray queued in ray slot 2s+1
   PF_CAMERA = 1u << 16,           // pending ray is the camera ray
+  PF_NMED_SHIFT = 17,             // media on the stack (0..kMediaMax)
+  PF_NMED_MASK = 0x1Fu << 17,
   PF_CHUNK_SHIFT = 24,            // packed batches: chunk of the path's job (0 otherwise); also
   PF_CHUNK_MASK = 0xFFu << 24,    // the bits of ray_o.w of the path's rays
 };
+// Medium stack of a path (LightRayInfo's media, core/include/Hasty/LightRayInfo.h:51):
+// the first kMaxMedia entries in the path's own slots; a path nested deeper
+// takes one overflow block of kMediaBlock entries from the batch's pool
+// (P.med_pool, P.counts[kMediaPoolCounter]), for kMediaMax entries in all.
+// A push beyond that, or with the pool exhausted, is dropped and counted
+// (ST_MEDIA_OVERFLOW).
 constexpr int kMaxMedia = 4;
+constexpr int kMediaBlock = 16;
+constexpr int kMediaMax = kMaxMedia + kMediaBlock;
+static_assert(kMediaMax < 32, "the stack depth has 5 bits in the flags");
 
 struct PathsDev {
   uint64_t* rng;        // PCG32 state
@@ -37,6 +46,10 @@ struct PathsDev {
   float4* nee_t;        // xyz: medium transmittance along the light ray, w: sampled light triangle (-1: env)
   float4* med;          // 4 per path: medium transmittance xyz, IOR
   int32_t* med_geom;    // 4 per path: OBJ shape id of the medium
+  int32_t* med_block;   // per path: its overflow block in med_pool (-1: none)
+  float4* med_pool;     // overflow blocks: kMediaBlock entries each (transmittance, IOR)
+  int32_t* med_pool_geom;
+  int32_t med_pool_blocks;
   float4* ray_o;        // 2 per path
   float4* ray_d;        // 2 per path
   float4* hit;          // 2 per path: t, u, v, triangle (-1 miss)
@@ -51,10 +64,13 @@ struct PathsDev {
   int32_t capacity;
 };
 
-enum StatIndex { ST_RAYS = 0, ST_SHADED, ST_PATHS, ST_NAN, ST_MEDIA_OVERFLOW, ST_TRIAL_CAP, ST_COUNT };
+// ST_STACK_OVERFLOW: rays whose traversal stack was full when a subtree had
+// to be pushed (the subtree is skipped; the hit may then not be the closest).
+enum StatIndex { ST_RAYS = 0, ST_SHADED, ST_PATHS, ST_NAN, ST_MEDIA_OVERFLOW, ST_TRIAL_CAP, ST_STACK_OVERFLOW, ST_COUNT };
 constexpr int kCountSlots = 8;
 constexpr int kFetchCounter = 4;   // counts[4]: rays handed out by the persistent trace kernels
 constexpr int kSampleCount = 5;    // counts[5]: length of the sample queue
+constexpr int kMediaPoolCounter = 6;   // counts[6]: medium overflow blocks handed out in this batch
 
 struct BatchDesc {
   uint64_t seed;

@@ -41,7 +41,7 @@ class Stats(ctypes.Structure):
                 ("nan_samples", ctypes.c_uint64), ("media_overflow", ctypes.c_uint64), ("trial_cap", ctypes.c_uint64),
                 ("kernel_ms", ctypes.c_double), ("trace_ms", ctypes.c_double), ("shade_ms", ctypes.c_double),
                 ("trace_launches", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("path_ms", ctypes.c_double),
-                ("path_launches", ctypes.c_uint64)]
+                ("path_launches", ctypes.c_uint64), ("stack_overflow", ctypes.c_uint64)]
 
 
 class BatchConfig(ctypes.Structure):
@@ -53,7 +53,8 @@ class BatchStats(ctypes.Structure):
     _fields_ = [("device_ms", ctypes.c_double), ("wall_ms", ctypes.c_double), ("samples", ctypes.c_uint64),
                 ("rays", ctypes.c_uint64), ("shaded", ctypes.c_uint64), ("nan_samples", ctypes.c_uint64),
                 ("saturated", ctypes.c_uint64), ("iterations", ctypes.c_uint64), ("paths_in_flight", ctypes.c_int64),
-                ("engine_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_uint64)]
+                ("engine_bytes", ctypes.c_int64), ("kernel_launches", ctypes.c_uint64),
+                ("media_overflow", ctypes.c_uint64)]
 
 
 class PmStats(ctypes.Structure):

@@ -14,6 +14,9 @@ Workloads (sizes as the benchmark configurations state them):
   * ``sphere_field``  - N subdivision-3 icospheres on a ground plane under a
     procedural FP32 sky with a Gaussian sun (1.02M tris at N=800).
   * ``textured_room`` - textured quads (albedo, roughness, metallic, normal maps).
+  * ``nested_media``  - concentric glass shells, each its own OBJ shape (the
+    medium stack nests deeper than four), and a textured wall without
+    texture coordinates (the texture's no-UV colour).
 """
 from __future__ import annotations
 
@@ -25,6 +28,7 @@ import numpy as np
 
 __all__ = [
     "write_pfm", "write_pnm", "write_pam", "icosphere", "cornell_box", "sphere_field", "textured_room", "stress_scene",
+    "nested_media",
     "sky_environment", "roughness_to_ns",
 ]
 
@@ -462,3 +466,44 @@ def textured_room(out_dir, seed=0, width=64, height=48, spp=16, max_depth=8, tex
                 "roulette_start_depth": roulette_start_depth, "roulette_q": roulette_q,
                 "max_depth": max_depth, "use_mis": use_mis}
     return _write_job(out_dir, scene, settings, seed, mtl, ow)
+
+
+def nested_media(out_dir, seed=0, width=32, height=24, spp=4, max_depth=24, shells=6, roulette_start_depth=6,
+                 roulette_q=0.2):
+    """Concentric smooth-glass icosphere shells (subdivision 2), each its own
+    OBJ shape and material (seeded IOR in [1.3, 1.7] and tint, which is the
+    medium's transmittance), so a path reaching the core nests `shells` media
+    (the medium stack of core/src/LightRayInfo.cpp:8-38 keyed by shape). A
+    ground plane, a quad light, and a back wall whose material has an albedo
+    texture but whose mesh has no texture coordinates (the texture's no-UV
+    colour, core/include/Hasty/Texture.h:98-101)."""
+    rng = np.random.default_rng(seed)
+    os.makedirs(out_dir, exist_ok=True)
+    ow = _ObjWriter()
+    mtl = [_mtl_entry("ground", kd=(0.6, 0.6, 0.55)),
+           _mtl_entry("wall", kd=(0.5, 0.5, 0.5), map_kd="wall.ppm"),
+           _mtl_entry("light", kd=(0, 0, 0), ke=(40.0, 40.0, 40.0))]
+    write_pnm(os.path.join(out_dir, "wall.ppm"), rng.uniform(0.2, 0.9, (8, 8, 3)))
+    g = 6.0
+    v, f = _quad((-g, 0, -g), (-g, 0, g), (g, 0, g), (g, 0, -g))
+    ow.add("ground", v, f, "ground")
+    v, f = _quad((-g, 0, -2.5), (g, 0, -2.5), (g, 4, -2.5), (-g, 4, -2.5))
+    ow.add("wall", v, f, "wall")
+    ls = 0.8
+    v, f = _quad((-ls, 3.5, -ls), (ls, 3.5, -ls), (ls, 3.5, ls), (-ls, 3.5, ls))
+    ow.add("light", v, f, "light")
+    sv, sf = icosphere(2)
+    c = np.array([0.0, 1.1, 0.0])
+    r = 1.0
+    for k in range(shells):
+        name = f"glass{k}"
+        tint = 1.0 - rng.uniform(0.0, 0.25, 3)
+        mtl.append(_mtl_entry(name, kd=tint, ks=0.5, roughness=0.0, ior=float(rng.uniform(1.3, 1.7)), dissolve=0.0))
+        ow.add(f"shell{k}", sv * r + c, sf, name, normals=sv, smooth=True)
+        r *= 0.8
+    scene = {"camera": {"position": [0.0, 1.4, 4.2], "look_at": [0.0, 1.0, 0.0]},
+             "world": {"background_color": [0.05, 0.05, 0.08]}}
+    settings = {"num_samples": spp, "num_threads": 8, "width": width, "height": height,
+                "roulette_start_depth": roulette_start_depth, "roulette_q": roulette_q, "max_depth": max_depth,
+                "use_mis": True}
+    return _write_job(out_dir, scene, settings, seed, "".join(mtl), ow)

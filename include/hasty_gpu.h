@@ -88,7 +88,7 @@ typedef struct hasty_stats {
   uint64_t shaded;             /* non-emissive surface vertices shaded */
   uint64_t paths;              /* camera samples started */
   uint64_t nan_samples;        /* samples dropped for NaN radiance */
-  uint64_t media_overflow;     /* medium-stack pushes beyond 4 nested media */
+  uint64_t media_overflow;     /* medium-stack pushes dropped (beyond 20 nested media) */
   uint64_t trial_cap;          /* rejection loops stopped at the trial limit */
   double kernel_ms;            /* device time of the passes rendered so far */
   double trace_ms;             /* device time in closest-hit kernels (stage timing on) */
@@ -97,6 +97,7 @@ typedef struct hasty_stats {
   uint64_t kernel_launches;    /* all kernel launches of the passes rendered so far */
   double path_ms;              /* device time in the path kernel (stage timing on) */
   uint64_t path_launches;      /* path-kernel launches */
+  uint64_t stack_overflow;     /* rays whose BVH traversal stack overflowed (a subtree skipped) */
 } hasty_stats;
 
 int hasty_last_error(char* buf, size_t len);
@@ -243,6 +244,7 @@ typedef struct hasty_batch_stats {
   int64_t paths_in_flight;     /* path slots of all lanes / both engines together */
   int64_t engine_bytes;        /* device memory of the lanes or engines (path state, fixed-point sums) */
   uint64_t kernel_launches;    /* packed: kernels launched */
+  uint64_t media_overflow;     /* medium-stack pushes dropped (beyond 20 nested media; regen: beyond 4) */
 } hasty_batch_stats;
 
 /* Renders passes[i] further passes of jobs[i] (all from ctx) in one run and

@@ -35,6 +35,7 @@ def _load(path: str, prefix: str) -> ctypes.CDLL:
     if prefix == "hor":
         L.hor_info.argtypes = [P, P]
         L.hor_set_seed.argtypes = [P, ctypes.c_uint64]
+        L.hor_set_ulp_nudge.argtypes = [I]
         L.hor_intersect.argtypes = [P, P, ctypes.c_int64, I, P, P, P, P, P]
         L.hor_tri_ids.argtypes = [P, P, P]
         L.hor_rng_stream.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, I, P]
@@ -94,6 +95,11 @@ class Oracle(_Base):
 
     def set_seed(self, seed: int) -> None:
         self.L.hor_set_seed(self.h, ctypes.c_uint64(seed))
+
+    def set_ulp_nudge(self, on: bool) -> None:
+        """Process-wide: per-sample sin/cos/atan2/acos/pow results moved by one
+        ulp (measures how often a last-ulp math difference changes a sample)."""
+        self.L.hor_set_ulp_nudge(1 if on else 0)
 
     def render_rows(self, pass0: int, npasses: int, y0: int, row_stride: int, n_rows: int, nthreads: int = 0) -> dict:
         """Full-width rows y0, y0 + row_stride, ... (n_rows of them) over

@@ -64,6 +64,10 @@ void hor_info(void* p, int64_t* out) {
 
 void hor_set_seed(void* p, uint64_t seed) { static_cast<Handle*>(p)->sc.settings.seed = seed; }
 
+// Process-wide test switch: per-sample math-library results moved by one ulp
+// (see nudge_ulp in oracle_core.hpp).
+void hor_set_ulp_nudge(int on) { g_ulp_nudge = on != 0; }
+
 // Sums over passes [pass0, pass0+npasses) for the pixel window (x0,y0,w,h):
 // color (NaN samples dropped, as PathTracing.cpp:132-142), its square,
 // normal and albedo AOVs. Buffers are w*h*3 doubles, row-major.

@@ -6,12 +6,14 @@
 
 namespace hor {
 
+bool g_ulp_nudge = false;
+
 // ============================================================ sampling ====
 V2 sample_disk_uniformly(Rng& r, float& pdf) {
   float alpha = r.uniform01f() * float(2.0 * kPi);
   float rad = std::sqrt(r.uniform01f());
   pdf = float(kInvPi);
-  return V2{rad * std::cos(alpha), rad * std::sin(alpha)};
+  return V2{rad * ncos(alpha), rad * nsin(alpha)};
 }
 
 V2 sample_ngon_uniformly(Rng& r, int blades, float rotation, float& pdf) {
@@ -23,11 +25,11 @@ V2 sample_ngon_uniformly(Rng& r, int blades, float rotation, float& pdf) {
   do {
     s = sample_disk_uniformly(r, pdf);
     float rad = std::sqrt(s.x * s.x + s.y * s.y);
-    float ang = std::atan2(s.y, s.x);
+    float ang = natan2(s.y, s.x);
     ang -= rotation;
     ang += float(2.0 * kPi) * (1.0f + FLT_EPSILON);
     ang = std::fmod(ang, per);
-    float px = rad * std::cos(ang), py = rad * std::sin(ang);
+    float px = rad * ncos(ang), py = rad * nsin(ang);
     outside = (nx * px + ny * py + d) > 0.0f;
   } while (outside);
   float area_sector = 0.5 * std::sin(per);
@@ -62,7 +64,7 @@ V3 sample_hemisphere_cos(Rng& r, const V3& n, float& pdf) {
     float phi = 2.0f * float(kPi) * xi2;
     c = std::sqrt(xi1);
     float s = std::sqrt(1.0f - xi1);
-    float cp = std::cos(phi), sp = std::sin(phi);
+    float cp = ncos(phi), sp = nsin(phi);
     V3 rv(s * cp, s * sp, c);
     Rotation rot(V3(0, 0, 1), n);
     dir = normalize(rot.apply(rv));
@@ -84,22 +86,22 @@ V3 sample_cosine_lobe(Rng& r, const V3& lobe, float e, float& pdf) {
     float xi1 = r.uniform01f();
     float xi2 = r.uniform01f();
     float phi = 2.0f * float(kPi) * xi2;
-    c = std::pow(xi1, 1.0f / (e + 1.0f));
+    c = npow(xi1, 1.0f / (e + 1.0f));
     float s = std::sqrt(1.0f - c * c);
-    float cp = std::cos(phi), sp = std::sin(phi);
+    float cp = ncos(phi), sp = nsin(phi);
     V3 rv(s * cp, s * sp, c);
     Rotation rot(V3(0, 0, 1), lobe);
     dir = normalize(rot.apply(rv));
     c = dot(dir, lobe);
   } while (c <= 0.0f);
-  pdf = (e + 1.0f) * 0.5f * float(kInvPi) * std::pow(c, e);
+  pdf = (e + 1.0f) * 0.5f * float(kInvPi) * npow(c, e);
   return dir;
 }
 
 float eval_cosine_lobe_pdf(const V3& lobe, float e, const V3& d) {
   float c = dot(lobe, d);
   if (c < 0.0f) return 0.0f;
-  return (e + 1.0f) * 0.5f * float(kInvPi) * std::pow(c, e);
+  return (e + 1.0f) * 0.5f * float(kInvPi) * npow(c, e);
 }
 
 V3 sample_triangle_uniformly(Rng& r) {
@@ -156,7 +158,7 @@ V3 sample_dggx(Rng& r, const V3& n, float a, const V3& d1, float& pdf) {
     float phi = 2.0f * float(kPi) * xi2;
     float c = std::sqrt((1.0f - xi1) / (xi1 * (a * a - 1.0f) + 1.0f));
     float s = std::sqrt(1.0f - c * c);
-    float cp = std::cos(phi), sp = std::sin(phi);
+    float cp = ncos(phi), sp = nsin(phi);
     V3 rv(s * cp, s * sp, c);
     Rotation rot(V3(0, 0, 1), n);
     h = normalize(rot.apply(rv));
@@ -195,8 +197,8 @@ V3 sample_ggx_vndf(const V3& wo, float ax, float ay, float xi1, float xi2) {
   float rr = std::sqrt(xi1);
   float a = 1.0f / (1.0f + vh.z);
   float phi = float(kPi) * ((xi2 < a) ? (xi2 / a) : (1.0f + (xi2 - a) / (1.0f - a)));
-  float p1 = rr * std::cos(phi);
-  float p2 = rr * std::sin(phi) * (xi2 < a ? 1.0f : vh.z);
+  float p1 = rr * ncos(phi);
+  float p2 = rr * nsin(phi) * (xi2 < a ? 1.0f : vh.z);
   float p3 = std::sqrt(std::max(0.0f, 1.0f - p1 * p1 - p2 * p2));
   V3 nh = p1 * t1 + p2 * t2 + p3 * vh;
   return normalize(V3(ax * nh.x, ay * nh.y, std::max(0.0f, nh.z)));
@@ -569,7 +571,7 @@ float Env::density(const V3& d) const {
   float th, ph; sph_from_dir(d, th, ph);
   float u = ph * float(0.5 * kInvPi);
   float v = 1.0f - th * float(kInvPi);
-  float s = std::sin(th);
+  float s = nsin(th);
   size_t W = size_t(tex.w), H = size_t(tex.h);
   size_t x = std::min(size_t(u * float(W)), W - 1);
   size_t y = std::min(size_t((1.0f - v) * float(H)), H - 1);
@@ -912,7 +914,7 @@ float LightRayInfo::outside_ior(const Hit& h) const {
 V3 beers_law(const V3& T, float d) {              // core/include/Hasty/PathTracing.h:46-59
   if (T == V3(1, 1, 1)) return V3(1, 1, 1);
   V3 r;
-  for (int i = 0; i < 3; ++i) r[i] = T[i] <= 0.0f ? 0.0f : std::pow(T[i], 1.0f * d);
+  for (int i = 0; i < 3; ++i) r[i] = T[i] <= 0.0f ? 0.0f : npow(T[i], 1.0f * d);
   return r;
 }
 

@@ -6,6 +6,8 @@
 // statistically/per-sample with the CUDA integrator. Each function names the
 // reference lines it restates (paths relative to the reference project).
 #pragma once
+#include <limits>
+#include <cstring>
 #include <cmath>
 #include <cfloat>
 #include <cstdint>
@@ -96,17 +98,38 @@ struct Rotation {
 inline V3 reflect(const V3& inc, const V3& n) { return inc - 2.0f * dot(n, inc) * n; }
 inline V3 reflect_across(const V3& out, const V3& n) { return reflect(-out, n); }
 
+// Test switch (hor_set_ulp_nudge, off by default): moves every result of the
+// per-sample sin, cos, atan2, acos and pow calls by one ulp, up or down by a
+// hash of the argument's bits. With it on, the oracle measures how often a
+// last-ulp change of the math library changes a sample (a branch decision
+// flips), which is the kind of difference CUDA's device functions make
+// against the host's. Off, these wrappers are the plain calls.
+extern bool g_ulp_nudge;
+template <class T>
+inline T nudge_ulp(T r, T x) {
+  if (!g_ulp_nudge) return r;
+  uint64_t b = 0;
+  std::memcpy(&b, &x, sizeof(T));
+  const bool up = ((b * 0x9E3779B97F4A7C15ull) >> 63) != 0;
+  return std::nextafter(r, up ? std::numeric_limits<T>::infinity() : -std::numeric_limits<T>::infinity());
+}
+template <class T> inline T nsin(T x) { return nudge_ulp(T(std::sin(x)), x); }
+template <class T> inline T ncos(T x) { return nudge_ulp(T(std::cos(x)), x); }
+template <class T> inline T nacos(T x) { return nudge_ulp(T(std::acos(x)), x); }
+template <class T> inline T natan2(T y, T x) { return nudge_ulp(T(std::atan2(y, x)), T(y + x)); }
+template <class T> inline T npow(T a, T e) { return nudge_ulp(T(std::pow(a, e)), a); }
+
 // SphericalCoordinates, VMath.h:672-700 (y up).
 struct SphDir { float cosTheta, sinTheta; V3 dir; };
 inline SphDir sph_to_dir(float theta, float phi) {
-  SphDir r; r.cosTheta = std::cos(theta); r.sinTheta = std::sin(theta);
-  float sp = std::sin(phi), cp = std::cos(phi);
+  SphDir r; r.cosTheta = ncos(theta); r.sinTheta = nsin(theta);
+  float sp = nsin(phi), cp = ncos(phi);
   r.dir = V3(r.sinTheta * cp, r.cosTheta, r.sinTheta * sp);
   return r;
 }
 inline void sph_from_dir(const V3& d, float& theta, float& phi) {
-  theta = std::acos(d.y);
-  phi = std::atan2(d.z, d.x);
+  theta = nacos(d.y);
+  phi = natan2(d.z, d.x);
   phi = phi < 0.0f ? phi + float(2.0 * kPi) : phi;
 }
 

@@ -13,7 +13,12 @@ Fixtures:
   * kat_sampling.npz - Sample.cpp / BRDF.cpp sampling routines (aperture
                       polygon, cosine hemisphere, triangle, GGX VNDF, Fresnel,
                       refraction, sphere, Rodrigues rotation, Smith/GGX D).
-  * scenes/<name>/  - small seeded render jobs (OBJ/MTL/JSON/images).
+  * scenes/<name>/  - small seeded render jobs (OBJ/MTL/JSON/images): a
+                      Cornell box; a sphere field with sky, DoF and
+                      dispersive glass; a textured room (maps, anisotropy,
+                      glass), with and without MIS; six nested glass shells
+                      (the medium stack deeper than four) with a textured wall
+                      that has no texture coordinates.
   * render_<name>.npz - estimateRadiance (core/src/PathTracing.cpp:21-95)
                       sums over passes 0..P-1 and pass-0 per-sample values,
                       with the project's per-(seed, pixel, pass) PCG streams.
@@ -51,6 +56,7 @@ GOLDEN_SCENES = {
                                            env_size=(64, 32), vary_glass_ior=True, box=4.0),
     "room": lambda d: scenes.textured_room(d, seed=2, width=32, height=24, spp=4),
     "room_nomis": lambda d: scenes.textured_room(d, seed=3, width=32, height=24, spp=4, use_mis=False),
+    "nested": lambda d: scenes.nested_media(d, seed=5, width=32, height=24, spp=4),
 }
 
 

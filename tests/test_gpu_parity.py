@@ -12,7 +12,7 @@ from oracle.oracle import Oracle
 pytestmark = pytest.mark.gpu
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-SCENES = ["cornell", "field", "room", "room_nomis"]
+SCENES = ["cornell", "field", "room", "room_nomis", "nested"]
 
 
 def golden_job(name):
@@ -103,41 +103,27 @@ def test_sixteen_passes_match_reference(name):
     job.render_passes(P, sync=True)
     col, n = job.read_sums()
     assert n == P
+    assert job.stats()["stack_overflow"] == 0
     rel = np.abs(col - g["color"]) / np.maximum(1.0, np.abs(g["color"]))
     assert (rel.max(-1) <= 1e-3).mean() >= 0.9, (rel.max(-1) <= 1e-3).mean()
     assert abs(col.mean() - g["color"].mean()) <= 0.02 * abs(g["color"].mean()) + 1e-6
 
 
-@pytest.mark.parametrize("name", ["cornell", "field", "room"])
+@pytest.mark.parametrize("name", ["cornell", "field", "room", "nested"])
 def test_image_ztest(name):
-    """Per-pixel means at S = 64 spp against the oracle at 16*S spp from the
-    same streams: |mean_gpu - mean_cpu| <= 4 sigma per pixel, sigma from the
-    per-sample variance of the oracle's 16*S samples for both estimates (its
-    own Monte Carlo noise included). Sun and caustic paths make the radiance
-    heavy-tailed, so the sample variance can underestimate sigma on a few
-    pixels: at most 0.5% of pixels may exceed 4 sigma, and the signed
-    z-scores must show no bias."""
-    S = 64
+    """Per-pixel means at S = 64 spp (seed 777, passes 0..63) against the
+    oracle at 16 S spp on later passes, with the oracle's own null image
+    (zstat.ztest: exceedances, block exceedances and bias within the null's)."""
+    from zstat import gpu_moments, oracle_ref_and_null, ztest
+    S, N = 64, 1024
     job = _job(golden_job(name))
     job.set_seed(777)
-    job.render_passes(S, sync=True)
-    g, n = job.read_sums()
-    assert n == S
+    w, h = job.width, job.height
+    (gs, gs2), = gpu_moments(job, S, [(0, 0, w, h)])
     ora = Oracle(golden_job(name))
     ora.set_seed(777)
-    w, h = job.width, job.height
-    N = 16 * S
-    r = ora.render(0, N, 0, 0, w, h)
-    # per-pixel channel mean
-    sc = r["color"].mean(-1)
-    mc = sc / N
-    # variance of the channel mean of one sample, from the per-channel second moments (upper bound)
-    var_c = np.maximum((r["color_sq"] / N - (r["color"] / N) ** 2).mean(-1), 0.0)
-    mg = g.mean(-1) / S
-    sig = np.sqrt(var_c / S + var_c / N) + 1e-6 + 1e-5 * np.abs(mc)
-    z = (mg - mc) / sig
-    assert (np.abs(z) > 4.0).mean() <= 0.005, ((np.abs(z) > 4.0).mean(), np.abs(z).max())
-    assert abs(z.mean()) <= 0.25, z.mean()
+    cs, cs2, ns, ns2 = oracle_ref_and_null(ora, S, N, 0, 0, w, h)
+    ztest(f"golden {name}", gs, gs2, S, cs, cs2, N, ns, ns2)
 
 
 def test_device_bsdf_matches_reference():
@@ -155,3 +141,19 @@ def test_device_bsdf_matches_reference():
         assert good.mean() >= 0.995, (name, good.mean())
         if which == 0:
             assert (debug_bsdf(0, g["inputs"], g["replay"])[:, 11] == g["sample"][:, 11]).mean() >= 0.995
+
+
+def test_nested_media_beyond_four():
+    """Six nested glass shells: paths reaching the core nest deeper than the
+    four media a path keeps in its own slots. The wavefront keeps them in
+    overflow blocks and drops none (its sums are the reference's, tested
+    above); the regeneration engine, which keeps four, drops some, which
+    shows the deep stacks occur."""
+    from hastyrenderer_gb300 import batch_render
+    job = _job(golden_job("nested"))
+    job.render_passes(64, sync=True)
+    assert job.stats()["media_overflow"] == 0
+    packed = _job(golden_job("nested"))
+    assert batch_render([packed], [64])["media_overflow"] == 0
+    capped = _job(golden_job("nested"))
+    assert batch_render([capped], [64], mode=1)["media_overflow"] > 0

@@ -41,7 +41,7 @@ def test_sampling_kat_matches_reference(which):
     assert _rel(ours[ok], ref[ok]).max() <= 1e-6
 
 
-@pytest.mark.parametrize("name", ["cornell", "field", "room", "room_nomis"])
+@pytest.mark.parametrize("name", ["cornell", "field", "room", "room_nomis", "nested"])
 def test_render_matches_reference(name):
     """estimateRadiance over 16 passes of a seeded job: per-pixel sums equal to
     the reference's own integrator on the same streams."""
