@@ -193,8 +193,11 @@ void upload_scene(hasty_job& j) {
   s.bvh_kind = p.binary ? 0 : 1;
   s.nodes = reinterpret_cast<const float4*>(j.upload(p.bvh.nodes));
   s.isect_tris = reinterpret_cast<const float4*>(j.upload(p.bvh.tris));
+  s.n_nodes = int32_t(p.bvh.nodes.size() / (p.binary ? 16 : 20));
   s.mats = j.upload(h.mats);
   s.textures = j.upload(h.textures);
+  s.n_mats = int32_t(h.mats.size());
+  s.n_textures = int32_t(h.textures.size());
   s.tex_pool = j.upload(h.tex_pool);
   s.tex_pool8 = j.upload(h.tex_pool8);
   s.n_light_tris = int32_t(h.light_tris.size());

@@ -86,9 +86,11 @@ struct SceneDev {
   int32_t bvh_kind;           // 0: binary, 1: wide
   const float4* nodes;
   const float4* isect_tris;   // 3 x float4 per leaf-ordered triangle: v0 (w = global id), v0-v1, v2-v0
+  int32_t n_nodes;            // nodes of `nodes` (for the bounds-checked build)
   // materials and textures
   const MaterialDev* mats;
   const TextureDev* textures;
+  int32_t n_mats, n_textures;
   const float* tex_pool;
   const uint8_t* tex_pool8;
   // lights

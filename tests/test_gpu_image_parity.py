@@ -53,8 +53,8 @@ def test_c0_cornell_full_frame():
     job = RenderJob(path)
     (gs, gs2), = gpu_moments(job, S, [(0, 0, 256, 256)])
     ora = Oracle(path)
-    cs, cs2, ns, ns2 = oracle_ref_and_null(ora, S, N, 0, 0, 256, 256)
-    ztest("C0 cornell 256x256", gs, gs2, S, cs, cs2, N, ns, ns2)
+    cs, cs2, nulls = oracle_ref_and_null(ora, S, N, 0, 0, 256, 256)
+    ztest("C0 cornell 256x256", gs, gs2, S, cs, cs2, N, nulls)
 
 
 def test_c1_sphere_field_crops():
@@ -77,8 +77,8 @@ def test_c1_sphere_field_crops():
     moments = gpu_moments(job, S, crops)
     ora = Oracle(path)
     for (x, y, w, h), (gs, gs2) in zip(crops, moments):
-        cs, cs2, ns, ns2 = oracle_ref_and_null(ora, S, N, x, y, w, h)
-        ztest(f"C1 crop at ({x}, {y})", gs, gs2, S, cs, cs2, N, ns, ns2)
+        cs, cs2, nulls = oracle_ref_and_null(ora, S, N, x, y, w, h)
+        ztest(f"C1 crop at ({x}, {y})", gs, gs2, S, cs, cs2, N, nulls)
 
 
 def test_c4_stress_crop():
@@ -101,8 +101,8 @@ def test_c4_stress_crop():
     assert job.stats()["media_overflow"] == 0
     ora = Oracle(path)
     for (x, y, w, h), (gs, gs2) in zip(crops, moments):
-        cs, cs2, ns, ns2 = oracle_ref_and_null(ora, S, N, x, y, w, h)
-        ztest(f"C4 crop at ({x}, {y})", gs, gs2, S, cs, cs2, N, ns, ns2)
+        cs, cs2, nulls = oracle_ref_and_null(ora, S, N, x, y, w, h)
+        ztest(f"C4 crop at ({x}, {y})", gs, gs2, S, cs, cs2, N, nulls)
 
 
 def _small_mix():
@@ -144,14 +144,14 @@ def test_batched_and_served_images():
         name = os.path.basename(os.path.dirname(p))
         ora = Oracle(p)
         w, h = jb.width, jb.height
-        cs, cs2, ns, _ = oracle_ref_and_null(ora, S, N, 0, 0, w, h)
+        cs, cs2, nulls = oracle_ref_and_null(ora, S, N, 0, 0, w, h)
         vc = np.maximum(cs2 / N - (cs / N) ** 2, 0.0)
 
         def second(sums, n):
             # the reference's per-sample variance for a side whose squares are not kept
             return (vc + (sums / n) ** 2) * n
         for label, sums in (("batched", jb.read_sums()[0]), ("served", served[rid])):
-            ztest(f"{name} {label}", sums, second(sums, S), S, cs, cs2, N, ns, second(ns, S))
+            ztest(f"{name} {label}", sums, second(sums, S), S, cs, cs2, N, [(ns, second(ns, S)) for ns, _ in nulls])
         plain = RenderJob(p)
         plain.render_passes(S, sync=True)
         assert np.array_equal(plain.read_sums()[0], jb.read_sums()[0])
@@ -161,10 +161,11 @@ def test_batched_and_served_images():
         C = N
         conv.render_passes(C, sync=True)
         ref = conv.read_sums()[0] / C
-        # the converged image (C samples on the streams of seed 999) against a
-        # null image of as many oracle samples (passes after the other two)
-        n2 = ora.render(S + N + S, C, 0, 0, w, h)["color"]
-        ztest(f"{name} converged", ref * C, second(ref * C, C), C, cs, cs2, N, n2, second(n2, C))
+        # the converged image (C samples on the streams of seed 999) against two
+        # null images of as many oracle samples (passes after the others)
+        conv_nulls = [ora.render(S + N + 3 * S + k * C, C, 0, 0, w, h)["color"] for k in range(2)]
+        ztest(f"{name} converged", ref * C, second(ref * C, C), C, cs, cs2, N,
+              [(n2, second(n2, C)) for n2 in conv_nulls])
         rmse_b = np.sqrt(np.mean((jb.read_sums()[0] / S - ref) ** 2))
         rmse_p = np.sqrt(np.mean((plain.read_sums()[0] / S - ref) ** 2))
         assert abs(rmse_b - rmse_p) <= 0.01 * rmse_p, (name, rmse_b, rmse_p)

@@ -76,8 +76,12 @@ def test_intersect_full_size_scene(tmp_path):
 @pytest.mark.parametrize("name", SCENES)
 def test_first_pass_matches_reference(name):
     """Pass 0 of each golden job: every camera sample follows the same random
-    stream as in the reference's own estimateRadiance, so nearly every pixel
-    equals the reference's value (1e-3 relative); AOVs likewise."""
+    stream as in the reference's own estimateRadiance, so every pixel equals
+    the reference's value to float rounding (1e-5 relative), AOVs to 1e-4.
+    (The oracle measures how often a one-ulp change of the per-sample
+    sin/cos/atan2/acos/pow results changes a sample of these scenes: never,
+    so CUDA's device math, which differs from glibc's in the last ulps, is
+    expected to match on every sample.)"""
     g = np.load(os.path.join(GOLDEN, f"render_{name}.npz"))
     job = _job(golden_job(name))
     job.render_passes(1, sync=True)
@@ -87,16 +91,20 @@ def test_first_pass_matches_reference(name):
     assert n == 1
     ref = g["sample_color"]
     ref = np.where(np.isnan(ref).any(-1, keepdims=True), 0.0, ref)
-    close = np.all(np.abs(col - ref) <= 1e-3 * np.maximum(1.0, np.abs(ref)), axis=-1)
-    assert close.mean() >= 0.97, close.mean()
+    rel = np.abs(col - ref).max(-1) / np.maximum(1.0, np.abs(ref).max(-1))
+    bad = int((rel > 1e-5).sum())
+    print(f"[{name}] first pass: {bad} of {rel.size} samples beyond 1e-5, max {rel.max():.3g}")
+    assert bad == 0, (name, bad, float(rel.max()))
     for ours, key in ((nrm, "sample_normal"), (alb, "sample_albedo")):
-        c2 = np.all(np.abs(ours - g[key]) <= 1e-4 + 1e-4 * np.abs(g[key]), axis=-1)
-        assert c2.mean() >= 0.99, (key, c2.mean())
+        off = int((np.abs(ours - g[key]) > 1e-4 + 1e-4 * np.abs(g[key])).any(-1).sum())
+        assert off == 0, (name, key, off)
 
 
 @pytest.mark.parametrize("name", SCENES)
 def test_sixteen_passes_match_reference(name):
-    """16 passes against the reference's sums over the same 16 streams."""
+    """16 passes against the reference's sums over the same 16 streams:
+    every pixel to 1e-5 relative but at most two, each listed (a path that
+    flipped a branch on a last-ulp math difference)."""
     g = np.load(os.path.join(GOLDEN, f"render_{name}.npz"))
     job = _job(golden_job(name))
     P = int(g["passes"])
@@ -104,9 +112,14 @@ def test_sixteen_passes_match_reference(name):
     col, n = job.read_sums()
     assert n == P
     assert job.stats()["stack_overflow"] == 0
-    rel = np.abs(col - g["color"]) / np.maximum(1.0, np.abs(g["color"]))
-    assert (rel.max(-1) <= 1e-3).mean() >= 0.9, (rel.max(-1) <= 1e-3).mean()
-    assert abs(col.mean() - g["color"].mean()) <= 0.02 * abs(g["color"].mean()) + 1e-6
+    assert job.stats()["media_overflow"] == 0
+    rel = np.abs(col - g["color"]).max(-1) / np.maximum(1.0, np.abs(g["color"]).max(-1))
+    bad = np.argwhere(rel > 1e-5)
+    print(f"[{name}] 16 passes: {len(bad)} of {rel.size} pixels beyond 1e-5: "
+          f"{[(int(y), int(x), float(rel[y, x])) for y, x in bad[:8]]}")
+    # a sample whose path flips a branch on a last-ulp difference between
+    # CUDA's and the host's sin/cos/pow/acos/atan2 (about one in 10^4 samples)
+    assert len(bad) <= 2, (name, bad.tolist())
 
 
 @pytest.mark.parametrize("name", ["cornell", "field", "room", "nested"])
@@ -122,25 +135,38 @@ def test_image_ztest(name):
     (gs, gs2), = gpu_moments(job, S, [(0, 0, w, h)])
     ora = Oracle(golden_job(name))
     ora.set_seed(777)
-    cs, cs2, ns, ns2 = oracle_ref_and_null(ora, S, N, 0, 0, w, h)
-    ztest(f"golden {name}", gs, gs2, S, cs, cs2, N, ns, ns2)
+    cs, cs2, nulls = oracle_ref_and_null(ora, S, N, 0, 0, w, h)
+    ztest(f"golden {name}", gs, gs2, S, cs, cs2, N, nulls)
 
 
 def test_device_bsdf_matches_reference():
     """Device PrincipledBRDF sample/evaluate/pdf on the reference's
-    known-answer cases (replayed uniforms): within 1e-5 relative on >= 99.5%
-    of cases (CUDA's sinf/cosf/powf differ from glibc's by an ulp or two)."""
+    known-answer cases (replayed uniforms): values within 1e-5 relative
+    (denominator max(1e-3, |ref|)) on every case but the counted few, each
+    listed; the draw count of sample() (which decisions it took) equal on
+    every case."""
     from hastyrenderer_gb300 import debug_bsdf
     g = np.load(os.path.join(GOLDEN, "kat_bsdf.npz"))
     for which, name, cols in ((0, "sample", 11), (1, "evaluate", 9), (2, "pdf", 1)):
-        ours = debug_bsdf(which, g["inputs"], g["replay"])[:, :cols]
+        full = debug_bsdf(which, g["inputs"], g["replay"])
+        ours = full[:, :cols]
         ref = g[name][:, :cols]
         ok = np.isfinite(ref).all(1)
         rel = np.abs(ours - ref) / np.maximum(1e-3, np.abs(ref))
-        good = (rel <= 1e-5).all(1) | ~ok
-        assert good.mean() >= 0.995, (name, good.mean())
+        bad = np.nonzero(~((rel <= 1e-5).all(1) | ~ok))[0]
+        print(f"[kat {name}] {len(bad)} of {len(ref)} cases beyond 1e-5: "
+              f"{[(int(i), float(rel[i].max())) for i in bad[:8]]}")
+        assert len(bad) <= KAT_BEYOND[name], (name, len(bad), bad[:20].tolist())
         if which == 0:
-            assert (debug_bsdf(0, g["inputs"], g["replay"])[:, 11] == g["sample"][:, 11]).mean() >= 0.995
+            draws = int((full[:, 11] != g["sample"][:, 11]).sum())
+            assert draws == 0, draws
+
+
+# Known-answer cases allowed beyond 1e-5, from the printed counts on GB300:
+# sample() case 572 differs by 1.0e-4 relative (its sampled direction comes
+# from sin/cos of a near-grazing angle, where CUDA's and glibc's last-ulp
+# differences are amplified); evaluate() and pdf() match on every case.
+KAT_BEYOND = {"sample": 1, "evaluate": 0, "pdf": 0}
 
 
 def test_nested_media_beyond_four():
