@@ -429,8 +429,7 @@ def tuned_batch_args(args, jobs, ctx):
         for c in calib:
             c.close()
         res["source"] = "tuned now"
-    info = {k: res[k] for k in ("mode", "lanes", "paths_in_flight", "regen_fraction", "samples_per_s", "source")
-            if k in res}
+    info = {k: res[k] for k in autotune.KNOBS + ("samples_per_s", "source") if k in res}
     info["candidates"] = len(res.get("trials", []))
     return autotune.batch_args(res), info
 
@@ -452,6 +451,8 @@ def main():
     ap.add_argument("--duration", type=float, default=120.0, help="serve: seconds of arrivals")
     ap.add_argument("--policy", type=int, default=0, help="serve: 0 round robin, 1 shortest remaining first")
     ap.add_argument("--no-tune", action="store_true", help="batch/serve: skip the autotuner (defaults)")
+    ap.add_argument("--lane-paths", type=int, default=0,
+                    help="batch/serve: path slots per render lane instead of the tuned value (profiling small batches)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 3 if args.workload == "batch" else 16
@@ -612,6 +613,8 @@ def run_batch(args):
     resident = [RenderJob(j["path"], ctx) for j in jobs]
     load_s = time.perf_counter() - t0
     eargs, tune = tuned_batch_args(args, jobs, ctx)   # (tuning is not part of the end-to-end time)
+    if args.lane_paths:
+        eargs = dict(eargs, mode=0, lanes=eargs.get("lanes", 2), paths_in_flight=args.lane_paths)
     for r in resident:
         r.reset()
     t1 = time.perf_counter()
@@ -727,13 +730,14 @@ def run_serve(args):
     ctx = Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0)
     eargs, tune = tuned_batch_args(args, jobs, ctx)
     lanes = eargs.get("lanes", 2)
-    paths = eargs.get("paths_in_flight", 1 << 24)
+    paths = eargs.get("paths_in_flight", 1 << 24) if eargs.get("mode", 0) == 0 else 1 << 24
+    shapes = {k: eargs[k] for k in ("resolve_threads", "sample_threads", "trace_blocks_per_sm") if k in eargs}
     pool = jobs[: max(1, len(jobs) // 2)]
     base = os.path.dirname(os.path.dirname(pool[0]["path"]))
     reqs = workloads.poisson_requests(pool, os.path.join(base, f"requests_{args.rate:g}_{args.duration:g}"),
                                       rate=args.rate, duration=args.duration, seed=1)
     cfg = dict(memory_budget=120 << 30, max_resident_jobs=32, max_resident_scenes=32, lanes=lanes,
-               paths_in_flight=paths, policy=args.policy)
+               paths_in_flight=paths, policy=args.policy, **shapes)
     srv = Server(ctx, **cfg)
     t0 = time.perf_counter()
     for j in pool:                       # warm the scene cache: one cheap request per scene

@@ -265,18 +265,22 @@ BATCH_REGEN = 1    # HASTY_BATCH_REGEN
 
 
 def batch_render(jobs, passes, paths_in_flight: int = 0, regen_fraction: float = 0.0, max_iterations: int = 0,
-                 mode: int = BATCH_PACKED, lanes: int = 0, ctx: Context | None = None) -> dict:
+                 mode: int = BATCH_PACKED, lanes: int = 0, resolve_threads: int = 0, sample_threads: int = 0,
+                 trace_blocks_per_sm: int = 0, ctx: Context | None = None) -> dict:
     """Renders passes[i] further passes of jobs[i] in one multi-job run and
     adds the results to each job's accumulators. mode BATCH_PACKED (default):
     the jobs' passes packed into batches of paths_in_flight camera samples on
     `lanes` alternating render lanes (results bit-identical to render_passes);
     BATCH_REGEN: path regeneration over a shared pool in one CUDA-graph
-    launch. Returns the batch statistics."""
+    launch. resolve_threads / sample_threads / trace_blocks_per_sm: block
+    shapes of the packed batches' kernels (0: defaults). Returns the batch
+    statistics."""
     ctx = ctx or jobs[0].ctx
     n = len(jobs)
     handles = (ctypes.c_void_p * n)(*[j._h.value for j in jobs])
     ps = (ctypes.c_int32 * n)(*[int(p) for p in passes])
-    cfg = native.BatchConfig(int(paths_in_flight), float(regen_fraction), int(max_iterations), int(mode), int(lanes))
+    cfg = native.BatchConfig(int(paths_in_flight), float(regen_fraction), int(max_iterations), int(mode), int(lanes),
+                             int(resolve_threads), int(sample_threads), int(trace_blocks_per_sm), 0)
     st = native.BatchStats()
     check(native.lib().hasty_batch_render(ctx._h, handles, ps, n, ctypes.byref(cfg), ctypes.byref(st)))
     return {k: getattr(st, k) for k, _ in native.BatchStats._fields_}

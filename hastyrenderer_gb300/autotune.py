@@ -1,12 +1,13 @@
 """Autotuner of the batching launch parameters.
 
-Packed batches have two knobs that set how full the GPU stays: the number of
-render lanes (batches in flight at once, on their own streams) and the path
-slots of each lane (the queue size: camera samples per batch). The
+Packed batches have these knobs: the number of render lanes (batches in
+flight at once, on their own streams), the path slots of each lane (the
+queue size: camera samples per batch), the block shapes of the two shading
+kernels, and the closest-hit grid's blocks per SM while batches overlap. The
 regeneration engine has its pool size and regeneration threshold.
-tune_batch() times hasty_batch_render over a calibration set of resident jobs
-for every candidate, keeps the fastest by device time, and writes the result
-as JSON (one file per GPU name) so later runs reuse it.
+tune_batch() times hasty_batch_render over a calibration set of resident
+jobs, stage by stage, keeps the fastest by device time, and writes the
+result as JSON (one file per GPU name) so later runs reuse it.
 
     from hastyrenderer_gb300 import autotune
     best = autotune.tune_batch(jobs, passes=4)      # jobs: resident RenderJobs
@@ -20,9 +21,14 @@ import time
 
 LANES = [2, 3, 4]
 LANE_PATHS = [1 << 22, 1 << 23, 1 << 24]
+RESOLVE_THREADS = [128, 256]
+SAMPLE_THREADS = [256, 512]
+TRACE_BLOCKS = [4, 5, 6]
 REGEN_POOLS = [1 << 21, 1 << 22, 1 << 23]
 REGEN = [0.75, 0.9, 1.0]
-VERSION = 2
+VERSION = 3
+KNOBS = ("mode", "lanes", "paths_in_flight", "resolve_threads", "sample_threads", "trace_blocks_per_sm",
+         "regen_fraction")
 
 
 def default_path(gpu_name: str = "") -> str:
@@ -35,43 +41,52 @@ def batch_args(result: dict) -> dict:
     """hasty_batch_render keyword arguments of a tuning result."""
     out = {"mode": int(result.get("mode", 0)), "paths_in_flight": int(result["paths_in_flight"])}
     if out["mode"] == 0:
-        out["lanes"] = int(result["lanes"])
+        for k in ("lanes", "resolve_threads", "sample_threads", "trace_blocks_per_sm"):
+            if result.get(k):
+                out[k] = int(result[k])
     else:
         out["regen_fraction"] = float(result["regen_fraction"])
     return out
 
 
-def candidates(modes=(0, 1)) -> list[dict]:
-    out = []
-    if 0 in modes:
-        out += [{"mode": 0, "lanes": l, "paths_in_flight": p} for l in LANES for p in LANE_PATHS]
-    if 1 in modes:
-        out += [{"mode": 1, "paths_in_flight": p, "regen_fraction": f} for p in REGEN_POOLS for f in REGEN]
-    return out
-
-
-def tune_batch(jobs, passes: int = 4, cands=None, out_path: str | None = None, repeats: int = 2) -> dict:
-    """Times every candidate on `jobs` (each renders `passes` passes per
-    trial; the jobs' accumulators are reset before and after) and returns the
-    fastest with {"samples_per_s", "trials"}."""
+def _time(jobs, passes, cand, repeats):
     from .api import batch_render
-    cands = cands or candidates()
+    best_ms, samples = None, 0
+    for _ in range(repeats):
+        for j in jobs:
+            j.reset()
+        st = batch_render(jobs, [passes] * len(jobs), **batch_args(cand))
+        samples = st["samples"]
+        best_ms = st["device_ms"] if best_ms is None else min(best_ms, st["device_ms"])
+    return dict(cand, device_ms=best_ms, samples_per_s=samples / (best_ms * 1e-3))
+
+
+def tune_batch(jobs, passes: int = 4, out_path: str | None = None, repeats: int = 2, regen: bool = True) -> dict:
+    """Times candidates on `jobs` (each renders `passes` passes per trial; the
+    jobs' accumulators are reset before and after), in stages: packed lanes
+    x paths per lane (queue size), then the shading kernels' block shapes,
+    then the closest-hit grid cap, each stage keeping the best so far; the
+    regeneration engine's pool x refill threshold beside them. Returns the
+    fastest with {"samples_per_s", "trials"}."""
     trials = []
-    n = len(jobs)
-    for c in cands:
-        best_ms = None
-        samples = 0
-        for _ in range(repeats):
-            for j in jobs:
-                j.reset()
-            st = batch_render(jobs, [passes] * n, **batch_args(c))
-            samples = st["samples"]
-            best_ms = st["device_ms"] if best_ms is None else min(best_ms, st["device_ms"])
-        trials.append(dict(c, device_ms=best_ms, samples_per_s=samples / (best_ms * 1e-3)))
+
+    def best_of(cands):
+        res = [_time(jobs, passes, c, repeats) for c in cands]
+        trials.extend(res)
+        return max(res, key=lambda t: t["samples_per_s"])
+
+    top = best_of([{"mode": 0, "lanes": l, "paths_in_flight": p} for l in LANES for p in LANE_PATHS])
+    base = {k: top[k] for k in ("mode", "lanes", "paths_in_flight")}
+    top = best_of([dict(base, resolve_threads=r, sample_threads=t) for r in RESOLVE_THREADS for t in SAMPLE_THREADS])
+    base.update(resolve_threads=top["resolve_threads"], sample_threads=top["sample_threads"])
+    top = best_of([dict(base, trace_blocks_per_sm=b) for b in TRACE_BLOCKS])
+    if regen:
+        r = best_of([{"mode": 1, "paths_in_flight": p, "regen_fraction": f} for p in REGEN_POOLS for f in REGEN])
+        top = max(top, r, key=lambda t: t["samples_per_s"])
     for j in jobs:
         j.reset()
-    best = max(trials, key=lambda t: t["samples_per_s"])
-    result = dict(best, trials=trials, calibration={"jobs": n, "passes": passes}, when=time.time(), version=VERSION)
+    result = dict({k: top[k] for k in KNOBS if k in top}, samples_per_s=top["samples_per_s"], trials=trials,
+                  calibration={"jobs": len(jobs), "passes": passes}, when=time.time(), version=VERSION)
     if out_path:
         os.makedirs(os.path.dirname(out_path), exist_ok=True)
         with open(out_path, "w") as fh:

@@ -2,6 +2,7 @@
 
     python -m hastyrenderer_gb300.build            # library + CLI
     python -m hastyrenderer_gb300.build --oracle   # also the CPU oracle under oracle/
+    python -m hastyrenderer_gb300.build --debug-bounds   # the bounds-checked variant, lib/bounds/
 
 CUDA sources are compiled for sm_103a only; `integrator.cu` without FMA
 contraction (products and sums round like the reference's scalar C++), and
@@ -75,33 +76,40 @@ def _compile(src: str, cmd: list[str], obj: str, verbose: bool) -> str:
     return obj
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> str:
-    """Compile the CUDA/C++ sources; returns the path of libhasty_gb300.so."""
+def build(verbose: bool = False, jobs: int | None = None, debug_bounds: bool = False) -> str:
+    """Compile the CUDA/C++ sources; returns the path of libhasty_gb300.so.
+    debug_bounds: the bounds-checked variant (HASTY_DEBUG_BOUNDS: device
+    index checks that record a status bit and skip the access), written to
+    lib/bounds/ beside the regular build."""
     home = cuda_home()
     nvcc = os.path.join(home, "bin", "nvcc")
     cxx = os.environ.get("CXX", "g++")
-    os.makedirs(OBJ, exist_ok=True)
+    lib = os.path.join(LIB, "bounds") if debug_bounds else LIB
+    objdir = os.path.join(lib, "obj")
+    extra = ["-DHASTY_DEBUG_BOUNDS=1"] if debug_bounds else []
+    os.makedirs(objdir, exist_ok=True)
     tasks = []
     for f in CU_SOURCES:
         src = os.path.join(CSRC, f)
-        obj = os.path.join(OBJ, f + ".o")
-        cmd = [nvcc] + ARCH + NVCC_COMMON + CU_EXTRA.get(f, []) + EXTRA_NVCC + ["-c", src, "-o", obj]
+        obj = os.path.join(objdir, f + ".o")
+        cmd = [nvcc] + ARCH + NVCC_COMMON + CU_EXTRA.get(f, []) + EXTRA_NVCC + extra + ["-c", src, "-o", obj]
         tasks.append((src, cmd, obj))
     for f in CPP_SOURCES + ["cli.cpp"]:
         src = os.path.join(CSRC, f)
-        obj = os.path.join(OBJ, f + ".o")
-        cmd = [cxx] + CXX_FLAGS + ["-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(home, "include"), "-c", src, "-o", obj]
+        obj = os.path.join(objdir, f + ".o")
+        cmd = [cxx] + CXX_FLAGS + extra + ["-I" + INCLUDE, "-I" + CSRC, "-I" + os.path.join(home, "include"), "-c", src,
+                                           "-o", obj]
         tasks.append((src, cmd, obj))
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda t: _compile(t[0], t[1], t[2], verbose), tasks))
     lib_objs = [o for o in objs if not o.endswith("cli.cpp.o")]
-    so = os.path.join(LIB, "libhasty_gb300.so")
+    so = os.path.join(lib, "libhasty_gb300.so")
     link = [nvcc] + ARCH + ["-shared", "-o", so] + lib_objs + ["-lpthread"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
-    exe = os.path.join(LIB, "hasty_gpu_render")
-    link = [nvcc] + ARCH + ["-o", exe, os.path.join(OBJ, "cli.cpp.o"), "-L" + LIB, "-lhasty_gb300",
+    exe = os.path.join(lib, "hasty_gpu_render")
+    link = [nvcc] + ARCH + ["-o", exe, os.path.join(objdir, "cli.cpp.o"), "-L" + lib, "-lhasty_gb300",
                             "-Xlinker", "-rpath=$ORIGIN"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
@@ -129,7 +137,7 @@ def build_oracle(with_reference: bool | None = None, verbose: bool = False) -> N
 
 
 if __name__ == "__main__":
-    so = build(verbose="-v" in sys.argv)
+    so = build(verbose="-v" in sys.argv, debug_bounds="--debug-bounds" in sys.argv)
     print(so)
     if "--oracle" in sys.argv:
         build_oracle(verbose="-v" in sys.argv)

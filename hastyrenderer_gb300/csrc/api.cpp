@@ -26,6 +26,9 @@
 
 namespace hasty {
 // integrator.cu
+uint32_t bounds_status_integrator();
+uint32_t bounds_status_trace();
+uint32_t bounds_status_photon();
 void launch_debug_bsdf(int which, const float* in, int n, const uint32_t* replay, int n_replay, float* out, cudaStream_t st);
 // trace.cu
 void host_trace_rays(int kind, const float4* nodes, const float4* tris, const float* rays, int64_t n, float4* hits);
@@ -866,6 +869,18 @@ int hasty_debug_tri_ids(hasty_job* job, int32_t* geom, int32_t* prim, size_t n) 
     for (size_t i = 0; i < n; ++i) { geom[i] = int32_t(job->host.tri_attr[i].geom); prim[i] = int32_t(job->host.tri_attr[i].prim); }
     return HASTY_OK;
   });
+}
+
+int hasty_debug_bounds_status(uint32_t* flags) {
+#ifdef HASTY_DEBUG_BOUNDS
+  if (!flags) return fail(HASTY_ERR_ARG, "null argument");
+  *flags = hasty::bounds_status_integrator() | hasty::bounds_status_trace() | hasty::bounds_status_photon();
+  return HASTY_OK;
+#else
+  (void)flags;
+  return fail(HASTY_ERR_MISSING, "bounds checks are compiled into the bounds-checked build only "
+                                 "(python -m hastyrenderer_gb300.build --debug-bounds)");
+#endif
 }
 
 int hasty_debug_bsdf(int which, const float* in, size_t n_cases, const uint32_t* replay, size_t n_replay, float* out) {

@@ -9,7 +9,8 @@
 // flag the checks compile to nothing.
 //
 // Every translation unit that checks has its own status word (device
-// variables are per module); each provides a reader (bounds_status_*).
+// variables are per module); each provides a reader (bounds_status_*). The
+// bits are HASTY_BOUNDS_* of hasty_gpu.h.
 #pragma once
 #include <cstdint>
 
@@ -29,12 +30,14 @@ enum BoundsBit : uint32_t {
 
 }  // namespace hasty
 
-#if defined(HASTY_DEBUG_BOUNDS) && defined(__CUDA_ARCH__)
+#if defined(HASTY_DEBUG_BOUNDS) && defined(__CUDACC__)
 namespace hasty {
 namespace {
 __device__ unsigned int g_bounds_status;
 }
 }  // namespace hasty
+#endif
+#if defined(HASTY_DEBUG_BOUNDS) && defined(__CUDA_ARCH__)
 // True when `cond` holds; otherwise records `bit` and is false.
 #define HASTY_IN_BOUNDS(cond, bit) ((cond) ? true : (atomicOr(&::hasty::g_bounds_status, unsigned(bit)), false))
 #else

@@ -10,6 +10,7 @@
 #pragma once
 #include <cstdint>
 #include <cfloat>
+#include "bounds.cuh"
 #include "hasty_types.h"
 
 // Which large shading routines are compiled out of line (one shared copy,
@@ -381,6 +382,7 @@ __device__ __forceinline__ V3 eval_concentrated(float nswi, V3 albedo, float m, 
 
 // ------------------------------------------------------------ textures --
 __device__ __forceinline__ void tex_lookup(const SceneDev& sc, int ti, float u0, float v0, float* out) {
+  if (!HASTY_IN_BOUNDS(ti >= 0 && ti < sc.n_textures, BB_TEXTURE)) ti = 0;
   const TextureDev td = sc.textures[ti];
   float u = td.clamp_u ? clampf(u0, 0.0f, 1.0f - FLT_EPSILON) : fmod1p1(u0);
   float omv = td.clamp_v ? clampf(1.0f - v0, 0.0f, 1.0f - FLT_EPSILON) : fmod1p1(1.0f - v0);
@@ -567,6 +569,7 @@ HFN_INTER Inter make_inter(const SceneDev& sc, int tri, V3 b, V3 ng) {
   const float* p = sc.tri_pos + 9 * int64_t(tri);
   V3 x0 = ld3(p), x1 = ld3(p + 3), x2 = ld3(p + 6);
   it.tri = tri; it.geom = a.geom; it.mat = a.mat;
+  if (!HASTY_IN_BOUNDS(a.mat >= 0 && a.mat < sc.n_mats, BB_MATERIAL)) it.mat = 0;
   it.x = b.x * x0 + b.y * x1 + b.z * x2;
   it.ng = ng;
   it.h = 0.0f;
@@ -607,6 +610,7 @@ HFN_INTER Inter make_inter(const SceneDev& sc, int tri, V3 b, V3 ng) {
 
 // Hit record (t, u, v, triangle) -> interaction (Scene.cpp:294-302).
 __device__ __forceinline__ Inter inter_from_hit(const SceneDev& sc, int tri, float u, float v) {
+  if (!HASTY_IN_BOUNDS(tri >= 0 && tri < sc.n_tris, BB_TRI)) tri = 0;
   V3 b(1.0f - u - v, u, v);
   V3 ng = normalize(tri_ng_raw(sc.tri_pos + 9 * int64_t(tri)));
   return make_inter(sc, tri, b, ng);
@@ -614,6 +618,7 @@ __device__ __forceinline__ Inter inter_from_hit(const SceneDev& sc, int tri, flo
 
 // Only the position of a hit (what the light-pdf needs).
 __device__ __forceinline__ V3 hit_point(const SceneDev& sc, int tri, float u, float v) {
+  if (!HASTY_IN_BOUNDS(tri >= 0 && tri < sc.n_tris, BB_TRI)) tri = 0;
   const float* p = sc.tri_pos + 9 * int64_t(tri);
   V3 b(1.0f - u - v, u, v);
   return b.x * ld3(p) + b.y * ld3(p + 3) + b.z * ld3(p + 6);

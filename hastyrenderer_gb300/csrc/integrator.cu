@@ -53,7 +53,9 @@ struct Media {
   __device__ Media(const PathsDev& P_, int s_, int count)
       : n(count), P(P_), s(s_), med(P_.med + kMaxMedia * int64_t(s_)), geom(P_.med_geom + kMaxMedia * int64_t(s_)) {}
   __device__ int64_t pool_index(int k) const {
-    return int64_t(P.med_block[s]) * kMediaBlock + (k - kMaxMedia);
+    int64_t b = P.med_block[s];
+    if (!HASTY_IN_BOUNDS(b >= 0 && b < P.med_pool_blocks && k - kMaxMedia < kMediaBlock, BB_MEDIA)) b = 0;
+    return b * kMediaBlock + (k - kMaxMedia);
   }
   __device__ float4 entry(int k) const { return k < kMaxMedia ? med[k] : P.med_pool[pool_index(k)]; }
   __device__ int32_t geom_at(int k) const { return k < kMaxMedia ? geom[k] : P.med_pool_geom[pool_index(k)]; }
@@ -254,6 +256,7 @@ __device__ __forceinline__ ResolveRes resolve_path(const SceneDev& sc, const Pat
     float4 h = P.hit[2 * s + 1];
     float4 nc = P.nee_c[s], nt = P.nee_t[s];
     int ltri = __float_as_int(nt.w), htri = __float_as_int(h.w);
+    if (!HASTY_IN_BOUNDS(htri < sc.n_tris, BB_TRI)) htri = -1;
     bool vis = ltri >= 0 ? (htri == ltri) : (htri < 0 || sc.mats[sc.tri_attr[htri].mat].is_light);
     if (vis) {
       V3 o = xyz(P.ray_o[2 * s + 1]), d = xyz(P.ray_d[2 * s + 1]);
@@ -276,6 +279,7 @@ __device__ __forceinline__ ResolveRes resolve_path(const SceneDev& sc, const Pat
   } else {
     float4 h = P.hit[2 * s];
     int htri = __float_as_int(h.w);
+    if (!HASTY_IN_BOUNDS(htri < sc.n_tris, BB_TRI)) htri = -1;
     V3 o = xyz(P.ray_o[2 * s]), d = xyz(P.ray_d[2 * s]);
     float4 thr4 = P.thr[s];
     V3 thr = xyz(thr4);
@@ -376,7 +380,9 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
     V3 oL, dL; int ltri = -1;
     if (xi < sc.p_surface) {
       uint32_t kk = sample_cdf(sc.light_cdf, uint32_t(sc.n_light_tris), r, sc.light_guide, sc.light_guide_log2);
+      if (!HASTY_IN_BOUNDS(kk < uint32_t(sc.n_light_tris), BB_LIGHT)) kk = 0;
       ltri = sc.light_tris[kk];
+      if (!HASTY_IN_BOUNDS(ltri >= 0 && ltri < sc.n_tris, BB_TRI)) ltri = 0;
       V3 bb = triangle_uniform(r);
       const float* lp = sc.tri_pos + 9 * int64_t(ltri);
       V3 xl = bb.x * ld3(lp) + bb.y * ld3(lp + 3) + bb.z * ld3(lp + 6);
@@ -449,16 +455,17 @@ __device__ __forceinline__ SampleRes sample_path(const SceneDev& sc, const Paths
 // 256: 903 (shading 8.32 -> 8.00 ms per step), 512: 888 (the larger blocks
 // interleave worse with the other render lane's tracing).
 constexpr int kResolveThreads = 256;
-template <class Src>
-__global__ void __launch_bounds__(kResolveThreads, 4) k_resolve(const __grid_constant__ Src src, PathsDev P, int q) {
-  constexpr int kWarps = kResolveThreads / 32;
+template <class Src, int RT = kResolveThreads>
+__global__ void __launch_bounds__(RT, 1024 / RT) k_resolve(const __grid_constant__ Src src, PathsDev P, int q) {
+  constexpr int kWarps = RT / 32;
   __shared__ uint32_t s_cnt[kWarps][3];
   __shared__ uint32_t s_base;
   const uint32_t n_in = P.counts[q];
   if (blockIdx.x * blockDim.x >= n_in) return;    // whole block past the queue
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < n_in;
-  const int s = valid ? P.pq[q][i] : 0;
+  bool valid = i < n_in;
+  int s = valid ? P.pq[q][i] : 0;
+  if (valid && !HASTY_IN_BOUNDS(s >= 0 && s < P.capacity, BB_QUEUE)) { valid = false; s = 0; }
   ResolveRes res;
   res.sample = false;
   res.shaded = 0;
@@ -501,8 +508,8 @@ __global__ void __launch_bounds__(kResolveThreads, 4) k_resolve(const __grid_con
 // samples/s (shading ms per step): 128: 903 (8.00), 256: 942 (7.41),
 // 512: 946 (7.17), 1024: 904-929 (7.25).
 constexpr int kSampleThreads = 512;
-template <class Src>
-__global__ void __launch_bounds__(kSampleThreads, 2) k_sample(const __grid_constant__ Src src, PathsDev P, int q) {
+template <class Src, int ST = kSampleThreads>
+__global__ void __launch_bounds__(ST, 1024 / ST) k_sample(const __grid_constant__ Src src, PathsDev P, int q) {
   const uint32_t n_in = P.counts[kSampleCount];
   uint32_t* pq_cnt = &P.counts[q ^ 1];
   uint32_t* rq_cnt = &P.counts[2 + (q ^ 1)];
@@ -510,8 +517,9 @@ __global__ void __launch_bounds__(kSampleThreads, 2) k_sample(const __grid_const
   int32_t* rq_out = P.rq[q ^ 1];
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if ((i & ~31u) >= n_in) return;
-  const bool valid = i < n_in;
+  bool valid = i < n_in;
   int s = valid ? P.sq[i] : 0;
+  if (valid && !HASTY_IN_BOUNDS(s >= 0 && s < P.capacity, BB_QUEUE)) { valid = false; s = 0; }
   SampleRes res;
   res.keep = res.emitB = res.emitL = false;
   res.overflow = res.capped = 0;
@@ -563,6 +571,7 @@ __device__ __forceinline__ float4 closest_hit(const SceneDev& sc, float4 o, floa
   typename PathTrav<KIND>::T::Entry stack[PathTrav<KIND>::T::kDepth];
   tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
   tr.any = first_hit;
+  HASTY_TRAV_LIMITS(tr, sc.n_nodes, sc.n_tris);
   while (!tr.step(sc.nodes, sc.isect_tris, stack)) {}
   overflows += tr.overflow ? 1u : 0u;
   return make_float4(tr.best.t, tr.best.u, tr.best.v, __int_as_float(tr.best.tri));
@@ -734,10 +743,14 @@ void launch_shade(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, int
   k_sample<OneJob><<<(max_paths + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(src, p, q);
 }
 
-void launch_shade_packed(const ChunkTable& t, const PathsDev& p, int q, int max_paths, cudaStream_t st) {
+void launch_shade_packed(const ChunkTable& t, const PathsDev& p, int q, int max_paths, cudaStream_t st,
+                         int resolve_threads, int sample_threads) {
   cudaMemsetAsync(&p.counts[kSampleCount], 0, sizeof(uint32_t), st);
-  k_resolve<ChunkTable><<<(max_paths + kResolveThreads - 1) / kResolveThreads, kResolveThreads, 0, st>>>(t, p, q);
-  k_sample<ChunkTable><<<(max_paths + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(t, p, q);
+  // block shapes chosen per batch (the autotuner's candidates); 1024 threads per SM each
+  if (resolve_threads == 128) k_resolve<ChunkTable, 128><<<(max_paths + 127) / 128, 128, 0, st>>>(t, p, q);
+  else k_resolve<ChunkTable, 256><<<(max_paths + 255) / 256, 256, 0, st>>>(t, p, q);
+  if (sample_threads == 256) k_sample<ChunkTable, 256><<<(max_paths + 255) / 256, 256, 0, st>>>(t, p, q);
+  else k_sample<ChunkTable, 512><<<(max_paths + 511) / 512, 512, 0, st>>>(t, p, q);
 }
 
 namespace {
@@ -1235,3 +1248,6 @@ void launch_fixed_to_double(const unsigned long long* acc, int npix, double* c, 
 }
 
 }  // namespace hasty
+
+// Status word of this file's bounds checks (bounds-checked build).
+HASTY_BOUNDS_READER(bounds_status_integrator)

@@ -72,6 +72,8 @@ void PackedLanes::launch(const std::vector<PackedJob>& jobs, const std::vector<P
     tt.c[c].nodes = j.sc.nodes;
     tt.c[c].tris = j.sc.isect_tris;
     tt.c[c].nee_first_hit = j.sc.n_light_tris == 0 ? 1 : 0;
+    tt.c[c].n_nodes = j.sc.n_nodes;
+    tt.c[c].n_tris = j.sc.n_tris;
     slot += int64_t(ch.n_passes) * j.npix;
     max_depth = std::max(max_depth, j.sc.max_depth);
   }
@@ -86,7 +88,8 @@ void PackedLanes::launch(const std::vector<PackedJob>& jobs, const std::vector<P
   cudaStream_t ls = lane_stream[lane];
   if (lane_free_valid[lane]) ck(cudaStreamWaitEvent(ls, lane_free[lane], 0), "lane wait");
   if (start) ck(cudaEventRecord(start, ls), "event");
-  const int trace_cap = overlap && n_lanes > 1 ? lane_trace_blocks() : 0;
+  const int trace_cap =
+      overlap && n_lanes > 1 ? (trace_blocks_per_sm > 0 ? trace_blocks_per_sm : lane_trace_blocks()) : 0;
   const int n_paths = ct.n_paths;
   const bool path_kernel = jobs[size_t(chunks[0].job)].path_kernel;
   if (path_kernel) {
@@ -98,7 +101,7 @@ void PackedLanes::launch(const std::vector<PackedJob>& jobs, const std::vector<P
       launch_trace_packed(tt, p, q, 2 * n_paths, ls, trace_cap);
       ck(cudaMemsetAsync(&p.counts[q ^ 1], 0, sizeof(uint32_t), ls), "memset count");
       ck(cudaMemsetAsync(&p.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), ls), "memset count");
-      launch_shade_packed(ct, p, q, n_paths, ls);
+      launch_shade_packed(ct, p, q, n_paths, ls, resolve_threads, sample_threads);
     }
   }
   ck(cudaEventRecord(lane_done[lane], ls), "lane event");
@@ -210,6 +213,11 @@ void batch_render_packed(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes
   const int64_t lane_paths = packed_lane_paths(cfg ? cfg->paths_in_flight : 0, largest);
   PackedLanes L;
   L.init(ctx, n_lanes, lane_paths);
+  if (cfg) {
+    L.resolve_threads = cfg->resolve_threads;
+    L.sample_threads = cfg->sample_threads;
+    L.trace_blocks_per_sm = cfg->trace_blocks_per_sm;
+  }
   cudaEvent_t a = nullptr, b = nullptr;
   ck(cudaEventCreate(&a), "event");
   ck(cudaEventCreate(&b), "event");

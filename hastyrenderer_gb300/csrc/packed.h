@@ -53,6 +53,9 @@ struct PackedLanes {
   std::vector<void*> allocs;
   int64_t bytes = 0;
   int next_lane = 0;
+  // block shapes of the shading kernels and the closest-hit grid cap while
+  // batches overlap (the autotuner's knobs; 0: defaults)
+  int resolve_threads = 0, sample_threads = 0, trace_blocks_per_sm = 0;
   uint64_t batches = 0, launches = 0;
 
   PackedLanes() = default;

@@ -544,3 +544,6 @@ void launch_pm_gather(const SceneDev& sc, const PmMapDev& map, const PmPixelsDev
 }
 
 }  // namespace hasty
+
+// Status word of this file's bounds checks (bounds-checked build).
+HASTY_BOUNDS_READER(bounds_status_photon)

@@ -519,6 +519,9 @@ int hasty_server_start(hasty_ctx* ctx, const hasty_server_config* cfg, hasty_ser
     if (cfg) s->cfg = *cfg;
     clamp_config(s->cfg);
     s->lanes.init(ctx, s->cfg.lanes, s->cfg.paths_in_flight);
+    s->lanes.resolve_threads = s->cfg.resolve_threads;
+    s->lanes.sample_threads = s->cfg.sample_threads;
+    s->lanes.trace_blocks_per_sm = s->cfg.trace_blocks_per_sm;
     s->slots.assign(size_t(s->cfg.max_resident_jobs), nullptr);
     s->t0 = Clock::now();
     s->note_peak();

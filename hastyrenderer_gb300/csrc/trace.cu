@@ -103,6 +103,7 @@ __global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
   if (!kPersistent<KIND>) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
       int rid = rq[i];
+      if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
       float4 o = P.ray_o[rid], d = P.ray_d[rid];
       Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
       P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
@@ -117,11 +118,13 @@ __global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
       n, &P.counts[kFetchCounter],
       [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
         rid = rq[k];
+        if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
         float4 o = P.ray_o[rid], d = P.ray_d[rid];
         tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
         tr.any = nee_any && (rid & 1);
         nodes = sc.nodes;
         tris = sc.isect_tris;
+        HASTY_TRAV_LIMITS(tr, sc.n_nodes, sc.n_tris);
       },
       [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
   add_overflows(&P.stats[ST_STACK_OVERFLOW], overflows);
@@ -146,6 +149,7 @@ __global__ void TRACE_BOUNDS k_trace_packed(const __grid_constant__ TraceTable T
   if (!kPersistent<KIND>) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
       int rid = rq[i];
+      if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
       float4 o = P.ray_o[rid], d = P.ray_d[rid];
       const TraceChunk& c = T.c[__float_as_uint(o.w)];
       Hit h = trace_any<KIND>(c.nodes, c.tris, o.x, o.y, o.z, d.x, d.y, d.z);
@@ -157,12 +161,14 @@ __global__ void TRACE_BOUNDS k_trace_packed(const __grid_constant__ TraceTable T
       n, &P.counts[kFetchCounter],
       [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
         rid = rq[k];
+        if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
         float4 o = P.ray_o[rid], d = P.ray_d[rid];
         const TraceChunk& c = T.c[__float_as_uint(o.w)];
         tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
         tr.any = c.nee_first_hit != 0 && (rid & 1);   // as k_trace
         nodes = c.nodes;
         tris = c.tris;
+        HASTY_TRAV_LIMITS(tr, c.n_nodes, c.n_tris);
       },
       [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
   add_overflows(&P.stats[ST_STACK_OVERFLOW], overflows);
@@ -179,6 +185,7 @@ __global__ void TRACE_BOUNDS k_trace_multi(PathsDev P, MultiDev m) {
   if (!kPersistent<KIND>) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
       int rid = rq[i];
+      if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
       const SceneDev& sc = m.jobs[m.slot_meta[rid >> 1].x].sc;
       float4 o = P.ray_o[rid], d = P.ray_d[rid];
       Hit h = trace_any<KIND>(sc.nodes, sc.isect_tris, o.x, o.y, o.z, d.x, d.y, d.z);
@@ -190,12 +197,14 @@ __global__ void TRACE_BOUNDS k_trace_multi(PathsDev P, MultiDev m) {
       n, &P.counts[kFetchCounter],
       [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
         rid = rq[k];
+        if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
         const SceneDev& sc = m.jobs[m.slot_meta[rid >> 1].x].sc;
         float4 o = P.ray_o[rid], d = P.ray_d[rid];
         tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
         tr.any = sc.n_light_tris == 0 && (rid & 1);   // as k_trace
         nodes = sc.nodes;
         tris = sc.isect_tris;
+        HASTY_TRAV_LIMITS(tr, sc.n_nodes, sc.n_tris);
       },
       [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
   add_overflows(&P.stats[ST_STACK_OVERFLOW], overflows);
@@ -285,3 +294,6 @@ void host_trace_rays(int kind, const float4* nodes, const float4* tris, const fl
 }
 
 }  // namespace hasty
+
+// Status word of this file's bounds checks (bounds-checked build).
+HASTY_BOUNDS_READER(bounds_status_trace)

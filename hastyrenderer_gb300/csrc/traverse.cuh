@@ -20,6 +20,8 @@
 #include <cstdint>
 #include <cstring>
 
+#include "bounds.cuh"
+
 namespace hasty {
 namespace {
 
@@ -162,6 +164,9 @@ struct TravBinary {
   int link, sp;
   bool any;   // stop at the first triangle hit (visibility only); set after init
   bool overflow;   // a subtree was skipped because the stack was full
+#ifdef HASTY_DEBUG_BOUNDS
+  int32_t lim_nodes = 0x7FFFFFFF, lim_tris = 0x7FFFFFFF;   // bounds-checked build: array sizes
+#endif
 
   HDI void init(float ox_, float oy_, float oz_, float dx_, float dy_, float dz_) {
     ox = ox_; oy = oy_; oz = oz_; dx = dx_; dy = dy_; dz = dz_;
@@ -176,6 +181,9 @@ struct TravBinary {
 
   HDI bool step(const float4* nodes, const float4* tris, int* stack) {
     while (link >= 0) {
+#ifdef HASTY_DEBUG_BOUNDS
+      if (!HASTY_IN_BOUNDS(link < lim_nodes, BB_NODE)) return true;
+#endif
       float4 n0 = ld(&nodes[4 * link + 0]);
       float4 n1 = ld(&nodes[4 * link + 1]);
       float4 n2 = ld(&nodes[4 * link + 2]);
@@ -212,6 +220,9 @@ struct TravBinary {
     int first = code >> 3, cnt = code & 7;
     for (int k = 0; k < cnt; ++k) {
       int ti = first + k;
+#ifdef HASTY_DEBUG_BOUNDS
+      if (!HASTY_IN_BOUNDS(ti >= 0 && ti < lim_tris, BB_LEAF_TRI)) return true;
+#endif
       tri_test(ox, oy, oz, dx, dy, dz, ld(&tris[3 * ti]), ld(&tris[3 * ti + 1]), ld(&tris[3 * ti + 2]), best);
     }
     if (sp == 0 || (any && best.tri >= 0)) return true;
@@ -301,6 +312,9 @@ struct TravWide {
   // not necessarily the closest). Set after init.
   bool any;
   bool overflow;   // a node group was skipped because the stack was full
+#ifdef HASTY_DEBUG_BOUNDS
+  int32_t lim_nodes = 0x7FFFFFFF, lim_tris = 0x7FFFFFFF;   // bounds-checked build: array sizes
+#endif
 
   HDI void init(float ox_, float oy_, float oz_, float dx_, float dy_, float dz_) {
     ox = ox_; oy = oy_; oz = oz_; dx = dx_; dy = dy_; dz = dz_;
@@ -321,6 +335,9 @@ struct TravWide {
       uint32_t b = lowest_bit(tg.y);
       tg.y &= tg.y - 1u;
       int ti = int(tg.x + b);
+#ifdef HASTY_DEBUG_BOUNDS
+      if (!HASTY_IN_BOUNDS(ti >= 0 && ti < lim_tris, BB_LEAF_TRI)) return true;
+#endif
       tri_test(ox, oy, oz, dx, dy, dz, ld(&tris[3 * ti]), ld(&tris[3 * ti + 1]), ld(&tris[3 * ti + 2]), best);
     }
     if (any && best.tri >= 0) return true;
@@ -337,6 +354,9 @@ struct TravWide {
       if (sp < kWideStack) stack[sp++] = ng; else overflow = true;
     }
 
+#ifdef HASTY_DEBUG_BOUNDS
+    if (!HASTY_IN_BOUNDS(node < uint32_t(lim_nodes), BB_NODE)) return true;
+#endif
     float4 f0 = ld(&nodes[5 * node + 0]);
     float4 f1 = ld(&nodes[5 * node + 1]);
     float4 f2 = ld(&nodes[5 * node + 2]);
@@ -387,6 +407,13 @@ struct TravWide {
     return false;
   }
 };
+
+// Array sizes for the bounds-checked build's traversal checks (no-op otherwise).
+#ifdef HASTY_DEBUG_BOUNDS
+#define HASTY_TRAV_LIMITS(tr, n_nodes, n_tris) ((tr).lim_nodes = (n_nodes), (tr).lim_tris = (n_tris))
+#else
+#define HASTY_TRAV_LIMITS(tr, n_nodes, n_tris) ((void)0)
+#endif
 
 HDI Hit trace_wide(const float4* nodes, const float4* tris, float ox, float oy, float oz, float dx, float dy, float dz) {
   TravWide tr;

@@ -115,6 +115,7 @@ struct TraceChunk {
   const float4* nodes;
   const float4* tris;
   int32_t nee_first_hit;   // light rays stop at their first hit (environment-only lighting)
+  int32_t n_nodes, n_tris; // sizes of nodes and tris (the bounds-checked build checks them)
   int32_t pad;
 };
 struct TraceTable {
@@ -127,7 +128,10 @@ static_assert(sizeof(ChunkTable) < 32000, "kernel parameters are limited to 3276
 void launch_raygen_packed(const ChunkTable& t, const PathsDev& p, cudaStream_t stream);
 void launch_trace_packed(const TraceTable& t, const PathsDev& p, int q, int max_rays, cudaStream_t stream,
                          int blocks_per_sm = 0);
-void launch_shade_packed(const ChunkTable& t, const PathsDev& p, int q, int max_paths, cudaStream_t stream);
+// resolve_threads 128 or 256, sample_threads 256 or 512 (block shapes; any
+// other value takes 256 / 512).
+void launch_shade_packed(const ChunkTable& t, const PathsDev& p, int q, int max_paths, cudaStream_t stream,
+                         int resolve_threads = 256, int sample_threads = 512);
 // Adds slots [first_slot, first_slot + n_passes * npix) (passes in order) into
 // FP64 accumulators of npix pixels.
 void launch_accumulate_range(const PathsDev& p, int first_slot, int npix, int n_passes, double* acc_color,

@@ -10,7 +10,9 @@ import ctypes
 import os
 import re
 
-LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libhasty_gb300.so")
+# HASTY_LIB selects another build of the library (the bounds-checked one, in tests).
+LIB_PATH = os.environ.get("HASTY_LIB") or os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib",
+                                                        "libhasty_gb300.so")
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "hasty_gpu.h")
 
 HASTY_OK = 0
@@ -46,7 +48,9 @@ class Stats(ctypes.Structure):
 
 class BatchConfig(ctypes.Structure):
     _fields_ = [("paths_in_flight", ctypes.c_int64), ("regen_fraction", ctypes.c_float),
-                ("max_iterations", ctypes.c_int32), ("mode", ctypes.c_int32), ("lanes", ctypes.c_int32)]
+                ("max_iterations", ctypes.c_int32), ("mode", ctypes.c_int32), ("lanes", ctypes.c_int32),
+                ("resolve_threads", ctypes.c_int32), ("sample_threads", ctypes.c_int32),
+                ("trace_blocks_per_sm", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class BatchStats(ctypes.Structure):
@@ -68,7 +72,8 @@ class ServerConfig(ctypes.Structure):
     _fields_ = [("paths_in_flight", ctypes.c_int64), ("lanes", ctypes.c_int32), ("max_resident_jobs", ctypes.c_int32),
                 ("max_resident_scenes", ctypes.c_int32), ("loader_threads", ctypes.c_int32),
                 ("memory_budget", ctypes.c_int64), ("quantum_samples", ctypes.c_int64), ("policy", ctypes.c_int32),
-                ("pad", ctypes.c_int32)]
+                ("resolve_threads", ctypes.c_int32), ("sample_threads", ctypes.c_int32),
+                ("trace_blocks_per_sm", ctypes.c_int32)]
 
 
 class ServerResult(ctypes.Structure):
@@ -144,6 +149,7 @@ def lib() -> ctypes.CDLL:
         "hasty_debug_pm_map": [P, P, P, P, P, P, P, P],
         "hasty_job_render_pass_static": [P, I, P],
         "hasty_debug_static_scratch": [P, P, P],
+        "hasty_debug_bounds_status": [P],
         "hasty_server_start": [P, P, P],
         "hasty_server_submit": [P, ctypes.c_char_p, ctypes.c_int32, P, P],
         "hasty_server_poll": [P, P, SZ, P, ctypes.c_int32],

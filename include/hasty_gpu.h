@@ -230,6 +230,10 @@ typedef struct hasty_batch_config {
   int32_t max_iterations;      /* regen: device-side loop bound; 0 = 50M */
   int32_t mode;                /* HASTY_BATCH_PACKED or HASTY_BATCH_REGEN */
   int32_t lanes;               /* packed: render lanes (batches in flight), 1..4; 0 = 2 */
+  int32_t resolve_threads;     /* packed: block size of the resolve kernel, 128 or 256; 0 = 256 */
+  int32_t sample_threads;      /* packed: block size of the sample kernel, 256 or 512; 0 = 512 */
+  int32_t trace_blocks_per_sm; /* packed: closest-hit blocks per SM while batches overlap; 0 = 5 */
+  int32_t pad;
 } hasty_batch_config;
 
 typedef struct hasty_batch_stats {
@@ -285,7 +289,9 @@ typedef struct hasty_server_config {
   int64_t memory_budget;       /* device bytes; 0 = 120 GB */
   int64_t quantum_samples;     /* camera samples of one request per batch at most; 0 = paths_in_flight / 4 */
   int32_t policy;              /* HASTY_SERVE_ROUND_ROBIN (0) or HASTY_SERVE_SHORTEST_FIRST */
-  int32_t pad;
+  int32_t resolve_threads;     /* block shapes, as hasty_batch_config; 0 = defaults */
+  int32_t sample_threads;
+  int32_t trace_blocks_per_sm;
 } hasty_server_config;
 
 typedef struct hasty_server_result {
@@ -349,6 +355,23 @@ int hasty_server_stop(hasty_server* srv);
  * job is synced (hasty_job_sync) before the second call.
  * No counterpart in the reference (it renders through its own buffers). */
 int hasty_job_render_pass_static(hasty_job* job, int pass, double* d_color);
+/* Bounds-checked build only (python -m hastyrenderer_gb300.build
+ * --debug-bounds, which writes lib/bounds/libhasty_gb300.so): the device
+ * kernels check the indices they read through (queue entries, ray ids, BVH
+ * nodes and leaf triangles, hit triangles, materials, textures, light
+ * triangles, medium-stack blocks) and on a bad one skip the access and set
+ * a bit; this returns the bits set since the last call (HASTY_BOUNDS_*) and
+ * clears them. The regular build returns HASTY_ERR_MISSING. No counterpart
+ * in the reference. */
+#define HASTY_BOUNDS_QUEUE 1u
+#define HASTY_BOUNDS_NODE 2u
+#define HASTY_BOUNDS_LEAF_TRI 4u
+#define HASTY_BOUNDS_TRI 8u
+#define HASTY_BOUNDS_MATERIAL 16u
+#define HASTY_BOUNDS_TEXTURE 32u
+#define HASTY_BOUNDS_LIGHT 64u
+#define HASTY_BOUNDS_MEDIA 128u
+int hasty_debug_bounds_status(uint32_t* flags);
 /* Test hook (no device needed): the static scratch's pixel limit, the bytes a
  * frame of that many pixels carves from it, and its size. */
 int hasty_debug_static_scratch(int64_t* max_pixels, int64_t* bytes_needed, int64_t* capacity);

@@ -53,6 +53,16 @@ def test_static_scratch_holds_its_largest_frame():
     assert lib.hasty_debug_static_scratch(None, None, None) == -1
 
 
+def test_bounds_status_only_in_the_checked_build():
+    """The regular library answers the bounds-status query with
+    HASTY_ERR_MISSING (the checks are compiled into the checked build only)."""
+    lib = native.lib()
+    flags = ctypes.c_uint32(0)
+    if native.LIB_PATH.endswith(os.path.join("bounds", "libhasty_gb300.so")):
+        pytest.skip("the bounds-checked library is loaded")
+    assert lib.hasty_debug_bounds_status(ctypes.byref(flags)) == -7
+
+
 def test_cli_argument_errors(tmp_path):
     exe = os.path.join(os.path.dirname(native.LIB_PATH), "hasty_gpu_render")
     r = subprocess.run([exe], capture_output=True, text=True)

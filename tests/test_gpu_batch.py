@@ -42,16 +42,20 @@ def test_alone_equals_mixed(mode):
         assert jm.read_sums()[1] == p
 
 
-@pytest.mark.parametrize("lanes,paths", [(2, 0), (1, 3000), (2, 2500), (3, 4000), (4, 1100)])
-def test_packed_equals_single_job_path(lanes, paths):
+@pytest.mark.parametrize("lanes,paths,shapes", [(2, 0, (0, 0, 0)), (1, 3000, (128, 256, 4)), (2, 2500, (0, 0, 0)),
+                                                (3, 4000, (256, 256, 6)), (4, 1100, (128, 512, 0))])
+def test_packed_equals_single_job_path(lanes, paths, shapes):
     """Packed batches (small lanes force many batches, chunks split across
-    batches and several jobs per batch) give exactly the single-job path's
-    sums, a second call continuing the pass sequence."""
+    batches and several jobs per batch; the tuner's block shapes) give
+    exactly the single-job path's sums, a second call continuing the pass
+    sequence."""
     from hastyrenderer_gb300.api import batch_render
     passes = [5, 7, 3, 6]
     packed = [_job(n) for n in NAMES]
-    st = batch_render(packed, passes, paths_in_flight=paths, lanes=lanes)
-    st2 = batch_render(packed, [2, 1, 3, 2], paths_in_flight=paths, lanes=lanes)
+    kw = dict(paths_in_flight=paths, lanes=lanes, resolve_threads=shapes[0], sample_threads=shapes[1],
+              trace_blocks_per_sm=shapes[2])
+    st = batch_render(packed, passes, **kw)
+    batch_render(packed, [2, 1, 3, 2], **kw)
     assert st["samples"] == sum(p * j.width * j.height for p, j in zip(passes, packed))
     if paths:
         assert st["iterations"] >= st["samples"] // paths     # batches
