@@ -53,19 +53,21 @@ WORKLOAD_BATCH = "mixed_64_jobs_cornell_or_field50_200_800_128x128_to_1024x768_s
 # Algorithmic bytes per shaded vertex: path state read + write (2 x 96 B) and
 # the triangle's attributes (92 B); texel reads are not counted.
 B_SHADE = 2 * 96 + 92
-# Per-unit hardware counters of the wavefront kernels from ncu captures of
-# the 800-icosphere field (1080p, 8-pass batches of 16.6M paths, averaged over
-# the 12 bounces): DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum)
-# per traced ray (461.4 MB per closest-hit launch over 3.57M rays) and per
-# shaded vertex (1678.8 MB per resolve + sample launch pair over 1.407M
-# vertices), and for the closest-hit kernel warp instructions and thread
-# instructions per ray (smsp__inst_executed.sum,
-# smsp__thread_inst_executed.sum; None until captured). They give each
-# kernel's traffic, and the closest-hit kernel's issue rate, for the units a
-# launch processed.
+# Per-unit hardware counters of the wavefront kernels, per scene class, from
+# small ncu captures (three launches each of k_trace, k_resolve and k_sample
+# after the first three): DRAM bytes (dram__bytes_read.sum +
+# dram__bytes_write.sum) per traced ray and per shaded vertex, and for the
+# closest-hit kernel warp instructions and thread instructions per ray
+# (smsp__inst_executed.sum, smsp__thread_inst_executed.sum). Classes: "plain"
+# (the 1080p 800-sphere field), "cornell" (the 256x256 box), "mix:<kind>"
+# (one job of each scene kind of the 64-job mix, rendered alone). None where
+# not captured. They give each kernel's traffic and the closest-hit kernel's
+# issue rate for the units a launch processed; a run covering several classes
+# weights them by each class's rays and vertices.
 COUNTERS = {
-    "k_trace": {"dram_bytes_per_ray": 461.4e6 / 3.57e6, "warp_inst_per_ray": None, "thread_inst_per_ray": None},
-    "k_resolve+k_sample": {"dram_bytes_per_vertex": 1678.8e6 / 1.407e6},
+    "plain": {"k_trace": {"dram_bytes_per_ray": 461.4e6 / 3.57e6, "warp_inst_per_ray": None,
+                          "thread_inst_per_ray": None},
+              "k_resolve+k_sample": {"dram_bytes_per_vertex": 1678.8e6 / 1.407e6}},
 }
 REF_PASSES_PER_STEP = 8      # reference arm: passes of the CPU sample per step
 ISSUE_PER_SM_PER_CLOCK = 4   # warp instructions per SM and clock (one per scheduler)
@@ -150,6 +152,11 @@ def mix_jobs():
     from hastyrenderer_gb300 import workloads
     base = os.environ.get("HASTY_BENCH_MIX", os.path.join(tempfile.gettempdir(), "hasty_bench_mix"))
     return workloads.mixed_jobs(base, n_jobs=64, seed=0)
+
+
+def scene_class(job: dict) -> str:
+    """Scene kind of a mix job: cornell, field50, field200 or field800."""
+    return f"{job['kind']}{job['spheres'] or ''}"
 
 
 def replica_seed(rank: int) -> int:
@@ -322,49 +329,67 @@ def run_reference_arm(args, rank: int):
 # Rooflines of the wavefront kernels from a stage-timed run (one render lane,
 # so each kernel's time is its own).
 
-def kernel_rooflines(workload: str, stage: dict, hbm: float, peak_kind: str, sm_mhz, costs):
+def _weighted(by_class: dict, kernel: str, field: str, unit: str):
+    """Sum over scene classes of COUNTERS[class][kernel][field] times the
+    class's units; None when a class that did work has no capture."""
+    total = 0.0
+    for cls, u in by_class.items():
+        if not u.get(unit):
+            continue
+        v = COUNTERS.get(cls, {}).get(kernel, {}).get(field)
+        if v is None:
+            return None
+        total += v * u[unit]
+    return total
+
+
+def kernel_rooflines(stage: dict, hbm: float, peak_kind: str, sm_mhz, costs):
     """stage: trace_ms, shade_ms, trace_launches, path_ms, path_launches,
-    rays, shaded, paths of a stage-timed run (wavefront jobs, path-kernel
-    jobs or both). Returns (kernels, dominant)."""
+    rays, shaded, paths and by_class (rays, shaded, paths per scene class) of
+    a stage-timed run (wavefront jobs, path-kernel jobs or both). Returns
+    (kernels, dominant)."""
     kernels = []
     mhz = sm_mhz or 2070.0
+    issue_peak = SMS * ISSUE_PER_SM_PER_CLOCK * mhz * 1e-3
+    issue_kind = f"{SMS} SMs x {ISSUE_PER_SM_PER_CLOCK} schedulers x {mhz:.0f} MHz (median under load)"
+    by_class = stage["by_class"]
+    classes = sorted(by_class)
     if stage["path_launches"]:
         n = stage["path_launches"]
         ms = stage["path_ms"] / n
-        c = COUNTERS.get(workload, {}).get("k_paths", {})
         k = {"kernel": "k_paths", "unit_of_work": "camera sample", "units_per_launch": stage["paths"] / n,
-             "ms_per_launch": ms, "bound": "issue", "unit": "G warp-inst/s",
-             "traffic": c["dram_bytes_per_sample"] * stage["paths"] / n if c.get("dram_bytes_per_sample") else None}
-        if c.get("warp_inst_per_sample"):
-            ach = c["warp_inst_per_sample"] * stage["paths"] / n / (ms * 1e-3) * 1e-9
-            peak = SMS * ISSUE_PER_SM_PER_CLOCK * mhz * 1e-3
-            k.update(achieved=ach, peak=peak, frac=ach / peak,
-                     peak_kind=f"{SMS} SMs x {ISSUE_PER_SM_PER_CLOCK} schedulers x {mhz:.0f} MHz (median under load)",
-                     active_lanes_per_inst=c["thread_inst_per_sample"] / c["warp_inst_per_sample"])
+             "ms_per_launch": ms, "bound": "issue", "unit": "G warp-inst/s"}
+        dram = _weighted(by_class, "k_paths", "dram_bytes_per_sample", "paths")
+        inst = _weighted(by_class, "k_paths", "warp_inst_per_sample", "paths")
+        k["traffic"] = dram / n if dram is not None else None
+        if inst is not None:
+            ach = inst / n / (ms * 1e-3) * 1e-9
+            k.update(achieved=ach, peak=issue_peak, frac=ach / issue_peak, peak_kind=issue_kind)
         else:
-            k.update(achieved=None, peak=None, frac=None, note="instruction counts not captured for this workload")
+            k.update(achieved=None, peak=None, frac=None, note="instruction counts not captured for these scenes")
         kernels.append(k)
     if not stage["trace_launches"]:
         dominant = dict(max(kernels, key=lambda k: k["ms_per_launch"] * 1.0))
         dominant["note"] = "dominant kernel by device time, timed alone (stage timing keeps one render lane)"
         return kernels, dominant
     n = max(stage["trace_launches"], 1)
-    cnt = COUNTERS.get(workload, {})
     rays_l = stage["rays"] / n
     trace_ms = stage["trace_ms"] / n
-    k_trace = {"kernel": "k_trace", "unit_of_work": "traced ray", "units_per_launch": rays_l, "ms_per_launch": trace_ms}
-    c = cnt.get("k_trace", {})
-    k_trace["traffic"] = c["dram_bytes_per_ray"] * rays_l if c.get("dram_bytes_per_ray") else None
-    if c.get("warp_inst_per_ray"):
-        achieved = c["warp_inst_per_ray"] * rays_l / (trace_ms * 1e-3) * 1e-9
-        peak = SMS * ISSUE_PER_SM_PER_CLOCK * mhz * 1e-3
-        k_trace.update(bound="issue", achieved=achieved, peak=peak, unit="G warp-inst/s", frac=achieved / peak,
-                       peak_kind=f"{SMS} SMs x {ISSUE_PER_SM_PER_CLOCK} schedulers x {mhz:.0f} MHz (median under load)",
-                       active_lanes_per_inst=c["thread_inst_per_ray"] / c["warp_inst_per_ray"],
-                       warp_inst_per_ray=c["warp_inst_per_ray"])
+    k_trace = {"kernel": "k_trace", "unit_of_work": "traced ray", "units_per_launch": rays_l,
+               "ms_per_launch": trace_ms, "scene_classes": classes}
+    dram = _weighted(by_class, "k_trace", "dram_bytes_per_ray", "rays")
+    k_trace["traffic"] = dram / n if dram is not None else None
+    inst = _weighted(by_class, "k_trace", "warp_inst_per_ray", "rays")
+    tinst = _weighted(by_class, "k_trace", "thread_inst_per_ray", "rays")
+    if inst is not None:
+        achieved = inst / n / (trace_ms * 1e-3) * 1e-9
+        k_trace.update(bound="issue", achieved=achieved, peak=issue_peak, unit="G warp-inst/s",
+                       frac=achieved / issue_peak, peak_kind=issue_kind,
+                       warp_inst_per_ray=inst / max(stage["rays"], 1),
+                       active_lanes_per_inst=tinst / inst if tinst else None)
     else:
         k_trace.update(bound="issue", achieved=None, peak=None, unit="G warp-inst/s", frac=None,
-                       note="instruction counts not captured for this workload")
+                       note="instruction counts not captured for these scenes")
     if costs:
         model = 32 + 16 + 64 * costs["nodes_per_ray"] + 48 * costs["tris_per_ray"]
         k_trace["hbm_model"] = {"bytes_per_ray": model, "note": "ray + hit + 64 B per binary-BVH node visit and 48 B per "
@@ -375,12 +400,11 @@ def kernel_rooflines(workload: str, stage: dict, hbm: float, peak_kind: str, sm_
     shade_ms = stage["shade_ms"] / n
     alg = B_SHADE * verts_l
     ach = alg / (shade_ms * 1e-3) * 1e-9
-    c = cnt.get("k_resolve+k_sample", {})
+    dram = _weighted(by_class, "k_resolve+k_sample", "dram_bytes_per_vertex", "shaded")
     k_shade = {"kernel": "k_resolve+k_sample", "unit_of_work": "shaded vertex", "units_per_launch": verts_l,
                "ms_per_launch": shade_ms, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                "frac": ach / hbm, "peak_kind": peak_kind, "bytes_per_unit": B_SHADE,
-               "algorithmic_bytes_per_launch": alg,
-               "traffic": c["dram_bytes_per_vertex"] * verts_l if c.get("dram_bytes_per_vertex") else None}
+               "algorithmic_bytes_per_launch": alg, "traffic": dram / n if dram is not None else None}
     kernels += [k_trace, k_shade]
     # dominant by total device time of the run
     totals = {"k_paths": stage["path_ms"], "k_trace": stage["trace_ms"], "k_resolve+k_sample": stage["shade_ms"]}
@@ -389,13 +413,14 @@ def kernel_rooflines(workload: str, stage: dict, hbm: float, peak_kind: str, sm_
     return kernels, dominant
 
 
-def stage_split(job_list, passes_list):
+def stage_split(job_list, passes_list, classes):
     """Renders the jobs one after another with stage timing and returns the
     summed stage times and work for the rooflines: rays and shaded vertices
-    of the wavefront jobs, camera samples of the path-kernel jobs."""
+    of the wavefront jobs, camera samples of the path-kernel jobs, in total
+    and per scene class (classes[i] names job i's)."""
     out = {"trace_ms": 0.0, "shade_ms": 0.0, "trace_launches": 0, "rays": 0, "shaded": 0, "kernel_ms": 0.0,
-           "path_ms": 0.0, "path_launches": 0, "paths": 0}
-    for job, p in zip(job_list, passes_list):
+           "path_ms": 0.0, "path_launches": 0, "paths": 0, "by_class": {}}
+    for job, p, cls in zip(job_list, passes_list, classes):
         path_kernel = job.info.path_kernel
         job.set_stage_timing(True)
         s0 = job.stats()
@@ -404,11 +429,15 @@ def stage_split(job_list, passes_list):
         job.set_stage_timing(False)
         for k in ("trace_ms", "shade_ms", "trace_launches", "kernel_ms", "path_ms", "path_launches"):
             out[k] += s1[k] - s0[k]
+        c = out["by_class"].setdefault(cls, {"rays": 0, "shaded": 0, "paths": 0})
         if path_kernel:
-            out["paths"] += s1["paths"] - s0["paths"]
+            for k in ("paths",):
+                out[k] += s1[k] - s0[k]
+                c[k] += s1[k] - s0[k]
         else:
-            out["rays"] += s1["rays"] - s0["rays"]
-            out["shaded"] += s1["shaded"] - s0["shaded"]
+            for k in ("rays", "shaded"):
+                out[k] += s1[k] - s0[k]
+                c[k] += s1[k] - s0[k]
     return out
 
 
@@ -451,6 +480,9 @@ def main():
     ap.add_argument("--duration", type=float, default=120.0, help="serve: seconds of arrivals")
     ap.add_argument("--policy", type=int, default=0, help="serve: 0 round robin, 1 shortest remaining first")
     ap.add_argument("--no-tune", action="store_true", help="batch/serve: skip the autotuner (defaults)")
+    ap.add_argument("--serve-stress", action="store_true", help="stress: also serve the job through hasty_server_*")
+    ap.add_argument("--jobs", type=int, default=64, help="batch: the first N jobs of the 64-job mix (profiling)")
+    ap.add_argument("--mix-job", type=int, default=-1, help="plain: render job K of the 64-job mix instead (profiling)")
     ap.add_argument("--lane-paths", type=int, default=0,
                     help="batch/serve: path slots per render lane instead of the tuned value (profiling small batches)")
     args = ap.parse_args()
@@ -497,16 +529,23 @@ def run_single(args):
     import torch
     from hastyrenderer_gb300 import Context, RenderJob
     dist, rank, world, local_rank = _dist_setup(args)
-    if args.workload == "plain":
+    if args.workload == "plain" and args.mix_job >= 0:
+        mj = mix_jobs()[args.mix_job] if rank == 0 else None
+        wl, passes, cls = f"mix_job_{args.mix_job}", args.spp_per_step, None
+    elif args.workload == "plain":
         job_path = make_plain_job(_bench_dir("hasty_bench_c1")) if rank == 0 else None
-        wl, passes = WORKLOAD_PLAIN, args.spp_per_step
+        wl, passes, cls = WORKLOAD_PLAIN, args.spp_per_step, "plain"
     else:
         job_path = make_cornell_job(_bench_dir("hasty_bench_c0")) if rank == 0 else None
-        wl, passes = WORKLOAD_CORNELL, 64
+        wl, passes, cls = WORKLOAD_CORNELL, 64, "cornell"
     if dist is not None:
         dist.barrier()
-    job_path = os.path.join(_bench_dir("hasty_bench_c1" if args.workload == "plain" else "hasty_bench_c0"),
-                            "renderJob.json")
+    if args.workload == "plain" and args.mix_job >= 0:
+        mj = mix_jobs()[args.mix_job]
+        job_path, cls = mj["path"], "mix:" + scene_class(mj)
+    else:
+        job_path = os.path.join(_bench_dir("hasty_bench_c1" if args.workload == "plain" else "hasty_bench_c0"),
+                                "renderJob.json")
     torch.cuda.init()
     ctx = Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0)
 
@@ -528,6 +567,10 @@ def run_single(args):
     e2e_s = time.perf_counter() - t0
     assert n_est == args.steps * passes
     del est
+    job.sync()
+    # every ray and vertex this process shades (for per-unit ncu counters,
+    # which cover all launches of the process)
+    work = {k: job.stats()[k] for k in ("rays", "shaded", "paths")}
 
     # device-resident timing (both render lanes, as a user's render runs)
     job.reset()
@@ -550,7 +593,10 @@ def run_single(args):
         if dist is not None:
             dist.barrier()
     s1 = job.stats()
-    stage = stage_split([job] * args.steps, [passes] * args.steps)
+    s2 = job.stats()
+    stage = stage_split([job] * args.steps, [passes] * args.steps, [cls] * args.steps)
+    for k in work:
+        work[k] += s2[k] + stage[k]
     t = max_over_ranks(max((s1["kernel_ms"] - s0["kernel_ms"]) * 1e-3, 1e-9), dist, "cuda")
     samples = args.steps * passes * W * H
     clocks = sampler.summary()
@@ -559,7 +605,7 @@ def run_single(args):
         cpu, costs = (None, None)
         if not args.no_cpu_baseline:
             cpu, costs = cpu_baseline(args.workload, args.cpu_budget)
-        kernels, roof = kernel_rooflines(args.workload, stage, hbm, peak_kind, clocks.get("sm_mhz"), costs)
+        kernels, roof = kernel_rooflines(stage, hbm, peak_kind, clocks.get("sm_mhz"), costs)
         line = {
             "metric": "samples/s", "value": samples * world / t, "unit": "samples/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
@@ -575,6 +621,7 @@ def run_single(args):
             "wall_ms_per_step": wall / args.steps * 1e3,
             "gpu_launches": s1["kernel_launches"] - s0["kernel_launches"],
             "roofline": roof, "kernels": kernels, "cpu_baseline": cpu,
+            "work_in_process": work,
             "e2e": {"value": samples * world / e2e_s, "unit": "samples/s",
                     "h2d_bytes_per_step": int(info.device_bytes // args.steps), "d2h_bytes_per_step": W * H * 3 * 4,
                     "includes": "job load (parse, BVH build, upload) + steps + a colour read-back per step",
@@ -600,7 +647,7 @@ def run_batch(args):
         return
     torch.cuda.init()
     t_gen = time.perf_counter()
-    jobs = mix_jobs()
+    jobs = mix_jobs()[: max(1, args.jobs)]
     gen_s = time.perf_counter() - t_gen
     ctx = Context(local_rank, Context.BINARY_BVH if args.bvh == "binary" else 0)
     spp = [j["spp"] for j in jobs]
@@ -640,7 +687,7 @@ def run_batch(args):
             ms = s1["kernel_ms"] - s0["kernel_ms"]
             plain_ms += ms
             plain_rays += s1["rays"] - s0["rays"]
-            key = f"{j['kind']}{j['spheres'] or ''}"
+            key = scene_class(j)
             c = per_class.setdefault(key, {"samples": 0, "plain_ms": 0.0})
             c["samples"] += workloads.job_samples(j)
             c["plain_ms"] += ms
@@ -672,14 +719,14 @@ def run_batch(args):
     # stage split on 1/8 of every job's passes (one render lane, for the rooflines)
     for r in resident:
         r.reset()
-    stage = stage_split(resident, [max(1, p // 8) for p in spp])
+    stage = stage_split(resident, [max(1, p // 8) for p in spp], ["mix:" + scene_class(j) for j in jobs])
     for r in resident:
         r.release_paths()
         r.close()
     cpu, costs = (None, None)
     if not args.no_cpu_baseline:
         cpu, costs = cpu_baseline("batch", args.cpu_budget)
-    kernels, roof = kernel_rooflines("batch", stage, hbm, peak_kind, clocks.get("sm_mhz"), costs)
+    kernels, roof = kernel_rooflines(stage, hbm, peak_kind, clocks.get("sm_mhz"), costs)
     batch_sps = total * args.steps / (dev_ms * 1e-3)
     plain_sps = total / (plain_ms * 1e-3)
     for c in per_class.values():
@@ -688,7 +735,8 @@ def run_batch(args):
         "metric": "samples/s", "value": batch_sps, "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes)",
-        "config": {"workload": WORKLOAD_BATCH, "jobs": len(jobs), "samples_per_step": total,
+        "config": {"workload": WORKLOAD_BATCH if len(jobs) == 64 else f"first_{len(jobs)}_jobs_of_the_mix",
+                   "jobs": len(jobs), "samples_per_step": total,
                    "step": "every job's full pass count in one hasty_batch_render call",
                    "batching": eargs, "l2": "working set > L2 (path state + scenes), no flush",
                    "parallelism": "one GPU"},
@@ -937,8 +985,36 @@ def run_stress(args):
         "estimate_finite": bool(np.isfinite(est).all()), "media_overflow": s1["media_overflow"],
         "trial_cap": s1["trial_cap"], "clocks": sampler.summary(),
     }
+    if args.serve_stress:
+        line["served"] = serve_stress(job, path, args.steps)
     print(json.dumps(line), flush=True)
     job.close()
+
+
+def serve_stress(job, path, passes):
+    """The stress job served: one request of `passes` passes through
+    hasty_server_* (scene loaded by the server's loader threads), its latency
+    and rate, and its sums against the single-job path's for the same passes
+    and seed (bit-identical expected)."""
+    import numpy as np
+    from hastyrenderer_gb300 import Server
+    job.reset()
+    job.render_passes(passes, sync=True)
+    plain = job.read_sums()[0]
+    seed = job.info.seed
+    with Server(paths_in_flight=1 << 24, lanes=2) as srv:
+        t0 = time.perf_counter()
+        rid = srv.submit(path, passes=passes, seed=seed)
+        srv.wait_idle(-1)
+        res = srv.poll(wait_ms=0)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        sums = srv.read_sums(rid)
+    r = res[0]
+    return {"status": r["status"], "latency_ms": r["latency_ms"], "wall_s": wall,
+            "samples_per_s_device": r["samples"] / max(st["device_ms"] * 1e-3, 1e-9),
+            "samples_per_s_wall": r["samples"] / wall, "equal_to_single_job_path": bool(np.array_equal(sums, plain)),
+            "note": "latency includes the server's scene load (parse, BVH build, upload)"}
 
 
 
