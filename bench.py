@@ -54,20 +54,33 @@ WORKLOAD_BATCH = "mixed_64_jobs_cornell_or_field50_200_800_128x128_to_1024x768_s
 # the triangle's attributes (92 B); texel reads are not counted.
 B_SHADE = 2 * 96 + 92
 # Per-unit hardware counters of the wavefront kernels, per scene class, from
-# small ncu captures (three launches each of k_trace, k_resolve and k_sample
-# after the first three): DRAM bytes (dram__bytes_read.sum +
-# dram__bytes_write.sum) per traced ray and per shaded vertex, and for the
+# small ncu captures (every k_trace, k_resolve and k_sample launch of a
+# one-step run: three batches of 2 passes, of 64 for the Cornell box workload,
+# divided by the rays and vertices the process traced and shaded): DRAM
+# bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced ray and
+# per shaded vertex, and for the
 # closest-hit kernel warp instructions and thread instructions per ray
 # (smsp__inst_executed.sum, smsp__thread_inst_executed.sum). Classes: "plain"
 # (the 1080p 800-sphere field), "cornell" (the 256x256 box), "mix:<kind>"
-# (one job of each scene kind of the 64-job mix, rendered alone). None where
-# not captured. They give each kernel's traffic and the closest-hit kernel's
+# (one job of each scene kind of the 64-job mix, rendered alone; a class
+# without a capture gives null). They give each kernel's traffic and the closest-hit kernel's
 # issue rate for the units a launch processed; a run covering several classes
 # weights them by each class's rays and vertices.
 COUNTERS = {
-    "plain": {"k_trace": {"dram_bytes_per_ray": 461.4e6 / 3.57e6, "warp_inst_per_ray": None,
-                          "thread_inst_per_ray": None},
-              "k_resolve+k_sample": {"dram_bytes_per_vertex": 1678.8e6 / 1.407e6}},
+    "plain": {"k_trace": {"dram_bytes_per_ray": 128.67, "warp_inst_per_ray": 227.73, "thread_inst_per_ray": 4535.8},
+              "k_resolve+k_sample": {"dram_bytes_per_vertex": 1038.97}},
+    "cornell": {"k_trace": {"dram_bytes_per_ray": 79.65, "warp_inst_per_ray": 74.53, "thread_inst_per_ray": 1054.89},
+                "k_resolve+k_sample": {"dram_bytes_per_vertex": 862.87}},
+    "mix:cornell": {"k_trace": {"dram_bytes_per_ray": 73.15, "warp_inst_per_ray": 69.71, "thread_inst_per_ray": 1036.48},
+                    "k_resolve+k_sample": {"dram_bytes_per_vertex": 817.28}},
+    "mix:field50": {"k_trace": {"dram_bytes_per_ray": 78.50, "warp_inst_per_ray": 58.44, "thread_inst_per_ray": 1178.49},
+                    "k_resolve+k_sample": {"dram_bytes_per_vertex": 871.84}},
+    "mix:field200": {"k_trace": {"dram_bytes_per_ray": 89.84, "warp_inst_per_ray": 100.99,
+                                 "thread_inst_per_ray": 1966.27},
+                     "k_resolve+k_sample": {"dram_bytes_per_vertex": 916.45}},
+    "mix:field800": {"k_trace": {"dram_bytes_per_ray": 134.29, "warp_inst_per_ray": 224.96,
+                                 "thread_inst_per_ray": 4318.20},
+                     "k_resolve+k_sample": {"dram_bytes_per_vertex": 1016.86}},
 }
 REF_PASSES_PER_STEP = 8      # reference arm: passes of the CPU sample per step
 ISSUE_PER_SM_PER_CLOCK = 4   # warp instructions per SM and clock (one per scheduler)

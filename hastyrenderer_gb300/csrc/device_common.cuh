@@ -329,7 +329,12 @@ __device__ __forceinline__ Prob compute_probability(float m, float s, float t, f
   p.FD = p.refr ? fresnel_dielectric(cos_o, p.cosT, eo, er) : 1.0f;
   float mD = (1.0f - t) * (1.0f - m) * (1.0f - 0.5f * s);
   float mS = mixf(mixf(0.5f * s, p.FD, t), 1.0f, m);
-  float mR = float((1.0 - double(p.FD)) * double(t) * (1.0 - double(m)));
+  // t = +0 with FD <= 1 and m <= 1: the double product is a non-negative
+  // value times +0 times a non-negative value, i.e. +0, so the FP64 pipe
+  // (a small fraction of the FP32 rate on this GPU) is skipped for it
+  float mR = (__float_as_uint(t) == 0u && p.FD <= 1.0f && m <= 1.0f)
+                 ? 0.0f
+                 : float((1.0 - double(p.FD)) * double(t) * (1.0 - double(m)));
   if (!(lobes & kLobeDiffuse)) mD = 0.0f;
   if (!(lobes & kLobeConcentrated)) { mS = 0.0f; mR = 0.0f; }
   float sum = mD + mS + mR;
@@ -359,6 +364,7 @@ __device__ __forceinline__ void anisotropy_params(const Inter& it, V3 ns, float 
 __device__ __forceinline__ V3 eval_diffuse(float nswi, V3 albedo, float nscale, float m, float s, float t) {
   if (nswi < 0.0f) return V3();
   float k = HINVPI_F * nscale * (1.0f - 0.5f * s);
+  if (t == 0.0f && m == 0.0f) return albedo * k;   // the double product is k exactly (1 - (+/-0) = 1)
   double kd = double(k) * (1.0 - double(t)) * (1.0 - double(m));
   return albedo * float(kd);
 }

@@ -156,18 +156,18 @@ std::vector<PackedChunk> pack_batch(const std::vector<PackedJob>& jobs, const st
   return out;
 }
 
-std::vector<int> class_order(const std::vector<PackedJob>& jobs, const std::vector<int>& order, bool path_kernel) {
+std::vector<int> class_order(const std::vector<PackedJob>& jobs, const std::vector<int>& order, int cls) {
   std::vector<int> out;
-  for (int j : order) if (jobs[size_t(j)].path_kernel == path_kernel) out.push_back(j);
+  for (int j : order) if (kernel_class(jobs[size_t(j)]) == cls) out.push_back(j);
   return out;
 }
 
 std::vector<PackedChunk> pack_next(const std::vector<PackedJob>& jobs, const std::vector<int>& order,
                                    std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots,
-                                   int64_t job_samples, bool& path_turn) {
-  for (int attempt = 0; attempt < 2; ++attempt) {
-    const bool cls = path_turn;
-    path_turn = !path_turn;
+                                   int64_t job_samples, int& turn) {
+  for (int attempt = 0; attempt < kKernelClasses; ++attempt) {
+    const int cls = ((turn % kKernelClasses) + kKernelClasses) % kKernelClasses;
+    turn = cls + 1;
     std::vector<PackedChunk> c = pack_batch(jobs, class_order(jobs, order, cls), pass_base, left, slots, job_samples);
     if (!c.empty()) return c;
   }
@@ -203,6 +203,7 @@ void batch_render_packed(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes
     for (int a = 0; a < 3; ++a) pj[i].acc[a] = j->acc[a];
     pj[i].npix = j->sd.width * j->sd.height;
     pj[i].path_kernel = j->path_kernel;
+    pj[i].simple_trace = simple_trace_bvh(j->sd);
     base[i] = uint32_t(j->samples_done);
     left[i] = passes[i];
     largest = std::max<int64_t>(largest, pj[i].npix);
@@ -223,9 +224,9 @@ void batch_render_packed(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes
   ck(cudaEventCreate(&b), "event");
   ck(cudaEventRecord(a, L.acc_stream), "event");
   L.wait_for(L.acc_stream);
-  bool path_turn = true;
+  int turn = 0;
   for (;;) {
-    std::vector<PackedChunk> chunks = pack_next(pj, order, base, left, lane_paths, 0, path_turn);
+    std::vector<PackedChunk> chunks = pack_next(pj, order, base, left, lane_paths, 0, turn);
     if (chunks.empty()) break;
     bool more = false;
     for (int i : order) more = more || left[size_t(i)] > 0;

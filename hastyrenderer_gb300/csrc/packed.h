@@ -28,7 +28,14 @@ struct PackedJob {
   double* acc[3] = {nullptr, nullptr, nullptr};   // FP64 sums: colour, normal, albedo (npix x 3 each)
   int32_t npix = 0;
   bool path_kernel = false;                      // rendered by the path kernel (use_path_kernel)
+  bool simple_trace = false;                     // closest hits one ray per thread (simple_trace_bvh)
 };
+
+// Kernel class of a job; a batch holds jobs of one class: 0 wavefront with
+// the persistent closest-hit kernel, 1 wavefront with one ray per thread
+// (BVHs of a few nodes), 2 path kernel.
+constexpr int kKernelClasses = 3;
+inline int kernel_class(const PackedJob& j) { return j.path_kernel ? 2 : (j.simple_trace ? 1 : 0); }
 
 // n_passes consecutive passes of job `job` from pass_base.
 struct PackedChunk {
@@ -93,13 +100,14 @@ struct PackedLanes {
 std::vector<PackedChunk> pack_batch(const std::vector<PackedJob>& jobs, const std::vector<int>& order,
                                     std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots,
                                     int64_t job_samples = 0);
-// Jobs of `order` in one kernel class (path kernel or wavefront), order kept.
-std::vector<int> class_order(const std::vector<PackedJob>& jobs, const std::vector<int>& order, bool path_kernel);
-// Alternates the two kernel classes between consecutive batches while both
-// have passes left, so batches of either class run side by side on the lanes.
+// Jobs of `order` in one kernel class (kernel_class), order kept.
+std::vector<int> class_order(const std::vector<PackedJob>& jobs, const std::vector<int>& order, int cls);
+// Cycles through the kernel classes between consecutive batches while more
+// than one has passes left, so batches of different classes run side by side
+// on the lanes (`turn`: the class to try first, advanced past the one taken).
 std::vector<PackedChunk> pack_next(const std::vector<PackedJob>& jobs, const std::vector<int>& order,
                                    std::vector<uint32_t>& pass_base, std::vector<int32_t>& left, int64_t slots,
-                                   int64_t job_samples, bool& path_turn);
+                                   int64_t job_samples, int& turn);
 
 // Path slots of a lane: 16M camera samples (whole frames of the largest
 // job at least), or `requested` when positive.

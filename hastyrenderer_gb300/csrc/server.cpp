@@ -256,7 +256,7 @@ void hasty_server::batch_loop() {
   cudaEvent_t origin = nullptr;       // reference point of the batches' device times
   cudaStream_t copy_stream = nullptr;
   double covered_ms = 0.0;            // device time counted so far ends here (ms after origin)
-  bool path_turn = true;              // kernel class of the next batch (pack_next)
+  int turn = 0;                       // kernel class of the next batch (pack_next)
   auto take_event = [&]() {
     if (!spare.empty()) { cudaEvent_t e = spare.back(); spare.pop_back(); return e; }
     cudaEvent_t e = nullptr;
@@ -310,6 +310,7 @@ void hasty_server::batch_loop() {
         j.seed = r->seed;
         j.npix = int32_t(r->npix);
         j.path_kernel = use_path_kernel(ctx, j.sc);
+        j.simple_trace = simple_trace_bvh(j.sc);
         for (int a = 0; a < 3; ++a) j.acc[a] = r->d_acc + size_t(a) * 3 * r->npix;
         pass_base[size_t(r->slot)] = 0;
         left[size_t(r->slot)] = r->passes;
@@ -318,7 +319,7 @@ void hasty_server::batch_loop() {
       // one batch per free lane
       while (int(inflight.size()) < lanes.n_lanes && !order.empty()) {
         std::vector<PackedChunk> chunks =
-            pack_next(jobs, order, pass_base, left, lanes.lane_paths, cfg.quantum_samples, path_turn);
+            pack_next(jobs, order, pass_base, left, lanes.lane_paths, cfg.quantum_samples, turn);
         if (chunks.empty()) break;
         InFlight f;
         f.start = take_event();

@@ -95,7 +95,28 @@ __device__ __forceinline__ uint32_t persistent_trace(uint32_t n, uint32_t* next,
   return overflows;
 }
 
-template <int KIND>
+// One ray per thread over a grid-sized stride, for BVHs of a few nodes
+// (short rays of similar length: the dynamic fetch's bookkeeping and its
+// partly idle warps can cost more than it saves there). Same steps per ray
+// as persistent_trace, so the same hits.
+template <int KIND, class Fetch, class Done>
+__device__ __forceinline__ uint32_t simple_trace(uint32_t n, Fetch fetch, Done done) {
+  typename TravOf<KIND>::T tr;
+  typename TravOf<KIND>::T::Entry stack[TravOf<KIND>::T::kDepth];
+  const float4* nodes = nullptr;
+  const float4* tris = nullptr;
+  int rid = 0;
+  uint32_t overflows = 0;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    fetch(k, tr, nodes, tris, rid);
+    while (!tr.step(nodes, tris, stack)) {}
+    done(rid, tr.best);
+    overflows += tr.overflow ? 1u : 0u;
+  }
+  return overflows;
+}
+
+template <int KIND, bool SIMPLE = false>
 __global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
   const uint32_t n = P.counts[2 + q];
   if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
@@ -114,19 +135,19 @@ __global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
   // environment are visible iff they hit nothing (Scene.cpp:575-585 with no
   // emissive triangle), so they stop at their first hit.
   const bool nee_any = sc.n_light_tris == 0;
-  const uint32_t overflows = persistent_trace<KIND>(
-      n, &P.counts[kFetchCounter],
-      [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
-        rid = rq[k];
-        if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
-        float4 o = P.ray_o[rid], d = P.ray_d[rid];
-        tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
-        tr.any = nee_any && (rid & 1);
-        nodes = sc.nodes;
-        tris = sc.isect_tris;
-        HASTY_TRAV_LIMITS(tr, sc.n_nodes, sc.n_tris);
-      },
-      [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
+  auto fetch = [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
+    rid = rq[k];
+    if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
+    float4 o = P.ray_o[rid], d = P.ray_d[rid];
+    tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
+    tr.any = nee_any && (rid & 1);
+    nodes = sc.nodes;
+    tris = sc.isect_tris;
+    HASTY_TRAV_LIMITS(tr, sc.n_nodes, sc.n_tris);
+  };
+  auto done = [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); };
+  const uint32_t overflows = SIMPLE ? simple_trace<KIND>(n, fetch, done)
+                                    : persistent_trace<KIND>(n, &P.counts[kFetchCounter], fetch, done);
   add_overflows(&P.stats[ST_STACK_OVERFLOW], overflows);
 }
 
@@ -141,7 +162,7 @@ __global__ void k_trace_rays(SceneDev sc, const float* rays, int n, float4* hits
 
 // Packed multi-job batches: each ray names its chunk in ray_o.w (bits), and
 // the chunk's BVH comes from the kernel-parameter table.
-template <int KIND>
+template <int KIND, bool SIMPLE = false>
 __global__ void TRACE_BOUNDS k_trace_packed(const __grid_constant__ TraceTable T, PathsDev P, int q) {
   const uint32_t n = P.counts[2 + q];
   if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
@@ -157,20 +178,20 @@ __global__ void TRACE_BOUNDS k_trace_packed(const __grid_constant__ TraceTable T
     }
     return;
   }
-  const uint32_t overflows = persistent_trace<KIND>(
-      n, &P.counts[kFetchCounter],
-      [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
-        rid = rq[k];
-        if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
-        float4 o = P.ray_o[rid], d = P.ray_d[rid];
-        const TraceChunk& c = T.c[__float_as_uint(o.w)];
-        tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
-        tr.any = c.nee_first_hit != 0 && (rid & 1);   // as k_trace
-        nodes = c.nodes;
-        tris = c.tris;
-        HASTY_TRAV_LIMITS(tr, c.n_nodes, c.n_tris);
-      },
-      [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); });
+  auto fetch = [&](uint32_t k, typename TravOf<KIND>::T& tr, const float4*& nodes, const float4*& tris, int& rid) {
+    rid = rq[k];
+    if (!HASTY_IN_BOUNDS(rid >= 0 && rid < 2 * P.capacity, BB_QUEUE)) rid = 0;
+    float4 o = P.ray_o[rid], d = P.ray_d[rid];
+    const TraceChunk& c = T.c[__float_as_uint(o.w)];
+    tr.init(o.x, o.y, o.z, d.x, d.y, d.z);
+    tr.any = c.nee_first_hit != 0 && (rid & 1);   // as k_trace
+    nodes = c.nodes;
+    tris = c.tris;
+    HASTY_TRAV_LIMITS(tr, c.n_nodes, c.n_tris);
+  };
+  auto done = [&](int rid, const Hit& h) { P.hit[rid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri)); };
+  const uint32_t overflows = SIMPLE ? simple_trace<KIND>(n, fetch, done)
+                                    : persistent_trace<KIND>(n, &P.counts[kFetchCounter], fetch, done);
   add_overflows(&P.stats[ST_STACK_OVERFLOW], overflows);
 }
 
@@ -237,6 +258,20 @@ int persistent_blocks(PersistentShape s, int cap_per_sm) {
 
 }  // namespace
 
+// Wide BVHs of at most this many nodes are traced one ray per thread
+// (simple_trace); HASTY_TRACE_SIMPLE_NODES overrides it (tuning). Cornell
+// box, 36 triangles: closest hits 0.268 -> 0.235 ms per bounce launch, 664 ->
+// 707 M samples/s.
+constexpr int kSimpleTraceNodes = 64;
+int simple_trace_nodes() {
+  static const int v = [] {
+    const char* e = std::getenv("HASTY_TRACE_SIMPLE_NODES");
+    return e ? std::atoi(e) : kSimpleTraceNodes;
+  }();
+  return v;
+}
+bool simple_trace_bvh(const SceneDev& sc) { return sc.bvh_kind == 1 && sc.n_nodes <= simple_trace_nodes(); }
+
 // The persistent kernels take rays through P.counts[kFetchCounter], cleared
 // on the stream before each launch. Grids: the SMs' resident blocks (at most
 // blocks_per_sm per SM when given), fewer when the queue bound is smaller.
@@ -257,10 +292,15 @@ void launch_trace_packed(const TraceTable& t, const PathsDev& p, int q, int max_
   static PersistentShape shape[2] = {{0, 0}, {0, 0}};
   const int k = t.bvh_kind == 1 ? 1 : 0;
   if (!shape[k].sms) shape[k] = k ? persistent_shape(k_trace_packed<1>) : persistent_shape(k_trace_packed<0>);
-  int blocks = k ? std::min(persistent_blocks(shape[k], blocks_per_sm), std::max(1, (max_rays + 127) / 128))
-                 : std::max(1, (max_rays + 127) / 128);
+  int max_nodes = 0;
+  for (int c = 0; c < t.n; ++c) max_nodes = std::max(max_nodes, t.c[c].n_nodes);
+  const int simple = k && max_nodes <= simple_trace_nodes() ? 1 : 0;
+  const int grid = persistent_blocks(shape[k], blocks_per_sm);
+  int blocks = k && !simple ? std::min(grid, std::max(1, (max_rays + 127) / 128))
+                            : std::min(8 * grid, std::max(1, (max_rays + 127) / 128));
   cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
-  if (k) k_trace_packed<1><<<blocks, 128, 0, st>>>(t, p, q);
+  if (k && simple) k_trace_packed<1, true><<<blocks, 128, 0, st>>>(t, p, q);
+  else if (k) k_trace_packed<1><<<blocks, 128, 0, st>>>(t, p, q);
   else k_trace_packed<0><<<blocks, 128, 0, st>>>(t, p, q);
 }
 
@@ -268,10 +308,13 @@ void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cu
   static PersistentShape shape[2] = {{0, 0}, {0, 0}};
   int k = sc.bvh_kind == 1 ? 1 : 0;
   if (!shape[k].sms) shape[k] = k ? persistent_shape(k_trace<1>) : persistent_shape(k_trace<0>);
-  int blocks = k ? std::min(persistent_blocks(shape[k], blocks_per_sm), std::max(1, (max_rays + 127) / 128))
-                 : std::max(1, (max_rays + 127) / 128);
+  const int simple = simple_trace_bvh(sc) ? 1 : 0;
+  const int grid = persistent_blocks(shape[k], blocks_per_sm);
+  int blocks = k && !simple ? std::min(grid, std::max(1, (max_rays + 127) / 128))
+                            : std::min(8 * grid, std::max(1, (max_rays + 127) / 128));
   cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
-  if (k) k_trace<1><<<blocks, 128, 0, st>>>(sc, p, q);
+  if (k && simple) k_trace<1, true><<<blocks, 128, 0, st>>>(sc, p, q);
+  else if (k) k_trace<1><<<blocks, 128, 0, st>>>(sc, p, q);
   else k_trace<0><<<blocks, 128, 0, st>>>(sc, p, q);
 }
 

@@ -84,6 +84,10 @@ void launch_raygen(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, cu
 // blocks_per_sm > 0 caps the persistent wide-BVH grid at that many resident
 // blocks per SM (room for another stream's kernels); 0: all that fit.
 void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cudaStream_t stream, int blocks_per_sm = 0);
+// True when sc's closest hits run one ray per thread instead of the
+// persistent kernel: a wide BVH of at most simple_trace_nodes() nodes.
+int simple_trace_nodes();
+bool simple_trace_bvh(const SceneDev& sc);
 void launch_shade(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, int q, int max_paths, cudaStream_t stream);
 void launch_accumulate(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, double* acc_color, double* acc_normal,
                        double* acc_albedo, cudaStream_t stream);
