@@ -69,10 +69,10 @@ B_SHADE = 2 * 96 + 92
 COUNTERS = {
     "plain": {"k_trace": {"dram_bytes_per_ray": 128.67, "warp_inst_per_ray": 227.73, "thread_inst_per_ray": 4535.8},
               "k_resolve+k_sample": {"dram_bytes_per_vertex": 1038.97}},
-    "cornell": {"k_trace": {"dram_bytes_per_ray": 79.65, "warp_inst_per_ray": 74.53, "thread_inst_per_ray": 1054.89},
-                "k_resolve+k_sample": {"dram_bytes_per_vertex": 862.87}},
-    "mix:cornell": {"k_trace": {"dram_bytes_per_ray": 73.15, "warp_inst_per_ray": 69.71, "thread_inst_per_ray": 1036.48},
-                    "k_resolve+k_sample": {"dram_bytes_per_vertex": 817.28}},
+    "cornell": {"k_trace": {"dram_bytes_per_ray": 80.77, "warp_inst_per_ray": 63.33, "thread_inst_per_ray": 982.99},
+                "k_resolve+k_sample": {"dram_bytes_per_vertex": 863.61}},
+    "mix:cornell": {"k_trace": {"dram_bytes_per_ray": 73.41, "warp_inst_per_ray": 60.67, "thread_inst_per_ray": 986.99},
+                    "k_resolve+k_sample": {"dram_bytes_per_vertex": 819.35}},
     "mix:field50": {"k_trace": {"dram_bytes_per_ray": 78.50, "warp_inst_per_ray": 58.44, "thread_inst_per_ray": 1178.49},
                     "k_resolve+k_sample": {"dram_bytes_per_vertex": 871.84}},
     "mix:field200": {"k_trace": {"dram_bytes_per_ray": 89.84, "warp_inst_per_ray": 100.99,
