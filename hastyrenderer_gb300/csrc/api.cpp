@@ -347,8 +347,6 @@ void render_batch(hasty_job& j, int n_passes, int lane, bool more_batches) {
     for (int bounce = 0; bounce < j.sd.max_depth; ++bounce) {
       int q = bounce & 1;
       timed(1, [&] { launch_trace(j.sd, pd, q, 2 * max_paths, ls, trace_cap); });
-      ck(cudaMemsetAsync(&pd.counts[q ^ 1], 0, sizeof(uint32_t), ls), "memset count");
-      ck(cudaMemsetAsync(&pd.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), ls), "memset count");
       timed(2, [&] { launch_shade(j.sd, pd, b, q, max_paths, ls); });
     }
     j.trace_launches += uint64_t(j.sd.max_depth);

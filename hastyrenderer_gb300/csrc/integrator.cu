@@ -209,6 +209,8 @@ __global__ void __launch_bounds__(256) k_raygen(const __grid_constant__ Src src,
     uint32_t n = max_depth_of(src) > 0 ? uint32_t(n_paths) : 0u;
     P.counts[0] = n; P.counts[1] = 0; P.counts[2] = n; P.counts[3] = 0;
     P.counts[kMediaPoolCounter] = 0;
+    P.counts[kFetchCounter] = 0;   // for the first closest-hit launch
+    P.counts[kSampleCount] = 0;
     atomicAdd(&P.stats[ST_PATHS], (unsigned long long)n_paths);
   }
   if (s >= n_paths) return;
@@ -461,6 +463,7 @@ __global__ void __launch_bounds__(RT, 1024 / RT) k_resolve(const __grid_constant
   __shared__ uint32_t s_cnt[kWarps][3];
   __shared__ uint32_t s_base;
   const uint32_t n_in = P.counts[q];
+  if (blockIdx.x == 0 && threadIdx.x == 0) P.counts[kFetchCounter] = 0;   // for the next closest-hit launch
   if (blockIdx.x * blockDim.x >= n_in) return;    // whole block past the queue
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool valid = i < n_in;
@@ -736,8 +739,8 @@ void launch_raygen_packed(const ChunkTable& t, const PathsDev& p, cudaStream_t s
   k_raygen<ChunkTable><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(t, p);
 }
 
+// The sample-queue counter is cleared by the closest-hit launch before.
 void launch_shade(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, int q, int max_paths, cudaStream_t st) {
-  cudaMemsetAsync(&p.counts[kSampleCount], 0, sizeof(uint32_t), st);
   const OneJob src{sc, b};
   k_resolve<OneJob><<<(max_paths + kResolveThreads - 1) / kResolveThreads, kResolveThreads, 0, st>>>(src, p, q);
   k_sample<OneJob><<<(max_paths + kSampleThreads - 1) / kSampleThreads, kSampleThreads, 0, st>>>(src, p, q);
@@ -745,7 +748,6 @@ void launch_shade(const SceneDev& sc, const PathsDev& p, const BatchDesc& b, int
 
 void launch_shade_packed(const ChunkTable& t, const PathsDev& p, int q, int max_paths, cudaStream_t st,
                          int resolve_threads, int sample_threads) {
-  cudaMemsetAsync(&p.counts[kSampleCount], 0, sizeof(uint32_t), st);
   // block shapes chosen per batch (the autotuner's candidates); 1024 threads per SM each
   if (resolve_threads == 128) k_resolve<ChunkTable, 128><<<(max_paths + 127) / 128, 128, 0, st>>>(t, p, q);
   else k_resolve<ChunkTable, 256><<<(max_paths + 255) / 256, 256, 0, st>>>(t, p, q);

@@ -99,8 +99,6 @@ void PackedLanes::launch(const std::vector<PackedJob>& jobs, const std::vector<P
     for (int bounce = 0; bounce < max_depth; ++bounce) {
       const int q = bounce & 1;
       launch_trace_packed(tt, p, q, 2 * n_paths, ls, trace_cap);
-      ck(cudaMemsetAsync(&p.counts[q ^ 1], 0, sizeof(uint32_t), ls), "memset count");
-      ck(cudaMemsetAsync(&p.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), ls), "memset count");
       launch_shade_packed(ct, p, q, n_paths, ls, resolve_threads, sample_threads);
     }
   }

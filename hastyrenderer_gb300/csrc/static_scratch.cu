@@ -115,8 +115,6 @@ extern "C" int hasty_job_render_pass_static(hasty_job* job, int pass, double* d_
     for (int bounce = 0; bounce < job->sd.max_depth; ++bounce) {
       int q = bounce & 1;
       launch_trace(job->sd, p, q, 2 * npix, job->stream);
-      ck(cudaMemsetAsync(&p.counts[q ^ 1], 0, sizeof(uint32_t), job->stream), "clear counter");
-      ck(cudaMemsetAsync(&p.counts[2 + (q ^ 1)], 0, sizeof(uint32_t), job->stream), "clear counter");
       launch_shade(job->sd, p, b, q, npix, job->stream);
     }
     launch_accumulate(job->sd, p, b, d_color, sum_normal, sum_albedo, job->stream);

@@ -46,6 +46,18 @@ template <int KIND> constexpr bool kPersistent = KIND == 1;
 template <int KIND> struct TravOf { using T = TravBinary; };
 template <> struct TravOf<1> { using T = TravWide; };
 
+// First thread of a bounce's closest-hit launch: counts the rays and clears
+// the queue counters the bounce's shading kernels fill (path and ray queue
+// q^1, the sample queue), which nothing reads until then, so the host
+// enqueues no memsets between the kernels. (The fetch counter this launch
+// uses was cleared by the kernel before it: ray generation or resolve.)
+__device__ __forceinline__ void start_bounce_counters(const PathsDev& P, int q, uint32_t n) {
+  P.counts[q ^ 1] = 0;
+  P.counts[2 + (q ^ 1)] = 0;
+  P.counts[kSampleCount] = 0;
+  if (n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
+}
+
 // Adds this warp's count of rays whose traversal stack overflowed to `stat`
 // (one atomic per warp, only when there are any).
 __device__ __forceinline__ void add_overflows(unsigned long long* stat, uint32_t mine) {
@@ -119,7 +131,7 @@ __device__ __forceinline__ uint32_t simple_trace(uint32_t n, Fetch fetch, Done d
 template <int KIND, bool SIMPLE = false>
 __global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
   const uint32_t n = P.counts[2 + q];
-  if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
+  if (blockIdx.x == 0 && threadIdx.x == 0) start_bounce_counters(P, q, n);
   const int32_t* rq = P.rq[q];
   if (!kPersistent<KIND>) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -165,7 +177,7 @@ __global__ void k_trace_rays(SceneDev sc, const float* rays, int n, float4* hits
 template <int KIND, bool SIMPLE = false>
 __global__ void TRACE_BOUNDS k_trace_packed(const __grid_constant__ TraceTable T, PathsDev P, int q) {
   const uint32_t n = P.counts[2 + q];
-  if (blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&P.stats[ST_RAYS], (unsigned long long)n);
+  if (blockIdx.x == 0 && threadIdx.x == 0) start_bounce_counters(P, q, n);
   const int32_t* rq = P.rq[q];
   if (!kPersistent<KIND>) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -272,9 +284,11 @@ int simple_trace_nodes() {
 }
 bool simple_trace_bvh(const SceneDev& sc) { return sc.bvh_kind == 1 && sc.n_nodes <= simple_trace_nodes(); }
 
-// The persistent kernels take rays through P.counts[kFetchCounter], cleared
-// on the stream before each launch. Grids: the SMs' resident blocks (at most
-// blocks_per_sm per SM when given), fewer when the queue bound is smaller.
+// The persistent kernels take rays through P.counts[kFetchCounter]: cleared
+// on the stream before each launch of the engine's kernel, and by the kernel
+// before it (ray generation, resolve) for the wavefront's. Grids: the SMs'
+// resident blocks (at most blocks_per_sm per SM when given), fewer when the
+// queue bound is smaller.
 void launch_trace_multi(const PathsDev& p, const MultiDev& m, int bvh_kind, int max_rays, cudaStream_t st,
                         int blocks_per_sm) {
   static PersistentShape shape[2] = {{0, 0}, {0, 0}};
@@ -298,7 +312,6 @@ void launch_trace_packed(const TraceTable& t, const PathsDev& p, int q, int max_
   const int grid = persistent_blocks(shape[k], blocks_per_sm);
   int blocks = k && !simple ? std::min(grid, std::max(1, (max_rays + 127) / 128))
                             : std::min(8 * grid, std::max(1, (max_rays + 127) / 128));
-  cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
   if (k && simple) k_trace_packed<1, true><<<blocks, 128, 0, st>>>(t, p, q);
   else if (k) k_trace_packed<1><<<blocks, 128, 0, st>>>(t, p, q);
   else k_trace_packed<0><<<blocks, 128, 0, st>>>(t, p, q);
@@ -312,7 +325,6 @@ void launch_trace(const SceneDev& sc, const PathsDev& p, int q, int max_rays, cu
   const int grid = persistent_blocks(shape[k], blocks_per_sm);
   int blocks = k && !simple ? std::min(grid, std::max(1, (max_rays + 127) / 128))
                             : std::min(8 * grid, std::max(1, (max_rays + 127) / 128));
-  cudaMemsetAsync(&p.counts[kFetchCounter], 0, sizeof(uint32_t), st);
   if (k && simple) k_trace<1, true><<<blocks, 128, 0, st>>>(sc, p, q);
   else if (k) k_trace<1><<<blocks, 128, 0, st>>>(sc, p, q);
   else k_trace<0><<<blocks, 128, 0, st>>>(sc, p, q);
