@@ -59,8 +59,9 @@ B_SHADE = 2 * 96 + 92
 # divided by the rays and vertices the process traced and shaded): DRAM
 # bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced ray and
 # per shaded vertex, and for the
-# closest-hit kernel warp instructions and thread instructions per ray
-# (smsp__inst_executed.sum, smsp__thread_inst_executed.sum). Classes: "plain"
+# closest-hit kernel warp instructions and thread instructions per ray and
+# the shading pair's warp instructions per vertex (smsp__inst_executed.sum,
+# smsp__thread_inst_executed.sum). Classes: "plain"
 # (the 1080p 800-sphere field), "cornell" (the 256x256 box), "mix:<kind>"
 # (one job of each scene kind of the 64-job mix, rendered alone; a class
 # without a capture gives null). They give each kernel's traffic and the closest-hit kernel's
@@ -68,19 +69,19 @@ B_SHADE = 2 * 96 + 92
 # weights them by each class's rays and vertices.
 COUNTERS = {
     "plain": {"k_trace": {"dram_bytes_per_ray": 128.67, "warp_inst_per_ray": 227.73, "thread_inst_per_ray": 4535.8},
-              "k_resolve+k_sample": {"dram_bytes_per_vertex": 1038.97}},
+              "k_resolve+k_sample": {"dram_bytes_per_vertex": 1038.97, "warp_inst_per_vertex": 183.84}},
     "cornell": {"k_trace": {"dram_bytes_per_ray": 80.77, "warp_inst_per_ray": 63.33, "thread_inst_per_ray": 982.99},
-                "k_resolve+k_sample": {"dram_bytes_per_vertex": 863.61}},
+                "k_resolve+k_sample": {"dram_bytes_per_vertex": 863.61, "warp_inst_per_vertex": 147.53}},
     "mix:cornell": {"k_trace": {"dram_bytes_per_ray": 73.41, "warp_inst_per_ray": 60.67, "thread_inst_per_ray": 986.99},
-                    "k_resolve+k_sample": {"dram_bytes_per_vertex": 819.35}},
+                    "k_resolve+k_sample": {"dram_bytes_per_vertex": 819.35, "warp_inst_per_vertex": 146.09}},
     "mix:field50": {"k_trace": {"dram_bytes_per_ray": 78.50, "warp_inst_per_ray": 58.44, "thread_inst_per_ray": 1178.49},
-                    "k_resolve+k_sample": {"dram_bytes_per_vertex": 871.84}},
+                    "k_resolve+k_sample": {"dram_bytes_per_vertex": 871.84, "warp_inst_per_vertex": 181.70}},
     "mix:field200": {"k_trace": {"dram_bytes_per_ray": 89.84, "warp_inst_per_ray": 100.99,
                                  "thread_inst_per_ray": 1966.27},
-                     "k_resolve+k_sample": {"dram_bytes_per_vertex": 916.45}},
+                     "k_resolve+k_sample": {"dram_bytes_per_vertex": 916.45, "warp_inst_per_vertex": 189.78}},
     "mix:field800": {"k_trace": {"dram_bytes_per_ray": 134.29, "warp_inst_per_ray": 224.96,
                                  "thread_inst_per_ray": 4318.20},
-                     "k_resolve+k_sample": {"dram_bytes_per_vertex": 1016.86}},
+                     "k_resolve+k_sample": {"dram_bytes_per_vertex": 1016.86, "warp_inst_per_vertex": 188.57}},
 }
 REF_PASSES_PER_STEP = 8      # reference arm: passes of the CPU sample per step
 ISSUE_PER_SM_PER_CLOCK = 4   # warp instructions per SM and clock (one per scheduler)
@@ -418,6 +419,12 @@ def kernel_rooflines(stage: dict, hbm: float, peak_kind: str, sm_mhz, costs):
                "ms_per_launch": shade_ms, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                "frac": ach / hbm, "peak_kind": peak_kind, "bytes_per_unit": B_SHADE,
                "algorithmic_bytes_per_launch": alg, "traffic": dram / n if dram is not None else None}
+    # the same launches against the issue rate (the pair is latency-bound: neither bound is reached)
+    inst = _weighted(by_class, "k_resolve+k_sample", "warp_inst_per_vertex", "shaded")
+    if inst is not None:
+        ach_i = inst / n / (shade_ms * 1e-3) * 1e-9
+        k_shade["issue"] = {"achieved": ach_i, "peak": issue_peak, "unit": "G warp-inst/s", "frac": ach_i / issue_peak,
+                            "warp_inst_per_vertex": inst / max(stage["shaded"], 1), "peak_kind": issue_kind}
     kernels += [k_trace, k_shade]
     # dominant by total device time of the run
     totals = {"k_paths": stage["path_ms"], "k_trace": stage["trace_ms"], "k_resolve+k_sample": stage["shade_ms"]}
