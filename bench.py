@@ -660,7 +660,7 @@ def run_batch(args):
     one through the single-job path, with bit-identical images."""
     import numpy as np
     import torch
-    from hastyrenderer_gb300 import Context, RenderJob, batch_render, workloads
+    from hastyrenderer_gb300 import Context, RenderJob, batch_render, load_jobs, workloads
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if rank != 0:
@@ -677,7 +677,7 @@ def run_batch(args):
     # end to end through the C ABI: load every job (parse, BVH build, upload),
     # one batched render, every job's colour estimate read to the host
     t0 = time.perf_counter()
-    resident = [RenderJob(j["path"], ctx) for j in jobs]
+    resident = load_jobs([j["path"] for j in jobs], ctx)   # parse, BVH build, upload on all host threads
     load_s = time.perf_counter() - t0
     eargs, tune = tuned_batch_args(args, jobs, ctx)   # (tuning is not part of the end-to-end time)
     if args.lane_paths:
@@ -776,8 +776,9 @@ def run_batch(args):
                               "note": "1/8 of every job's passes with stage timing (one render lane), scaled by 8"},
         "cpu_baseline": cpu,
         "e2e": {"value": total / e2e_s, "unit": "samples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "includes": "loading all 64 jobs (parse, BVH build, upload) + one batched render + every colour "
-                            "estimate read to the host", "load_s": load_s, "scene_generation_s": gen_s},
+                "includes": "loading all the jobs (hasty_jobs_load on all host threads: parse, BVH build, upload) + "
+                            "one batched render + every colour estimate read to the host", "load_s": load_s,
+                "scene_generation_s": gen_s},
         "autotune": tune, "clocks": clocks, "peak_hbm_gbs": hbm, "peak_kind": peak_kind,
     }
     print(json.dumps(line), flush=True)

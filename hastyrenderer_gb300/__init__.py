@@ -5,6 +5,7 @@ holds the ctypes binding (`native`), a Python mirror of the reference's job
 interface (`api`), the in-tree build (`build`) and seeded scene generators
 (`scenes`).
 """
-from .api import AOV_ALBEDO, AOV_COLOR, AOV_NORMAL, Context, HastyError, RenderJob, Server, batch_render, debug_bsdf  # noqa: F401
+from .api import (AOV_ALBEDO, AOV_COLOR, AOV_NORMAL, Context, HastyError, RenderJob, Server, batch_render,  # noqa: F401
+                  debug_bsdf, load_jobs)
 
 __version__ = "0.1.0"

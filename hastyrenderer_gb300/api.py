@@ -16,7 +16,7 @@ import numpy as np
 from . import native
 from .native import AOV_ALBEDO, AOV_COLOR, AOV_NORMAL, HastyError, check
 
-__all__ = ["Context", "RenderJob", "debug_bsdf", "AOV_COLOR", "AOV_NORMAL", "AOV_ALBEDO", "HastyError"]
+__all__ = ["Context", "RenderJob", "load_jobs", "debug_bsdf", "AOV_COLOR", "AOV_NORMAL", "AOV_ALBEDO", "HastyError"]
 
 
 class Context:
@@ -51,6 +51,25 @@ def default_context() -> Context:
     if _default_ctx is None:
         _default_ctx = Context(0)
     return _default_ctx
+
+
+def load_jobs(paths, ctx: Context | None = None, threads: int = 0) -> list:
+    """Loads several render jobs at once (hasty_jobs_load: parse, BVH build
+    and upload of different jobs overlap on `threads` host threads, 0: all).
+    Returns one RenderJob per path, in order; raises on the first failure
+    (then no job stays loaded)."""
+    ctx = ctx or default_context()
+    n = len(paths)
+    enc = [p.encode() for p in paths]
+    arr = (ctypes.c_char_p * max(n, 1))(*enc)
+    handles = (ctypes.c_void_p * max(n, 1))()
+    check(native.lib().hasty_jobs_load(ctx._h, arr, n, int(threads), handles))
+    jobs = []
+    for i in range(n):
+        j = RenderJob(None, ctx)
+        j._h = ctypes.c_void_p(handles[i])
+        jobs.append(j)
+    return jobs
 
 
 class RenderJob:

@@ -13,9 +13,12 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <sys/stat.h>
+#include <thread>
 #include <vector>
 
 #include "bvh_build.h"
@@ -450,6 +453,45 @@ int hasty_job_load(hasty_ctx* ctx, const char* path, hasty_job** out) {
   return guarded([&] {
     if (!ctx || !path || !out) throw ApiError{HASTY_ERR_ARG, "null argument"};
     *out = load_job(ctx, path, true).release();
+    return HASTY_OK;
+  });
+}
+
+int hasty_jobs_load(hasty_ctx* ctx, const char* const* paths, size_t n, int32_t threads, hasty_job** out) {
+  return guarded([&] {
+    if (!ctx || (n && (!paths || !out))) throw ApiError{HASTY_ERR_ARG, "null argument"};
+    for (size_t i = 0; i < n; ++i) {
+      if (!paths[i]) throw ApiError{HASTY_ERR_ARG, "null path"};
+      out[i] = nullptr;
+    }
+    std::vector<std::unique_ptr<hasty_job>> jobs(n);
+    std::atomic<size_t> next{0};
+    std::atomic<bool> failed{false};
+    std::mutex mu;
+    std::exception_ptr first;   // the failure of the lowest-numbered failing job
+    size_t first_i = n;
+    auto worker = [&] {
+      cudaSetDevice(ctx->device);
+      for (;;) {
+        const size_t i = next.fetch_add(1);
+        if (i >= n || failed.load()) return;
+        try {
+          jobs[i] = load_job(ctx, paths[i], true);
+        } catch (...) {
+          std::lock_guard<std::mutex> lk(mu);
+          if (i < first_i) { first_i = i; first = std::current_exception(); }
+          failed = true;
+        }
+      }
+    };
+    size_t nt = threads > 0 ? size_t(threads) : size_t(std::max(1u, std::thread::hardware_concurrency()));
+    nt = std::max<size_t>(1, std::min(nt, n));
+    std::vector<std::thread> pool;
+    for (size_t k = 1; k < nt; ++k) pool.emplace_back(worker);
+    worker();
+    for (std::thread& t : pool) t.join();
+    if (first) std::rethrow_exception(first);   // the loaded jobs are freed with `jobs`
+    for (size_t i = 0; i < n; ++i) out[i] = jobs[i].release();
     return HASTY_OK;
   });
 }

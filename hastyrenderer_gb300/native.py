@@ -115,6 +115,7 @@ def lib() -> ctypes.CDLL:
         "hasty_ctx_create": [I, ctypes.c_uint32, P],
         "hasty_ctx_destroy": [P],
         "hasty_job_load": [P, ctypes.c_char_p, P],
+        "hasty_jobs_load": [P, P, SZ, ctypes.c_int32, P],
         "hasty_job_destroy": [P],
         "hasty_job_info_get": [P, P],
         "hasty_job_set_seed": [P, U64],

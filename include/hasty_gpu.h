@@ -107,6 +107,14 @@ int hasty_ctx_create(int device, uint32_t flags, hasty_ctx** out);
 int hasty_ctx_destroy(hasty_ctx* ctx);
 
 int hasty_job_load(hasty_ctx* ctx, const char* render_job_path, hasty_job** out);
+/* Loads n jobs as hasty_job_load would, on `threads` host threads at once
+ * (0: as many as the host has, at most n): parse, BVH build and upload of
+ * different jobs overlap. out[i] receives job i. All or nothing: on the first
+ * failure no job is returned (out[] is left null) and the status and
+ * hasty_last_error are that job's. For a batch or server front end that
+ * starts from many renderJob files (no reference counterpart: the reference
+ * loads one job per process, apps/PathTracingViewer.cpp:34-37). */
+int hasty_jobs_load(hasty_ctx* ctx, const char* const* render_job_paths, size_t n, int32_t threads, hasty_job** out);
 int hasty_job_destroy(hasty_job* job);
 int hasty_job_info_get(hasty_job* job, hasty_job_info* out);
 int hasty_job_set_seed(hasty_job* job, uint64_t seed);      /* also clears the accumulators */

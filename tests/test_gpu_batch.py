@@ -124,3 +124,25 @@ def test_release_paths_between_renders():
     b.render_passes(2, sync=True)
     for x, y in zip(_sums(a), _sums(b)):
         assert np.array_equal(x, y)
+
+
+def test_jobs_loaded_together_equal_loaded_alone(tmp_path):
+    """hasty_jobs_load (several host threads) gives jobs whose renders equal
+    those of jobs loaded one by one; a missing file fails the whole call with
+    HASTY_ERR_LOAD and returns no job."""
+    from hastyrenderer_gb300 import HastyError, load_jobs
+    paths = [os.path.join(GOLDEN, "scenes", n, "renderJob.json") for n in NAMES + NAMES]
+    together = load_jobs(paths, threads=4)
+    assert len(together) == len(paths)
+    for p, jt in zip(paths, together):
+        alone = _job(os.path.basename(os.path.dirname(p)))
+        assert (jt.width, jt.height, jt.info.n_triangles) == (alone.width, alone.height, alone.info.n_triangles)
+        jt.render_passes(2, sync=True)
+        alone.render_passes(2, sync=True)
+        for a, b in zip(_sums(jt), _sums(alone)):
+            assert np.array_equal(a, b), p
+        jt.close()
+        alone.close()
+    with pytest.raises(HastyError) as err:
+        load_jobs(paths[:2] + [str(tmp_path / "missing" / "renderJob.json")] + paths[2:3], threads=2)
+    assert err.value.code == -2, err.value   # HASTY_ERR_LOAD
