@@ -83,7 +83,7 @@ COUNTERS = {
                                  "thread_inst_per_ray": 4318.20},
                      "k_resolve+k_sample": {"dram_bytes_per_vertex": 1016.86, "warp_inst_per_vertex": 188.57}},
 }
-REF_PASSES_PER_STEP = 8      # reference arm: passes of the CPU sample per step
+REF_PASSES_PER_STEP = 64     # reference arm: passes of the CPU sample per step (about 4 s on the mix)
 ISSUE_PER_SM_PER_CLOCK = 4   # warp instructions per SM and clock (one per scheduler)
 SMS = 152
 
