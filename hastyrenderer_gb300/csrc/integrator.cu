@@ -699,6 +699,10 @@ __global__ void __launch_bounds__(kPathBlockThreads, HASTY_PATH_MIN_BLOCKS) k_pa
 // the passes were grouped into batches (single job, packed batches, serving).
 // A sample whose radiance has a NaN is dropped with its AOVs
 // (core/src/PathTracing.cpp:132-142).
+#ifndef HASTY_ACC_UNROLL
+#define HASTY_ACC_UNROLL 4
+#endif
+constexpr int kAccUnroll = HASTY_ACC_UNROLL;
 __global__ void k_accumulate(PathsDev P, int first, int n_passes, int npix, double* acc_c, double* acc_n,
                              double* acc_a) {
   int px = blockIdx.x * blockDim.x + threadIdx.x;
@@ -706,14 +710,28 @@ __global__ void k_accumulate(PathsDev P, int first, int n_passes, int npix, doub
   double c[3], n[3], a[3];
   for (int q = 0; q < 3; ++q) { c[q] = acc_c[3 * px + q]; n[q] = acc_n[3 * px + q]; a[q] = acc_a[3 * px + q]; }
   unsigned nan = 0;
-  for (int k = 0; k < n_passes; ++k) {
-    int64_t s = first + int64_t(k) * npix + px;
-    float4 cc = P.out_color[s];
-    if (cc.x != cc.x || cc.y != cc.y || cc.z != cc.z) { ++nan; continue; }
-    float4 nn = P.out_normal[s], aa = P.out_albedo[s];
+  auto add = [&](float4 cc, float4 nn, float4 aa) {
+    if (cc.x != cc.x || cc.y != cc.y || cc.z != cc.z) { ++nan; return; }
     c[0] += cc.x; c[1] += cc.y; c[2] += cc.z;
     n[0] += nn.x; n[1] += nn.y; n[2] += nn.z;
     a[0] += aa.x; a[1] += aa.y; a[2] += aa.z;
+  };
+  // kAccUnroll passes' loads are issued before their adds (which stay in
+  // pass order), so a thread has that many passes' reads in flight
+  int k = 0;
+  for (; k + kAccUnroll <= n_passes; k += kAccUnroll) {
+    float4 cc[kAccUnroll], nn[kAccUnroll], aa[kAccUnroll];
+#pragma unroll
+    for (int u = 0; u < kAccUnroll; ++u) {
+      const int64_t s = first + int64_t(k + u) * npix + px;
+      cc[u] = P.out_color[s]; nn[u] = P.out_normal[s]; aa[u] = P.out_albedo[s];
+    }
+#pragma unroll
+    for (int u = 0; u < kAccUnroll; ++u) add(cc[u], nn[u], aa[u]);
+  }
+  for (; k < n_passes; ++k) {
+    const int64_t s = first + int64_t(k) * npix + px;
+    add(P.out_color[s], P.out_normal[s], P.out_albedo[s]);
   }
   for (int q = 0; q < 3; ++q) { acc_c[3 * px + q] = c[q]; acc_n[3 * px + q] = n[q]; acc_a[3 * px + q] = a[q]; }
   if (nan) atomicAdd(&P.stats[ST_NAN], (unsigned long long)nan);
