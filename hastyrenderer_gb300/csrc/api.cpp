@@ -18,6 +18,7 @@
 #include <mutex>
 #include <string>
 #include <sys/stat.h>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -487,7 +488,13 @@ int hasty_jobs_load(hasty_ctx* ctx, const char* const* paths, size_t n, int32_t 
     size_t nt = threads > 0 ? size_t(threads) : size_t(std::max(1u, std::thread::hardware_concurrency()));
     nt = std::max<size_t>(1, std::min(nt, n));
     std::vector<std::thread> pool;
-    for (size_t k = 1; k < nt; ++k) pool.emplace_back(worker);
+    for (size_t k = 1; k < nt; ++k) {
+      try {
+        pool.emplace_back(worker);
+      } catch (const std::system_error&) {
+        break;   // fewer threads: the ones running (and this one) take the rest
+      }
+    }
     worker();
     for (std::thread& t : pool) t.join();
     if (first) std::rethrow_exception(first);   // the loaded jobs are freed with `jobs`
