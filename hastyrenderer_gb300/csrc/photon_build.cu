@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(kThreads) k_sort_hist(const int32_t* coord, in
 
 // Stable scatter: an element's position is its digit's offset for the tile
 // (scanned histogram), plus the elements of that digit before it in the
-// tile (earlier rounds, earlier warps of this round, earlier lanes).
+// tile (earlier loop iterations, earlier warps of this iteration, earlier lanes).
 __global__ void __launch_bounds__(kThreads) k_sort_scatter(const int32_t* coord, int32_t lo, int shift, uint32_t n,
                                                            const uint32_t* perm_in, uint32_t* perm_out,
                                                            const uint32_t* hist, uint32_t nb) {
