@@ -132,6 +132,8 @@ template <int KIND, bool SIMPLE = false>
 __global__ void TRACE_BOUNDS k_trace(SceneDev sc, PathsDev P, int q) {
   const uint32_t n = P.counts[2 + q];
   if (blockIdx.x == 0 && threadIdx.x == 0) start_bounce_counters(P, q, n);
+  // blocks past the queue exit at once (the persistent blocks before them take all the rays)
+  if (blockIdx.x * blockDim.x >= n) return;
   const int32_t* rq = P.rq[q];
   if (!kPersistent<KIND>) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -178,6 +180,8 @@ template <int KIND, bool SIMPLE = false>
 __global__ void TRACE_BOUNDS k_trace_packed(const __grid_constant__ TraceTable T, PathsDev P, int q) {
   const uint32_t n = P.counts[2 + q];
   if (blockIdx.x == 0 && threadIdx.x == 0) start_bounce_counters(P, q, n);
+  // blocks past the queue exit at once (the persistent blocks before them take all the rays)
+  if (blockIdx.x * blockDim.x >= n) return;
   const int32_t* rq = P.rq[q];
   if (!kPersistent<KIND>) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
