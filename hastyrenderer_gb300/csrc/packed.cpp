@@ -257,6 +257,44 @@ void batch_render_packed(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes
 
 }  // namespace
 
+extern "C" int hasty_debug_pack(const int32_t* npix, const int32_t* passes, const int32_t* cls, size_t n_jobs,
+                                int64_t slots, int64_t job_samples, int32_t* out, size_t max_chunks, size_t* n_out) {
+  return guarded([&] {
+    if (!n_out || (n_jobs && (!npix || !passes || !cls)) || (max_chunks && !out) || slots <= 0)
+      throw ApiError{HASTY_ERR_ARG, "bad argument"};
+    std::vector<PackedJob> pj(n_jobs);
+    std::vector<uint32_t> base(n_jobs, 0u);
+    std::vector<int32_t> left(n_jobs);
+    std::vector<int> order;
+    for (size_t i = 0; i < n_jobs; ++i) {
+      if (npix[i] <= 0 || npix[i] > slots || passes[i] < 0 || cls[i] < 0 || cls[i] >= kKernelClasses)
+        throw ApiError{HASTY_ERR_ARG, "bad job"};
+      pj[i].npix = npix[i];
+      pj[i].path_kernel = cls[i] == 2;
+      pj[i].simple_trace = cls[i] == 1;
+      left[i] = passes[i];
+      if (passes[i] > 0) order.push_back(int(i));
+    }
+    size_t n = 0;
+    int turn = 0;
+    for (int32_t batch = 0;; ++batch) {
+      const std::vector<PackedChunk> chunks = pack_next(pj, order, base, left, slots, job_samples, turn);
+      if (chunks.empty()) break;
+      for (const PackedChunk& c : chunks) {
+        if (n < max_chunks) {
+          out[4 * n] = batch;
+          out[4 * n + 1] = c.job;
+          out[4 * n + 2] = int32_t(c.pass_base);
+          out[4 * n + 3] = c.n_passes;
+        }
+        ++n;
+      }
+    }
+    *n_out = n;
+    return HASTY_OK;
+  });
+}
+
 extern "C" int hasty_batch_render(hasty_ctx* ctx, hasty_job** jobs, const int32_t* passes, size_t n_jobs,
                                   const hasty_batch_config* cfg, hasty_batch_stats* out) {
   return guarded([&] {

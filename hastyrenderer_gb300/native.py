@@ -150,6 +150,7 @@ def lib() -> ctypes.CDLL:
         "hasty_debug_pm_map": [P, P, P, P, P, P, P, P],
         "hasty_job_render_pass_static": [P, I, P],
         "hasty_debug_static_scratch": [P, P, P],
+        "hasty_debug_pack": [P, P, P, SZ, I64, I64, P, SZ, P],
         "hasty_debug_bounds_status": [P],
         "hasty_server_start": [P, P, P],
         "hasty_server_submit": [P, ctypes.c_char_p, ctypes.c_int32, P, P],

@@ -383,6 +383,16 @@ int hasty_debug_bounds_status(uint32_t* flags);
 /* Test hook (no device needed): the static scratch's pixel limit, the bytes a
  * frame of that many pixels carves from it, and its size. */
 int hasty_debug_static_scratch(int64_t* max_pixels, int64_t* bytes_needed, int64_t* capacity);
+/* Test hook (no device needed): the packed-batch plan hasty_batch_render
+ * and the server follow, for n_jobs jobs of npix[i] pixels, passes[i]
+ * passes and kernel class cls[i] (0 wavefront with the persistent
+ * closest-hit kernel, 1 wavefront with one ray per thread, 2 path kernel),
+ * `slots` path slots per batch and at most job_samples camera samples of one
+ * job per batch (0: no limit). Writes one (batch, job, first pass, passes)
+ * quadruple of int32 per chunk, in launch order, up to max_chunks, and the
+ * number of chunks planned into n_out. */
+int hasty_debug_pack(const int32_t* npix, const int32_t* passes, const int32_t* cls, size_t n_jobs, int64_t slots,
+                     int64_t job_samples, int32_t* out, size_t max_chunks, size_t* n_out);
 
 /* Closest hits of n rays given as n x 6 host floats (origin, direction):
  * global triangle index (-1 miss), t, u, v. */
