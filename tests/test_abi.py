@@ -39,6 +39,11 @@ def test_errors_are_status_codes():
     assert lib.hasty_job_snapshot_get(None, 0, None, None) == -1
     assert lib.hasty_job_write_outputs_async(None, b".", 0) == -1
     assert lib.hasty_job_outputs_wait(None) == -1
+    # several jobs at once: a null context or path list is an argument error
+    out = (ctypes.c_void_p * 2)()
+    paths = (ctypes.c_char_p * 2)(b"a/renderJob.json", b"b/renderJob.json")
+    assert lib.hasty_jobs_load(None, paths, 2, 0, out) == -1
+    assert lib.hasty_debug_pack(None, None, None, 1, 10, 0, None, 0, None) == -1
 
 
 def test_static_scratch_holds_its_largest_frame():
