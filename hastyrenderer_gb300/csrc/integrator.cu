@@ -191,11 +191,16 @@ __device__ __forceinline__ bool start_path(const SceneDev& sc, const PathsDev& P
   P.rng[s] = r.state;
   P.thr[s] = make_float4(1.f, 1.f, 1.f, 0.f);
   P.rad[s] = make_float4(0.f, 0.f, 0.f, __uint_as_float(PF_CAMERA | PF_PEND_B | chunk_bits));
-  P.out_color[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-  P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-  P.out_albedo[s] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (!keep_media_block) P.med_block[s] = -1;
-  if (sc.max_depth <= 0) return false;
+  if (sc.max_depth <= 0) {
+    // a traced path writes its outputs itself (normal and albedo when its
+    // camera ray is resolved, colour when it ends, at the latest at the last
+    // bounce); an untraced one leaves zeros
+    P.out_color[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    P.out_normal[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    P.out_albedo[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return false;
+  }
   P.ray_o[2 * s] = f4(o, __uint_as_float(uint32_t(sp.chunk)));
   P.ray_d[2 * s] = f4(d, 0.f);
   return true;
