@@ -660,7 +660,7 @@ def run_batch(args):
     one through the single-job path, with bit-identical images."""
     import numpy as np
     import torch
-    from hastyrenderer_gb300 import Context, RenderJob, batch_render, load_jobs, workloads
+    from hastyrenderer_gb300 import Context, batch_render, load_jobs, workloads
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if rank != 0:
